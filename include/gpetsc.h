@@ -1,0 +1,300 @@
+/*
+ * gpetsc.h -- C ABI of libgpetsc.so, the GB300 (sm_103a) implementation of
+ * lee101/mojo-petsc4py's sequential Krylov path.
+ *
+ * Two layers:
+ *
+ *  1. gp_*  Device layer.  Opaque handles for a CSR matrix, a preconditioner
+ *     and a Krylov solver; vectors are device pointers (float64).  Every
+ *     function returns 0 on success or a nonzero status (see GP_ERR_*), with
+ *     the message available from gp_last_error().  Nothing throws across the
+ *     ABI.  `stream` arguments are cudaStream_t values passed as void*; NULL
+ *     is the legacy default stream.  Calls that return a host value (a
+ *     reduction, a solve result) synchronize before returning.
+ *
+ *  2. mp_*  The reference's own host ABI (src/capi.mojo:32-424, declared for
+ *     ctypes in python/mojopetsc4py/_lib.py:23-87): the same 59 names, the
+ *     same argument order and meaning, host pointers for every buffer, int64
+ *     for every index and size, double for every scalar.  Each call copies its
+ *     inputs to the GPU, runs the CUDA kernels of layer 1 and copies the
+ *     outputs back, so a caller of the reference's library can switch to this
+ *     one without changing a call.  The reference passes addresses as int64;
+ *     on LP64 targets a pointer argument has the same calling convention.
+ *
+ * Index arrays on the device are int32 (the reference stores int64; no value
+ * depends on it): matrices must have fewer than 2^31 rows and nonzeros.
+ */
+#ifndef GPETSC_H
+#define GPETSC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status */
+enum {
+  GP_OK = 0,
+  GP_ERR_ARG = 1,         /* bad argument: size, null pointer, alias, type */
+  GP_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  GP_ERR_TIMEOUT = 3,     /* a device wait ran out of its iteration budget */
+  GP_ERR_NOT_SETUP = 4,   /* object used before set-up */
+  GP_ERR_UNSUPPORTED = 5, /* option not available on the device path */
+  GP_ERR_NUMERIC = 6,
+  GP_ERR_INTERNAL = 7
+};
+
+/* Library version (major*10000 + minor*100 + patch). */
+int gp_version(void);
+/* Message of the last failed call on this host thread. */
+const char *gp_last_error(void);
+/* Number of visible CUDA devices (0 when none). */
+int gp_device_count(int *count);
+int gp_set_device(int device);
+
+/* ------------------------------------------------------------ Mat */
+typedef struct gp_mat_s *gp_mat;
+
+/* CSR from host arrays in the reference's SeqAIJ layout (int64 indptr and
+ * indices, ascending columns per row).  Replaces the Mat storage of
+ * python/mojopetsc4py/PETSc/Mat.py:310-344 (setValuesCSR) on the device. */
+int gp_mat_create(gp_mat *out, int64_t nrows, int64_t ncols, int64_t nnz,
+                  const int64_t *indptr, const int64_t *indices, const double *values);
+/* Same from int32 host arrays. */
+int gp_mat_create_i32(gp_mat *out, int64_t nrows, int64_t ncols, int64_t nnz,
+                      const int32_t *indptr, const int32_t *indices, const double *values);
+int gp_mat_destroy(gp_mat A);
+/* New values for the same pattern (host or device pointer). */
+int gp_mat_set_values(gp_mat A, const double *values, int on_device, void *stream);
+/* Device pointer of the values array (valid until gp_mat_destroy). */
+int gp_mat_values_ptr(gp_mat A, double **d_values);
+int gp_mat_info(gp_mat A, int64_t *nrows, int64_t *ncols, int64_t *nnz);
+/* y = A x.        Replaces MatMult_SeqAIJ (src/ported.mojo:380-391). */
+int gp_mat_mult(gp_mat A, const double *x, double *y, void *stream);
+/* y = A x + v.    Replaces MatMultAdd_SeqAIJ (src/ported.mojo:394-405). */
+int gp_mat_mult_add(gp_mat A, const double *x, const double *v, double *y, void *stream);
+/* y = A^T x.      Replaces MatMultTranspose_SeqAIJ (src/ported.mojo:408-431). */
+int gp_mat_mult_transpose(gp_mat A, const double *x, double *y, void *stream);
+/* d = diag(A).    Replaces MatGetDiagonal_SeqAIJ (src/ported.mojo:434-447). */
+int gp_mat_get_diagonal(gp_mat A, double *d, void *stream);
+
+/* ------------------------------------------------------------ Vec */
+/* Elementwise operations (src/ported.mojo:75-341, src/simdvec.mojo:40-319).
+ * Operand roles per op (y is written):
+ *   0 copy y=x, 1 set y=alpha, 2 scale y*=alpha, 3 shift y+=alpha,
+ *   4 axpy y+=alpha x, 5 aypx y=x+alpha y, 6 axpby y=alpha x+beta y,
+ *   7 axpbypcz y=alpha x+beta w+gamma y, 8 waxpy y=alpha x+w,
+ *   9 pointwise mult y=x.*w, 10 divide y=x./w, 11 min, 12 max, 13 maxabs,
+ *   14 reciprocal (y), 15 exp, 16 log, 17 sqrtabs, 18 abs, 19 chop(alpha),
+ *   20 swap(y,x), 21 zero, 22 scale-set y=x*alpha, 23 divide y=y/alpha.
+ * Scalar branches follow the reference (VecAYPX alpha 0/1, VecAXPBY beta 0 /
+ * alpha 0, VecSet alpha 0). */
+int gp_vec_map(int op, int64_t n, double *y, const double *x, const double *w,
+               double alpha, double beta, double gamma, void *stream);
+/* y += sum_k alpha[k] x[k]; alpha and the pointer array on the host. */
+int gp_vec_maxpy(int64_t n, double *y, int64_t nv, const double *alpha,
+                 const double *const *xs, void *stream);
+/* Reductions into host memory: 0 dot(x,y), 1 sum x^2, 2 sum|x|, 3 sum x,
+ * 4 (x.y, x.x), 5 max|x| (first NaN adopted).  Replaces the blocked
+ * reductions of src/simdvec.mojo:332-488. */
+int gp_vec_reduce(int op, int64_t n, const double *x, const double *y, double *out,
+                  void *stream);
+/* VecMin/VecMax (src/ported.mojo:165-196): value and first index. */
+int gp_vec_minmax(int64_t n, const double *x, int is_max, int64_t *idx, double *val,
+                  void *stream);
+/* max |x_i / y_i| with x_i where y_i == 0 (src/simdvec.mojo:491-500). */
+int gp_vec_max_pointwise_divide(int64_t n, const double *x, const double *y, double *out,
+                                void *stream);
+
+/* ------------------------------------------------------------ PC */
+typedef struct gp_pc_s *gp_pc;
+
+/* Preconditioner options; defaults are those of
+ * python/mojopetsc4py/PETSc/PC.py:108-148. */
+typedef struct {
+  int32_t type;        /* 0 none, 2 jacobi, 4 sor, 5 ilu, 6 icc */
+  int32_t jacobi_type; /* 0 diagonal, 1 rowmax, 2 rowl1, 3 rowsum */
+  int32_t use_abs;
+  int32_t fix_diag;
+  double rowl1_scale;
+  double omega;
+  double fshift;
+  int32_t sor_flag;    /* MatSORType bits, default 12|16 */
+  int32_t levels;      /* factor levels of fill */
+  int32_t ordering;    /* 0 natural, 1 rcm */
+  int32_t reserved;
+} gp_pc_options;
+
+void gp_pc_options_default(gp_pc_options *o);
+int gp_pc_create(gp_pc *out);
+int gp_pc_destroy(gp_pc pc);
+int gp_pc_set_options(gp_pc pc, const gp_pc_options *o);
+/* Set-up for the operator A: Jacobi diagonals, SOR diagonal, or the ILU/IC
+ * symbolic phase (host) followed by the numeric factorisation (device).
+ * Replaces PC.setUp (python/mojopetsc4py/PETSc/PC.py:315-492). */
+int gp_pc_setup(gp_pc pc, gp_mat A, void *stream);
+/* y = M^-1 x.  Replaces KSP_PCApply (src/ksp.mojo:155-198). */
+int gp_pc_apply(gp_pc pc, const double *x, double *y, void *stream);
+/* Jacobi's symmetric half (src/ksp.mojo:201-208); other types apply M^-1. */
+int gp_pc_apply_symmetric(gp_pc pc, const double *x, double *y, void *stream);
+/* Factor sizes and host copies in the reference's layout (ILU: bi, bj, ba,
+ * bdiag of n+1; IC: bi, bj, ba, bdiag of n+1).  Any output may be NULL. */
+int gp_pc_factor_info(gp_pc pc, int64_t *n, int64_t *nslots);
+int gp_pc_factor_get(gp_pc pc, int64_t *bi, int64_t *bj, double *ba, int64_t *bdiag,
+                     int64_t *perm);
+
+/* ------------------------------------------------------------ KSP */
+typedef struct gp_ksp_s *gp_ksp;
+
+/* Solver options; the fields of the reference's cfg/cfgi blocks
+ * (src/ksp.mojo:13-23, python/mojopetsc4py/PETSc/KSP.py:457-494). */
+typedef struct {
+  int32_t type;        /* 2 cg, 6 bcgs, 12 gmres, 40 fgmres */
+  int32_t normtype;    /* 1 none, 2 preconditioned, 3 unpreconditioned, 4 natural */
+  int32_t pc_side;     /* 0 left, 1 right, 2 symmetric */
+  int32_t guess_zero;
+  int32_t min_it;
+  int32_t chknorm;
+  int32_t convmaxits;
+  int32_t max_it;
+  int32_t restart;
+  int32_t orthog;      /* 0 classical Gram-Schmidt */
+  int32_t cgstype;     /* 0 never, 1 if needed, 2 always */
+  int32_t seed_rhs;    /* nonzero guess: rnorm0 from rhs_norm */
+  double rtol, atol, divtol, haptol, breakdowntol, rhs_norm;
+} gp_ksp_options;
+
+typedef struct {
+  int64_t its;
+  int64_t reason;   /* KSPConvergedReason ordinal */
+  double rnorm;
+} gp_ksp_result;
+
+void gp_ksp_options_default(gp_ksp_options *o);
+int gp_ksp_create(gp_ksp *out);
+int gp_ksp_destroy(gp_ksp ksp);
+int gp_ksp_set_options(gp_ksp ksp, const gp_ksp_options *o);
+/* Solve A x = b with preconditioner pc; b and x are device vectors.  The
+ * residual history (its+1 norms) goes to hist (host, may be NULL).
+ * Replaces mp_ksp_solve_{cg,bcgs,gmres,fgmres} (src/capi.mojo:383-424)
+ * behind KSP.solve (python/mojopetsc4py/PETSc/KSP.py:367-449). */
+int gp_ksp_solve(gp_ksp ksp, gp_mat A, gp_pc pc, const double *b, double *x,
+                 gp_ksp_result *result, double *hist, int64_t hist_len, void *stream);
+
+/* ------------------------------------------------------------ mp_* (reference host ABI) */
+/* Mat (src/capi.mojo:32-65) */
+void mp_mat_mult(const double *x, double *y, const int64_t *irow, const int64_t *icol,
+                 const double *data, int64_t nrow);
+void mp_mat_mult_add(const double *x, double *y, const int64_t *irow, const int64_t *icol,
+                     const double *data, int64_t nrow);
+void mp_mat_mult_transpose(const double *x, double *y, const int64_t *irow,
+                           const int64_t *icol, const double *data, int64_t nrow,
+                           int64_t ncols);
+void mp_mat_get_diagonal(double *diag, const int64_t *irow, const int64_t *icol,
+                         const double *data, int64_t nrow);
+void mp_mat_scale(double *data, int64_t nnz, double alpha);
+void mp_mat_zero_entries(double *data, int64_t nnz);
+/* Vec (src/capi.mojo:69-238) */
+void mp_vec_pointwise_mult(double *w, const double *x, const double *y, int64_t n);
+void mp_vec_pointwise_divide(double *w, const double *x, const double *y, int64_t n);
+void mp_vec_pointwise_min(double *w, const double *x, const double *y, int64_t n);
+void mp_vec_pointwise_max(double *w, const double *x, const double *y, int64_t n);
+void mp_vec_pointwise_max_abs(double *w, const double *x, const double *y, int64_t n);
+void mp_vec_norm(const double *x, int64_t ntype, double *z, int64_t n);
+void mp_vec_dot(const double *x, const double *y, double *val, int64_t n);
+void mp_vec_tdot(const double *x, const double *y, double *val, int64_t n);
+void mp_vec_dot_norm2(const double *x, const double *y, double *sval, double *rval, int64_t n);
+void mp_vec_sum(const double *x, double *val, int64_t n);
+void mp_vec_mean(const double *x, double *val, int64_t n);
+void mp_vec_max(const double *x, int64_t *idx, double *z, int64_t n);
+void mp_vec_min(const double *x, int64_t *idx, double *z, int64_t n);
+void mp_vec_normalize(double *x, double *v, int64_t n);
+void mp_vec_reciprocal(double *x, int64_t n);
+void mp_vec_exp(double *x, int64_t n);
+void mp_vec_log(double *x, int64_t n);
+void mp_vec_sqrtabs(double *x, int64_t n);
+void mp_vec_chop(double *x, int64_t n, double tol);
+void mp_vec_abs(double *x, int64_t n);
+void mp_vec_conjugate(double *x, int64_t n);
+void mp_vec_copy(const double *x, double *y, int64_t n);
+void mp_vec_swap(double *x, double *y, int64_t n);
+void mp_vec_set(double *x, double alpha, int64_t n);
+void mp_vec_zero_entries(double *x, int64_t n);
+void mp_vec_scale(double *x, double alpha, int64_t n);
+void mp_vec_shift(double *x, double alpha, int64_t n);
+void mp_vec_axpy(double *y, double alpha, const double *x, int64_t n);
+void mp_vec_aypx(double *y, double alpha, const double *x, int64_t n);
+void mp_vec_axpby(double *y, double alpha, double beta, const double *x, int64_t n);
+void mp_vec_axpbypcz(double *z, double alpha, double beta, double gamma, const double *x,
+                     const double *y, int64_t n);
+void mp_vec_waxpy(double *w, double alpha, const double *x, const double *y, int64_t n);
+void mp_vec_maxpy(double *y, int64_t nv, const double *alpha, const int64_t *x, int64_t n);
+void mp_vec_max_pointwise_divide(const double *x, const double *y, double *rval, int64_t n);
+/* PC and factorisation (src/capi.mojo:242-379) */
+int64_t mp_mat_get_diagonal_markers(const int64_t *irow, const int64_t *icol, int64_t *diag,
+                                    int64_t nrow);
+void mp_pc_jacobi_setup(double *diag, int64_t jtype, int64_t useabs, int64_t fixdiag,
+                        double scale, const int64_t *irow, const int64_t *icol,
+                        const double *data, int64_t nrow, double *didx);
+void mp_pc_jacobi_setup_symmetric(double *diagsqrt, int64_t jtype, const int64_t *irow,
+                                  const int64_t *icol, const double *data, int64_t nrow);
+void mp_pc_jacobi_apply(double *y, const double *x, const double *diag, int64_t n);
+void mp_pc_sor_apply(const double *x, double *y, const int64_t *irow, const int64_t *icol,
+                     const double *data, const int64_t *dmark, double *idiag, double *mdiag,
+                     double *t, double omega, double fshift, int64_t flag, int64_t nrow);
+void mp_pc_ilu_apply(const double *b, double *x, double *tmp, const int64_t *bi,
+                     const int64_t *bj, const double *ba, const int64_t *bdiag,
+                     const int64_t *r, const int64_t *c, int64_t nrow);
+int64_t mp_pc_icc_apply(const double *b, double *x, const int64_t *ui, const int64_t *uj,
+                        const double *ua, const int64_t *udiag, const int64_t *c,
+                        double *scratch, int64_t nrow);
+int64_t mp_pc_ilu_numeric(double *ba, double *rtmp, const int64_t *irow, const int64_t *icol,
+                          const double *data, const int64_t *bi, const int64_t *bj,
+                          const int64_t *bdiag, const int64_t *r, const int64_t *ic,
+                          int64_t nrow);
+void mp_pc_icc_numeric(double *ua, double *rtmp, int64_t *il, int64_t *c2r,
+                       const int64_t *irow, const int64_t *icol, const double *data,
+                       const int64_t *ui, const int64_t *uj, const int64_t *udiag,
+                       const int64_t *r, const int64_t *riip, int64_t nrow);
+int64_t mp_ilu_symbolic_ilu0(int64_t *bi, int64_t *bj, int64_t *bdiag, const int64_t *adiag,
+                             const int64_t *irow, const int64_t *icol, int64_t nrow);
+int64_t mp_ilu_symbolic(int64_t *bi, int64_t *bj, int64_t *bjlvl, int64_t *bdiag,
+                        const int64_t *irow, const int64_t *icol, const int64_t *r,
+                        const int64_t *ic, int64_t levels, int64_t cap, int64_t *scratch,
+                        int64_t nrow);
+void mp_ilu_contiguous_lu(const int64_t *bjsrc, int64_t *bi, int64_t *bdiag, int64_t *bj,
+                          int64_t n);
+int64_t mp_icc_symbolic(int64_t *ui, int64_t *uj, int64_t *ujlvl, int64_t *udiag,
+                        const int64_t *irow, const int64_t *icol, const int64_t *r,
+                        const int64_t *riip, int64_t levels, int64_t cap, int64_t *scratch,
+                        int64_t nrow, int64_t scratchlen);
+void mp_icc_contiguous_cholesky(const int64_t *ujsrc, const int64_t *ui, const int64_t *udiag,
+                                int64_t *bi, int64_t *bdiag, int64_t *bj, int64_t n);
+void mp_ordering_rcm(int64_t *perm, int64_t *level, int64_t *visited, int64_t *queue,
+                     const int64_t *irow, const int64_t *icol, int64_t nrow);
+/* KSP (src/capi.mojo:383-424); cfg/cfgi/pci/pcf as in src/ksp.mojo:13-23 */
+void mp_ksp_solve_cg(int64_t n, const int64_t *irow, const int64_t *icol, const double *data,
+                     const int64_t *pci, const double *pcf, double *pstmp, double *work,
+                     double *cfg, int64_t *cfgi, const double *b, double *x);
+void mp_ksp_solve_bcgs(int64_t n, const int64_t *irow, const int64_t *icol, const double *data,
+                       const int64_t *pci, const double *pcf, double *pstmp, double *work,
+                       double *cfg, int64_t *cfgi, const double *b, double *x);
+void mp_ksp_solve_gmres(int64_t n, const int64_t *irow, const int64_t *icol, const double *data,
+                        const int64_t *pci, const double *pcf, double *pstmp, double *work,
+                        double *vv, double *hs, double *cfg, int64_t *cfgi, const double *b,
+                        double *x);
+void mp_ksp_solve_fgmres(int64_t n, const int64_t *irow, const int64_t *icol,
+                         const double *data, const int64_t *pci, const double *pcf,
+                         double *pstmp, double *work, double *vv, double *prevec, double *hs,
+                         double *cfg, int64_t *cfgi, const double *b, double *x);
+/* Status of the last mp_* call on this thread (the reference's mp_* entries
+ * return nothing; this reports a CUDA or argument failure instead of hiding
+ * it). */
+int mp_last_status(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPETSC_H */

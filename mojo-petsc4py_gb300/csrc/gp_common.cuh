@@ -1,0 +1,211 @@
+// Shared device/host infrastructure for the GB300 Krylov library.
+//
+// Conventions used across every translation unit:
+//   * Row/column indices are int32 on the device; values are float64 (the
+//     mixed-precision form adds float32 copies).  Sizes cross the C ABI as
+//     int64 and are checked to fit int32.
+//   * Every floating-point step that mirrors a reference loop is written with
+//     explicit round-to-nearest intrinsics (__dmul_rn, __dadd_rn, ...), so no
+//     multiply-add is contracted into an FMA and each element is computed by
+//     the same sequence of rounded operations as the sequential CPU code.
+//   * Reductions are deterministic: a fixed grid, a fixed per-thread stride,
+//     a fixed shuffle/shared-memory tree, and a last-block-done final pass
+//     over the per-block partials in index order.
+//   * Every spin-wait carries an iteration budget; when it runs out the
+//     kernel records an error code in device memory and moves on.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+
+namespace gp {
+
+// ------------------------------------------------------------------ errors
+enum Status : int {
+  GP_OK = 0,
+  GP_ERR_ARG = 1,        // bad argument (size, null, type)
+  GP_ERR_CUDA = 2,       // a CUDA runtime call failed
+  GP_ERR_TIMEOUT = 3,    // a device spin-wait ran out of budget
+  GP_ERR_NOT_SETUP = 4,  // object used before set-up
+  GP_ERR_UNSUPPORTED = 5,
+  GP_ERR_NUMERIC = 6,    // zero pivot etc. reported by a set-up kernel
+  GP_ERR_INTERNAL = 7,
+};
+
+void set_error(const std::string& msg);
+const char* last_error();
+
+#define GP_CUDA(call)                                                           \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess) {                                                    \
+      ::gp::set_error(std::string(#call) + ": " + cudaGetErrorString(e_) +      \
+                      " (" __FILE__ ":" + std::to_string(__LINE__) + ")");      \
+      return ::gp::GP_ERR_CUDA;                                                 \
+    }                                                                           \
+  } while (0)
+
+#define GP_CHECK_LAUNCH()                                                       \
+  do {                                                                          \
+    cudaError_t e_ = cudaGetLastError();                                        \
+    if (e_ != cudaSuccess) {                                                    \
+      ::gp::set_error(std::string("kernel launch: ") + cudaGetErrorString(e_) + \
+                      " (" __FILE__ ":" + std::to_string(__LINE__) + ")");      \
+      return ::gp::GP_ERR_CUDA;                                                 \
+    }                                                                           \
+  } while (0)
+
+#define GP_TRY(expr)                       \
+  do {                                     \
+    int s_ = (expr);                       \
+    if (s_ != ::gp::GP_OK) return s_;      \
+  } while (0)
+
+// ------------------------------------------------------------------ device
+constexpr int kBlock = 256;        // default block for streaming kernels
+constexpr int kRedBlock = 256;     // block for reductions
+constexpr int kMaxRedGrid = 2048;  // partials buffer size per reduction slot
+
+int num_sms();  // cached SM count of the current device
+int red_grid(int64_t n);  // deterministic reduction grid for length n
+
+// Device error word written by kernels (spin timeouts, numeric failures).
+struct DevErr {
+  int code;
+  int where;
+};
+
+// Bit pattern a "not yet computed" entry holds in the value-as-flag arrays of
+// the sync-free triangular sweeps: a signalling NaN with a fixed payload.
+// Arithmetic never produces a signalling NaN (results are quiet), so a stored
+// result can never equal it.
+constexpr unsigned long long kPending = 0x7FF4DEAD0BADF00DULL;
+
+__device__ __forceinline__ double ld_relaxed(const double* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return __longlong_as_double((long long)v);
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed_bits(const double* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_relaxed(double* p, double v) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(__double_as_longlong(v))
+               : "memory");
+}
+
+__device__ __forceinline__ int ld_acquire_i32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_i32(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// exact-rounded arithmetic helpers (no contraction)
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double div_(double a, double b) { return __ddiv_rn(a, b); }
+
+// ------------------------------------------------------------------ reduction
+// Deterministic block reduction of NR doubles (result valid in thread 0).
+template <int NR>
+__device__ __forceinline__ void block_sum(double (&v)[NR]) {
+  __shared__ double sh[NR][kRedBlock / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int r = 0; r < NR; r++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[r] = add(v[r], __shfl_down_sync(0xffffffffu, v[r], o));
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int r = 0; r < NR; r++) sh[r][wid] = v[r];
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      double t = lane < nw ? sh[r][lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t = add(t, __shfl_down_sync(0xffffffffu, t, o));
+      v[r] = t;
+    }
+  }
+  __syncthreads();
+}
+
+// Scratch for one deterministic multi-block reduction: per-block partials and
+// the last-block-done ticket.
+struct RedSlot {
+  double* partials;    // [stride * NRmax]
+  unsigned* ticket;    // one counter, returns to zero after every use
+  int stride;          // >= gridDim.x of every kernel that uses the slot
+};
+
+// Every block writes its NR partial sums; the last block to arrive sums the
+// partials in index order and returns true in all of its threads with the
+// totals in `out` (valid in thread 0).  The ticket is reset for the next use.
+template <int NR>
+__device__ __forceinline__ bool grid_finish(double (&v)[NR], RedSlot slot, double (&out)[NR]) {
+  __shared__ bool last;
+  block_sum<NR>(v);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int r = 0; r < NR; r++) slot.partials[r * slot.stride + blockIdx.x] = v[r];
+    __threadfence();
+    unsigned t = atomicAdd(slot.ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double acc[NR];
+#pragma unroll
+  for (int r = 0; r < NR; r++) acc[r] = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+#pragma unroll
+    for (int r = 0; r < NR; r++)
+      acc[r] = add(acc[r], ld_relaxed(&slot.partials[r * slot.stride + b]));
+  }
+  block_sum<NR>(acc);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int r = 0; r < NR; r++) out[r] = acc[r];
+    *slot.ticket = 0u;
+  }
+  return true;
+}
+
+// A vector operand that is either a fixed device pointer or a device-resident
+// pointer slot read at kernel start (solver loops keep "basis vector `it`" in
+// such a slot, so one captured kernel serves every step).
+struct DRef {
+  double* p;
+  double* const* ind;
+  static DRef of(double* q) { return DRef{q, nullptr}; }
+  static DRef of(const double* q) { return DRef{const_cast<double*>(q), nullptr}; }
+  static DRef at(double* const* q) { return DRef{nullptr, q}; }
+  __device__ __forceinline__ double* get() const {
+    return ind ? *(double* const volatile*)ind : p;
+  }
+};
+
+// Gate: kernels of a captured solver loop run only while the solver's state
+// word equals the value they were captured for.
+__device__ __forceinline__ bool gated_off(const int* gate, int want) {
+  return gate != nullptr && *(volatile const int*)gate != want;
+}
+
+}  // namespace gp

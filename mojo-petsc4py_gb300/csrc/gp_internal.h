@@ -1,0 +1,93 @@
+// Internal host API shared by the translation units of libgpetsc.so.  Not part
+// of the public C ABI (that is include/gpetsc.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "gp_common.cuh"
+
+namespace gp {
+
+// Reduction scratch owned by the library for one stream user (standalone Vec
+// and Mat calls).  Solvers carry their own.
+struct Scratch {
+  RedSlot slot{};
+  double* d_out = nullptr;   // device result words
+  double* h_out = nullptr;   // pinned host mirror
+  long long* d_idx = nullptr;
+  long long* h_idx = nullptr;
+  int device = -1;
+  int stride = 0;
+};
+int scratch_get(Scratch** out, int64_t n_needed_grid);
+
+// ------------------------------------------------------------- Vec kernels
+enum MapOp : int {
+  OP_COPY, OP_SET, OP_SCALE, OP_SHIFT, OP_AXPY, OP_AYPX, OP_AXPBY, OP_AXPBYPCZ,
+  OP_WAXPY, OP_PMULT, OP_PDIV, OP_PMIN, OP_PMAX, OP_PMAXABS, OP_RECIP, OP_EXP,
+  OP_LOG, OP_SQRTABS, OP_ABS, OP_CHOP, OP_SWAP, OP_ZERO, OP_SCALESET, OP_DIVS
+};
+// Elementwise op over n entries.  Scalars alpha/beta/gamma are host values.
+// Operand roles follow the reference kernels: see gp_vec.cu for each op.
+int vec_map(cudaStream_t s, int op, int64_t n, double* y, const double* x,
+            const double* w, double alpha, double beta, double gamma);
+int vec_maxpy(cudaStream_t s, int64_t n, double* y, int nv, const double* alpha_host,
+              const double* const* xs_host);
+
+enum RedOp : int { RED_DOT, RED_NORM2SQ, RED_ASUM, RED_SUM, RED_DOTNORM2, RED_NORMINF };
+// Reductions return their result(s) to host memory (synchronous).
+int vec_reduce(cudaStream_t s, int op, int64_t n, const double* x, const double* y,
+               double* out_host);
+int vec_minmax(cudaStream_t s, int64_t n, const double* x, int is_max, long long* idx,
+               double* val);
+int vec_max_pointwise_divide(cudaStream_t s, int64_t n, const double* x, const double* y,
+                             double* out_host);
+
+// Device-scalar forms used inside solvers (gate-aware, result stays on device).
+struct DevReduceArgs {
+  const int* gate;
+  int want;
+  RedSlot slot;
+};
+
+// ------------------------------------------------------------- CSR matrix
+struct Csr {
+  int n = 0;        // rows
+  int ncols = 0;
+  int64_t nnz = 0;
+  int* rowptr = nullptr;     // device, n+1
+  int* colind = nullptr;     // device, nnz
+  double* val = nullptr;     // device, nnz
+  float* val32 = nullptr;    // device, nnz (mixed-precision copy, lazily made)
+  int* diagpos = nullptr;    // device, n: slot of a_ii or -1
+  // transpose (built on demand): rows of A^T in ascending original row order
+  int* t_rowptr = nullptr;
+  int* t_colind = nullptr;
+  int* t_src = nullptr;      // slot in A of each A^T entry
+  // host pattern copy for set-up analysis
+  std::vector<int> h_rowptr, h_colind;
+  bool owns = true;
+  int device = -1;
+};
+
+int csr_create(Csr** out, int64_t nrows, int64_t ncols, int64_t nnz, const int64_t* h_rowptr,
+               const int64_t* h_colind, const double* h_val, cudaStream_t s);
+int csr_create_i32(Csr** out, int64_t nrows, int64_t ncols, int64_t nnz,
+                   const int32_t* h_rowptr, const int32_t* h_colind, const double* h_val,
+                   cudaStream_t s);
+int csr_set_values(Csr* A, const double* val, int on_device, cudaStream_t s);
+int csr_destroy(Csr* A);
+int csr_build_transpose(Csr* A, cudaStream_t s);
+int csr_make_val32(Csr* A, cudaStream_t s);
+
+// y = A x (fp64); optional fused dot p.y into a device scalar with finisher
+int spmv(cudaStream_t s, const Csr* A, DRef x, DRef y, const int* gate = nullptr, int want = 0);
+int spmv_add(cudaStream_t s, const Csr* A, const double* x, const double* v, double* y);
+int spmv_t(cudaStream_t s, Csr* A, const double* x, double* y);
+int mat_diagonal(cudaStream_t s, const Csr* A, double* d);
+int spmv_grid(const Csr* A);
+
+}  // namespace gp

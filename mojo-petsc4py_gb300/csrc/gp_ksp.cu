@@ -1,0 +1,1377 @@
+// Device-resident Krylov drivers.
+//
+//   KSPConvergedDefault          src/ksp.mojo:96-152   -> conv_default()
+//   KSP_PCApply / BAorAB / ...   src/ksp.mojo:155-265  -> pc_apply / apply_ba()
+//   KSPSolve_CG                  src/ksp.mojo:271-389  -> solve_cg()
+//   KSPSolve_BCGS                src/ksp.mojo:395-505  -> solve_bcgs()
+//   KSPSolve_GMRES (+CGS, UpdateHessenberg, BuildSoln)  src/ksp.mojo:533-769
+//   KSPSolve_FGMRES              src/ksp.mojo:775-903
+//
+// Every scalar of the iteration (alpha, beta, the residual norm, the
+// Hessenberg matrix and its Givens rotations, the converged reason) lives in
+// device memory.  The vector work of one iteration is captured once into the
+// body of a CUDA-graph WHILE node; small single-thread "control" kernels carry
+// the reference's scalar logic and branch structure and set the gate words
+// that switch the following vector kernels on or off.  The whole solve is one
+// graph launch with no host round trip; the control kernel at the end of the
+// body sets the loop condition from the device state, with a hard cap on the
+// number of trips so the loop always ends.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gp_ksp.h"
+
+namespace gp {
+
+enum Reason : int {
+  R_RTOL = 2, R_ATOL = 3, R_ITS = 4, R_HAPPY = 7, R_NULL = -2, R_DIVITS = -3, R_DTOL = -4,
+  R_BREAKDOWN = -5, R_INDEF_PC = -8, R_NANORINF = -9, R_INDEF_MAT = -10
+};
+enum Norm : int { N_NONE = 1, N_PRECOND = 2, N_UNPRECOND = 3, N_NATURAL = 4 };
+enum Phase : int { PH_DONE = 0, PH_RESTART = 1, PH_STEP = 2, PH_BUILD = 3 };
+
+// KSPConvergedDefault, src/ksp.mojo:96-152.
+__device__ int conv_default(KspState* st, int n, double rnorm) {
+  if (st->convmaxits && n >= st->max_it) return R_ITS;
+  if (st->normtype == N_NONE) return 0;
+  if (!n && !st->seeded) {
+    double rnorm0 = rnorm;
+    if (st->seed_rhs) {
+      double snorm = st->rhs_norm;
+      if (!snorm) snorm = rnorm;
+      rnorm0 = snorm;
+    }
+    st->rnorm0 = rnorm0;
+    const double ttol = mul(st->rtol, rnorm0);
+    st->ttol = ttol > st->atol ? ttol : st->atol;
+    st->seeded = 1;
+  }
+  if (n <= st->chknorm) return 0;
+  if (rnorm != rnorm || fabs(rnorm) == INFINITY) return R_NANORINF;
+  if (n < st->min_it) return 0;
+  if (rnorm <= st->ttol) {
+    if (rnorm < st->atol) return R_ATOL;
+    return R_RTOL;
+  }
+  if (rnorm >= mul(st->divtol, st->rnorm0)) return R_DTOL;
+  return 0;
+}
+
+// ------------------------------------------------------------ vector kernels
+static int vgrid(int n) { return std::max(1, std::min((n + 255) / 256, num_sms() * 8)); }
+
+#define GRID_LOOP(i, n)                                                          \
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
+
+__global__ void k_copy_d(const int* gate, int want, int n, DRef xr, DRef yr) {
+  if (gated_off(gate, want)) return;
+  const double* x = xr.get();
+  double* y = yr.get();
+  GRID_LOOP(i, n) y[i] = x[i];
+}
+
+__global__ void k_zero_d(const int* gate, int want, int n, DRef yr) {
+  if (gated_off(gate, want)) return;
+  double* y = yr.get();
+  GRID_LOOP(i, n) y[i] = 0.0;
+}
+
+// y = y + (sgn * a) x      (VecAXPY with a device scalar)
+__global__ void k_axpy_d(const int* gate, int want, int n, DRef yr, const double* a, double sgn,
+                         DRef xr) {
+  if (gated_off(gate, want)) return;
+  double* y = yr.get();
+  const double* x = xr.get();
+  const double al = mul(sgn, *a);
+  GRID_LOOP(i, n) y[i] = add(y[i], mul(al, x[i]));
+}
+
+// y = x + alpha y (VecAYPX, general branch) with a host scalar
+__global__ void k_aypx_h(const int* gate, int want, int n, DRef yr, double alpha, DRef xr) {
+  if (gated_off(gate, want)) return;
+  double* y = yr.get();
+  const double* x = xr.get();
+  GRID_LOOP(i, n) y[i] = add(x[i], mul(alpha, y[i]));
+}
+
+// VecAYPX(y, *a, x) with the reference's branch structure decided on the
+// device: a == 0 copies, a == 1 adds, otherwise x + a y.
+__global__ void k_aypx_d(const int* gate, int want, int n, DRef yr, const double* a, DRef xr) {
+  if (gated_off(gate, want)) return;
+  double* y = yr.get();
+  const double* x = xr.get();
+  const double al = *a;
+  if (al == 0.0) {
+    GRID_LOOP(i, n) y[i] = x[i];
+  } else if (al == 1.0) {
+    GRID_LOOP(i, n) y[i] = add(y[i], mul(al, x[i]));
+  } else {
+    GRID_LOOP(i, n) y[i] = add(x[i], mul(al, y[i]));
+  }
+}
+
+// z = a x + b y + c z      (VecAXPBYPCZ with device scalars)
+__global__ void k_axpbypcz_d(const int* gate, int want, int n, DRef zr, const double* a,
+                             const double* b, const double* c, DRef xr, DRef yr) {
+  if (gated_off(gate, want)) return;
+  double* z = zr.get();
+  const double* x = xr.get();
+  const double* y = yr.get();
+  const double al = *a, be = *b, ga = *c;
+  GRID_LOOP(i, n) z[i] = add(add(mul(al, x[i]), mul(be, y[i])), mul(ga, z[i]));
+}
+
+// w = (sgn * a) x + y      (VecWAXPY)
+__global__ void k_waxpy_d(const int* gate, int want, int n, DRef wr, const double* a, double sgn,
+                          DRef xr, DRef yr) {
+  if (gated_off(gate, want)) return;
+  double* w = wr.get();
+  const double* x = xr.get();
+  const double* y = yr.get();
+  const double al = mul(sgn, *a);
+  GRID_LOOP(i, n) w[i] = add(mul(al, x[i]), y[i]);
+}
+
+// x = x * (*a)   (VecScale)  or  x = x / (*a) when *a > 0 (VecNormalize)
+template <bool DIVIDE>
+__global__ void k_scale_d(const int* gate, int want, int n, DRef xr, const double* a) {
+  if (gated_off(gate, want)) return;
+  double* x = xr.get();
+  const double al = *a;
+  if (DIVIDE) {
+    if (!(al > 0.0)) return;
+    GRID_LOOP(i, n) x[i] = div_(x[i], al);
+  } else {
+    GRID_LOOP(i, n) x[i] = mul(x[i], al);
+  }
+}
+
+// CG update: x = x + a p; r = r + (-a) w
+__global__ void k_cg_xr(const int* gate, int want, int n, double* __restrict__ x,
+                        double* __restrict__ r, const double* __restrict__ p,
+                        const double* __restrict__ w, const double* a) {
+  if (gated_off(gate, want)) return;
+  const double al = *a, nal = -al;
+  GRID_LOOP(i, n) {
+    x[i] = add(x[i], mul(al, p[i]));
+    r[i] = add(r[i], mul(nal, w[i]));
+  }
+}
+
+// ------------------------------------------------------------ reductions
+enum DRed : int { D_DOT, D_NRM, D_DOTNRM };
+
+// Deterministic reduction into device scalars: out_raw receives the sum,
+// out_sqrt receives sqrt(|sum|) (the 2-norm, or sqrt|beta| for the natural
+// norm).  D_DOTNRM writes (x.y, x.x) to out_raw[0], out_raw2.
+template <int OP>
+__global__ void __launch_bounds__(kRedBlock) k_dred(const int* gate, int want, int n, DRef xr,
+                                                    DRef yr, RedSlot slot, double* out_raw,
+                                                    double* out_sqrt, double* out_raw2) {
+  if (gated_off(gate, want)) return;
+  constexpr int NR = OP == D_DOTNRM ? 2 : 1;
+  const double* __restrict__ x = xr.get();
+  const double* __restrict__ y = OP == D_NRM ? x : yr.get();
+  double v[NR];
+#pragma unroll
+  for (int r = 0; r < NR; r++) v[r] = 0.0;
+  GRID_LOOP(i, n) {
+    const double a = x[i];
+    if (OP == D_DOTNRM) {
+      v[0] = add(v[0], mul(a, y[i]));
+      v[NR - 1] = add(v[NR - 1], mul(a, a));
+    } else {
+      v[0] = add(v[0], mul(a, y[i]));
+    }
+  }
+  double tot[NR];
+  if (grid_finish<NR>(v, slot, tot) && threadIdx.x == 0) {
+    if (out_raw) *out_raw = tot[0];
+    if (out_sqrt) *out_sqrt = __dsqrt_rn(fabs(tot[0]));
+    if (OP == D_DOTNRM && out_raw2) *out_raw2 = tot[NR - 1];
+  }
+}
+
+// VecMDot of x against `*count` contiguous basis vectors (ld = n): one pass
+// over x and the basis, per-block partial sums for every vector, last block
+// folds the partials.  Used by classical Gram-Schmidt.
+constexpr int kMaxBasis = 64;
+__global__ void __launch_bounds__(kRedBlock) k_mdot(const int* gate, int want, int n, DRef xr,
+                                                    const double* __restrict__ basis,
+                                                    const int* count, RedSlot slot,
+                                                    double* __restrict__ out) {
+  if (gated_off(gate, want)) return;
+  const double* __restrict__ x = xr.get();
+  const int k = *count;
+  __shared__ double sh[kRedBlock / 32][kMaxBasis];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < k; j0 += 8) {
+    double v[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) v[q] = 0.0;
+    const int jn = min(8, k - j0);
+    GRID_LOOP(i, n) {
+      const double a = x[i];
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if (q < jn) v[q] = add(v[q], mul(a, basis[(size_t)(j0 + q) * n + i]));
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[q] = add(v[q], __shfl_down_sync(0xffffffffu, v[q], o));
+      if (lane == 0 && q < jn) sh[wid][j0 + q] = v[q];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < k) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = add(t, sh[w][threadIdx.x]);
+    slot.partials[(size_t)threadIdx.x * slot.stride + blockIdx.x] = t;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(slot.ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x < k) {
+    double t = 0.0;
+    for (int b = 0; b < (int)gridDim.x; b++)
+      t = add(t, ld_relaxed(&slot.partials[(size_t)threadIdx.x * slot.stride + b]));
+    out[threadIdx.x] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *slot.ticket = 0u;
+}
+
+// y = (from_zero ? 0 : y) + sum_{j < *count} coef_j basis_j, ascending j per
+// element (simdvec.maxpy, VecMAXPBY with beta = 0).
+__global__ void k_maxpy_dyn(const int* gate, int want, int n, DRef yr,
+                            const double* __restrict__ basis, const double* __restrict__ coef,
+                            const int* count, int from_zero) {
+  if (gated_off(gate, want)) return;
+  double* __restrict__ y = yr.get();
+  const int k = *count;
+  GRID_LOOP(i, n) {
+    double v = from_zero ? 0.0 : y[i];
+    for (int j = 0; j < k; j++) v = add(v, mul(coef[j], basis[(size_t)j * n + i]));
+    y[i] = v;
+  }
+}
+
+// ------------------------------------------------------------ loop control
+constexpr int G_ON = 5;  // g[G_ON] == 1 while the driver runs
+
+__device__ __forceinline__ void finish(KspState* st, double rnorm, int its, int reason) {
+  st->rnorm = rnorm;
+  st->its = its;
+  st->reason = reason;
+}
+
+// Record the result and switch every gate of the loop body off.
+__device__ __forceinline__ void stop(KspState* st, double rnorm, int its, int reason) {
+  finish(st, rnorm, its, reason);
+  st->active = 0;
+  st->phase = PH_DONE;
+#pragma unroll
+  for (int k = 0; k < 16; k++) st->g[k] = 0;
+}
+
+// End of the loop body: keep looping while the driver is active and under the
+// trip cap (every driver needs at most one trip per iteration, plus restarts).
+__global__ void k_loop_ctrl(cudaGraphConditionalHandle h, KspState* st) {
+  st->trips += 1;
+  const bool run = st->active == 1;
+  const int cap = st->max_it * 2 + 64;
+  if (run && st->trips >= cap) stop(st, st->rnorm, st->its, st->reason ? st->reason : R_DIVITS);
+  cudaGraphSetConditional(h, (run && st->trips < cap) ? 1u : 0u);
+}
+
+// ================================================================== CG
+// gates: g[0] PC + ||z|| after the update, g[3] ||r||, g[4] natural norm,
+//        g[1] PC after the test, g[2] recompute beta, g[5] on
+__global__ void k_cg_init(KspState* st, double* hist) {
+  const double dp = st->dp;
+  hist[0] = dp;
+  const int reason = conv_default(st, 0, dp);
+  st->i = 0;
+  st->dpi = 0.0;
+  st->betaold = 1.0;
+  if (reason) {
+    stop(st, dp, 0, reason);
+    return;
+  }
+  st->active = 1;
+  const int nt = st->normtype;
+  st->g[G_ON] = 1;
+  st->g[1] = (nt != N_PRECOND && nt != N_NATURAL) ? 1 : 0;
+  st->g[2] = (nt != N_NATURAL) ? 1 : 0;
+  st->g[0] = st->g[3] = st->g[4] = 0;
+}
+
+// top of iteration i: breakdown tests, the beta/betaold ratio, dpiold
+__global__ void k_cg_a(KspState* st) {
+  if (st->active != 1) return;
+  const int i = st->i;
+  st->its = i + 1;
+  const double beta = st->beta;
+  if (beta == 0.0) {
+    stop(st, st->dp, i + 1, R_ATOL);
+    return;
+  }
+  if (i > 0 && mul(beta, st->betaold) < 0.0) {
+    stop(st, st->dp, i + 1, R_INDEF_PC);
+    return;
+  }
+  st->bcoef = i == 0 ? 0.0 : div_(beta, st->betaold);
+  st->dpiold = st->dpi;
+}
+
+__device__ __forceinline__ int sgn(double x) { return x < 0.0 ? -1 : (x == 0.0 ? 0 : 1); }
+
+// after dpi = p.Ap: indefinite-matrix test and a = beta / dpi
+__global__ void k_cg_b(KspState* st) {
+  if (st->active != 1) return;
+  const int i = st->i;
+  const double dpi = st->dpi;
+  st->betaold = st->beta;
+  if (dpi == 0.0 || (i > 0 && sgn(dpi) * sgn(st->dpiold) < 0)) {
+    stop(st, st->dp, i + 1, R_INDEF_MAT);
+    return;
+  }
+  st->a = div_(st->beta, dpi);
+  const int nt = st->normtype;
+  const bool now = st->chknorm < i + 2;
+  st->g[0] = (nt == N_PRECOND && now) ? 1 : 0;
+  st->g[3] = (nt == N_UNPRECOND && now) ? 1 : 0;
+  st->g[4] = (nt == N_NATURAL) ? 1 : 0;
+  if (!(st->g[0] || st->g[3] || st->g[4])) st->dp = 0.0;
+}
+
+// residual norm recorded, convergence test, gates for the tail of the body
+__global__ void k_cg_c(KspState* st, double* hist) {
+  if (st->active != 1) return;
+  const int i = st->i, its = i + 1;
+  const double dp = st->dp;
+  hist[its] = dp;
+  const int reason = conv_default(st, its, dp);
+  if (reason) {
+    stop(st, dp, its, reason);
+    return;
+  }
+  const int nt = st->normtype;
+  st->g[1] = ((nt != N_PRECOND && nt != N_NATURAL) || st->chknorm >= i + 2) ? 1 : 0;
+  st->g[2] = (nt != N_NATURAL || st->chknorm >= i + 2) ? 1 : 0;
+}
+
+__global__ void k_cg_d(KspState* st) {
+  if (st->active != 1) return;
+  st->i += 1;
+  if (st->i >= st->max_it) stop(st, st->dp, st->its, R_DIVITS);
+}
+
+// ================================================================== BCGS
+// gates: g[5] on, g[6] "d2 == 0" branch, g[7] regular update, g[0] ||r||
+__global__ void k_bcgs_init(KspState* st, double* hist) {
+  const double dp = st->dp;
+  hist[0] = dp;
+  const int reason = conv_default(st, 0, dp);
+  st->i = 0;
+  st->its = 0;
+  st->rhoold = st->alpha = st->omegaold = st->omega = st->rho = 1.0;
+  st->c_one = 1.0;
+  if (reason) {
+    stop(st, dp, 0, reason);
+    return;
+  }
+  st->active = 1;
+  st->g[G_ON] = 1;
+}
+
+__global__ void k_bcgs_a(KspState* st) {
+  if (st->active != 1) return;
+  st->bbeta = mul(div_(st->rho, st->rhoold), div_(st->alpha, st->omegaold));
+  st->c_omb = mul(-st->omegaold, st->bbeta);
+}
+
+__global__ void k_bcgs_b(KspState* st) {
+  if (st->active != 1) return;
+  if (st->d1 == 0.0) {
+    stop(st, st->dp, st->its, R_BREAKDOWN);
+    return;
+  }
+  st->alpha = div_(st->rho, st->d1);
+}
+
+__global__ void k_bcgs_c(KspState* st) {
+  if (st->active != 1) return;
+  if (st->d2 == 0.0) {
+    st->g[6] = 1;
+    st->g[7] = 0;
+    st->g[0] = 0;
+    return;
+  }
+  st->g[6] = 0;
+  st->g[7] = 1;
+  st->omega = div_(st->d1, st->d2);
+  st->g[0] = (st->normtype != N_NONE && st->chknorm < st->i + 2) ? 1 : 0;
+}
+
+// d2 == 0: S.S decides between a breakdown and convergence
+__global__ void k_bcgs_c2(KspState* st) {
+  if (st->active != 1 || !st->g[6]) return;
+  if (st->d1 != 0.0) stop(st, st->dp, st->its, R_BREAKDOWN);
+}
+
+__global__ void k_bcgs_c3(KspState* st) {
+  if (st->active != 1 || !st->g[6]) return;
+  stop(st, 0.0, st->its + 1, R_RTOL);
+}
+
+__global__ void k_bcgs_d(KspState* st, double* hist) {
+  if (st->active != 1) return;
+  st->rhoold = st->rho;
+  st->omegaold = st->omega;
+  st->its += 1;
+  const int its = st->its;
+  hist[its] = st->dp;
+  const int reason = conv_default(st, its, st->dp);
+  if (reason) {
+    stop(st, st->dp, its, reason);
+    return;
+  }
+  if (st->rho == 0.0) {
+    stop(st, st->dp, its, R_BREAKDOWN);
+    return;
+  }
+  st->i += 1;
+  if (st->i >= st->max_it) stop(st, st->dp, its, R_DIVITS);
+}
+
+// ================================================================== GMRES
+// hs block (src/ksp.mojo:32-39, 919-935), HH(a,b) = hh[b (m+2) + a]
+struct Hs {
+  double *hh, *hes, *cc, *ss, *rs;
+  __device__ Hs(double* hs, int m) {
+    hh = hs;
+    hes = hh + (m + 2) * (m + 1);
+    cc = hes + (m + 1) * (m + 1);
+    ss = cc + (m + 1);
+    rs = ss + (m + 1);
+  }
+};
+
+// gates: g[0] restart phase, g[1] Arnoldi step, g[2] build, g[3] residual from
+// A x, g[4] residual = b, g[5] on, g[6] solution update in build, g[7] CGS
+// refinement, g[8] FGMRES build update, g[9] FGMRES residual, g[10] FGMRES
+// scale v_{it+1}, g[11] FGMRES scale v_0, g[12] FGMRES zero TEMP.  Every gate
+// is set or cleared by a control kernel that precedes its kernels in the body.
+__device__ void gm_set_phase(KspState* st, int ph) {
+  st->phase = ph;
+  st->g[0] = ph == PH_RESTART;
+  st->g[1] = ph == PH_STEP;
+  st->g[2] = ph == PH_BUILD;
+}
+
+// KSPGMRESUpdateHessenberg, src/ksp.mojo:589-629
+__device__ int gm_update_hessenberg(Hs& H, int it, int m, int hapend, double* res) {
+  double* hh = H.hh;
+  for (int j = 1; j <= it; j++) {
+    const int idx = it * (m + 2) + (j - 1);
+    const double tt = hh[idx];
+    const double h1 = hh[idx + 1];
+    hh[idx] = add(mul(H.cc[j - 1], tt), mul(H.ss[j - 1], h1));
+    hh[idx + 1] = sub(mul(H.cc[j - 1], h1), mul(H.ss[j - 1], tt));
+  }
+  if (!hapend) {
+    const int base = it * (m + 2) + it;
+    const double a = hh[base], b = hh[base + 1];
+    const double tt = __dsqrt_rn(add(mul(a, a), mul(b, b)));
+    if (tt == 0.0) {
+      *res = 0.0;
+      return R_NULL;
+    }
+    H.cc[it] = div_(a, tt);
+    H.ss[it] = div_(b, tt);
+    H.rs[it + 1] = mul(-H.ss[it], H.rs[it]);
+    H.rs[it] = mul(H.cc[it], H.rs[it]);
+    hh[base] = add(mul(H.cc[it], a), mul(H.ss[it], b));
+    *res = fabs(H.rs[it + 1]);
+    return 0;
+  }
+  *res = 0.0;
+  return 0;
+}
+
+__global__ void k_gm_init(KspState* st) {
+  st->its = 0;
+  st->itcount = 0;
+  st->reason = 0;
+  st->res = 0.0;
+  st->prev_rnorm = -1.0;
+  st->c_one = 1.0;
+  st->active = 1;
+#pragma unroll
+  for (int k = 0; k < 16; k++) st->g[k] = 0;
+  st->g[G_ON] = 1;
+}
+
+__global__ void k_gm_restart_prep(KspState* st) {
+  // residual source for this cycle (KSPInitialResidual's guess_zero branch)
+  if (!st->g[0]) return;
+  st->g[3] = st->guess_zero ? 0 : 1;
+  st->g[4] = st->guess_zero ? 1 : 0;
+}
+
+__global__ void k_gm_restart_ctrl(KspState* st, double* hs, double* hist, double* vv, int n) {
+  if (!st->g[0]) return;
+  Hs H(hs, st->m);
+  const double res = st->res;
+  if (st->prev_rnorm > 0.0 && fabs(sub(res, st->prev_rnorm)) > mul(st->breakdowntol, st->cfg8)) {
+    stop(st, res, st->its, R_BREAKDOWN);
+    return;
+  }
+  H.rs[0] = res;
+  st->cfg8 = res;
+  hist[st->its] = res;
+  st->reason = !res ? R_ATOL : conv_default(st, st->its, res);
+  st->it = 0;
+  st->hapend = 0;
+  st->g[3] = st->g[4] = 0;
+  if (st->reason == 0 && st->it < st->m && st->its < st->max_it) {
+    st->vv_it = vv;
+    st->vv_it1 = vv + n;
+    gm_set_phase(st, PH_STEP);
+  } else {
+    gm_set_phase(st, PH_BUILD);
+  }
+}
+
+// classical Gram-Schmidt bookkeeping around the MDot / MAXPY pair
+// (src/ksp.mojo:533-586).  pass 0: zero the column and set the count.
+__global__ void k_gm_cgs0(KspState* st, double* hs) {
+  if (!st->g[1]) return;
+  Hs H(hs, st->m);
+  const int it = st->it, m = st->m;
+  for (int j = 0; j <= it; j++) {
+    H.hh[it * (m + 2) + j] = 0.0;
+    H.hes[it * (m + 1) + j] = 0.0;
+  }
+  st->kcount = it + 1;
+  st->g[7] = st->cgstype == 2 ? 1 : 0;
+}
+
+// negate the projections and fold them into the Hessenberg column
+__global__ void k_gm_cgs1(KspState* st, double* hs, double* lhh, int gate_idx) {
+  if (!st->g[gate_idx]) return;
+  Hs H(hs, st->m);
+  const int it = st->it, m = st->m;
+  double hnrm = 0.0;
+  for (int j = 0; j <= it; j++) {
+    lhh[j] = -lhh[j];
+    H.hh[it * (m + 2) + j] = sub(H.hh[it * (m + 2) + j], lhh[j]);
+    H.hes[it * (m + 1) + j] = sub(H.hes[it * (m + 1) + j], lhh[j]);
+    hnrm = add(hnrm, mul(lhh[j], lhh[j]));
+  }
+  if (gate_idx == 1) st->red[1] = __dsqrt_rn(hnrm);
+}
+
+// REFINE_IFNEEDED: refine when ||v_{it+1}|| < ||h||
+__global__ void k_gm_cgs_ifneeded(KspState* st) {
+  if (!st->g[1]) return;
+  if (st->red[0] < st->red[1]) st->g[7] = 1;
+}
+
+__global__ void k_gm_step_ctrl(KspState* st, double* hs, double* hist, double* vv, int n) {
+  if (!st->g[1]) return;
+  Hs H(hs, st->m);
+  const int m = st->m;
+  int it = st->it;
+  const double tt = st->tt;
+  H.hh[it * (m + 2) + it + 1] = tt;
+  H.hes[it * (m + 1) + it + 1] = tt;
+  double hapbnd = fabs(div_(tt, H.rs[it]));
+  hapbnd = hapbnd > st->haptol ? st->haptol : hapbnd;
+  const int hapend = tt < hapbnd ? 1 : 0;
+  st->hapend = hapend;
+  double res;
+  int reason = gm_update_hessenberg(H, it, m, hapend, &res);
+  st->res = res;
+  it += 1;
+  st->it = it;
+  st->its += 1;
+  hist[st->its] = res;
+  if (!reason) {
+    reason = conv_default(st, st->its, res);
+    if (hapend) {
+      if (st->normtype == N_NONE)
+        reason = R_HAPPY;
+      else if (reason == 0)
+        reason = R_BREAKDOWN;
+    }
+  }
+  st->reason = reason;
+  st->g[7] = 0;
+  if (reason == 0 && it < m && st->its < st->max_it) {
+    st->vv_it = vv + (size_t)it * n;
+    st->vv_it1 = vv + (size_t)(it + 1) * n;
+  } else {
+    gm_set_phase(st, PH_BUILD);
+  }
+}
+
+// KSPGMRESBuildSoln's back substitution (src/ksp.mojo:632-664); the vector
+// part follows as gated kernels.
+__global__ void k_gm_backsub(KspState* st, double* hs) {
+  if (!st->g[2]) return;
+  Hs H(hs, st->m);
+  const int m = st->m, it = st->it - 1;
+  st->itb = it;
+  st->g[6] = 0;
+  int breason = 0;
+  if (it >= 0) {
+    double* hh = H.hh;
+    double* rs = H.rs;
+    if (hh[it * (m + 2) + it] != 0.0) {
+      rs[it] = div_(rs[it], hh[it * (m + 2) + it]);
+      for (int ii = 1; ii <= it && !breason; ii++) {
+        const int k = it - ii;
+        double tt = rs[k];
+        for (int j = k + 1; j <= it; j++) tt = sub(tt, mul(hh[j * (m + 2) + k], rs[j]));
+        if (hh[k * (m + 2) + k] == 0.0) {
+          breason = R_BREAKDOWN;
+          break;
+        }
+        rs[k] = div_(tt, hh[k * (m + 2) + k]);
+      }
+    } else {
+      breason = R_BREAKDOWN;
+    }
+    if (!breason) {
+      st->g[6] = 1;
+      st->kcount = it + 1;
+    }
+  }
+  st->red[2] = breason;
+}
+
+__global__ void k_gm_build_ctrl(KspState* st) {
+  if (!st->g[2]) return;
+  st->g[6] = 0;
+  st->itcount += st->it;
+  const int breason = (int)st->red[2];
+  if (st->reason == 0 && breason != 0) st->reason = breason;
+  if (st->itcount >= st->max_it) {
+    stop(st, st->res, st->its, st->reason ? st->reason : R_DIVITS);
+    return;
+  }
+  if (st->reason != 0) {
+    stop(st, st->res, st->its, st->reason);
+    return;
+  }
+  st->prev_rnorm = st->res;
+  st->guess_zero = 0;
+  gm_set_phase(st, PH_RESTART);
+}
+
+// ================================================================== FGMRES
+__global__ void k_fg_start_ctrl(KspState* st, double* hs, double* hist, double* vv,
+                                double* prevec, int n) {
+  if (!st->g[0]) return;
+  Hs H(hs, st->m);
+  const double res = st->res;
+  st->it = 0;
+  st->hapend = 0;
+  H.rs[0] = res;
+  hist[st->its] = res;
+  st->reason = conv_default(st, st->its, res);
+  st->g[9] = 0;
+  st->g[11] = 0;
+  if (st->reason == 0) {
+    st->inv = div_(1.0, res);
+    st->g[11] = 1;  // scale v_0 by 1/res
+    st->vv_scale = vv;
+  }
+  if (st->reason == 0 && st->it < st->m && st->its < st->max_it) {
+    st->vv_it = vv;
+    st->vv_it1 = vv + n;
+    st->pv_it = prevec;
+    gm_set_phase(st, PH_STEP);
+  } else {
+    gm_set_phase(st, PH_BUILD);
+  }
+}
+
+__global__ void k_fg_step_ctrl(KspState* st, double* hs, double* hist, double* vv,
+                               double* prevec, int n) {
+  st->g[10] = 0;
+  st->g[11] = 0;
+  st->g[12] = 0;
+  if (!st->g[1]) return;
+  Hs H(hs, st->m);
+  const int m = st->m;
+  int it = st->it;
+  const double tt = st->tt;
+  H.hh[it * (m + 2) + it + 1] = tt;
+  H.hes[it * (m + 1) + it + 1] = tt;
+  double hapbnd = fabs(div_(tt, H.rs[it]));
+  hapbnd = hapbnd > st->haptol ? st->haptol : hapbnd;
+  int hapend = 0;
+  if (tt > hapbnd) {
+    st->inv = div_(1.0, tt);
+    st->vv_scale = st->vv_it1;
+    st->g[10] = 1;  // v_{it+1} *= 1/tt
+  } else {
+    st->g[12] = 1;  // TEMP = 0
+    hapend = 1;
+  }
+  st->hapend = hapend;
+  double res;
+  int reason = gm_update_hessenberg(H, it, m, hapend, &res);
+  st->res = res;
+  st->g[7] = 0;
+  if (reason) {
+    st->reason = reason;
+    gm_set_phase(st, PH_BUILD);
+    return;
+  }
+  it += 1;
+  st->it = it;
+  st->its += 1;
+  hist[st->its] = res;
+  reason = conv_default(st, st->its, res);
+  if (hapend && reason == 0) reason = R_BREAKDOWN;
+  st->reason = reason;
+  if (reason == 0 && it < m && st->its < st->max_it) {
+    st->vv_it = vv + (size_t)it * n;
+    st->vv_it1 = vv + (size_t)(it + 1) * n;
+    st->pv_it = prevec + (size_t)it * n;
+  } else {
+    gm_set_phase(st, PH_BUILD);
+  }
+}
+
+// KSPFGMRESBuildSoln's back substitution (src/ksp.mojo:880-903)
+__global__ void k_fg_backsub(KspState* st, double* hs) {
+  if (!st->g[2]) return;
+  Hs H(hs, st->m);
+  const int m = st->m, it = st->it - 1;
+  st->g[8] = 0;
+  if (it < 0) return;
+  double* hh = H.hh;
+  double* rs = H.rs;
+  if (hh[it * (m + 2) + it] != 0.0)
+    rs[it] = div_(rs[it], hh[it * (m + 2) + it]);
+  else
+    rs[it] = 0.0;
+  for (int ii = 1; ii <= it; ii++) {
+    const int k = it - ii;
+    double tt = rs[k];
+    for (int j = k + 1; j <= it; j++) tt = sub(tt, mul(hh[j * (m + 2) + k], rs[j]));
+    rs[k] = div_(tt, hh[k * (m + 2) + k]);
+  }
+  st->kcount = it + 1;
+  st->g[8] = 1;
+}
+
+__global__ void k_fg_build_ctrl(KspState* st) {
+  if (!st->g[2]) return;
+  st->g[8] = 0;
+  st->g[11] = 0;
+  if (st->its >= st->max_it) {
+    stop(st, st->res, st->its, st->reason ? st->reason : R_DIVITS);
+    return;
+  }
+  if (st->reason != 0) {
+    stop(st, st->res, st->its, st->reason);
+    return;
+  }
+  st->g[9] = 1;  // residual, then a new cycle
+  gm_set_phase(st, PH_RESTART);
+}
+
+// ================================================================== host side
+
+int ksp_create(Ksp** out) {
+  *out = new Ksp();
+  return GP_OK;
+}
+
+static void drop_graph(Ksp* k) {
+  if (k->exec) cudaGraphExecDestroy(k->exec);
+  if (k->graph) cudaGraphDestroy(k->graph);
+  k->exec = nullptr;
+  k->graph = nullptr;
+  k->cap_A = k->cap_pc = nullptr;
+}
+
+int ksp_destroy(Ksp* k) {
+  if (!k) return GP_OK;
+  drop_graph(k);
+  void* ptrs[] = {k->work, k->vv, k->prevec, k->hs, k->lhh, k->hist, k->st, k->slot.partials,
+                  k->slot.ticket};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (k->h_st) cudaFreeHost(k->h_st);
+  if (k->stream) cudaStreamDestroy(k->stream);
+  delete k;
+  return GP_OK;
+}
+
+static int grow(double** p, size_t* have, size_t need) {
+  if (*have >= need && *p) return GP_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  GP_CUDA(cudaMalloc(p, std::max<size_t>(need, 1) * sizeof(double)));
+  *have = need;
+  return 1000;  // signals "reallocated" to the caller
+}
+
+// Allocate (or keep) the workspace for this solve.  Returns whether any buffer
+// moved, which invalidates a captured graph.
+static int ensure(Ksp* k, int n, bool* moved) {
+  const KspOptions& o = k->opt;
+  const int m = o.restart;
+  *moved = false;
+  if (!k->stream) GP_CUDA(cudaStreamCreateWithFlags(&k->stream, cudaStreamNonBlocking));
+  if (!k->st) {
+    GP_CUDA(cudaMalloc(&k->st, sizeof(KspState)));
+    GP_CUDA(cudaMallocHost(&k->h_st, sizeof(KspState)));
+    GP_CUDA(cudaMalloc(&k->slot.partials, (size_t)kMaxBasis * kMaxRedGrid * sizeof(double)));
+    GP_CUDA(cudaMalloc(&k->slot.ticket, sizeof(unsigned)));
+    GP_CUDA(cudaMemset(k->slot.ticket, 0, sizeof(unsigned)));
+    k->slot.stride = kMaxRedGrid;
+    *moved = true;
+  }
+  const bool gm = o.type == KSP_GMRES || o.type == KSP_FGMRES;
+  int r;
+  r = grow(&k->work, &k->work_n, (size_t)(gm ? 2 : 7) * n);
+  if (r != GP_OK && r != 1000) return r;
+  *moved |= r == 1000;
+  if (gm) {
+    r = grow(&k->vv, &k->vv_n, (size_t)(m + 1) * n);
+    if (r != GP_OK && r != 1000) return r;
+    *moved |= r == 1000;
+    const size_t hs = (size_t)(m + 2) * (m + 1) + (size_t)(m + 1) * (m + 1) + 2 * (m + 1) +
+                      2 * (m + 2);
+    r = grow(&k->hs, &k->hs_n, hs);
+    if (r != GP_OK && r != 1000) return r;
+    *moved |= r == 1000;
+    size_t lhn = k->lhh ? (size_t)kMaxBasis : 0;
+    r = grow(&k->lhh, &lhn, kMaxBasis);
+    if (r != GP_OK && r != 1000) return r;
+    *moved |= r == 1000;
+    if (o.type == KSP_FGMRES) {
+      r = grow(&k->prevec, &k->pv_n, (size_t)(m + 2) * n);
+      if (r != GP_OK && r != 1000) return r;
+      *moved |= r == 1000;
+    }
+  }
+  size_t hc = (size_t)k->hist_cap;
+  r = grow(&k->hist, &hc, (size_t)o.max_it + 2);
+  if (r != GP_OK && r != 1000) return r;
+  *moved |= r == 1000;
+  k->hist_cap = (int)hc;
+  return GP_OK;
+}
+
+namespace {
+
+// launch helpers bound to one solve
+struct Run {
+  Ksp* k;
+  Csr* A;
+  Pc* pc;
+  int n;
+  cudaStream_t s;
+  const int* G(int idx) const { return &k->st->g[idx]; }
+  double* S(double KspState::*f) const { return &(k->st->*f); }
+  int grid() const { return vgrid(n); }
+
+  int copy(const int* g, DRef x, DRef y) const {
+    k_copy_d<<<grid(), 256, 0, s>>>(g, 1, n, x, y);
+    GP_CHECK_LAUNCH();
+    return GP_OK;
+  }
+  int zero(const int* g, DRef y) const {
+    k_zero_d<<<grid(), 256, 0, s>>>(g, 1, n, y);
+    GP_CHECK_LAUNCH();
+    return GP_OK;
+  }
+  template <int OP>
+  int red(const int* g, DRef x, DRef y, double* raw, double* sq, double* raw2 = nullptr) const {
+    k_dred<OP><<<red_grid(n), kRedBlock, 0, s>>>(g, 1, n, x, y, k->slot, raw, sq, raw2);
+    GP_CHECK_LAUNCH();
+    return GP_OK;
+  }
+  int matmult(const int* g, DRef x, DRef y) const { return spmv(s, A, x, y, g, 1); }
+  int pcapply(const int* g, DRef x, DRef y) const { return pc_apply(pc, x, y, s, g, 1); }
+  int pcsym(const int* g, DRef x, DRef y) const { return pc_apply_symmetric(pc, x, y, s, g, 1); }
+  // KSP_PCApplyBAorAB, src/ksp.mojo:246-265
+  int apply_ba(const int* g, int side, DRef x, DRef y, DRef w) const {
+    if (side == 1) {
+      GP_TRY(pcapply(g, x, w));
+      return matmult(g, w, y);
+    }
+    if (side == 0) {
+      GP_TRY(matmult(g, x, w));
+      return pcapply(g, w, y);
+    }
+    GP_TRY(pcsym(g, x, w));
+    GP_TRY(matmult(g, w, y));
+    GP_TRY(copy(g, y, w));
+    return pcsym(g, w, y);
+  }
+  // KSPInitialResidual, src/ksp.mojo:221-243
+  int initial_residual(int side, int guess_zero, DRef x, DRef vt1, DRef vt2, DRef vres,
+                       DRef b) const {
+    if (!guess_zero) {
+      GP_TRY(matmult(nullptr, x, vt1));
+      GP_TRY(copy(nullptr, b, vt2));
+      k_axpy_d<<<grid(), 256, 0, s>>>(nullptr, 1, n, vt2, S(&KspState::c_one), -1.0, vt1);
+      GP_CHECK_LAUNCH();
+    } else {
+      GP_TRY(copy(nullptr, b, vt2));
+    }
+    if (side == 2) return pcsym(nullptr, vt2, vres);
+    if (side == 0) return pcapply(nullptr, vt2, vres);
+    return copy(nullptr, vt2, vres);
+  }
+};
+
+}  // namespace
+
+// ------------------------------------------------------------------ CG
+static int cg_prologue(const Run& r, const double* b, double* x) {
+  Ksp* k = r.k;
+  const KspOptions& o = k->opt;
+  const int n = r.n;
+  DRef R = DRef::of(k->work), Z = DRef::of(k->work + n);
+  if (!o.guess_zero) {
+    GP_TRY(r.matmult(nullptr, DRef::of(x), R));
+    k_aypx_h<<<r.grid(), 256, 0, r.s>>>(nullptr, 1, n, R, -1.0, DRef::of(b));
+    GP_CHECK_LAUNCH();
+  } else {
+    GP_TRY(r.copy(nullptr, DRef::of(b), R));
+  }
+  double* dp = r.S(&KspState::dp);
+  double* beta = r.S(&KspState::beta);
+  if (o.normtype == N_PRECOND) {
+    GP_TRY(r.pcapply(nullptr, R, Z));
+    GP_TRY(r.red<D_NRM>(nullptr, Z, Z, nullptr, dp));
+  } else if (o.normtype == N_UNPRECOND) {
+    GP_TRY(r.red<D_NRM>(nullptr, R, R, nullptr, dp));
+  } else if (o.normtype == N_NATURAL) {
+    GP_TRY(r.pcapply(nullptr, R, Z));
+    GP_TRY(r.red<D_DOT>(nullptr, Z, R, beta, dp));
+  }
+  k_cg_init<<<1, 1, 0, r.s>>>(k->st, k->hist);
+  GP_CHECK_LAUNCH();
+  GP_TRY(r.pcapply(r.G(1), R, Z));
+  GP_TRY(r.red<D_DOT>(r.G(2), Z, R, beta, nullptr));
+  return GP_OK;
+}
+
+static int cg_body(const Run& r, double* x) {
+  Ksp* k = r.k;
+  const int n = r.n;
+  double* R = k->work;
+  double* Z = k->work + n;
+  double* P = k->work + 2 * n;
+  double* W = Z;  // the reference's W = Z aliasing
+  KspState* st = k->st;
+  const int* on = r.G(G_ON);
+  k_cg_a<<<1, 1, 0, r.s>>>(st);
+  k_aypx_d<<<r.grid(), 256, 0, r.s>>>(on, 1, n, DRef::of(P), r.S(&KspState::bcoef), DRef::of(Z));
+  GP_CHECK_LAUNCH();
+  GP_TRY(r.matmult(on, DRef::of(P), DRef::of(W)));
+  GP_TRY(r.red<D_DOT>(on, DRef::of(P), DRef::of(W), r.S(&KspState::dpi), nullptr));
+  k_cg_b<<<1, 1, 0, r.s>>>(st);
+  k_cg_xr<<<r.grid(), 256, 0, r.s>>>(on, 1, n, x, R, P, W, r.S(&KspState::a));
+  GP_CHECK_LAUNCH();
+  const int nt = k->opt.normtype;
+  double* dp = r.S(&KspState::dp);
+  double* beta = r.S(&KspState::beta);
+  if (nt == N_PRECOND) {
+    GP_TRY(r.pcapply(r.G(0), DRef::of(R), DRef::of(Z)));
+    GP_TRY(r.red<D_NRM>(r.G(0), DRef::of(Z), DRef::of(Z), nullptr, dp));
+  } else if (nt == N_UNPRECOND) {
+    GP_TRY(r.red<D_NRM>(r.G(3), DRef::of(R), DRef::of(R), nullptr, dp));
+  } else if (nt == N_NATURAL) {
+    GP_TRY(r.pcapply(r.G(4), DRef::of(R), DRef::of(Z)));
+    GP_TRY(r.red<D_DOT>(r.G(4), DRef::of(Z), DRef::of(R), beta, dp));
+  }
+  k_cg_c<<<1, 1, 0, r.s>>>(st, k->hist);
+  GP_TRY(r.pcapply(r.G(1), DRef::of(R), DRef::of(Z)));
+  GP_TRY(r.red<D_DOT>(r.G(2), DRef::of(Z), DRef::of(R), beta, nullptr));
+  k_cg_d<<<1, 1, 0, r.s>>>(st);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+// ------------------------------------------------------------------ BCGS
+static int bcgs_prologue(const Run& r, const double* b, double* x) {
+  Ksp* k = r.k;
+  const KspOptions& o = k->opt;
+  const int n = r.n;
+  double* w = k->work;
+  DRef R = DRef::of(w), RP = DRef::of(w + n), V = DRef::of(w + 2 * n), T = DRef::of(w + 3 * n);
+  DRef P = DRef::of(w + 5 * n), GUESS = DRef::of(w + 6 * n);
+  GP_TRY(r.initial_residual(o.pc_side, o.guess_zero, DRef::of(x), V, T, R, DRef::of(b)));
+  if (o.pc_side == 1 && !o.guess_zero) {
+    GP_TRY(r.copy(nullptr, DRef::of(x), GUESS));
+    GP_TRY(r.zero(nullptr, DRef::of(x)));
+  }
+  if (o.normtype != N_NONE)
+    GP_TRY(r.red<D_NRM>(nullptr, R, R, nullptr, r.S(&KspState::dp)));
+  k_bcgs_init<<<1, 1, 0, r.s>>>(k->st, k->hist);
+  GP_CHECK_LAUNCH();
+  const int* on = r.G(G_ON);
+  GP_TRY(r.copy(on, R, RP));
+  GP_TRY(r.zero(on, P));
+  GP_TRY(r.zero(on, V));
+  return GP_OK;
+}
+
+static int bcgs_body(const Run& r, double* x) {
+  Ksp* k = r.k;
+  const int n = r.n, side = k->opt.pc_side;
+  double* w = k->work;
+  DRef R = DRef::of(w), RP = DRef::of(w + n), V = DRef::of(w + 2 * n), T = DRef::of(w + 3 * n);
+  DRef S = DRef::of(w + 4 * n), P = DRef::of(w + 5 * n), X = DRef::of(x);
+  KspState* st = k->st;
+  const int* on = r.G(G_ON);
+  GP_TRY(r.red<D_DOT>(on, R, RP, r.S(&KspState::rho), nullptr));
+  k_bcgs_a<<<1, 1, 0, r.s>>>(st);
+  k_axpbypcz_d<<<r.grid(), 256, 0, r.s>>>(on, 1, n, P, r.S(&KspState::c_one),
+                                           r.S(&KspState::c_omb), r.S(&KspState::bbeta), R, V);
+  GP_CHECK_LAUNCH();
+  GP_TRY(r.apply_ba(on, side, P, V, T));
+  GP_TRY(r.red<D_DOT>(on, V, RP, r.S(&KspState::d1), nullptr));
+  k_bcgs_b<<<1, 1, 0, r.s>>>(st);
+  k_waxpy_d<<<r.grid(), 256, 0, r.s>>>(on, 1, n, S, r.S(&KspState::alpha), -1.0, V, R);
+  GP_CHECK_LAUNCH();
+  GP_TRY(r.apply_ba(on, side, S, T, R));
+  // VecDotNorm2(S, T): (S.T, T.T) -- computed as (T.S, T.T), the same sums
+  GP_TRY(r.red<D_DOTNRM>(on, T, S, r.S(&KspState::d1), nullptr, r.S(&KspState::d2)));
+  k_bcgs_c<<<1, 1, 0, r.s>>>(st);
+  GP_TRY(r.red<D_DOT>(r.G(6), S, S, r.S(&KspState::d1), nullptr));
+  k_bcgs_c2<<<1, 1, 0, r.s>>>(st);
+  k_axpy_d<<<r.grid(), 256, 0, r.s>>>(r.G(6), 1, n, X, r.S(&KspState::alpha), 1.0, P);
+  k_bcgs_c3<<<1, 1, 0, r.s>>>(st);
+  k_axpbypcz_d<<<r.grid(), 256, 0, r.s>>>(r.G(7), 1, n, X, r.S(&KspState::alpha),
+                                           r.S(&KspState::omega), r.S(&KspState::c_one), P, S);
+  k_waxpy_d<<<r.grid(), 256, 0, r.s>>>(r.G(7), 1, n, R, r.S(&KspState::omega), -1.0, T, S);
+  GP_CHECK_LAUNCH();
+  GP_TRY(r.red<D_NRM>(r.G(0), R, R, nullptr, r.S(&KspState::dp)));
+  k_bcgs_d<<<1, 1, 0, r.s>>>(st, k->hist);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+static int bcgs_epilogue(const Run& r, double* x) {
+  Ksp* k = r.k;
+  const KspOptions& o = k->opt;
+  const int n = r.n;
+  double* w = k->work;
+  DRef T = DRef::of(w + 3 * n), GUESS = DRef::of(w + 6 * n), X = DRef::of(x);
+  // KSPUnwindPreconditioner (src/ksp.mojo:211-218)
+  if (o.pc_side == 1) {
+    GP_TRY(r.pcapply(nullptr, X, T));
+    GP_TRY(r.copy(nullptr, T, X));
+  }
+  if (o.pc_side == 1 && !o.guess_zero) {
+    k_axpy_d<<<r.grid(), 256, 0, r.s>>>(nullptr, 1, n, X, r.S(&KspState::c_one), 1.0, GUESS);
+    GP_CHECK_LAUNCH();
+  }
+  return GP_OK;
+}
+
+// ------------------------------------------------------------------ GMRES
+// classical Gram-Schmidt on v_{it+1} against v_0..v_it, with the optional
+// refinement pass (src/ksp.mojo:533-586)
+static int cgs_pass(const Run& r, int gate_idx) {
+  Ksp* k = r.k;
+  const int* g = r.G(gate_idx);
+  DRef v1 = DRef::at(&k->st->vv_it1);
+  k_mdot<<<red_grid(r.n), kRedBlock, 0, r.s>>>(g, 1, r.n, v1, k->vv, &k->st->kcount, k->slot,
+                                              k->lhh);
+  k_gm_cgs1<<<1, 1, 0, r.s>>>(k->st, k->hs, k->lhh, gate_idx);
+  k_maxpy_dyn<<<r.grid(), 256, 0, r.s>>>(g, 1, r.n, v1, k->vv, k->lhh, &k->st->kcount, 0);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+static int cgs(const Run& r) {
+  Ksp* k = r.k;
+  k_gm_cgs0<<<1, 1, 0, r.s>>>(k->st, k->hs);
+  GP_TRY(cgs_pass(r, 1));
+  if (k->opt.cgstype == 1) {
+    GP_TRY(r.red<D_NRM>(r.G(1), DRef::at(&k->st->vv_it1), DRef::at(&k->st->vv_it1), nullptr,
+                        &k->st->red[0]));
+    k_gm_cgs_ifneeded<<<1, 1, 0, r.s>>>(k->st);
+  }
+  if (k->opt.cgstype != 0) GP_TRY(cgs_pass(r, 7));
+  return GP_OK;
+}
+
+// the first cycle starts with a restart (no solution to build yet)
+__global__ void k_first_restart(KspState* st) { gm_set_phase(st, PH_RESTART); }
+
+static int gmres_prologue(const Run& r) {
+  k_gm_init<<<1, 1, 0, r.s>>>(r.k->st);
+  k_first_restart<<<1, 1, 0, r.s>>>(r.k->st);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+static int gmres_body(const Run& r, const double* b, double* x) {
+  Ksp* k = r.k;
+  const int n = r.n, side = k->opt.pc_side;
+  KspState* st = k->st;
+  DRef TEMP = DRef::of(k->work), TMATOP = DRef::of(k->work + n), VV0 = DRef::of(k->vv);
+  DRef X = DRef::of(x), B = DRef::of(b);
+  // ---- build the solution at the end of a cycle (KSPGMRESBuildSoln)
+  k_gm_backsub<<<1, 1, 0, r.s>>>(st, k->hs);
+  const int m = k->opt.restart;
+  double* rs = k->hs + (size_t)(m + 2) * (m + 1) + (size_t)(m + 1) * (m + 1) + 2 * (m + 1);
+  k_maxpy_dyn<<<r.grid(), 256, 0, r.s>>>(r.G(6), 1, n, TEMP, k->vv, rs, &st->kcount, 1);
+  GP_CHECK_LAUNCH();
+  if (side == 1) {  // KSPUnwindPreconditioner for right preconditioning
+    GP_TRY(r.pcapply(r.G(6), TEMP, TMATOP));
+    GP_TRY(r.copy(r.G(6), TMATOP, TEMP));
+  }
+  k_axpy_d<<<r.grid(), 256, 0, r.s>>>(r.G(6), 1, n, X, r.S(&KspState::c_one), 1.0, TEMP);
+  k_gm_build_ctrl<<<1, 1, 0, r.s>>>(st);
+  // ---- restart: r0 = M^-1 (b - A x) (or b), normalised
+  k_gm_restart_prep<<<1, 1, 0, r.s>>>(st);
+  GP_TRY(r.matmult(r.G(3), X, TEMP));
+  GP_TRY(r.copy(r.G(3), B, TMATOP));
+  k_axpy_d<<<r.grid(), 256, 0, r.s>>>(r.G(3), 1, n, TMATOP, r.S(&KspState::c_one), -1.0, TEMP);
+  GP_CHECK_LAUNCH();
+  GP_TRY(r.copy(r.G(4), B, TMATOP));
+  if (side == 2)
+    GP_TRY(r.pcsym(r.G(0), TMATOP, VV0));
+  else if (side == 0)
+    GP_TRY(r.pcapply(r.G(0), TMATOP, VV0));
+  else
+    GP_TRY(r.copy(r.G(0), TMATOP, VV0));
+  GP_TRY(r.red<D_NRM>(r.G(0), VV0, VV0, nullptr, r.S(&KspState::res)));
+  k_scale_d<true><<<r.grid(), 256, 0, r.s>>>(r.G(0), 1, n, VV0, r.S(&KspState::res));
+  k_gm_restart_ctrl<<<1, 1, 0, r.s>>>(st, k->hs, k->hist, k->vv, n);
+  GP_CHECK_LAUNCH();
+  // ---- one Arnoldi step
+  DRef vit = DRef::at(&st->vv_it), vit1 = DRef::at(&st->vv_it1);
+  GP_TRY(r.apply_ba(r.G(1), side, vit, vit1, TMATOP));
+  GP_TRY(cgs(r));
+  GP_TRY(r.red<D_NRM>(r.G(1), vit1, vit1, nullptr, r.S(&KspState::tt)));
+  k_scale_d<true><<<r.grid(), 256, 0, r.s>>>(r.G(1), 1, n, vit1, r.S(&KspState::tt));
+  k_gm_step_ctrl<<<1, 1, 0, r.s>>>(st, k->hs, k->hist, k->vv, n);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+// ------------------------------------------------------------------ FGMRES
+static int fgmres_prologue(const Run& r, const double* b, double* x) {
+  Ksp* k = r.k;
+  const int n = r.n;
+  k_gm_init<<<1, 1, 0, r.s>>>(k->st);
+  GP_CHECK_LAUNCH();
+  DRef TEMP = DRef::of(k->work), VV0 = DRef::of(k->vv);
+  if (!k->opt.guess_zero) {  // KSPFGMRESResidual, src/ksp.mojo:871-877
+    GP_TRY(r.matmult(nullptr, DRef::of(x), TEMP));
+    k_waxpy_d<<<r.grid(), 256, 0, r.s>>>(nullptr, 1, n, VV0, r.S(&KspState::c_one), -1.0, TEMP,
+                                         DRef::of(b));
+    GP_CHECK_LAUNCH();
+  } else {
+    GP_TRY(r.copy(nullptr, DRef::of(b), VV0));
+  }
+  k_first_restart<<<1, 1, 0, r.s>>>(k->st);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+
+static int fgmres_body(const Run& r, const double* b, double* x) {
+  Ksp* k = r.k;
+  const int n = r.n, m = k->opt.restart;
+  KspState* st = k->st;
+  DRef TEMP = DRef::of(k->work), VV0 = DRef::of(k->vv), X = DRef::of(x), B = DRef::of(b);
+  double* rs = k->hs + (size_t)(m + 2) * (m + 1) + (size_t)(m + 1) * (m + 1) + 2 * (m + 1);
+  // ---- build (KSPFGMRESBuildSoln) and the next residual
+  k_fg_backsub<<<1, 1, 0, r.s>>>(st, k->hs);
+  k_maxpy_dyn<<<r.grid(), 256, 0, r.s>>>(r.G(8), 1, n, TEMP, k->prevec, rs, &st->kcount, 1);
+  k_axpy_d<<<r.grid(), 256, 0, r.s>>>(r.G(8), 1, n, X, r.S(&KspState::c_one), 1.0, TEMP);
+  k_fg_build_ctrl<<<1, 1, 0, r.s>>>(st);
+  GP_CHECK_LAUNCH();
+  GP_TRY(r.matmult(r.G(9), X, TEMP));
+  k_waxpy_d<<<r.grid(), 256, 0, r.s>>>(r.G(9), 1, n, VV0, r.S(&KspState::c_one), -1.0, TEMP, B);
+  // ---- cycle start: ||r||, convergence test, v_0 = r / ||r|| (by reciprocal)
+  GP_TRY(r.red<D_NRM>(r.G(0), VV0, VV0, nullptr, r.S(&KspState::res)));
+  k_fg_start_ctrl<<<1, 1, 0, r.s>>>(st, k->hs, k->hist, k->vv, k->prevec, n);
+  k_scale_d<false><<<r.grid(), 256, 0, r.s>>>(r.G(11), 1, n, VV0, r.S(&KspState::inv));
+  GP_CHECK_LAUNCH();
+  // ---- one flexible Arnoldi step
+  DRef vit = DRef::at(&st->vv_it), vit1 = DRef::at(&st->vv_it1), pit = DRef::at(&st->pv_it);
+  GP_TRY(r.pcapply(r.G(1), vit, pit));
+  GP_TRY(r.matmult(r.G(1), pit, vit1));
+  GP_TRY(cgs(r));
+  GP_TRY(r.red<D_NRM>(r.G(1), vit1, vit1, nullptr, r.S(&KspState::tt)));
+  k_fg_step_ctrl<<<1, 1, 0, r.s>>>(st, k->hs, k->hist, k->vv, k->prevec, n);
+  k_scale_d<false><<<r.grid(), 256, 0, r.s>>>(r.G(10), 1, n, DRef::at(&st->vv_scale),
+                                              r.S(&KspState::inv));
+  GP_TRY(r.zero(r.G(12), TEMP));
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+// ------------------------------------------------------------------ solve
+
+static int capture(const Run& r, const double* b, double* x) {
+  Ksp* k = r.k;
+  drop_graph(k);
+  GP_CUDA(cudaGraphCreate(&k->graph, 0));
+  cudaGraphConditionalHandle h;
+  GP_CUDA(cudaGraphConditionalHandleCreate(&h, k->graph, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  GP_CUDA(cudaGraphAddNode(&node, k->graph, nullptr, nullptr, 0, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  GP_CUDA(cudaStreamBeginCaptureToGraph(r.s, body, nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeRelaxed));
+  int st = GP_OK;
+  switch (k->opt.type) {
+    case KSP_CG: st = cg_body(r, x); break;
+    case KSP_BCGS: st = bcgs_body(r, x); break;
+    case KSP_GMRES: st = gmres_body(r, b, x); break;
+    case KSP_FGMRES: st = fgmres_body(r, b, x); break;
+  }
+  if (st == GP_OK) {
+    k_loop_ctrl<<<1, 1, 0, r.s>>>(h, k->st);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error(std::string("loop control launch: ") + cudaGetErrorString(e));
+      st = GP_ERR_CUDA;
+    }
+  }
+  cudaGraph_t out = nullptr;
+  cudaError_t ec = cudaStreamEndCapture(r.s, &out);
+  if (st != GP_OK) {
+    drop_graph(k);
+    return st;
+  }
+  if (ec != cudaSuccess) {
+    set_error(std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ec));
+    drop_graph(k);
+    return GP_ERR_CUDA;
+  }
+  GP_CUDA(cudaGraphInstantiate(&k->exec, k->graph, 0));
+  return GP_OK;
+}
+
+int ksp_solve(Ksp* k, Csr* A, Pc* pc, const double* b, double* x, KspResult* res,
+              double* hist_out, int64_t hist_len, cudaStream_t caller) {
+  KspOptions& o = k->opt;
+  if (A->n != A->ncols) {
+    set_error("the solver matrix must be square");
+    return GP_ERR_ARG;
+  }
+  if (!pc->ready || pc->n != A->n) {
+    set_error("the preconditioner is not set up for an operator of this size");
+    return GP_ERR_NOT_SETUP;
+  }
+  if (o.type != KSP_CG && o.type != KSP_BCGS && o.type != KSP_GMRES && o.type != KSP_FGMRES) {
+    set_error("unsupported KSP type");
+    return GP_ERR_UNSUPPORTED;
+  }
+  const bool gm = o.type == KSP_GMRES || o.type == KSP_FGMRES;
+  if (gm && (o.restart < 1 || o.restart + 1 > kMaxBasis)) {
+    set_error("GMRES restart must be between 1 and " + std::to_string(kMaxBasis - 1));
+    return GP_ERR_UNSUPPORTED;
+  }
+  if (gm && o.orthog != 0) {
+    set_error("modified Gram-Schmidt is not available on the device path");
+    return GP_ERR_UNSUPPORTED;
+  }
+  if (o.max_it < 0) o.max_it = 0;
+  const int n = A->n;
+  k->n = n;
+  bool moved = false;
+  GP_TRY(ensure(k, n, &moved));
+  cudaStream_t s = k->stream;
+  cudaEvent_t ev;
+  GP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  GP_CUDA(cudaEventRecord(ev, caller));
+  GP_CUDA(cudaStreamWaitEvent(s, ev, 0));
+  // configuration into the device state
+  KspState& h = *k->h_st;
+  std::memset(&h, 0, sizeof(KspState));
+  h.rtol = o.rtol;
+  h.atol = o.atol;
+  h.divtol = o.divtol;
+  h.haptol = o.haptol;
+  h.breakdowntol = o.breakdowntol;
+  h.rhs_norm = o.rhs_norm;
+  h.normtype = o.normtype;
+  h.pc_side = o.pc_side;
+  h.guess_zero = o.guess_zero;
+  h.min_it = o.min_it;
+  h.chknorm = o.chknorm;
+  h.convmaxits = o.convmaxits;
+  h.max_it = o.max_it;
+  h.m = o.restart;
+  h.seed_rhs = o.seed_rhs;
+  h.cgstype = o.cgstype;
+  h.c_one = 1.0;
+  h.prev_rnorm = -1.0;
+  GP_CUDA(cudaMemcpyAsync(k->st, &h, sizeof(KspState), cudaMemcpyHostToDevice, s));
+  GP_CUDA(cudaMemsetAsync(k->hist, 0, (size_t)k->hist_cap * sizeof(double), s));
+  Run r{k, A, pc, n, s};
+  // prologue (direct launches)
+  switch (o.type) {
+    case KSP_CG: GP_TRY(cg_prologue(r, b, x)); break;
+    case KSP_BCGS: GP_TRY(bcgs_prologue(r, b, x)); break;
+    case KSP_GMRES: GP_TRY(gmres_prologue(r)); break;
+    case KSP_FGMRES: GP_TRY(fgmres_prologue(r, b, x)); break;
+  }
+  // the loop graph depends on the buffers and the body-shaping options
+  const int key[8] = {o.type, o.normtype, o.pc_side, o.restart, o.cgstype, n, pc->opt.type,
+                      pc->opt.sor_flag};
+  const bool same = !moved && k->exec && k->cap_A == A && k->cap_pc == pc &&
+                    std::equal(key, key + 8, k->cap_key) && k->cap_b == b && k->cap_x == x;
+  if (!same) {
+    GP_TRY(capture(r, b, x));
+    k->cap_A = A;
+    k->cap_pc = pc;
+    k->cap_b = b;
+    k->cap_x = x;
+    std::copy(key, key + 8, k->cap_key);
+  }
+  GP_CUDA(cudaGraphLaunch(k->exec, s));
+  if (o.type == KSP_BCGS) GP_TRY(bcgs_epilogue(r, x));
+  GP_CUDA(cudaMemcpyAsync(k->h_st, k->st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+  GP_CUDA(cudaEventRecord(ev, s));
+  GP_CUDA(cudaStreamWaitEvent(caller, ev, 0));
+  GP_CUDA(cudaStreamSynchronize(s));
+  cudaEventDestroy(ev);
+  GP_TRY(pc_check(pc, s));
+  res->its = h.its;
+  res->reason = h.reason;
+  res->rnorm = h.rnorm;
+  if (hist_out && hist_len > 0) {
+    const int64_t cnt = std::min<int64_t>(hist_len, std::min<int64_t>(h.its + 1, k->hist_cap));
+    GP_CUDA(cudaMemcpy(hist_out, k->hist, (size_t)cnt * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int64_t i = cnt; i < hist_len; i++) hist_out[i] = 0.0;
+  }
+  return GP_OK;
+}
+
+}  // namespace gp

@@ -1,0 +1,260 @@
+// SeqAIJ (CSR) matrix on the device: creation from host arrays, SpMV,
+// SpMV-add, SpMV-transpose and the diagonal.
+//
+//   MatMult_SeqAIJ           src/ported.mojo:380-391  -> k_spmv
+//   MatMultAdd_SeqAIJ        src/ported.mojo:394-405  -> k_spmv (init = v_i)
+//   MatMultTranspose_SeqAIJ  src/ported.mojo:408-431  -> k_spmv_t over A^T
+//   MatGetDiagonal_SeqAIJ    src/ported.mojo:434-447  -> k_diag
+//
+// The transpose is stored as a pattern (row pointers, the original row of each
+// entry, and the slot in A it came from), built once on the host from the
+// pattern with a stable counting sort.  Column c of A is then summed in
+// ascending original-row order, which is the order the reference's scatter
+// loop adds into y[c]: the gather is bit-identical to the scatter.
+#include <algorithm>
+#include <vector>
+
+#include "gp_internal.h"
+#include "gp_spmv.cuh"
+
+namespace gp {
+
+template <typename T>
+static int dev_upload(T** d, const T* h, size_t count, cudaStream_t s) {
+  GP_CUDA(cudaMalloc(d, std::max<size_t>(count, 1) * sizeof(T)));
+  if (count) GP_CUDA(cudaMemcpyAsync(*d, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  return GP_OK;
+}
+
+static int csr_finish(Csr* A, const double* h_val, cudaStream_t s) {
+  const int n = A->n;
+  std::vector<int> diag(std::max(n, 1), -1);
+  for (int i = 0; i < n; i++)
+    for (int j = A->h_rowptr[i]; j < A->h_rowptr[i + 1]; j++)
+      if (A->h_colind[j] == i) {
+        diag[i] = j;
+        break;
+      }
+  GP_TRY(dev_upload(&A->rowptr, A->h_rowptr.data(), (size_t)n + 1, s));
+  GP_TRY(dev_upload(&A->colind, A->h_colind.data(), (size_t)A->nnz, s));
+  GP_TRY(dev_upload(&A->val, h_val, (size_t)A->nnz, s));
+  GP_TRY(dev_upload(&A->diagpos, diag.data(), (size_t)n, s));
+  // the host staging vectors must stay alive until the copies land
+  GP_CUDA(cudaStreamSynchronize(s));
+  return GP_OK;
+}
+
+static int check_sizes(int64_t nrows, int64_t ncols, int64_t nnz) {
+  if (nrows < 0 || ncols < 0 || nnz < 0 || nrows > INT32_MAX - 1 || ncols > INT32_MAX - 1 ||
+      nnz > INT32_MAX - 1) {
+    set_error("matrix sizes must be non-negative and fit 32-bit indices");
+    return GP_ERR_ARG;
+  }
+  return GP_OK;
+}
+
+static int validate_pattern(const Csr* A) {
+  if (A->h_rowptr[0] != 0 || A->h_rowptr[A->n] != A->nnz) {
+    set_error("indptr must start at 0 and end at nnz");
+    return GP_ERR_ARG;
+  }
+  for (int i = 0; i < A->n; i++) {
+    if (A->h_rowptr[i + 1] < A->h_rowptr[i]) {
+      set_error("indptr must be non-decreasing");
+      return GP_ERR_ARG;
+    }
+    for (int j = A->h_rowptr[i]; j < A->h_rowptr[i + 1]; j++) {
+      int c = A->h_colind[j];
+      if (c < 0 || c >= A->ncols) {
+        set_error("column index out of range in row " + std::to_string(i));
+        return GP_ERR_ARG;
+      }
+    }
+  }
+  return GP_OK;
+}
+
+int csr_create(Csr** out, int64_t nrows, int64_t ncols, int64_t nnz, const int64_t* h_rowptr,
+               const int64_t* h_colind, const double* h_val, cudaStream_t s) {
+  GP_TRY(check_sizes(nrows, ncols, nnz));
+  Csr* A = new Csr();
+  A->n = (int)nrows;
+  A->ncols = (int)ncols;
+  A->nnz = nnz;
+  A->h_rowptr.resize(nrows + 1);
+  A->h_colind.resize(nnz);
+  for (int64_t i = 0; i <= nrows; i++) A->h_rowptr[i] = (int)h_rowptr[i];
+  for (int64_t j = 0; j < nnz; j++) A->h_colind[j] = (int)h_colind[j];
+  int st = validate_pattern(A);
+  if (st == GP_OK) st = csr_finish(A, h_val, s);
+  if (st != GP_OK) {
+    csr_destroy(A);
+    return st;
+  }
+  GP_CUDA(cudaGetDevice(&A->device));
+  *out = A;
+  return GP_OK;
+}
+
+int csr_create_i32(Csr** out, int64_t nrows, int64_t ncols, int64_t nnz,
+                   const int32_t* h_rowptr, const int32_t* h_colind, const double* h_val,
+                   cudaStream_t s) {
+  GP_TRY(check_sizes(nrows, ncols, nnz));
+  Csr* A = new Csr();
+  A->n = (int)nrows;
+  A->ncols = (int)ncols;
+  A->nnz = nnz;
+  A->h_rowptr.assign(h_rowptr, h_rowptr + nrows + 1);
+  A->h_colind.assign(h_colind, h_colind + nnz);
+  int st = validate_pattern(A);
+  if (st == GP_OK) st = csr_finish(A, h_val, s);
+  if (st != GP_OK) {
+    csr_destroy(A);
+    return st;
+  }
+  GP_CUDA(cudaGetDevice(&A->device));
+  *out = A;
+  return GP_OK;
+}
+
+int csr_set_values(Csr* A, const double* val, int on_device, cudaStream_t s) {
+  if (A->nnz == 0) return GP_OK;
+  GP_CUDA(cudaMemcpyAsync(A->val, val, (size_t)A->nnz * sizeof(double),
+                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  if (A->val32) {
+    cudaFree(A->val32);
+    A->val32 = nullptr;
+  }
+  return GP_OK;
+}
+
+int csr_destroy(Csr* A) {
+  if (!A) return GP_OK;
+  cudaFree(A->rowptr);
+  cudaFree(A->colind);
+  cudaFree(A->val);
+  cudaFree(A->val32);
+  cudaFree(A->diagpos);
+  cudaFree(A->t_rowptr);
+  cudaFree(A->t_colind);
+  cudaFree(A->t_src);
+  delete A;
+  return GP_OK;
+}
+
+int csr_build_transpose(Csr* A, cudaStream_t s) {
+  if (A->t_rowptr) return GP_OK;
+  const int n = A->n, m = A->ncols;
+  std::vector<int> trp(m + 1, 0), tcol(std::max<int64_t>(A->nnz, 1)), tsrc(std::max<int64_t>(A->nnz, 1));
+  for (int64_t j = 0; j < A->nnz; j++) trp[A->h_colind[j] + 1]++;
+  for (int c = 0; c < m; c++) trp[c + 1] += trp[c];
+  std::vector<int> fill(trp.begin(), trp.end() - 1);
+  for (int i = 0; i < n; i++)
+    for (int j = A->h_rowptr[i]; j < A->h_rowptr[i + 1]; j++) {
+      int c = A->h_colind[j];
+      int k = fill[c]++;
+      tcol[k] = i;
+      tsrc[k] = j;
+    }
+  GP_TRY(dev_upload(&A->t_rowptr, trp.data(), (size_t)m + 1, s));
+  GP_TRY(dev_upload(&A->t_colind, tcol.data(), (size_t)A->nnz, s));
+  GP_TRY(dev_upload(&A->t_src, tsrc.data(), (size_t)A->nnz, s));
+  GP_CUDA(cudaStreamSynchronize(s));
+  return GP_OK;
+}
+
+__global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = __double2float_rn(a[i]);
+}
+
+int csr_make_val32(Csr* A, cudaStream_t s) {
+  if (A->val32) return GP_OK;
+  GP_CUDA(cudaMalloc(&A->val32, std::max<int64_t>(A->nnz, 1) * sizeof(float)));
+  if (A->nnz) {
+    k_to_f32<<<num_sms() * 8, 256, 0, s>>>(A->nnz, A->val, A->val32);
+    GP_CHECK_LAUNCH();
+  }
+  return GP_OK;
+}
+
+// ------------------------------------------------------------------ kernels
+
+// y = A x, or y = v + A x when v is given (MatMultAdd starts each row's sum
+// from v_i).  Optional gate for use inside captured solver loops.
+__global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict__ rowptr,
+                                                    const int* __restrict__ colind,
+                                                    const double* __restrict__ val, DRef xr,
+                                                    const double* __restrict__ v, DRef yr,
+                                                    const int* gate, int want) {
+  if (gated_off(gate, want)) return;
+  const double* __restrict__ x = xr.get();
+  double* __restrict__ y = yr.get();
+  __shared__ SpmvSmem<double, double, double> sm;
+  const int r0 = blockIdx.x * kSpmvRows;
+  const int row = r0 + threadIdx.x;
+  double init = (v != nullptr && row < n) ? v[row] : 0.0;
+  double s = spmv_block_rows<double, double, double>(sm, n, r0, rowptr, colind, val, x, init);
+  if (row < n) y[row] = s;
+}
+
+// y = A^T x over the stored transpose pattern; values gathered through the
+// source slot so a value update needs no rebuild.
+__global__ void __launch_bounds__(kBlock) k_spmv_t(int m, const int* __restrict__ trp,
+                                                   const int* __restrict__ tcol,
+                                                   const int* __restrict__ tsrc,
+                                                   const double* __restrict__ val,
+                                                   const double* __restrict__ x,
+                                                   double* __restrict__ y) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m) return;
+  double s = 0.0;
+  for (int k = trp[c]; k < trp[c + 1]; k++) s = add(s, mul(val[tsrc[k]], x[tcol[k]]));
+  y[c] = s;
+}
+
+__global__ void k_diag(int n, const int* __restrict__ diagpos, const double* __restrict__ val,
+                       double* __restrict__ d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int p = diagpos[i];
+  d[i] = p >= 0 ? val[p] : 0.0;
+}
+
+int spmv_grid(const Csr* A) { return (A->n + kSpmvRows - 1) / kSpmvRows; }
+
+int spmv(cudaStream_t s, const Csr* A, DRef x, DRef y, const int* gate, int want) {
+  if (A->n == 0) return GP_OK;
+  k_spmv<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, nullptr, y,
+                                            gate, want);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+int spmv_add(cudaStream_t s, const Csr* A, const double* x, const double* v, double* y) {
+  if (A->n == 0) return GP_OK;
+  k_spmv<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, DRef::of(x),
+                                            v, DRef::of(y), nullptr, 0);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+int spmv_t(cudaStream_t s, Csr* A, const double* x, double* y) {
+  GP_TRY(csr_build_transpose(A, s));
+  if (A->ncols == 0) return GP_OK;
+  k_spmv_t<<<(A->ncols + kBlock - 1) / kBlock, kBlock, 0, s>>>(A->ncols, A->t_rowptr,
+                                                               A->t_colind, A->t_src, A->val,
+                                                               x, y);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+int mat_diagonal(cudaStream_t s, const Csr* A, double* d) {
+  if (A->n == 0) return GP_OK;
+  k_diag<<<(A->n + kBlock - 1) / kBlock, kBlock, 0, s>>>(A->n, A->diagpos, A->val, d);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+}  // namespace gp

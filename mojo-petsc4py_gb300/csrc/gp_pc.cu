@@ -1,0 +1,810 @@
+// Preconditioner set-up and apply kernels.
+//
+//   PCSetUp_Jacobi / _Symmetric, PCApply_Jacobi  src/ported.mojo:505-567
+//   MatInvertDiagonalForSOR_SeqAIJ, PCApply_SOR   src/ported.mojo:610-748
+//   ILUApplyFactor_SeqAIJ                         src/ported.mojo:864-899
+//   ICCApplyFactor_SeqAIJ                         src/ported.mojo:902-952
+//   MatILUFactorNumeric_SeqAIJ                    src/ported.mojo:957-1037
+//   MatICCFactorNumeric_SeqAIJ                    src/ported.mojo:1040-1124
+//
+// Triangular sweeps and numeric factorisations are sequential recurrences.
+// They run as sync-free sweeps: warps take 32 rows at a time, in dependency
+// level order, from a global ticket; a row reads each value it depends on
+// from a value-as-flag array, spinning (with an iteration budget) until the
+// producing row has stored it.  Every row computes its value with the same
+// rounded operations in the same order as the sequential loop, so the applies
+// and factors are bit-identical to the CPU recurrences.  Rows only wait on
+// rows with smaller tickets, which are already held by running warps, so the
+// sweep always makes progress.
+#include <algorithm>
+#include <vector>
+
+#include "gp_pc.h"
+
+namespace gp {
+
+constexpr int kSweepBlock = 256;
+constexpr int kSpinLimit = 1 << 22;   // polls per wait before giving up (~0.5 s)
+
+__device__ __forceinline__ void raise_err(DevErr* err, int code, int where) {
+  if (atomicCAS(&err->code, 0, code) == 0) err->where = where;
+}
+
+// Wait until *p holds a computed value (not the pending pattern).
+__device__ __forceinline__ double wait_value(const double* p, DevErr* err, int where) {
+  unsigned long long b = ld_relaxed_bits(p);
+  if (b != kPending) return __longlong_as_double((long long)b);
+  for (int spins = 0; spins < kSpinLimit; spins++) {
+    __nanosleep(32);
+    b = ld_relaxed_bits(p);
+    if (b != kPending) return __longlong_as_double((long long)b);
+  }
+  raise_err(err, GP_ERR_TIMEOUT, where);
+  return __longlong_as_double(0x7FF8000000000000LL);  // quiet NaN: dependents proceed
+}
+
+__device__ __forceinline__ bool wait_done(const int* p, int epoch, DevErr* err, int where) {
+  if (ld_acquire_i32(p) == epoch) return true;
+  for (int spins = 0; spins < kSpinLimit; spins++) {
+    __nanosleep(32);
+    if (ld_acquire_i32(p) == epoch) return true;
+  }
+  raise_err(err, GP_ERR_TIMEOUT, where);
+  return false;
+}
+
+// Dynamic row hand-out: each warp takes 32 consecutive positions of `order`.
+// The last warp to leave resets the ticket pair, so the next launch starts at
+// zero without a separate reset.
+template <class RowFn>
+__device__ __forceinline__ void sweep_rows(int n, const int* __restrict__ order,
+                                           unsigned* tickets, RowFn&& fn) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(&tickets[0], 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= (unsigned)n) break;
+    const unsigned k = base + lane;
+    if (k < (unsigned)n) fn(order[k]);
+    __syncwarp();
+  }
+  if (lane == 0) {
+    const unsigned total = gridDim.x * (blockDim.x / 32);
+    __threadfence();
+    if (atomicAdd(&tickets[1], 1u) == total - 1) {
+      tickets[0] = 0u;
+      tickets[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
+static int sweep_grid() { return num_sms() * 4; }
+
+// ------------------------------------------------------------------ Jacobi
+__global__ void k_jacobi_fill(int n, int jtype, int sym, int use_abs, int fix_diag, double scale,
+                              const int* __restrict__ rowptr, const double* __restrict__ val,
+                              const int* __restrict__ diagpos, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double d = 0.0;
+  if (jtype == 0) {
+    d = diagpos[i] >= 0 ? val[diagpos[i]] : 0.0;
+  } else {
+    for (int j = rowptr[i]; j < rowptr[i + 1]; j++) {
+      const double v = val[j];
+      if (jtype == 1) {
+        const double a = fabs(v);
+        d = a > d ? a : d;
+      } else if (jtype == 2) {
+        d = add(d, fabs(v));
+      } else {
+        d = add(d, v);
+      }
+    }
+  }
+  if (sym) {  // PCSetUp_Jacobi_Symmetric: 1/sqrt|d|, zero -> 1
+    out[i] = d < 0.0 ? div_(1.0, __dsqrt_rn(fabs(-d)))
+                     : (d > 0.0 ? div_(1.0, __dsqrt_rn(fabs(d))) : 1.0);
+    return;
+  }
+  if (jtype == 2) {  // rowl1: sign follows the true diagonal, optional blend
+    const double td = diagpos[i] >= 0 ? val[diagpos[i]] : 0.0;
+    if (td < 0.0) d = -d;
+    if (scale != 1.0) d = add(mul(scale, sub(d, td)), td);
+  }
+  d = (d == 0.0) ? 0.0 : div_(1.0, d);
+  if (use_abs) d = fabs(d);
+  if (fix_diag && d == 0.0) d = 1.0;
+  out[i] = d;
+}
+
+__global__ void k_pmult(const int* gate, int want, int n, DRef xr, const double* __restrict__ d,
+                        DRef yr) {
+  if (gated_off(gate, want)) return;
+  const double* __restrict__ x = xr.get();
+  double* __restrict__ y = yr.get();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    y[i] = mul(x[i], d[i]);
+}
+
+__global__ void k_copy_g(const int* gate, int want, int n, DRef xr, DRef yr) {
+  if (gated_off(gate, want)) return;
+  const double* __restrict__ x = xr.get();
+  double* __restrict__ y = yr.get();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    y[i] = x[i];
+}
+
+// ------------------------------------------------------------------ SOR
+__global__ void k_sor_diag(int n, double omega, double fshift, const int* __restrict__ diagpos,
+                           const double* __restrict__ val, double* __restrict__ idiag,
+                           double* __restrict__ mdiag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double a = val[diagpos[i]];
+  mdiag[i] = a;
+  idiag[i] = (omega == 1.0 && fshift <= 0.0) ? div_(1.0, a) : div_(omega, add(fshift, a));
+}
+
+__global__ void k_fill_pending(const int* gate, int want, int n, double* __restrict__ a,
+                               double* __restrict__ b) {
+  if (gated_off(gate, want)) return;
+  const double p = __longlong_as_double((long long)kPending);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    a[i] = p;
+    if (b) b[i] = p;
+  }
+}
+
+// Forward Gauss-Seidel half with zero initial guess: t_i = x_i - sum_{j<i}
+// a_ij y_j, y_i = t_i * idiag_i.  (MatSOR_SeqAIJ's zero-guess prologue.)
+__global__ void __launch_bounds__(kSweepBlock) k_sor_fwd(
+    const int* gate, int want, int n, const int* __restrict__ order, unsigned* tickets,
+    const int* __restrict__ rowptr, const int* __restrict__ colind, const double* __restrict__ val,
+    const int* __restrict__ diagpos, const double* __restrict__ idiag, DRef xr,
+    double* __restrict__ t, double* yf, DRef youtr, DevErr* err) {
+  if (gated_off(gate, want)) return;
+  const double* __restrict__ x = xr.get();
+  double* __restrict__ yout = youtr.get();
+  sweep_rows(n, order, tickets, [&](int i) {
+    double sum = x[i];
+    const int jend = diagpos[i];
+    for (int j = rowptr[i]; j < jend; j++)
+      sum = sub(sum, mul(val[j], wait_value(&yf[colind[j]], err, 1)));
+    t[i] = sum;
+    const double y = mul(sum, idiag[i]);
+    if (yout) yout[i] = y;
+    st_relaxed(&yf[i], y);
+  });
+}
+
+// Backward half.  use_t: relax from the forward value, (1 - omega) y_i +
+// (t_i - sum_{j>i} a_ij y_j) idiag_i; otherwise plain back substitution from x.
+__global__ void __launch_bounds__(kSweepBlock) k_sor_bwd(
+    const int* gate, int want, int n, const int* __restrict__ order, unsigned* tickets,
+    const int* __restrict__ rowptr, const int* __restrict__ colind, const double* __restrict__ val,
+    const int* __restrict__ diagpos, const double* __restrict__ idiag, DRef xr,
+    const double* __restrict__ t, const double* __restrict__ yf, double* yb, DRef youtr,
+    double omega, int use_t, DevErr* err) {
+  if (gated_off(gate, want)) return;
+  const double* __restrict__ x = xr.get();
+  double* __restrict__ yout = youtr.get();
+  const double om1 = sub(1.0, omega);
+  sweep_rows(n, order, tickets, [&](int i) {
+    double sum = use_t ? t[i] : x[i];
+    const int jend = rowptr[i + 1];
+    for (int j = diagpos[i] + 1; j < jend; j++)
+      sum = sub(sum, mul(val[j], wait_value(&yb[colind[j]], err, 2)));
+    const double y = use_t ? add(mul(om1, yf[i]), mul(sum, idiag[i])) : mul(sum, idiag[i]);
+    yout[i] = y;
+    st_relaxed(&yb[i], y);
+  });
+}
+
+// ------------------------------------------------------------------ ILU solve
+// Forward: yf_i = b_{r_i} - sum_{L(i)} ba_j yf_{bj_j}  (L rows, unit diagonal)
+__global__ void __launch_bounds__(kSweepBlock) k_ilu_fwd(
+    const int* gate, int want, int n, const int* __restrict__ order, unsigned* tickets,
+    const int* __restrict__ bi, const int* __restrict__ bj, const double* __restrict__ ba,
+    const int* __restrict__ perm_r, DRef br, double* yf, DevErr* err) {
+  if (gated_off(gate, want)) return;
+  const double* __restrict__ b = br.get();
+  sweep_rows(n, order, tickets, [&](int i) {
+    double sum = b[perm_r[i]];
+    const int jend = bi[i + 1];
+    for (int j = bi[i]; j < jend; j++) sum = sub(sum, mul(ba[j], wait_value(&yf[bj[j]], err, 3)));
+    st_relaxed(&yf[i], sum);
+  });
+}
+
+// Backward: yb_i = (yf_i - sum_{U(i)} ba_j yb_{bj_j}) * ba_{diag}; x_{c_i} = yb_i
+__global__ void __launch_bounds__(kSweepBlock) k_ilu_bwd(
+    const int* gate, int want, int n, const int* __restrict__ order, unsigned* tickets,
+    const int* __restrict__ bj, const double* __restrict__ ba, const int* __restrict__ bdiag,
+    const int* __restrict__ perm_c, const double* __restrict__ yf, double* yb, DRef xr,
+    DevErr* err) {
+  if (gated_off(gate, want)) return;
+  double* __restrict__ x = xr.get();
+  sweep_rows(n, order, tickets, [&](int i) {
+    const int v = bdiag[i + 1] + 1;
+    const int nz = bdiag[i] - bdiag[i + 1] - 1;
+    double sum = yf[i];
+    for (int j = 0; j < nz; j++)
+      sum = sub(sum, mul(ba[v + j], wait_value(&yb[bj[v + j]], err, 4)));
+    sum = mul(sum, ba[v + nz]);
+    x[perm_c[i]] = sum;
+    st_relaxed(&yb[i], sum);
+  });
+}
+
+// ------------------------------------------------------------------ IC solve
+// Forward (U^T D y = b in gather form): w_k = b_{c_k} + sum_{i<k, U(i,k)}
+// ua(i,k) w_i in ascending i -- the order the reference's scatter adds them --
+// and ys_k = w_k * ua_{diag(k)}.
+__global__ void __launch_bounds__(kSweepBlock) k_icc_fwd(
+    const int* gate, int want, int n, const int* __restrict__ order, unsigned* tickets,
+    const int* __restrict__ tptr, const int* __restrict__ trow, const int* __restrict__ tslot,
+    const double* __restrict__ ua, const int* __restrict__ bdiag,
+    const int* __restrict__ perm_c, DRef br, double* yf, double* __restrict__ ys,
+    DevErr* err) {
+  if (gated_off(gate, want)) return;
+  const double* __restrict__ b = br.get();
+  sweep_rows(n, order, tickets, [&](int k) {
+    double w = b[perm_c[k]];
+    const int eend = tptr[k + 1];
+    for (int e = tptr[k]; e < eend; e++)
+      w = add(w, mul(ua[tslot[e]], wait_value(&yf[trow[e]], err, 5)));
+    ys[k] = mul(w, ua[bdiag[k]]);
+    st_relaxed(&yf[k], w);
+  });
+}
+
+// Backward: z_i = ys_i + sum_{j in U(i) strict} ua_j z_{uj_j}; x_{c_i} = z_i
+__global__ void __launch_bounds__(kSweepBlock) k_icc_bwd(
+    const int* gate, int want, int n, const int* __restrict__ order, unsigned* tickets,
+    const int* __restrict__ bi, const int* __restrict__ bj, const double* __restrict__ ua,
+    const int* __restrict__ bdiag, const int* __restrict__ perm_c,
+    const double* __restrict__ ys, double* yb, DRef xr, DevErr* err) {
+  if (gated_off(gate, want)) return;
+  double* __restrict__ x = xr.get();
+  sweep_rows(n, order, tickets, [&](int i) {
+    double z = ys[i];
+    const int jend = bdiag[i];
+    for (int j = bi[i]; j < jend; j++) z = add(z, mul(ua[j], wait_value(&yb[bj[j]], err, 6)));
+    x[perm_c[i]] = z;
+    st_relaxed(&yb[i], z);
+  });
+}
+
+// ------------------------------------------------------------------ ILU numeric
+// Row i of the factor is accumulated in its own slots of `ba` (the reference's
+// dense `rtmp` restricted to the row's pattern; positions outside the pattern
+// are never stored or read back there either).
+__device__ __forceinline__ int ilu_find(int col, int i, const int* __restrict__ bi,
+                                        const int* __restrict__ bj,
+                                        const int* __restrict__ bdiag) {
+  if (col < i) {
+    int lo = bi[i], hi = bi[i + 1];
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      int c = bj[mid];
+      if (c == col) return mid;
+      if (c < col) lo = mid + 1; else hi = mid;
+    }
+    return -1;
+  }
+  if (col == i) return bdiag[i];
+  int lo = bdiag[i + 1] + 1, hi = bdiag[i];
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    int c = bj[mid];
+    if (c == col) return mid;
+    if (c < col) lo = mid + 1; else hi = mid;
+  }
+  return -1;
+}
+
+__global__ void __launch_bounds__(kSweepBlock) k_ilu_numeric(
+    int n, const int* __restrict__ order, unsigned* tickets, const int* __restrict__ arow,
+    const double* __restrict__ aval, const int* __restrict__ amap, const int* __restrict__ perm_r,
+    const int* __restrict__ bi, const int* __restrict__ bj, const int* __restrict__ bdiag,
+    double* ba, int* done, int epoch, DevErr* err) {
+  sweep_rows(n, order, tickets, [&](int i) {
+    // zero the row's slots, then load A's row r_i
+    for (int j = bi[i]; j < bi[i + 1]; j++) ba[j] = 0.0;
+    for (int j = bdiag[i + 1] + 1; j <= bdiag[i]; j++) ba[j] = 0.0;
+    const int ri = perm_r[i];
+    for (int j = arow[ri]; j < arow[ri + 1]; j++) {
+      const int s = amap[j];
+      if (s >= 0) ba[s] = aval[j];
+    }
+    // eliminate with each L entry in ascending column order
+    for (int k = bi[i]; k < bi[i + 1]; k++) {
+      const double pc = ba[k];
+      if (pc != 0.0) {
+        const int row = bj[k];
+        wait_done(&done[row], epoch, err, 7);
+        const double pv = __ldcg(&ba[bdiag[row]]);
+        const double m = mul(pc, pv);
+        ba[k] = m;
+        const int pj = bdiag[row + 1] + 1;
+        const int nz = bdiag[row] - bdiag[row + 1] - 1;
+        for (int j = 0; j < nz; j++) {
+          const int s = ilu_find(bj[pj + j], i, bi, bj, bdiag);
+          if (s >= 0) ba[s] = sub(ba[s], mul(m, __ldcg(&ba[pj + j])));
+        }
+      }
+    }
+    ba[bdiag[i]] = div_(1.0, ba[bdiag[i]]);
+    __threadfence();
+    st_release_i32(&done[i], epoch);
+  });
+}
+
+// ------------------------------------------------------------------ IC numeric
+// Up-looking row k: dk and the strict row accumulate A's values, then each
+// contributor row i (U(i,k) != 0) in the order the reference's il/c2r chains
+// visit them (recorded on the host): uikdi = -U(i,k)/d_i, dk += uikdi U(i,k),
+// row k += uikdi U(i, k+1:).  Unscaled rows live in `orig`; the scaled
+// off-diagonal U(i,k) = uikdi is written into `ba` by row k, the only writer.
+__device__ __forceinline__ int icc_find(int col, int k, const int* __restrict__ bi,
+                                        const int* __restrict__ bj, const int* __restrict__ bdiag) {
+  int lo = bi[k], hi = bdiag[k];
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    int c = bj[mid];
+    if (c == col) return mid;
+    if (c < col) lo = mid + 1; else hi = mid;
+  }
+  return -1;
+}
+
+__global__ void __launch_bounds__(kSweepBlock) k_icc_numeric(
+    int n, const int* __restrict__ order, unsigned* tickets, const int* __restrict__ arow,
+    const double* __restrict__ aval, const int* __restrict__ amap, const int* __restrict__ perm_r,
+    const int* __restrict__ bi, const int* __restrict__ bj, const int* __restrict__ bdiag,
+    const int* __restrict__ cptr, const int* __restrict__ crow, const int* __restrict__ cslot,
+    double* ba, double* orig, int* done, int epoch, DevErr* err) {
+  sweep_rows(n, order, tickets, [&](int k) {
+    for (int j = bi[k]; j <= bdiag[k]; j++) orig[j] = 0.0;
+    const int rk = perm_r[k];
+    for (int j = arow[rk]; j < arow[rk + 1]; j++) {
+      const int s = amap[j];
+      if (s >= 0) orig[s] = aval[j];
+    }
+    double dk = orig[bdiag[k]];
+    for (int e = cptr[k]; e < cptr[k + 1]; e++) {
+      const int i = crow[e], ili = cslot[e];
+      wait_done(&done[i], epoch, err, 8);
+      const double uik = __ldcg(&orig[ili]);
+      const double uikdi = mul(-uik, __ldcg(&ba[bdiag[i]]));
+      dk = add(dk, mul(uikdi, uik));
+      ba[ili] = uikdi;
+      const int jmax = bdiag[i];
+      for (int j = ili + 1; j < jmax; j++) {
+        const int s = icc_find(bj[j], k, bi, bj, bdiag);
+        if (s >= 0) orig[s] = add(orig[s], mul(uikdi, __ldcg(&orig[j])));
+      }
+    }
+    for (int j = bi[k]; j < bdiag[k]; j++) ba[j] = orig[j];
+    ba[bdiag[k]] = div_(1.0, dk);
+    __threadfence();
+    st_release_i32(&done[k], epoch);
+  });
+}
+
+// ================================================================== host side
+
+template <typename T>
+static int upload(T** d, const std::vector<T>& h, cudaStream_t s) {
+  GP_CUDA(cudaMalloc(d, std::max<size_t>(h.size(), 1) * sizeof(T)));
+  if (!h.empty())
+    GP_CUDA(cudaMemcpyAsync(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return GP_OK;
+}
+
+static int dalloc(double** p, int64_t n) {
+  GP_CUDA(cudaMalloc(p, std::max<int64_t>(n, 1) * sizeof(double)));
+  return GP_OK;
+}
+
+static void free_all(Pc* pc) {
+  void* ptrs[] = {pc->diag, pc->diagsqrt, pc->idiag, pc->mdiag, pc->bi, pc->bj, pc->bdiag,
+                  pc->perm_r, pc->perm_ic, pc->ba, pc->ba_orig, pc->done, pc->cptr, pc->crow,
+                  pc->cslot, pc->tptr, pc->trow, pc->tslot, pc->amap, pc->fwd.order,
+                  pc->bwd.order, pc->num.order, pc->yf, pc->yb, pc->ys, pc->t, pc->tickets,
+                  pc->err};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  PcOptions keep = pc->opt;
+  *pc = Pc();
+  pc->opt = keep;
+}
+
+int pc_create(Pc** out) {
+  *out = new Pc();
+  return GP_OK;
+}
+
+int pc_destroy(Pc* pc) {
+  if (!pc) return GP_OK;
+  free_all(pc);
+  delete pc;
+  return GP_OK;
+}
+
+static int plan(SweepPlan& p, int n, const std::vector<int>& dptr, const std::vector<int>& dcol,
+                bool forward, cudaStream_t s) {
+  std::vector<int> order;
+  level_order(n, dptr, dcol, forward, order, &p.nlevels);
+  GP_TRY(upload(&p.order, order, s));
+  return GP_OK;
+}
+
+int pc_check(Pc* pc, cudaStream_t s) {
+  if (!pc->err) return GP_OK;
+  DevErr h{};
+  GP_CUDA(cudaMemcpyAsync(&h, pc->err, sizeof(DevErr), cudaMemcpyDeviceToHost, s));
+  GP_CUDA(cudaStreamSynchronize(s));
+  if (h.code == 0) return GP_OK;
+  GP_CUDA(cudaMemsetAsync(pc->err, 0, sizeof(DevErr), s));
+  GP_CUDA(cudaStreamSynchronize(s));
+  set_error("preconditioner sweep wait ran out of budget (site " + std::to_string(h.where) +
+            ")");
+  return h.code;
+}
+
+static int check_sorted_with_diag(const Csr* A, const char* who) {
+  for (int i = 0; i < A->n; i++) {
+    bool diag = false;
+    for (int j = A->h_rowptr[i]; j < A->h_rowptr[i + 1]; j++) {
+      if (j > A->h_rowptr[i] && A->h_colind[j] <= A->h_colind[j - 1]) {
+        set_error(std::string(who) + ": columns must be strictly ascending in each row");
+        return GP_ERR_ARG;
+      }
+      if (A->h_colind[j] == i) diag = true;
+    }
+    if (!diag) {
+      set_error(std::string(who) + ": row " + std::to_string(i) + " has no diagonal entry");
+      return GP_ERR_ARG;
+    }
+  }
+  return GP_OK;
+}
+
+static int setup_sor(Pc* pc, cudaStream_t s) {
+  const Csr* A = pc->A;
+  const int n = A->n;
+  GP_TRY(check_sorted_with_diag(A, "SOR"));
+  GP_TRY(dalloc(&pc->idiag, n));
+  GP_TRY(dalloc(&pc->mdiag, n));
+  GP_TRY(dalloc(&pc->t, n));
+  GP_TRY(dalloc(&pc->yf, n));
+  GP_TRY(dalloc(&pc->yb, n));
+  std::vector<int> lp(n + 1, 0), lc, up(n + 1, 0), uc;
+  for (int i = 0; i < n; i++) {
+    for (int j = A->h_rowptr[i]; j < A->h_rowptr[i + 1]; j++) {
+      int c = A->h_colind[j];
+      if (c < i) lc.push_back(c);
+      if (c > i) uc.push_back(c);
+    }
+    lp[i + 1] = (int)lc.size();
+    up[i + 1] = (int)uc.size();
+  }
+  GP_TRY(plan(pc->fwd, n, lp, lc, true, s));
+  GP_TRY(plan(pc->bwd, n, up, uc, false, s));
+  if (n) {
+    k_sor_diag<<<(n + 255) / 256, 256, 0, s>>>(n, pc->opt.omega, pc->opt.fshift, A->diagpos,
+                                                A->val, pc->idiag, pc->mdiag);
+    GP_CHECK_LAUNCH();
+  }
+  return GP_OK;
+}
+
+static int perms(Pc* pc, std::vector<int>& r, std::vector<int>& ic) {
+  const Csr* A = pc->A;
+  const int n = A->n;
+  if (pc->opt.ordering == 1)
+    GP_TRY(rcm_order(A->h_rowptr, A->h_colind, n, r));
+  else {
+    r.resize(n);
+    for (int i = 0; i < n; i++) r[i] = i;
+  }
+  ic.assign(n, 0);
+  for (int i = 0; i < n; i++) ic[r[i]] = i;
+  return GP_OK;
+}
+
+static int setup_ilu(Pc* pc, cudaStream_t s) {
+  const Csr* A = pc->A;
+  const int n = A->n;
+  std::vector<int> r, ic;
+  GP_TRY(perms(pc, r, ic));
+  FactorPattern& P = pc->pat;
+  GP_TRY(ilu_symbolic(A, pc->opt.levels, r, ic, P));
+  // A slot -> factor slot of row ic[row]
+  std::vector<int> amap(std::max<int64_t>(A->nnz, 1), -1);
+  for (int i = 0; i < n; i++) {
+    const int ri = r[i];
+    for (int j = A->h_rowptr[ri]; j < A->h_rowptr[ri + 1]; j++) {
+      const int c = ic[A->h_colind[j]];
+      int lo, hi;
+      if (c < i) {
+        lo = P.bi[i];
+        hi = P.bi[i + 1];
+      } else if (c == i) {
+        amap[j] = P.bdiag[i];
+        continue;
+      } else {
+        lo = P.bdiag[i + 1] + 1;
+        hi = P.bdiag[i];
+      }
+      auto it = std::lower_bound(P.bj.begin() + lo, P.bj.begin() + hi, c);
+      if (it != P.bj.begin() + hi && *it == c) amap[j] = (int)(it - P.bj.begin());
+    }
+  }
+  // dependency lists: forward / numeric = L columns, backward = U columns
+  std::vector<int> lp(n + 1), lc(P.bj.begin(), P.bj.begin() + P.bi[n]);
+  for (int i = 0; i <= n; i++) lp[i] = P.bi[i];
+  std::vector<int> up(n + 1, 0), uc;
+  uc.reserve(P.nnz - P.bi[n]);
+  for (int i = 0; i < n; i++) {
+    for (int j = P.bdiag[i + 1] + 1; j < P.bdiag[i]; j++) uc.push_back(P.bj[j]);
+    up[i + 1] = (int)uc.size();
+  }
+  GP_TRY(plan(pc->fwd, n, lp, lc, true, s));
+  GP_TRY(plan(pc->bwd, n, up, uc, false, s));
+  GP_TRY(upload(&pc->bi, P.bi, s));
+  GP_TRY(upload(&pc->bj, P.bj, s));
+  GP_TRY(upload(&pc->bdiag, P.bdiag, s));
+  GP_TRY(upload(&pc->perm_r, r, s));
+  GP_TRY(upload(&pc->perm_ic, ic, s));
+  GP_TRY(upload(&pc->amap, amap, s));
+  GP_TRY(dalloc(&pc->ba, std::max(P.bdiag[0] + 1, 1)));
+  GP_CUDA(cudaMalloc(&pc->done, std::max(n, 1) * sizeof(int)));
+  GP_CUDA(cudaMemsetAsync(pc->done, 0, std::max(n, 1) * sizeof(int), s));
+  GP_TRY(dalloc(&pc->yf, n));
+  GP_TRY(dalloc(&pc->yb, n));
+  GP_CUDA(cudaStreamSynchronize(s));  // host vectors above go out of scope
+  return GP_OK;
+}
+
+static int setup_icc(Pc* pc, cudaStream_t s) {
+  const Csr* A = pc->A;
+  const int n = A->n;
+  std::vector<int> r, ic;
+  GP_TRY(perms(pc, r, ic));
+  FactorPattern& P = pc->pat;
+  GP_TRY(icc_symbolic(A, pc->opt.levels, r, ic, P));
+  std::vector<int> amap(std::max<int64_t>(A->nnz, 1), -1);
+  for (int k = 0; k < n; k++) {
+    const int rk = r[k];
+    for (int j = A->h_rowptr[rk]; j < A->h_rowptr[rk + 1]; j++) {
+      const int c = ic[A->h_colind[j]];
+      if (c < k) continue;
+      if (c == k) {
+        amap[j] = P.bdiag[k];
+        continue;
+      }
+      auto it = std::lower_bound(P.bj.begin() + P.bi[k], P.bj.begin() + P.bdiag[k], c);
+      if (it != P.bj.begin() + P.bdiag[k] && *it == c) amap[j] = (int)(it - P.bj.begin());
+    }
+  }
+  // contributor lists in the reference's il/c2r chain order
+  // (src/ported.mojo:1040-1124), simulated on the pattern alone
+  std::vector<int> c2r(n, n), il(n, 0), cptr(n + 1, 0), crow, cslot;
+  std::vector<std::vector<std::pair<int, int>>> visits(n);
+  for (int k = 0; k < n; k++) {
+    int i = c2r[k];
+    while (i < k) {
+      const int nexti = c2r[i];
+      const int ili = il[i];
+      visits[k].emplace_back(i, ili);
+      const int jmin = ili + 1, jmax = P.bi[i + 1];
+      if (jmin < jmax) {
+        il[i] = jmin;
+        const int cj = P.bj[jmin];
+        c2r[i] = c2r[cj];
+        c2r[cj] = i;
+      }
+      i = nexti;
+    }
+    const int jmin = P.bi[k], jmax = P.bi[k + 1] - 1;
+    if (jmin < jmax) {
+      il[k] = jmin;
+      const int cj = P.bj[jmin];
+      c2r[k] = c2r[cj];
+      c2r[cj] = k;
+    }
+  }
+  for (int k = 0; k < n; k++) {
+    for (auto& v : visits[k]) {
+      crow.push_back(v.first);
+      cslot.push_back(v.second);
+    }
+    cptr[k + 1] = (int)crow.size();
+  }
+  // transposed strict pattern, ascending source row (forward sweep order)
+  std::vector<int> tptr(n + 1, 0), trow(std::max(P.nnz - n, 1)), tslot(std::max(P.nnz - n, 1));
+  for (int i = 0; i < n; i++)
+    for (int j = P.bi[i]; j < P.bdiag[i]; j++) tptr[P.bj[j] + 1]++;
+  for (int k = 0; k < n; k++) tptr[k + 1] += tptr[k];
+  {
+    std::vector<int> fill(tptr.begin(), tptr.end() - 1);
+    for (int i = 0; i < n; i++)
+      for (int j = P.bi[i]; j < P.bdiag[i]; j++) {
+        const int k = P.bj[j];
+        trow[fill[k]] = i;
+        tslot[fill[k]] = j;
+        fill[k]++;
+      }
+  }
+  std::vector<int> up(n + 1, 0), uc;
+  for (int i = 0; i < n; i++) {
+    for (int j = P.bi[i]; j < P.bdiag[i]; j++) uc.push_back(P.bj[j]);
+    up[i + 1] = (int)uc.size();
+  }
+  std::vector<int> trow_deps(trow.begin(), trow.begin() + tptr[n]);
+  GP_TRY(plan(pc->num, n, cptr, crow, true, s));
+  GP_TRY(plan(pc->fwd, n, tptr, trow_deps, true, s));
+  GP_TRY(plan(pc->bwd, n, up, uc, false, s));
+  GP_TRY(upload(&pc->bi, P.bi, s));
+  GP_TRY(upload(&pc->bj, P.bj, s));
+  GP_TRY(upload(&pc->bdiag, P.bdiag, s));
+  GP_TRY(upload(&pc->perm_r, r, s));
+  GP_TRY(upload(&pc->perm_ic, ic, s));
+  GP_TRY(upload(&pc->amap, amap, s));
+  GP_TRY(upload(&pc->cptr, cptr, s));
+  GP_TRY(upload(&pc->crow, crow, s));
+  GP_TRY(upload(&pc->cslot, cslot, s));
+  GP_TRY(upload(&pc->tptr, tptr, s));
+  GP_TRY(upload(&pc->trow, trow, s));
+  GP_TRY(upload(&pc->tslot, tslot, s));
+  GP_TRY(dalloc(&pc->ba, std::max(P.nnz, 1)));
+  GP_TRY(dalloc(&pc->ba_orig, std::max(P.nnz, 1)));
+  GP_CUDA(cudaMalloc(&pc->done, std::max(n, 1) * sizeof(int)));
+  GP_CUDA(cudaMemsetAsync(pc->done, 0, std::max(n, 1) * sizeof(int), s));
+  GP_TRY(dalloc(&pc->yf, n));
+  GP_TRY(dalloc(&pc->yb, n));
+  GP_TRY(dalloc(&pc->ys, n));
+  GP_CUDA(cudaStreamSynchronize(s));
+  return GP_OK;
+}
+
+// Numeric factorisation on the device for the current values of A.
+static int factor_numeric(Pc* pc, cudaStream_t s) {
+  const Csr* A = pc->A;
+  const int n = A->n;
+  if (n == 0) return GP_OK;
+  pc->epoch = pc->epoch == INT32_MAX ? 1 : pc->epoch + 1;
+  if (pc->opt.type == PC_ILU) {
+    k_ilu_numeric<<<sweep_grid(), kSweepBlock, 0, s>>>(n, pc->fwd.order, pc->tickets,
+                                                        A->rowptr, A->val, pc->amap, pc->perm_r,
+                                                        pc->bi, pc->bj, pc->bdiag, pc->ba,
+                                                        pc->done, pc->epoch, pc->err);
+  } else {
+    k_icc_numeric<<<sweep_grid(), kSweepBlock, 0, s>>>(
+        n, pc->num.order, pc->tickets, A->rowptr, A->val, pc->amap, pc->perm_r, pc->bi, pc->bj,
+        pc->bdiag, pc->cptr, pc->crow, pc->cslot, pc->ba, pc->ba_orig, pc->done, pc->epoch,
+        pc->err);
+  }
+  GP_CHECK_LAUNCH();
+  return pc_check(pc, s);
+}
+
+int pc_setup(Pc* pc, Csr* A, cudaStream_t s) {
+  free_all(pc);
+  pc->A = A;
+  pc->n = A->n;
+  GP_CUDA(cudaGetDevice(&pc->device));
+  if (A->n != A->ncols) {
+    set_error("the preconditioner matrix must be square");
+    return GP_ERR_ARG;
+  }
+  const int n = A->n;
+  GP_CUDA(cudaMalloc(&pc->err, sizeof(DevErr)));
+  GP_CUDA(cudaMemsetAsync(pc->err, 0, sizeof(DevErr), s));
+  GP_CUDA(cudaMalloc(&pc->tickets, 4 * sizeof(unsigned)));
+  GP_CUDA(cudaMemsetAsync(pc->tickets, 0, 4 * sizeof(unsigned), s));
+  switch (pc->opt.type) {
+    case PC_NONE: break;
+    case PC_JACOBI:
+      GP_TRY(dalloc(&pc->diag, n));
+      GP_TRY(dalloc(&pc->diagsqrt, n));
+      if (n) {
+        const PcOptions& o = pc->opt;
+        k_jacobi_fill<<<(n + 255) / 256, 256, 0, s>>>(n, o.jacobi_type, 0, o.use_abs,
+                                                      o.fix_diag, o.rowl1_scale, A->rowptr,
+                                                      A->val, A->diagpos, pc->diag);
+        k_jacobi_fill<<<(n + 255) / 256, 256, 0, s>>>(n, o.jacobi_type, 1, 0, 0, 1.0,
+                                                      A->rowptr, A->val, A->diagpos,
+                                                      pc->diagsqrt);
+        GP_CHECK_LAUNCH();
+      }
+      break;
+    case PC_SOR: GP_TRY(setup_sor(pc, s)); break;
+    case PC_ILU:
+      GP_TRY(setup_ilu(pc, s));
+      GP_TRY(factor_numeric(pc, s));
+      break;
+    case PC_ICC:
+      GP_TRY(setup_icc(pc, s));
+      GP_TRY(factor_numeric(pc, s));
+      break;
+    default: set_error("unsupported PC type"); return GP_ERR_UNSUPPORTED;
+  }
+  pc->ready = true;
+  return GP_OK;
+}
+
+static int grid_for(int n) { return std::max(1, std::min((n + 255) / 256, num_sms() * 8)); }
+
+int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) {
+  if (!pc->ready) {
+    set_error("PC used before set-up");
+    return GP_ERR_NOT_SETUP;
+  }
+  const int n = pc->n;
+  if (n == 0) return GP_OK;
+  const int g = grid_for(n), sg = sweep_grid();
+  unsigned* tk0 = pc->tickets;
+  unsigned* tk1 = pc->tickets + 2;
+  switch (pc->opt.type) {
+    case PC_NONE:
+      k_copy_g<<<g, 256, 0, s>>>(gate, want, n, x, y);
+      break;
+    case PC_JACOBI:
+      k_pmult<<<g, 256, 0, s>>>(gate, want, n, x, pc->diag, y);
+      break;
+    case PC_SOR: {
+      const Csr* A = pc->A;
+      const int flag = pc->opt.sor_flag;
+      const bool fw = flag & kSorForward, bw = flag & kSorBackward;
+      k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
+      if (fw)
+        k_sor_fwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->fwd.order, tk0, A->rowptr,
+                                             A->colind, A->val, A->diagpos, pc->idiag, x, pc->t,
+                                             pc->yf, bw ? DRef::of((double*)nullptr) : y, pc->err);
+      if (bw)
+        k_sor_bwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->bwd.order, tk1, A->rowptr,
+                                             A->colind, A->val, A->diagpos, pc->idiag, x, pc->t,
+                                             pc->yf, pc->yb, y, pc->opt.omega, fw ? 1 : 0,
+                                             pc->err);
+      break;
+    }
+    case PC_ILU:
+      k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
+      k_ilu_fwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->fwd.order, tk0, pc->bi, pc->bj,
+                                           pc->ba, pc->perm_r, x, pc->yf, pc->err);
+      k_ilu_bwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->bwd.order, tk1, pc->bj, pc->ba,
+                                           pc->bdiag, pc->perm_r, pc->yf, pc->yb, y, pc->err);
+      break;
+    case PC_ICC:
+      k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
+      k_icc_fwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->fwd.order, tk0, pc->tptr,
+                                           pc->trow, pc->tslot, pc->ba, pc->bdiag, pc->perm_r, x,
+                                           pc->yf, pc->ys, pc->err);
+      k_icc_bwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->bwd.order, tk1, pc->bi, pc->bj,
+                                           pc->ba, pc->bdiag, pc->perm_r, pc->ys, pc->yb, y,
+                                           pc->err);
+      break;
+    default: set_error("unsupported PC type"); return GP_ERR_UNSUPPORTED;
+  }
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+int pc_apply_symmetric(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) {
+  if (pc->opt.type == PC_JACOBI) {
+    const int n = pc->n;
+    if (n == 0) return GP_OK;
+    k_pmult<<<grid_for(n), 256, 0, s>>>(gate, want, n, x, pc->diagsqrt, y);
+    GP_CHECK_LAUNCH();
+    return GP_OK;
+  }
+  return pc_apply(pc, x, y, s, gate, want);
+}
+
+}  // namespace gp

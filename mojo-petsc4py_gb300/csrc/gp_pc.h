@@ -1,0 +1,114 @@
+// Preconditioner objects: device data, host set-up analysis and applies.
+#pragma once
+
+#include <vector>
+
+#include "gp_internal.h"
+
+namespace gp {
+
+enum PcType : int { PC_NONE = 0, PC_JACOBI = 2, PC_SOR = 4, PC_ILU = 5, PC_ICC = 6 };
+
+// MatSORType bits (petscmat.h), as the reference uses them.
+constexpr int kSorForward = 1 | 4;    // SOR_FORWARD_SWEEP | SOR_LOCAL_FORWARD_SWEEP
+constexpr int kSorBackward = 2 | 8;   // SOR_BACKWARD_SWEEP | SOR_LOCAL_BACKWARD_SWEEP
+
+struct PcOptions {
+  int type = PC_NONE;
+  int jacobi_type = 0;   // 0 diagonal, 1 rowmax, 2 rowl1, 3 rowsum
+  int use_abs = 0;
+  int fix_diag = 1;
+  double rowl1_scale = 1.0;
+  double omega = 1.0;
+  double fshift = 0.0;
+  int sor_flag = 12 | 16;  // LOCAL_SYMMETRIC | ZERO_INITIAL_GUESS
+  int levels = 0;
+  int ordering = 0;      // 0 natural, 1 rcm
+};
+
+// Processing plan of one sync-free sweep: rows in dependency-level order and
+// a ticket pair for the dynamic row hand-out.
+struct SweepPlan {
+  int* order = nullptr;      // device, n
+  int nlevels = 0;
+};
+
+// Host copy of a factor pattern in the reference's layout.
+struct FactorPattern {
+  // ILU: L rows bi[i]..bi[i+1], U rows (reversed) ending on the diagonal at
+  // bdiag[i]; IC: row i = strict upper ascending then the diagonal slot
+  // bdiag[i] = bi[i+1]-1.
+  std::vector<int> bi, bj, bdiag;
+  std::vector<int> r, ic;   // row ordering and its inverse
+  int nnz = 0;              // number of factor slots
+};
+
+struct Pc {
+  PcOptions opt;
+  Csr* A = nullptr;  // operator the PC was set up from (not owned)
+  int n = 0;
+  int device = -1;
+  bool ready = false;
+  int epoch = 0;
+
+  // Jacobi
+  double* diag = nullptr;
+  double* diagsqrt = nullptr;
+
+  // SOR (uses A's arrays and diagpos)
+  double* idiag = nullptr;
+  double* mdiag = nullptr;
+
+  // factor (ILU / IC), reference layout on the device
+  FactorPattern pat;
+  int* bi = nullptr;
+  int* bj = nullptr;
+  int* bdiag = nullptr;
+  int* perm_r = nullptr;
+  int* perm_ic = nullptr;
+  double* ba = nullptr;      // factor values (what the solve reads)
+  double* ba_orig = nullptr; // IC: unscaled strict rows
+  int* done = nullptr;       // numeric row-done epochs
+  // IC numeric: chain-ordered contributor lists (row k <- (i, slot))
+  int* cptr = nullptr;
+  int* crow = nullptr;
+  int* cslot = nullptr;
+  // IC forward sweep: transposed strict pattern, ascending source row
+  int* tptr = nullptr;
+  int* trow = nullptr;
+  int* tslot = nullptr;
+  int* amap = nullptr;       // A slot -> factor slot (or -1)
+
+  SweepPlan fwd, bwd, num;
+  // sweep work: value-as-flag arrays and SOR checkpoint
+  double* yf = nullptr;
+  double* yb = nullptr;
+  double* ys = nullptr;      // IC: scaled forward values
+  double* t = nullptr;       // SOR checkpoint
+  unsigned* tickets = nullptr;  // [4]: (ticket, exits) x 2
+  DevErr* err = nullptr;
+};
+
+int pc_create(Pc** out);
+int pc_destroy(Pc* pc);
+int pc_setup(Pc* pc, Csr* A, cudaStream_t s);
+// y = M^-1 x (x, y distinct device vectors).  Gate for captured loops.
+int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate = nullptr, int want = 0);
+// Jacobi symmetric half; other types fall back to pc_apply.
+int pc_apply_symmetric(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate = nullptr,
+                       int want = 0);
+// Read and clear the device error word (spin timeouts).  Synchronizes s.
+int pc_check(Pc* pc, cudaStream_t s);
+
+// host analysis (gp_pcsetup.cu)
+int rcm_order(const std::vector<int>& rowptr, const std::vector<int>& colind, int n,
+              std::vector<int>& perm);
+int ilu_symbolic(const Csr* A, int levels, const std::vector<int>& r,
+                 const std::vector<int>& ic, FactorPattern& out);
+int icc_symbolic(const Csr* A, int levels, const std::vector<int>& r,
+                 const std::vector<int>& ic, FactorPattern& out);
+// Levels of a DAG given as dependency lists; forward (deps < i) or backward.
+void level_order(int n, const std::vector<int>& dptr, const std::vector<int>& dcol,
+                 bool forward, std::vector<int>& order, int* nlevels);
+
+}  // namespace gp

@@ -1,0 +1,414 @@
+// Vec kernels: elementwise maps, MAXPY and deterministic reductions.
+//
+// Maps follow the reference's per-element expressions and branch structure
+// (src/ported.mojo:75-341 over src/simdvec.mojo:40-319): every element is one
+// rounded operation sequence identical to the CPU loop, so maps are bit-exact.
+// Reductions (src/simdvec.mojo:332-500) sum in a fixed GPU order instead of
+// the CPU's 16-lane blocked order; they are reproducible run to run and agree
+// with the CPU sums to rounding.
+#include <algorithm>
+
+#include "gp_internal.h"
+
+namespace gp {
+
+// ------------------------------------------------------------------ maps
+
+template <int OP>
+__global__ void __launch_bounds__(kBlock) k_map(int64_t n, double* __restrict__ y,
+                                                const double* __restrict__ x,
+                                                const double* __restrict__ w, double alpha,
+                                                double beta, double gamma) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    if constexpr (OP == OP_COPY) {
+      y[i] = x[i];
+    } else if constexpr (OP == OP_SET) {
+      y[i] = alpha;
+    } else if constexpr (OP == OP_ZERO) {
+      y[i] = 0.0;
+    } else if constexpr (OP == OP_SCALE) {
+      y[i] = mul(y[i], alpha);
+    } else if constexpr (OP == OP_SCALESET) {  // x alpha into y
+      y[i] = mul(x[i], alpha);
+    } else if constexpr (OP == OP_DIVS) {  // y / alpha (VecNormalize)
+      y[i] = div_(y[i], alpha);
+    } else if constexpr (OP == OP_SHIFT) {
+      y[i] = add(y[i], alpha);
+    } else if constexpr (OP == OP_AXPY) {  // y + alpha x
+      y[i] = add(y[i], mul(alpha, x[i]));
+    } else if constexpr (OP == OP_AYPX) {  // x + alpha y
+      y[i] = add(x[i], mul(alpha, y[i]));
+    } else if constexpr (OP == OP_AXPBY) {  // alpha x + beta y
+      y[i] = add(mul(alpha, x[i]), mul(beta, y[i]));
+    } else if constexpr (OP == OP_AXPBYPCZ) {  // alpha x + beta w + gamma y
+      y[i] = add(add(mul(alpha, x[i]), mul(beta, w[i])), mul(gamma, y[i]));
+    } else if constexpr (OP == OP_WAXPY) {  // alpha x + w
+      y[i] = add(mul(alpha, x[i]), w[i]);
+    } else if constexpr (OP == OP_PMULT) {
+      y[i] = mul(x[i], w[i]);
+    } else if constexpr (OP == OP_PDIV) {
+      y[i] = div_(x[i], w[i]);
+    } else if constexpr (OP == OP_PMIN) {
+      double a = x[i], b = w[i];
+      y[i] = (b < a) ? b : a;
+    } else if constexpr (OP == OP_PMAX) {
+      double a = x[i], b = w[i];
+      y[i] = (b > a) ? b : a;
+    } else if constexpr (OP == OP_PMAXABS) {
+      double a = fabs(x[i]), b = fabs(w[i]);
+      y[i] = (b > a) ? b : a;
+    } else if constexpr (OP == OP_RECIP) {
+      double v = y[i];
+      y[i] = (v == 0.0) ? 0.0 : div_(1.0, v);
+    } else if constexpr (OP == OP_EXP) {
+      y[i] = exp(y[i]);
+    } else if constexpr (OP == OP_LOG) {
+      y[i] = log(y[i]);
+    } else if constexpr (OP == OP_SQRTABS) {
+      y[i] = __dsqrt_rn(fabs(y[i]));
+    } else if constexpr (OP == OP_ABS) {
+      y[i] = fabs(y[i]);
+    } else if constexpr (OP == OP_CHOP) {
+      if (fabs(y[i]) < alpha) y[i] = 0.0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_swap(int64_t n, double* a, double* b) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    double t = a[i];
+    a[i] = b[i];
+    b[i] = t;
+  }
+}
+
+static int map_grid(int64_t n) {
+  int64_t g = (n + kBlock - 1) / kBlock;
+  int64_t cap = (int64_t)num_sms() * 16;
+  return (int)std::max<int64_t>(1, std::min(g, cap));
+}
+
+template <int OP>
+static int launch_map(cudaStream_t s, int64_t n, double* y, const double* x, const double* w,
+                      double a, double b, double c) {
+  if (n <= 0) return GP_OK;
+  k_map<OP><<<map_grid(n), kBlock, 0, s>>>(n, y, x, w, a, b, c);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+// Host dispatch keeps the reference's scalar branch structure:
+//   VecSet alpha == 0 zeroes (ported.mojo:259-263); VecAYPX alpha == 0 copies
+//   and alpha == 1 is an AXPY (:285-294); VecAXPBY beta == 0 is a scale-and-set
+//   and alpha == 0 a VecScale (:297-308).
+int vec_map(cudaStream_t s, int op, int64_t n, double* y, const double* x, const double* w,
+            double alpha, double beta, double gamma) {
+  switch (op) {
+    case OP_COPY:
+      if (x == y || n <= 0) return GP_OK;
+      GP_CUDA(cudaMemcpyAsync(y, x, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      return GP_OK;
+    case OP_ZERO:
+      return launch_map<OP_ZERO>(s, n, y, x, w, 0, 0, 0);
+    case OP_SET:
+      if (alpha == 0.0) return launch_map<OP_ZERO>(s, n, y, x, w, 0, 0, 0);
+      return launch_map<OP_SET>(s, n, y, x, w, alpha, 0, 0);
+    case OP_SCALESET: return launch_map<OP_SCALESET>(s, n, y, x, w, alpha, 0, 0);
+    case OP_DIVS: return launch_map<OP_DIVS>(s, n, y, x, w, alpha, 0, 0);
+    case OP_SCALE: return launch_map<OP_SCALE>(s, n, y, x, w, alpha, 0, 0);
+    case OP_SHIFT: return launch_map<OP_SHIFT>(s, n, y, x, w, alpha, 0, 0);
+    case OP_AXPY: return launch_map<OP_AXPY>(s, n, y, x, w, alpha, 0, 0);
+    case OP_AYPX:
+      if (alpha == 0.0) return vec_map(s, OP_COPY, n, y, x, w, 0, 0, 0);
+      if (alpha == 1.0) return launch_map<OP_AXPY>(s, n, y, x, w, alpha, 0, 0);
+      return launch_map<OP_AYPX>(s, n, y, x, w, alpha, 0, 0);
+    case OP_AXPBY:
+      if (beta == 0.0) return launch_map<OP_SCALESET>(s, n, y, x, w, alpha, 0, 0);
+      if (alpha == 0.0) return launch_map<OP_SCALE>(s, n, y, x, w, beta, 0, 0);
+      return launch_map<OP_AXPBY>(s, n, y, x, w, alpha, beta, 0);
+    case OP_AXPBYPCZ: return launch_map<OP_AXPBYPCZ>(s, n, y, x, w, alpha, beta, gamma);
+    case OP_WAXPY: return launch_map<OP_WAXPY>(s, n, y, x, w, alpha, 0, 0);
+    case OP_PMULT: return launch_map<OP_PMULT>(s, n, y, x, w, 0, 0, 0);
+    case OP_PDIV: return launch_map<OP_PDIV>(s, n, y, x, w, 0, 0, 0);
+    case OP_PMIN: return launch_map<OP_PMIN>(s, n, y, x, w, 0, 0, 0);
+    case OP_PMAX: return launch_map<OP_PMAX>(s, n, y, x, w, 0, 0, 0);
+    case OP_PMAXABS: return launch_map<OP_PMAXABS>(s, n, y, x, w, 0, 0, 0);
+    case OP_RECIP: return launch_map<OP_RECIP>(s, n, y, x, w, 0, 0, 0);
+    case OP_EXP: return launch_map<OP_EXP>(s, n, y, x, w, 0, 0, 0);
+    case OP_LOG: return launch_map<OP_LOG>(s, n, y, x, w, 0, 0, 0);
+    case OP_SQRTABS: return launch_map<OP_SQRTABS>(s, n, y, x, w, 0, 0, 0);
+    case OP_ABS: return launch_map<OP_ABS>(s, n, y, x, w, 0, 0, 0);
+    case OP_CHOP: return launch_map<OP_CHOP>(s, n, y, x, w, alpha, 0, 0);
+    case OP_SWAP:
+      if (n <= 0) return GP_OK;
+      k_swap<<<map_grid(n), kBlock, 0, s>>>(n, y, const_cast<double*>(x));
+      GP_CHECK_LAUNCH();
+      return GP_OK;
+  }
+  set_error("vec_map: unknown op");
+  return GP_ERR_ARG;
+}
+
+// ------------------------------------------------------------------ MAXPY
+// y += sum_k alpha_k x_k, with the k-sum done per element in ascending k
+// (simdvec.mojo:503-518 runs k outermost; each element sees the same sequence
+// of rounded updates, so one pass over all k vectors is bit-identical).
+constexpr int kMaxpyChunk = 32;
+struct MaxpyArgs {
+  const double* x[kMaxpyChunk];
+  double a[kMaxpyChunk];
+  int nv;
+};
+
+__global__ void __launch_bounds__(kBlock) k_maxpy(int64_t n, double* __restrict__ y, MaxpyArgs args) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    double v = y[i];
+    for (int k = 0; k < args.nv; k++) v = add(v, mul(args.a[k], args.x[k][i]));
+    y[i] = v;
+  }
+}
+
+int vec_maxpy(cudaStream_t s, int64_t n, double* y, int nv, const double* alpha,
+              const double* const* xs) {
+  if (n <= 0) return GP_OK;
+  for (int k0 = 0; k0 < nv; k0 += kMaxpyChunk) {
+    MaxpyArgs args;
+    args.nv = std::min(kMaxpyChunk, nv - k0);
+    for (int k = 0; k < args.nv; k++) {
+      args.x[k] = xs[k0 + k];
+      args.a[k] = alpha[k0 + k];
+    }
+    k_maxpy<<<map_grid(n), kBlock, 0, s>>>(n, y, args);
+    GP_CHECK_LAUNCH();
+  }
+  return GP_OK;
+}
+
+// ------------------------------------------------------------------ reductions
+template <int OP>
+__global__ void __launch_bounds__(kRedBlock) k_reduce(int64_t n, const double* __restrict__ x,
+                                                      const double* __restrict__ y, RedSlot slot,
+                                                      double* out) {
+  constexpr int NR = (OP == RED_DOTNORM2) ? 2 : 1;
+  double v[NR];
+#pragma unroll
+  for (int r = 0; r < NR; r++) v[r] = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    double a = x[i];
+    if constexpr (OP == RED_DOT) {
+      v[0] = add(v[0], mul(a, y[i]));
+    } else if constexpr (OP == RED_NORM2SQ) {
+      v[0] = add(v[0], mul(a, a));
+    } else if constexpr (OP == RED_ASUM) {
+      v[0] = add(v[0], fabs(a));
+    } else if constexpr (OP == RED_SUM) {
+      v[0] = add(v[0], a);
+    } else if constexpr (OP == RED_DOTNORM2) {
+      v[0] = add(v[0], mul(a, y[i]));
+      v[1] = add(v[1], mul(a, a));
+    }
+  }
+  double tot[NR];
+  if (grid_finish<NR>(v, slot, tot) && threadIdx.x == 0) {
+#pragma unroll
+    for (int r = 0; r < NR; r++) out[r] = tot[r];
+  }
+}
+
+// max |x_i| with the first NaN adopted (simdvec.mojo:476-488), or, for the
+// pointwise-divide form, max |x_i / y_i| with x_i where y_i == 0 (:491-500).
+// Per-block results go to partials; the last block combines them.
+template <bool DIVIDE>
+__global__ void __launch_bounds__(kRedBlock) k_maxabs(int64_t n, const double* __restrict__ x,
+                                                      const double* __restrict__ y, RedSlot slot,
+                                                      double* out) {
+  __shared__ double sh[kRedBlock];
+  __shared__ bool last;
+  double m = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    double t;
+    if constexpr (DIVIDE) {
+      double yi = y[i];
+      t = fabs(yi == 0.0 ? x[i] : div_(x[i], yi));
+      if (t > m) m = t;  // NaN never adopted in this form
+    } else {
+      t = fabs(x[i]);
+      if (t > m || t != t) m = (m != m) ? m : t;  // NaN is sticky
+    }
+  }
+  auto comb = [](double a, double b) {
+    if (DIVIDE) return b > a ? b : a;
+    if (a != a) return a;
+    if (b != b) return b;
+    return b > a ? b : a;
+  };
+  sh[threadIdx.x] = m;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] = comb(sh[threadIdx.x], sh[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    slot.partials[blockIdx.x] = sh[0];
+    __threadfence();
+    last = atomicAdd(slot.ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    double r = 0.0;
+    for (int b = 0; b < (int)gridDim.x; b++) r = comb(r, ld_relaxed(&slot.partials[b]));
+    out[0] = r;
+    *slot.ticket = 0u;
+  }
+}
+
+int vec_reduce(cudaStream_t s, int op, int64_t n, const double* x, const double* y,
+               double* out_host) {
+  Scratch* sc;
+  GP_TRY(scratch_get(&sc, 0));
+  int nr = (op == RED_DOTNORM2) ? 2 : 1;
+  if (n <= 0) {
+    for (int r = 0; r < nr; r++) out_host[r] = 0.0;
+    return GP_OK;
+  }
+  int g = red_grid(n);
+  switch (op) {
+    case RED_DOT: k_reduce<RED_DOT><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out); break;
+    case RED_NORM2SQ:
+      k_reduce<RED_NORM2SQ><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out);
+      break;
+    case RED_ASUM: k_reduce<RED_ASUM><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out); break;
+    case RED_SUM: k_reduce<RED_SUM><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out); break;
+    case RED_DOTNORM2:
+      k_reduce<RED_DOTNORM2><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out);
+      break;
+    case RED_NORMINF:
+      k_maxabs<false><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out);
+      break;
+    default: set_error("vec_reduce: unknown op"); return GP_ERR_ARG;
+  }
+  GP_CHECK_LAUNCH();
+  GP_CUDA(cudaMemcpyAsync(sc->h_out, sc->d_out, nr * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GP_CUDA(cudaStreamSynchronize(s));
+  for (int r = 0; r < nr; r++) out_host[r] = sc->h_out[r];
+  return GP_OK;
+}
+
+int vec_max_pointwise_divide(cudaStream_t s, int64_t n, const double* x, const double* y,
+                             double* out_host) {
+  Scratch* sc;
+  GP_TRY(scratch_get(&sc, 0));
+  if (n <= 0) {
+    *out_host = 0.0;
+    return GP_OK;
+  }
+  k_maxabs<true><<<red_grid(n), kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out);
+  GP_CHECK_LAUNCH();
+  GP_CUDA(cudaMemcpyAsync(sc->h_out, sc->d_out, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GP_CUDA(cudaStreamSynchronize(s));
+  *out_host = sc->h_out[0];
+  return GP_OK;
+}
+
+// VecMax/VecMin (ported.mojo:165-196): the first index attaining the extreme,
+// strict comparison, so NaN entries never win; when x[0] itself is NaN the
+// scan never moves off it and the result is (NaN, 0).
+template <bool MAX>
+__global__ void __launch_bounds__(kRedBlock) k_minmax(int64_t n, const double* __restrict__ x,
+                                                      RedSlot slot, double* out,
+                                                      long long* oidx) {
+  __shared__ double sv[kRedBlock];
+  __shared__ long long si[kRedBlock];
+  __shared__ bool last;
+  double bv = 0.0;
+  long long bi = -1;
+  auto better = [](double av, long long ai, double bv_, long long bi_) {
+    // is (av, ai) better than (bv_, bi_)?
+    if (ai < 0) return false;
+    if (bi_ < 0) return true;
+    if (MAX ? (av > bv_) : (av < bv_)) return true;
+    if (av == bv_ && ai < bi_) return true;
+    return false;
+  };
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    double v = x[i];
+    if (v != v) continue;
+    if (better(v, i, bv, bi)) {
+      bv = v;
+      bi = i;
+    }
+  }
+  sv[threadIdx.x] = bv;
+  si[threadIdx.x] = bi;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o && better(sv[threadIdx.x + o], si[threadIdx.x + o], sv[threadIdx.x],
+                                  si[threadIdx.x])) {
+      sv[threadIdx.x] = sv[threadIdx.x + o];
+      si[threadIdx.x] = si[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    slot.partials[blockIdx.x] = sv[0];
+    slot.partials[slot.stride + blockIdx.x] = __longlong_as_double(si[0]);
+    __threadfence();
+    last = atomicAdd(slot.ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    double rv = 0.0;
+    long long ri = -1;
+    for (int b = 0; b < (int)gridDim.x; b++) {
+      double v = ld_relaxed(&slot.partials[b]);
+      long long ii = __double_as_longlong(ld_relaxed(&slot.partials[slot.stride + b]));
+      if (better(v, ii, rv, ri)) {
+        rv = v;
+        ri = ii;
+      }
+    }
+    double x0 = x[0];
+    if (x0 != x0) {
+      rv = x0;
+      ri = 0;
+    }
+    out[0] = rv;
+    oidx[0] = ri;
+    *slot.ticket = 0u;
+  }
+}
+
+int vec_minmax(cudaStream_t s, int64_t n, const double* x, int is_max, long long* idx,
+               double* val) {
+  if (n <= 0) {
+    *idx = -1;
+    *val = is_max ? -1.7976931348623157e308 : 1.7976931348623157e308;
+    return GP_OK;
+  }
+  Scratch* sc;
+  GP_TRY(scratch_get(&sc, 0));
+  int g = red_grid(n);
+  if (is_max)
+    k_minmax<true><<<g, kRedBlock, 0, s>>>(n, x, sc->slot, sc->d_out, sc->d_idx);
+  else
+    k_minmax<false><<<g, kRedBlock, 0, s>>>(n, x, sc->slot, sc->d_out, sc->d_idx);
+  GP_CHECK_LAUNCH();
+  GP_CUDA(cudaMemcpyAsync(sc->h_out, sc->d_out, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GP_CUDA(cudaMemcpyAsync(sc->h_idx, sc->d_idx, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  GP_CUDA(cudaStreamSynchronize(s));
+  *val = sc->h_out[0];
+  *idx = sc->h_idx[0];
+  return GP_OK;
+}
+
+}  // namespace gp
