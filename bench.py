@@ -1,0 +1,412 @@
+"""Benchmark: solve time to rtol 1e-10 on the 3-D 7-point Poisson operator,
+128^3 (n = 2,097,152, nnz = 14,581,760), through the PETSc-compatible API on
+one GB300.
+
+One step = one KSP.solve of that system with CG + Jacobi (b uniform[-1, 1],
+seed 5, x0 = 0, rtol 1e-10, atol 1e-50, max_it 10000).  The matrix (217 MB)
+is larger than the 129 MB L2, so consecutive solves stream it from HBM.
+
+  value   device-resident solve time (b, x and the operator already in HBM)
+  e2e     the same solve through the public API with host arrays: the step
+          uploads b from host memory, solves, and reads x back
+  roofline  the SpMV kernel, timed alone with CUDA events (L2 flushed before
+          each launch), algorithmic bytes 12 nnz + 4 (n+1) + 16 n per launch
+  cpu_baseline  the CPU oracle (a single-threaded restatement of the
+          reference's algorithm) on the same system, a bounded sample of
+          iterations scaled by the iteration count
+
+`--impl reference` times the reference's CPU path (the oracle restatement;
+the Mojo reference cannot be built here) on the same workload and prints the
+same JSON line with "impl": "reference".
+
+Multi-GPU (torchrun): every rank solves its own replica of the system (the
+path is sequential; there is no data-path collective), barrier and max over
+ranks around the timed region.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "mojo-petsc4py_gb300"))
+
+K3 = 128
+RTOL = 1e-10
+MAX_IT = 10000
+METRIC = "solve ms to rtol 1e-10 (3-D 7-pt Poisson 128^3, CG+Jacobi, FP64)"
+
+
+def problem():
+    from mojopetsc4py import gallery
+
+    ip, ix, v = gallery.laplacian_3d(K3)
+    n = len(ip) - 1
+    b = np.random.default_rng(5).uniform(-1.0, 1.0, n)
+    return ip, ix, v, b
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(name):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        with open(path) as f:
+            m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("gloo")
+        pg = tdist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, value):
+    if pg is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ CPU leg
+def cpu_solve_sample(ip, ix, v, b, sample_its, full_its=None):
+    """The oracle's CG + Jacobi: a bounded run of `sample_its` iterations,
+    scaled to a full solve of `full_its` iterations."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.lib()
+    pc = O.OraclePC("jacobi", ip, ix, v)
+    t0 = time.perf_counter()
+    r = O.solve("cg", ip, ix, v, b, pc=pc, rtol=RTOL, atol=1e-50, divtol=1e30,
+                max_it=sample_its)
+    dt = time.perf_counter() - t0
+    per_it = dt / max(r["its"], 1)
+    return per_it, r
+
+
+def run_reference(args, world, rank, pg):
+    if rank != 0:
+        return
+    ip, ix, v, b = problem()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.lib()
+    # iteration count of the full solve, from one full oracle run in warm-up
+    full = O.solve("cg", ip, ix, v, b, pc=O.OraclePC("jacobi", ip, ix, v), rtol=RTOL,
+                   atol=1e-50, divtol=1e30, max_it=MAX_IT)
+    its = full["its"]
+    sample = 40
+    for _ in range(max(args.warmup - 1, 0)):
+        cpu_solve_sample(ip, ix, v, b, sample)
+    per = []
+    for _ in range(args.steps):
+        p, _ = cpu_solve_sample(ip, ix, v, b, sample)
+        per.append(p)
+    ms = float(np.mean(per)) * its * 1e3
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "poisson3d-7pt-128^3 cg+jacobi rtol 1e-10", "n": len(b),
+                   "nnz": int(ip[-1]), "iterations": its},
+        "cpu_baseline": {"value": round(ms, 3), "unit": "ms", "cores": 1, "kind": "port",
+                         "sample": f"{sample} CG+Jacobi iterations per step, scaled to the "
+                                   f"{its}-iteration solve (measured once in warm-up)"},
+        "e2e": {"value": round(ms, 3), "unit": "ms", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU leg
+def build_solver(PETSc, A, ksp_type, pc_type, **opts):
+    pc = PETSc.PC().create()
+    pc.setType(pc_type)
+    if pc_type == "sor":
+        pc.setSOROmega(opts.get("omega", 1.0))
+    pc.setOperators(A)
+    ksp = PETSc.KSP().create()
+    ksp.setPC(pc)
+    ksp.setType(ksp_type)
+    ksp.setOperators(A)
+    ksp.setTolerances(rtol=RTOL, atol=1e-50, divtol=1e30, max_it=MAX_IT)
+    if ksp_type in ("gmres", "fgmres"):
+        ksp.setGMRESRestart(30)
+    return ksp
+
+
+def time_solves(torch, ksp, bv, xv, steps):
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    for _ in range(steps):
+        ksp.solve(bv, xv)
+    ev1.record()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / steps
+
+
+def spmv_roofline(torch, PETSc, A, n, nnz, launches=20):
+    import ctypes
+
+    from mojopetsc4py import _device as dev
+    from mojopetsc4py._lib import check, lib
+
+    x = PETSc.Vec().createWithArray(np.random.default_rng(3).normal(size=n))
+    y = PETSc.Vec().createSeq(n)
+    h = A._device()
+    # flush by reading 512 MB, so L2 holds clean lines of another buffer and the
+    # kernel pays no write-back of a flush
+    flush = torch.ones(int(512 * 2**20 // 8), dtype=torch.float64, device="cuda")
+    xp, yp = x._dptr(), y._optr()
+    st = dev.stream_ptr()
+    for _ in range(3):
+        check(lib().gp_mat_mult(h, xp, yp, st))
+    times = []
+    for _ in range(launches):
+        flush.sum()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        check(lib().gp_mat_mult(h, xp, yp, st))
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    t = float(np.mean(times))
+    algo = 12 * nnz + 4 * (n + 1) + 8 * n + 8 * n
+    return algo, t, ctypes
+
+
+def run_spmv_only(args):
+    """SpMV launches alone on the benchmark matrix (the profiling target)."""
+    import torch
+
+    from mojopetsc4py import PETSc
+
+    ip, ix, v, _ = problem()
+    n, nnz = len(ip) - 1, int(ip[-1])
+    A = PETSc.Mat().createSeqAIJ((n, n), nnz=7)
+    A.setValuesCSR(ip, ix, v)
+    A.assemble()
+    algo, t, _ = spmv_roofline(torch, PETSc, A, n, nnz, launches=args.steps)
+    print(json.dumps({"kernel": "k_spmv", "algorithmic_bytes": algo, "launch_us": t * 1e6,
+                      "achieved_gbs": algo / t / 1e9}), flush=True)
+
+
+def run_ours(args, world, rank, local, pg):
+    import torch
+
+    torch.cuda.set_device(local)
+    from mojopetsc4py import PETSc
+
+    ip, ix, v, b = problem()
+    n, nnz = len(b), int(ip[-1])
+    A = PETSc.Mat().createSeqAIJ((n, n), nnz=7)
+    A.setValuesCSR(ip, ix, v)
+    A.assemble()
+    ksp = build_solver(PETSc, A, "cg", "jacobi")
+    bv = PETSc.Vec().createWithArray(b)
+    xv = PETSc.Vec().createSeq(n)
+    for _ in range(max(args.warmup, 3)):
+        ksp.solve(bv, xv)
+    its, reason = ksp.getIterationNumber(), ksp.getConvergedReason()
+    trips, top, body = ksp.getLaunchStats()
+
+    # ---- timed region: device-resident solves
+    barrier(pg)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        ms = time_solves(torch, ksp, bv, xv, args.steps)
+    barrier(pg)
+    ms = max_over_ranks(pg, ms)
+    clocks = clk.summary()
+
+    # ---- end to end through the public API with host arrays
+    xh = xv.getArray().copy()
+    barrier(pg)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        bv.setArray(b)
+        ksp.solve(bv, xv)
+        xh = xv.getArray()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) / args.steps * 1e3
+    e2e_ms = max_over_ranks(pg, e2e_ms)
+    resid = float(np.linalg.norm(b - _csr_matvec(ip, ix, v, xh)) / np.linalg.norm(b))
+
+    # ---- SpMV roofline (kernel alone, L2 flushed before each launch)
+    algo, t_spmv, _ = spmv_roofline(torch, PETSc, A, n, nnz)
+    peak, peak_kind = peaks()
+    achieved = algo / t_spmv / 1e9
+    traffic = profiled_traffic("spmv_fp64_poisson3d_128.md")
+
+    # ---- the other plain methods of this configuration (fewer repetitions)
+    methods = {"cg+jacobi": {"ms": round(ms, 3), "its": its, "reason": reason}}
+    if not args.quick:
+        for name, kt, pt, extra in (("cg+icc(0)", "cg", "icc", {}),
+                                    ("gmres(30)+ilu(0)", "gmres", "ilu", {}),
+                                    ("bcgs+sor(1.2)", "bcgs", "sor", {"omega": 1.2})):
+            k2 = build_solver(PETSc, A, kt, pt, **extra)
+            x2 = PETSc.Vec().createSeq(n)
+            k2.solve(bv, x2)
+            m2 = time_solves(torch, k2, bv, x2, 2)
+            methods[name] = {"ms": round(m2, 3), "its": k2.getIterationNumber(),
+                             "reason": k2.getConvergedReason()}
+
+    # ---- CPU baseline (rank 0 at N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sample = 30
+        per_it, _ = cpu_solve_sample(ip, ix, v, b, sample)
+        cpu = {"value": round(per_it * its * 1e3, 3), "unit": "ms", "cores": 1, "kind": "port",
+               "sample": f"{sample} CG+Jacobi iterations of the oracle on this host, scaled to "
+                         f"the {its}-iteration solve"}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": round(ms, 3), "unit": "ms", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 3),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "poisson3d-7pt-128^3 cg+jacobi rtol 1e-10", "n": n, "nnz": nnz,
+                   "iterations": its, "reason": reason, "true_rel_residual": resid,
+                   "l2": "inputs larger than L2 (matrix 217 MB)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": 8 * n,
+                "d2h_bytes_per_step": 8 * n + 1024},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": traffic, "kernel": "k_spmv (CSR fp64/int32)",
+                     "algorithmic_bytes": algo, "launch_us": round(t_spmv * 1e6, 2),
+                     "peak_kind": f"{peak_kind} hbm_gbs"},
+        "cpu_baseline": cpu,
+        "gpu_launches": int(args.steps * (top + trips * body)),
+        "clocks": clocks,
+        "methods": methods,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _csr_matvec(ip, ix, v, x):
+    rows = np.repeat(np.arange(len(ip) - 1), np.diff(ip))
+    return np.bincount(rows, weights=v * x[ix], minlength=len(ip) - 1)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="headline solve only")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--spmv-only", action="store_true", help="SpMV launches only")
+    args = ap.parse_args()
+    world, rank, local, pg = dist_setup()
+    if args.spmv_only:
+        run_spmv_only(args)
+    elif args.impl == "reference":
+        run_reference(args, world, rank, pg)
+    else:
+        run_ours(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

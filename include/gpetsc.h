@@ -182,6 +182,11 @@ int gp_ksp_set_options(gp_ksp ksp, const gp_ksp_options *o);
 int gp_ksp_solve(gp_ksp ksp, gp_mat A, gp_pc pc, const double *b, double *x,
                  gp_ksp_result *result, double *hist, int64_t hist_len, void *stream);
 
+/* Kernel-launch accounting of the last solve: loop trips, kernels outside the
+ * loop (prologue, epilogue) and kernels per trip.  Kernels launched =
+ * top_kernels + trips * body_kernels. */
+int gp_ksp_stats(gp_ksp ksp, int64_t *trips, int64_t *top_kernels, int64_t *body_kernels);
+
 /* ------------------------------------------------------------ mp_* (reference host ABI) */
 /* Mat (src/capi.mojo:32-65) */
 void mp_mat_mult(const double *x, double *y, const int64_t *irow, const int64_t *icol,

@@ -352,4 +352,12 @@ int gp_ksp_solve(gp_ksp ksp, gp_mat A, gp_pc pc, const double* b, double* x,
   })());
 }
 
+int gp_ksp_stats(gp_ksp ksp, int64_t* trips, int64_t* top_kernels, int64_t* body_kernels) {
+  if (!ksp) return bad("gp_ksp_stats: null argument");
+  if (trips) *trips = ksp->k->last_trips;
+  if (top_kernels) *top_kernels = ksp->k->top_kernels;
+  if (body_kernels) *body_kernels = ksp->k->body_kernels;
+  return GP_OK;
+}
+
 }  // extern "C"

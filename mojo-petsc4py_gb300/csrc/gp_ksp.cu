@@ -818,6 +818,7 @@ int ksp_destroy(Ksp* k) {
     if (p) cudaFree(p);
   if (k->h_st) cudaFreeHost(k->h_st);
   if (k->stream) cudaStreamDestroy(k->stream);
+  if (k->stream2) cudaStreamDestroy(k->stream2);
   delete k;
   return GP_OK;
 }
@@ -1231,49 +1232,106 @@ static int fgmres_body(const Run& r, const double* b, double* x) {
 
 // ------------------------------------------------------------------ solve
 
+// The whole solve as one graph: prologue kernels, a WHILE node whose body is
+// one iteration, the epilogue, and the read-back of the state block.
+static int count_kernels(cudaGraph_t g, int64_t* out) {
+  size_t cnt = 0;
+  GP_CUDA(cudaGraphGetNodes(g, nullptr, &cnt));
+  std::vector<cudaGraphNode_t> nodes(cnt);
+  if (cnt) GP_CUDA(cudaGraphGetNodes(g, nodes.data(), &cnt));
+  int64_t k = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType t;
+    GP_CUDA(cudaGraphNodeGetType(nd, &t));
+    if (t == cudaGraphNodeTypeKernel) k++;
+  }
+  *out = k;
+  return GP_OK;
+}
+
 static int capture(const Run& r, const double* b, double* x) {
   Ksp* k = r.k;
   drop_graph(k);
-  GP_CUDA(cudaGraphCreate(&k->graph, 0));
-  cudaGraphConditionalHandle h;
-  GP_CUDA(cudaGraphConditionalHandleCreate(&h, k->graph, 1, cudaGraphCondAssignDefault));
-  cudaGraphNodeParams cp = {};
-  cp.type = cudaGraphNodeTypeConditional;
-  cp.conditional.handle = h;
-  cp.conditional.type = cudaGraphCondTypeWhile;
-  cp.conditional.size = 1;
-  cudaGraphNode_t node;
-  GP_CUDA(cudaGraphAddNode(&node, k->graph, nullptr, nullptr, 0, &cp));
-  cudaGraph_t body = cp.conditional.phGraph_out[0];
-  GP_CUDA(cudaStreamBeginCaptureToGraph(r.s, body, nullptr, nullptr, 0,
-                                        cudaStreamCaptureModeRelaxed));
+  if (!k->stream2) GP_CUDA(cudaStreamCreateWithFlags(&k->stream2, cudaStreamNonBlocking));
+  GP_CUDA(cudaStreamBeginCapture(r.s, cudaStreamCaptureModeRelaxed));
   int st = GP_OK;
   switch (k->opt.type) {
-    case KSP_CG: st = cg_body(r, x); break;
-    case KSP_BCGS: st = bcgs_body(r, x); break;
-    case KSP_GMRES: st = gmres_body(r, b, x); break;
-    case KSP_FGMRES: st = fgmres_body(r, b, x); break;
+    case KSP_CG: st = cg_prologue(r, b, x); break;
+    case KSP_BCGS: st = bcgs_prologue(r, b, x); break;
+    case KSP_GMRES: st = gmres_prologue(r); break;
+    case KSP_FGMRES: st = fgmres_prologue(r, b, x); break;
   }
+  cudaGraph_t graph = nullptr;
+  cudaGraph_t body = nullptr;
+  cudaGraphConditionalHandle h = 0;
   if (st == GP_OK) {
-    k_loop_ctrl<<<1, 1, 0, r.s>>>(h, k->st);
-    cudaError_t e = cudaGetLastError();
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(r.s, &cs, nullptr, &graph, &deps, nullptr, &ndeps);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+    cudaGraphNode_t wnode = nullptr;
+    if (e == cudaSuccess) {
+      cudaGraphNodeParams cp = {};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      e = cudaGraphAddNode(&wnode, graph, deps, nullptr, ndeps, &cp);
+      if (e == cudaSuccess) body = cp.conditional.phGraph_out[0];
+    }
+    if (e == cudaSuccess)
+      e = cudaStreamUpdateCaptureDependencies(r.s, &wnode, nullptr, 1,
+                                              cudaStreamSetCaptureDependencies);
+    if (e == cudaSuccess)
+      e = cudaStreamBeginCaptureToGraph(k->stream2, body, nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeRelaxed);
     if (e != cudaSuccess) {
-      set_error(std::string("loop control launch: ") + cudaGetErrorString(e));
+      set_error(std::string("building the solver graph: ") + cudaGetErrorString(e));
       st = GP_ERR_CUDA;
+    } else {
+      Run rb = r;
+      rb.s = k->stream2;
+      switch (k->opt.type) {
+        case KSP_CG: st = cg_body(rb, x); break;
+        case KSP_BCGS: st = bcgs_body(rb, x); break;
+        case KSP_GMRES: st = gmres_body(rb, b, x); break;
+        case KSP_FGMRES: st = fgmres_body(rb, b, x); break;
+      }
+      if (st == GP_OK) k_loop_ctrl<<<1, 1, 0, k->stream2>>>(h, k->st);
+      cudaGraph_t bout = nullptr;
+      cudaError_t eb = cudaStreamEndCapture(k->stream2, &bout);
+      if (st == GP_OK && eb != cudaSuccess) {
+        set_error(std::string("body capture: ") + cudaGetErrorString(eb));
+        st = GP_ERR_CUDA;
+      }
+    }
+    if (st == GP_OK && k->opt.type == KSP_BCGS) st = bcgs_epilogue(r, x);
+    if (st == GP_OK) {
+      cudaError_t em = cudaMemcpyAsync(k->h_st, k->st, sizeof(KspState), cudaMemcpyDeviceToHost, r.s);
+      if (em != cudaSuccess) {
+        set_error(std::string("state read-back capture: ") + cudaGetErrorString(em));
+        st = GP_ERR_CUDA;
+      }
     }
   }
   cudaGraph_t out = nullptr;
   cudaError_t ec = cudaStreamEndCapture(r.s, &out);
   if (st != GP_OK) {
-    drop_graph(k);
+    if (out) cudaGraphDestroy(out);
     return st;
   }
   if (ec != cudaSuccess) {
     set_error(std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ec));
-    drop_graph(k);
     return GP_ERR_CUDA;
   }
+  k->graph = out;
   GP_CUDA(cudaGraphInstantiate(&k->exec, k->graph, 0));
+  int64_t top = 0, inner = 0;
+  GP_TRY(count_kernels(k->graph, &top));
+  GP_TRY(count_kernels(body, &inner));
+  k->top_kernels = top;
+  k->body_kernels = inner;
   return GP_OK;
 }
 
@@ -1335,29 +1393,20 @@ int ksp_solve(Ksp* k, Csr* A, Pc* pc, const double* b, double* x, KspResult* res
   GP_CUDA(cudaMemcpyAsync(k->st, &h, sizeof(KspState), cudaMemcpyHostToDevice, s));
   GP_CUDA(cudaMemsetAsync(k->hist, 0, (size_t)k->hist_cap * sizeof(double), s));
   Run r{k, A, pc, n, s};
-  // prologue (direct launches)
-  switch (o.type) {
-    case KSP_CG: GP_TRY(cg_prologue(r, b, x)); break;
-    case KSP_BCGS: GP_TRY(bcgs_prologue(r, b, x)); break;
-    case KSP_GMRES: GP_TRY(gmres_prologue(r)); break;
-    case KSP_FGMRES: GP_TRY(fgmres_prologue(r, b, x)); break;
-  }
-  // the loop graph depends on the buffers and the body-shaping options
-  const int key[8] = {o.type, o.normtype, o.pc_side, o.restart, o.cgstype, n, pc->opt.type,
-                      pc->opt.sor_flag};
+  // the solve graph depends on the buffers and on every option that shapes it
+  const int key[10] = {o.type, o.normtype, o.pc_side, o.restart, o.cgstype, n, pc->opt.type,
+                       pc->opt.sor_flag, o.guess_zero, (int)(pc->epoch & 0x7fffffff)};
   const bool same = !moved && k->exec && k->cap_A == A && k->cap_pc == pc &&
-                    std::equal(key, key + 8, k->cap_key) && k->cap_b == b && k->cap_x == x;
+                    std::equal(key, key + 10, k->cap_key) && k->cap_b == b && k->cap_x == x;
   if (!same) {
     GP_TRY(capture(r, b, x));
     k->cap_A = A;
     k->cap_pc = pc;
     k->cap_b = b;
     k->cap_x = x;
-    std::copy(key, key + 8, k->cap_key);
+    std::copy(key, key + 10, k->cap_key);
   }
   GP_CUDA(cudaGraphLaunch(k->exec, s));
-  if (o.type == KSP_BCGS) GP_TRY(bcgs_epilogue(r, x));
-  GP_CUDA(cudaMemcpyAsync(k->h_st, k->st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
   GP_CUDA(cudaEventRecord(ev, s));
   GP_CUDA(cudaStreamWaitEvent(caller, ev, 0));
   GP_CUDA(cudaStreamSynchronize(s));
@@ -1366,6 +1415,7 @@ int ksp_solve(Ksp* k, Csr* A, Pc* pc, const double* b, double* x, KspResult* res
   res->its = h.its;
   res->reason = h.reason;
   res->rnorm = h.rnorm;
+  k->last_trips = h.trips;
   if (hist_out && hist_len > 0) {
     const int64_t cnt = std::min<int64_t>(hist_len, std::min<int64_t>(h.its + 1, k->hist_cap));
     GP_CUDA(cudaMemcpy(hist_out, k->hist, (size_t)cnt * sizeof(double), cudaMemcpyDeviceToHost));

@@ -359,3 +359,10 @@ class KSP:
         self._reason = int(res.reason)
         self._rnorm = float(res.rnorm)
         self._history = hist
+
+    def getLaunchStats(self):
+        """(loop trips, kernels outside the loop, kernels per trip) of the last
+        solve; kernels launched = outside + trips * per_trip."""
+        t, a, b = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        check(lib().gp_ksp_stats(self._gp, ctypes.byref(t), ctypes.byref(a), ctypes.byref(b)))
+        return (t.value, a.value, b.value)
