@@ -396,7 +396,12 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline solve only")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--spmv-only", action="store_true", help="SpMV launches only")
+    ap.add_argument("--max-it", type=int, default=None,
+                    help="cap the iterations (profiling runs only; not a bench value)")
     args = ap.parse_args()
+    if args.max_it is not None:
+        global MAX_IT
+        MAX_IT = args.max_it
     world, rank, local, pg = dist_setup()
     if args.spmv_only:
         run_spmv_only(args)

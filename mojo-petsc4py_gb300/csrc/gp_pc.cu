@@ -412,7 +412,7 @@ static int dalloc(double** p, int64_t n) {
 
 static void free_all(Pc* pc) {
   void* ptrs[] = {pc->diag, pc->diagsqrt, pc->idiag, pc->mdiag, pc->bi, pc->bj, pc->bdiag,
-                  pc->perm_r, pc->perm_ic, pc->ba, pc->ba_orig, pc->done, pc->cptr, pc->crow,
+                  pc->perm_r, pc->perm_c, pc->perm_ic, pc->ba, pc->ba_orig, pc->done, pc->cptr, pc->crow,
                   pc->cslot, pc->tptr, pc->trow, pc->tslot, pc->amap, pc->fwd.order,
                   pc->bwd.order, pc->num.order, pc->yf, pc->yb, pc->ys, pc->t, pc->tickets,
                   pc->err};
@@ -517,19 +517,46 @@ static int perms(Pc* pc, std::vector<int>& r, std::vector<int>& ic) {
   return GP_OK;
 }
 
-static int setup_ilu(Pc* pc, cudaStream_t s) {
-  const Csr* A = pc->A;
-  const int n = A->n;
-  std::vector<int> r, ic;
-  GP_TRY(perms(pc, r, ic));
+// Sweep plans and device arrays of an ILU factor whose pattern is in pc->pat
+// (the reference layout).  Used after the symbolic phase and when a factor is
+// imported as it is.
+static int ilu_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
+  const int n = pc->n;
   FactorPattern& P = pc->pat;
-  GP_TRY(ilu_symbolic(A, pc->opt.levels, r, ic, P));
-  // A slot -> factor slot of row ic[row]
+  std::vector<int> lp(n + 1), lc(P.bj.begin(), P.bj.begin() + P.bi[n]);
+  for (int i = 0; i <= n; i++) lp[i] = P.bi[i];
+  std::vector<int> up(n + 1, 0), uc;
+  uc.reserve(std::max(P.nnz - P.bi[n], 0));
+  for (int i = 0; i < n; i++) {
+    for (int j = P.bdiag[i + 1] + 1; j < P.bdiag[i]; j++) uc.push_back(P.bj[j]);
+    up[i + 1] = (int)uc.size();
+  }
+  GP_TRY(plan(pc->fwd, n, lp, lc, true, s));
+  GP_TRY(plan(pc->bwd, n, up, uc, false, s));
+  GP_TRY(upload(&pc->bi, P.bi, s));
+  GP_TRY(upload(&pc->bj, P.bj, s));
+  GP_TRY(upload(&pc->bdiag, P.bdiag, s));
+  GP_TRY(upload(&pc->perm_r, P.r, s));
+  GP_TRY(upload(&pc->perm_c, perm_c, s));
+  GP_TRY(upload(&pc->perm_ic, P.ic, s));
+  GP_TRY(dalloc(&pc->ba, std::max(P.nnz, 1)));
+  GP_CUDA(cudaMalloc(&pc->done, std::max(n, 1) * sizeof(int)));
+  GP_CUDA(cudaMemsetAsync(pc->done, 0, std::max(n, 1) * sizeof(int), s));
+  GP_TRY(dalloc(&pc->yf, n));
+  GP_TRY(dalloc(&pc->yb, n));
+  GP_CUDA(cudaStreamSynchronize(s));  // host vectors above go out of scope
+  return GP_OK;
+}
+
+// A slot -> factor slot, for the numeric factorisation from A's values.
+static int ilu_amap(Pc* pc, const Csr* A, cudaStream_t s) {
+  const int n = A->n;
+  const FactorPattern& P = pc->pat;
   std::vector<int> amap(std::max<int64_t>(A->nnz, 1), -1);
   for (int i = 0; i < n; i++) {
-    const int ri = r[i];
+    const int ri = P.r[i];
     for (int j = A->h_rowptr[ri]; j < A->h_rowptr[ri + 1]; j++) {
-      const int c = ic[A->h_colind[j]];
+      const int c = P.ic[A->h_colind[j]];
       int lo, hi;
       if (c < i) {
         lo = P.bi[i];
@@ -545,58 +572,34 @@ static int setup_ilu(Pc* pc, cudaStream_t s) {
       if (it != P.bj.begin() + hi && *it == c) amap[j] = (int)(it - P.bj.begin());
     }
   }
-  // dependency lists: forward / numeric = L columns, backward = U columns
-  std::vector<int> lp(n + 1), lc(P.bj.begin(), P.bj.begin() + P.bi[n]);
-  for (int i = 0; i <= n; i++) lp[i] = P.bi[i];
-  std::vector<int> up(n + 1, 0), uc;
-  uc.reserve(P.nnz - P.bi[n]);
-  for (int i = 0; i < n; i++) {
-    for (int j = P.bdiag[i + 1] + 1; j < P.bdiag[i]; j++) uc.push_back(P.bj[j]);
-    up[i + 1] = (int)uc.size();
-  }
-  GP_TRY(plan(pc->fwd, n, lp, lc, true, s));
-  GP_TRY(plan(pc->bwd, n, up, uc, false, s));
-  GP_TRY(upload(&pc->bi, P.bi, s));
-  GP_TRY(upload(&pc->bj, P.bj, s));
-  GP_TRY(upload(&pc->bdiag, P.bdiag, s));
-  GP_TRY(upload(&pc->perm_r, r, s));
-  GP_TRY(upload(&pc->perm_ic, ic, s));
+  if (pc->amap) cudaFree(pc->amap);
+  pc->amap = nullptr;
   GP_TRY(upload(&pc->amap, amap, s));
-  GP_TRY(dalloc(&pc->ba, std::max(P.bdiag[0] + 1, 1)));
-  GP_CUDA(cudaMalloc(&pc->done, std::max(n, 1) * sizeof(int)));
-  GP_CUDA(cudaMemsetAsync(pc->done, 0, std::max(n, 1) * sizeof(int), s));
-  GP_TRY(dalloc(&pc->yf, n));
-  GP_TRY(dalloc(&pc->yb, n));
-  GP_CUDA(cudaStreamSynchronize(s));  // host vectors above go out of scope
+  GP_CUDA(cudaStreamSynchronize(s));
   return GP_OK;
 }
 
-static int setup_icc(Pc* pc, cudaStream_t s) {
+static int setup_ilu(Pc* pc, cudaStream_t s) {
   const Csr* A = pc->A;
-  const int n = A->n;
   std::vector<int> r, ic;
   GP_TRY(perms(pc, r, ic));
+  GP_TRY(ilu_symbolic(A, pc->opt.levels, r, ic, pc->pat));
+  // the factor lives in the permuted ordering; the solution is mapped back
+  // with the row ordering itself (python/mojopetsc4py/PETSc/PC.py:434-437)
+  GP_TRY(ilu_prepare(pc, r, s));
+  return ilu_amap(pc, A, s);
+}
+
+// Plans and device arrays of an IC factor in pc->pat: the transposed strict
+// pattern (forward sweep), the contributor lists in the order the
+// reference's il/c2r chains visit them (numeric factorisation), the strict
+// rows (backward sweep).
+static int icc_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
+  const int n = pc->n;
   FactorPattern& P = pc->pat;
-  GP_TRY(icc_symbolic(A, pc->opt.levels, r, ic, P));
-  std::vector<int> amap(std::max<int64_t>(A->nnz, 1), -1);
-  for (int k = 0; k < n; k++) {
-    const int rk = r[k];
-    for (int j = A->h_rowptr[rk]; j < A->h_rowptr[rk + 1]; j++) {
-      const int c = ic[A->h_colind[j]];
-      if (c < k) continue;
-      if (c == k) {
-        amap[j] = P.bdiag[k];
-        continue;
-      }
-      auto it = std::lower_bound(P.bj.begin() + P.bi[k], P.bj.begin() + P.bdiag[k], c);
-      if (it != P.bj.begin() + P.bdiag[k] && *it == c) amap[j] = (int)(it - P.bj.begin());
-    }
-  }
-  // contributor lists in the reference's il/c2r chain order
-  // (src/ported.mojo:1040-1124), simulated on the pattern alone
   std::vector<int> c2r(n, n), il(n, 0), cptr(n + 1, 0), crow, cslot;
   std::vector<std::vector<std::pair<int, int>>> visits(n);
-  for (int k = 0; k < n; k++) {
+  for (int k = 0; k < n; k++) {  // src/ported.mojo:1040-1124 on the pattern alone
     int i = c2r[k];
     while (i < k) {
       const int nexti = c2r[i];
@@ -626,7 +629,6 @@ static int setup_icc(Pc* pc, cudaStream_t s) {
     }
     cptr[k + 1] = (int)crow.size();
   }
-  // transposed strict pattern, ascending source row (forward sweep order)
   std::vector<int> tptr(n + 1, 0), trow(std::max(P.nnz - n, 1)), tslot(std::max(P.nnz - n, 1));
   for (int i = 0; i < n; i++)
     for (int j = P.bi[i]; j < P.bdiag[i]; j++) tptr[P.bj[j] + 1]++;
@@ -653,9 +655,9 @@ static int setup_icc(Pc* pc, cudaStream_t s) {
   GP_TRY(upload(&pc->bi, P.bi, s));
   GP_TRY(upload(&pc->bj, P.bj, s));
   GP_TRY(upload(&pc->bdiag, P.bdiag, s));
-  GP_TRY(upload(&pc->perm_r, r, s));
-  GP_TRY(upload(&pc->perm_ic, ic, s));
-  GP_TRY(upload(&pc->amap, amap, s));
+  GP_TRY(upload(&pc->perm_r, P.r, s));
+  GP_TRY(upload(&pc->perm_c, perm_c, s));
+  GP_TRY(upload(&pc->perm_ic, P.ic, s));
   GP_TRY(upload(&pc->cptr, cptr, s));
   GP_TRY(upload(&pc->crow, crow, s));
   GP_TRY(upload(&pc->cslot, cslot, s));
@@ -673,8 +675,41 @@ static int setup_icc(Pc* pc, cudaStream_t s) {
   return GP_OK;
 }
 
+static int icc_amap(Pc* pc, const Csr* A, cudaStream_t s) {
+  const int n = A->n;
+  const FactorPattern& P = pc->pat;
+  std::vector<int> amap(std::max<int64_t>(A->nnz, 1), -1);
+  for (int k = 0; k < n; k++) {
+    const int rk = P.r[k];
+    for (int j = A->h_rowptr[rk]; j < A->h_rowptr[rk + 1]; j++) {
+      const int c = P.ic[A->h_colind[j]];
+      if (c < k) continue;
+      if (c == k) {
+        amap[j] = P.bdiag[k];
+        continue;
+      }
+      auto it = std::lower_bound(P.bj.begin() + P.bi[k], P.bj.begin() + P.bdiag[k], c);
+      if (it != P.bj.begin() + P.bdiag[k] && *it == c) amap[j] = (int)(it - P.bj.begin());
+    }
+  }
+  if (pc->amap) cudaFree(pc->amap);
+  pc->amap = nullptr;
+  GP_TRY(upload(&pc->amap, amap, s));
+  GP_CUDA(cudaStreamSynchronize(s));
+  return GP_OK;
+}
+
+static int setup_icc(Pc* pc, cudaStream_t s) {
+  const Csr* A = pc->A;
+  std::vector<int> r, ic;
+  GP_TRY(perms(pc, r, ic));
+  GP_TRY(icc_symbolic(A, pc->opt.levels, r, ic, pc->pat));
+  GP_TRY(icc_prepare(pc, r, s));
+  return icc_amap(pc, A, s);
+}
+
 // Numeric factorisation on the device for the current values of A.
-static int factor_numeric(Pc* pc, cudaStream_t s) {
+int pc_factor_numeric(Pc* pc, cudaStream_t s) {
   const Csr* A = pc->A;
   const int n = A->n;
   if (n == 0) return GP_OK;
@@ -727,11 +762,11 @@ int pc_setup(Pc* pc, Csr* A, cudaStream_t s) {
     case PC_SOR: GP_TRY(setup_sor(pc, s)); break;
     case PC_ILU:
       GP_TRY(setup_ilu(pc, s));
-      GP_TRY(factor_numeric(pc, s));
+      GP_TRY(pc_factor_numeric(pc, s));
       break;
     case PC_ICC:
       GP_TRY(setup_icc(pc, s));
-      GP_TRY(factor_numeric(pc, s));
+      GP_TRY(pc_factor_numeric(pc, s));
       break;
     default: set_error("unsupported PC type"); return GP_ERR_UNSUPPORTED;
   }
@@ -779,15 +814,15 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
       k_ilu_fwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->fwd.order, tk0, pc->bi, pc->bj,
                                            pc->ba, pc->perm_r, x, pc->yf, pc->err);
       k_ilu_bwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->bwd.order, tk1, pc->bj, pc->ba,
-                                           pc->bdiag, pc->perm_r, pc->yf, pc->yb, y, pc->err);
+                                           pc->bdiag, pc->perm_c, pc->yf, pc->yb, y, pc->err);
       break;
     case PC_ICC:
       k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
       k_icc_fwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->fwd.order, tk0, pc->tptr,
-                                           pc->trow, pc->tslot, pc->ba, pc->bdiag, pc->perm_r, x,
+                                           pc->trow, pc->tslot, pc->ba, pc->bdiag, pc->perm_c, x,
                                            pc->yf, pc->ys, pc->err);
       k_icc_bwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->bwd.order, tk1, pc->bi, pc->bj,
-                                           pc->ba, pc->bdiag, pc->perm_r, pc->ys, pc->yb, y,
+                                           pc->ba, pc->bdiag, pc->perm_c, pc->ys, pc->yb, y,
                                            pc->err);
       break;
     default: set_error("unsupported PC type"); return GP_ERR_UNSUPPORTED;
@@ -805,6 +840,83 @@ int pc_apply_symmetric(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, 
     return GP_OK;
   }
   return pc_apply(pc, x, y, s, gate, want);
+}
+
+// A factor handed over in the reference's layout (the mp_* ABI): the pattern
+// and optionally its values, with the plans for the device sweeps.  When A is
+// given, the A-slot map for a numeric factorisation is built too.
+int pc_import_factor(Pc* pc, int type, const FactorPattern& pat, const std::vector<int>& perm_c,
+                     const double* ba_host, Csr* A, cudaStream_t s) {
+  free_all(pc);
+  pc->opt.type = type;
+  pc->n = (int)pat.bi.size() - 1;
+  pc->A = A;
+  pc->pat = pat;
+  GP_CUDA(cudaGetDevice(&pc->device));
+  GP_CUDA(cudaMalloc(&pc->err, sizeof(DevErr)));
+  GP_CUDA(cudaMemsetAsync(pc->err, 0, sizeof(DevErr), s));
+  GP_CUDA(cudaMalloc(&pc->tickets, 4 * sizeof(unsigned)));
+  GP_CUDA(cudaMemsetAsync(pc->tickets, 0, 4 * sizeof(unsigned), s));
+  if (type == PC_ILU) {
+    GP_TRY(ilu_prepare(pc, perm_c, s));
+    if (A) GP_TRY(ilu_amap(pc, A, s));
+  } else if (type == PC_ICC) {
+    GP_TRY(icc_prepare(pc, perm_c, s));
+    if (A) GP_TRY(icc_amap(pc, A, s));
+  } else {
+    set_error("pc_import_factor: ILU or IC only");
+    return GP_ERR_ARG;
+  }
+  if (ba_host && pat.nnz)
+    GP_CUDA(cudaMemcpyAsync(pc->ba, ba_host, (size_t)pat.nnz * sizeof(double),
+                            cudaMemcpyHostToDevice, s));
+  GP_CUDA(cudaStreamSynchronize(s));
+  pc->ready = true;
+  return GP_OK;
+}
+
+// Jacobi with its diagonals given (the reference's pci block carries them).
+int pc_import_jacobi(Pc* pc, int n, const double* diag, const double* diagsqrt, cudaStream_t s) {
+  free_all(pc);
+  pc->opt.type = PC_JACOBI;
+  pc->n = n;
+  GP_CUDA(cudaGetDevice(&pc->device));
+  GP_CUDA(cudaMalloc(&pc->err, sizeof(DevErr)));
+  GP_CUDA(cudaMemsetAsync(pc->err, 0, sizeof(DevErr), s));
+  GP_CUDA(cudaMalloc(&pc->tickets, 4 * sizeof(unsigned)));
+  GP_CUDA(cudaMemsetAsync(pc->tickets, 0, 4 * sizeof(unsigned), s));
+  GP_TRY(dalloc(&pc->diag, n));
+  GP_TRY(dalloc(&pc->diagsqrt, n));
+  if (n) {
+    GP_CUDA(cudaMemcpyAsync(pc->diag, diag, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (diagsqrt)
+      GP_CUDA(cudaMemcpyAsync(pc->diagsqrt, diagsqrt, (size_t)n * sizeof(double),
+                              cudaMemcpyHostToDevice, s));
+  }
+  GP_CUDA(cudaStreamSynchronize(s));
+  pc->ready = true;
+  return GP_OK;
+}
+
+// Jacobi set-up kernels into caller device buffers (the mp_* set-up entries).
+int jacobi_fill(const Csr* A, int jtype, int sym, int use_abs, int fix_diag, double scale,
+                double* out, cudaStream_t s) {
+  const int n = A->n;
+  if (!n) return GP_OK;
+  k_jacobi_fill<<<(n + 255) / 256, 256, 0, s>>>(n, jtype, sym, use_abs, fix_diag, scale,
+                                                A->rowptr, A->val, A->diagpos, out);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+// SOR diagonals for the current values (MatInvertDiagonalForSOR_SeqAIJ).
+int sor_diagonals(Pc* pc, cudaStream_t s) {
+  const int n = pc->n;
+  if (!n) return GP_OK;
+  k_sor_diag<<<(n + 255) / 256, 256, 0, s>>>(n, pc->opt.omega, pc->opt.fshift, pc->A->diagpos,
+                                              pc->A->val, pc->idiag, pc->mdiag);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
 }
 
 }  // namespace gp

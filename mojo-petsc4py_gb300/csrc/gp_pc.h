@@ -65,6 +65,7 @@ struct Pc {
   int* bj = nullptr;
   int* bdiag = nullptr;
   int* perm_r = nullptr;
+  int* perm_c = nullptr;     // where row i of the factor's solution goes
   int* perm_ic = nullptr;
   double* ba = nullptr;      // factor values (what the solve reads)
   double* ba_orig = nullptr; // IC: unscaled strict rows
@@ -100,9 +101,23 @@ int pc_apply_symmetric(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate =
 // Read and clear the device error word (spin timeouts).  Synchronizes s.
 int pc_check(Pc* pc, cudaStream_t s);
 
+int pc_factor_numeric(Pc* pc, cudaStream_t s);
+int pc_import_factor(Pc* pc, int type, const FactorPattern& pat, const std::vector<int>& perm_c,
+                     const double* ba_host, Csr* A, cudaStream_t s);
+int pc_import_jacobi(Pc* pc, int n, const double* diag, const double* diagsqrt, cudaStream_t s);
+int jacobi_fill(const Csr* A, int jtype, int sym, int use_abs, int fix_diag, double scale,
+                double* out, cudaStream_t s);
+int sor_diagonals(Pc* pc, cudaStream_t s);
+
 // host analysis (gp_pcsetup.cu)
 int rcm_order(const std::vector<int>& rowptr, const std::vector<int>& colind, int n,
               std::vector<int>& perm);
+int ilu_symbolic_rows(const Csr* A, int levels, const std::vector<int>& r,
+                      const std::vector<int>& ic,
+                      std::vector<std::vector<std::pair<int, int>>>& rows, std::vector<int>& nL);
+int icc_symbolic_rows(const Csr* A, int levels, const std::vector<int>& r,
+                      const std::vector<int>& ic,
+                      std::vector<std::vector<std::pair<int, int>>>& rows);
 int ilu_symbolic(const Csr* A, int levels, const std::vector<int>& r,
                  const std::vector<int>& ic, FactorPattern& out);
 int icc_symbolic(const Csr* A, int levels, const std::vector<int>& r,

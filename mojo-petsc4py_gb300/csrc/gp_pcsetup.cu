@@ -52,14 +52,16 @@ int rcm_order(const std::vector<int>& rowptr, const std::vector<int>& colind, in
   return GP_OK;
 }
 
-int ilu_symbolic(const Csr* A, int levels, const std::vector<int>& r, const std::vector<int>& ic,
-                 FactorPattern& out) {
+// Rows of the ILU(levels) pattern: ascending (column, level) pairs of each
+// permuted row, and the count of strictly lower entries in nL.
+int ilu_symbolic_rows(const Csr* A, int levels, const std::vector<int>& r,
+                      const std::vector<int>& ic,
+                      std::vector<std::vector<std::pair<int, int>>>& rows, std::vector<int>& nL) {
   const int n = A->n;
   const auto& rp = A->h_rowptr;
   const auto& ci = A->h_colind;
-  // staged rows: ascending columns with levels; nL[i] = strictly lower count
-  std::vector<std::vector<std::pair<int, int>>> rows(n);
-  std::vector<int> nL(n, 0);
+  rows.assign(n, {});
+  nL.assign(n, 0);
   for (int i = 0; i < n; i++) {
     std::map<int, int> row;
     const int ri = r[i];
@@ -89,6 +91,15 @@ int ilu_symbolic(const Csr* A, int levels, const std::vector<int>& r, const std:
     while (cnt < (int)rows[i].size() && rows[i][cnt].first < i) cnt++;
     nL[i] = cnt;
   }
+  return GP_OK;
+}
+
+int ilu_symbolic(const Csr* A, int levels, const std::vector<int>& r, const std::vector<int>& ic,
+                 FactorPattern& out) {
+  const int n = A->n;
+  std::vector<std::vector<std::pair<int, int>>> rows;
+  std::vector<int> nL;
+  GP_TRY(ilu_symbolic_rows(A, levels, r, ic, rows, nL));
   // reference layout
   out.bi.assign(n + 1, 0);
   int64_t total = 0;
@@ -119,12 +130,15 @@ int ilu_symbolic(const Csr* A, int levels, const std::vector<int>& r, const std:
   return GP_OK;
 }
 
-int icc_symbolic(const Csr* A, int levels, const std::vector<int>& r, const std::vector<int>& ic,
-                 FactorPattern& out) {
+// Rows of the IC(levels) pattern: the strictly upper (column, level) pairs of
+// each permuted row, ascending.
+int icc_symbolic_rows(const Csr* A, int levels, const std::vector<int>& r,
+                      const std::vector<int>& ic,
+                      std::vector<std::vector<std::pair<int, int>>>& rows) {
   const int n = A->n;
   const auto& rp = A->h_rowptr;
   const auto& ci = A->h_colind;
-  std::vector<std::vector<std::pair<int, int>>> rows(n);  // strict upper (col, level)
+  rows.assign(n, {});
   std::vector<std::vector<std::pair<int, int>>> colsrc(n);  // column k <- (prow, level)
   for (int k = 0; k < n; k++) {
     std::map<int, int> row;
@@ -151,6 +165,14 @@ int icc_symbolic(const Csr* A, int levels, const std::vector<int>& r, const std:
     rows[k].assign(row.begin(), row.end());
     for (const auto& e : rows[k]) colsrc[e.first].emplace_back(k, e.second);
   }
+  return GP_OK;
+}
+
+int icc_symbolic(const Csr* A, int levels, const std::vector<int>& r, const std::vector<int>& ic,
+                 FactorPattern& out) {
+  const int n = A->n;
+  std::vector<std::vector<std::pair<int, int>>> rows;
+  GP_TRY(icc_symbolic_rows(A, levels, r, ic, rows));
   out.bi.assign(n + 1, 0);
   int64_t total = 0;
   for (int k = 0; k < n; k++) total += rows[k].size() + 1;

@@ -1,0 +1,211 @@
+"""Device-resident Krylov solves against the CPU oracle on identical inputs.
+
+Parity bar: the same converged reason, the same iteration count for cg,
+gmres and fgmres, and the iterate within 1e-10 relative.  BiCGStab's
+iteration count is decided by which of two nearly equal residual estimates
+crosses rtol first, so it moves with the reduction order; it is held to the
+reference's own bound for that case (|difference| <= 20 iterations,
+iterate within 1e-8: tests/test_ksp_parity.py:264-283 of the reference)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import dense_to_csr, nonsym_banded, oracle_solve, spd_dense, tridiag_dense
+from mojopetsc4py import PETSc, gallery
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "published.json")))
+
+
+def solve_gpu(kt, pt, ip, ix, v, b, x0=None, pc_opts=None, ksp_opts=None, tol=None):
+    n = len(ip) - 1
+    A = PETSc.Mat().createSeqAIJ((n, n))
+    A.setValuesCSR(ip, ix, v)
+    A.assemble()
+    pc = PETSc.PC().create()
+    pc.setType(pt)
+    for k, val in (pc_opts or {}).items():
+        getattr(pc, k)(val)
+    pc.setOperators(A)
+    ksp = PETSc.KSP().create()
+    ksp.setPC(pc)
+    ksp.setType(kt)
+    ksp.setOperators(A)
+    ksp.setTolerances(**(tol or dict(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=2000)))
+    for k, val in (ksp_opts or {}).items():
+        getattr(ksp, k)(val)
+    ksp.setConvergenceHistory()
+    bv = PETSc.Vec().createWithArray(b)
+    xv = PETSc.Vec().createSeq(n)
+    if x0 is not None:
+        xv.setArray(x0)
+        ksp.setInitialGuessNonzero(True)
+    ksp.solve(bv, xv)
+    return {"x": xv.getArray().copy(), "its": ksp.getIterationNumber(),
+            "reason": ksp.getConvergedReason(), "rnorm": ksp.getResidualNorm(),
+            "history": ksp.getConvergenceHistory().copy()}
+
+
+def check(g, r, kt):
+    assert g["reason"] == r["reason"]
+    rel = np.linalg.norm(g["x"] - r["x"]) / max(np.linalg.norm(r["x"]), 1e-300)
+    if kt == "bcgs":
+        assert abs(g["its"] - r["its"]) <= GOLD["bcgs_tolerance"]
+        assert rel < 1e-8
+    else:
+        assert g["its"] == r["its"]
+        assert rel <= 1e-10
+        h = g["history"][: g["its"] + 1]
+        np.testing.assert_allclose(h, r["history"], rtol=1e-8, atol=1e-300)
+
+
+KTS = ["cg", "gmres", "fgmres", "bcgs"]
+PTS = ["none", "jacobi", "sor", "ilu", "icc"]
+
+
+@pytest.mark.parametrize("kt", KTS)
+@pytest.mark.parametrize("pt", PTS)
+def test_laplacian_matrix_of_methods(kt, pt):
+    ip, ix, v = gallery.laplacian_2d(32)
+    b = np.random.default_rng(5).normal(size=1024)
+    tol = dict(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=2000)
+    check(solve_gpu(kt, pt, ip, ix, v, b, tol=tol), oracle_solve(kt, ip, ix, v, b, pt, **tol), kt)
+
+
+@pytest.mark.parametrize("kt", ["gmres", "fgmres", "bcgs"])
+@pytest.mark.parametrize("pt", ["none", "jacobi", "sor", "ilu"])
+def test_nonsymmetric_convection_diffusion(kt, pt):
+    ip, ix, v = gallery.convection_diffusion_3d(10)
+    b = np.random.default_rng(7).uniform(-1, 1, 1000)
+    tol = dict(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=2000)
+    check(solve_gpu(kt, pt, ip, ix, v, b, tol=tol), oracle_solve(kt, ip, ix, v, b, pt, **tol), kt)
+
+
+@pytest.mark.parametrize("key", list(GOLD["iterations"]))
+def test_published_iteration_counts_on_gpu(key):
+    kt, pt = key.split("+")
+    for k, want in GOLD["iterations"][key].items():
+        k = int(k)
+        if k > 64 and kt in ("gmres", "fgmres"):
+            continue
+        ip, ix, v = gallery.laplacian_2d(k)
+        b = np.random.default_rng(5).normal(size=k * k)
+        g = solve_gpu(kt, pt, ip, ix, v, b)
+        if kt == "bcgs":
+            assert abs(g["its"] - want) <= GOLD["bcgs_tolerance"]
+        else:
+            assert g["its"] == want, (key, k)
+
+
+def test_readme_example_on_gpu():
+    ex = GOLD["readme_example"]
+    d = tridiag_dense(ex["n"])
+    ip, ix, v = dense_to_csr(d)
+    g = solve_gpu("cg", "ilu", ip, ix, v, np.ones(ex["n"]),
+                  tol=dict(rtol=ex["rtol"], max_it=ex["max_it"]))
+    assert g["its"] == ex["its"]
+    assert np.linalg.norm(np.ones(ex["n"]) - d @ g["x"]) < 1e-14
+
+
+@pytest.mark.parametrize("kt", KTS)
+def test_nonzero_initial_guess(kt):
+    d = spd_dense(60, 9)
+    ip, ix, v = dense_to_csr(d)
+    b = np.random.default_rng(10).normal(size=60)
+    x0 = np.random.default_rng(11).normal(size=60)
+    tol = dict(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=500)
+    check(solve_gpu(kt, "jacobi", ip, ix, v, b, x0=x0, tol=tol),
+          oracle_solve(kt, ip, ix, v, b, "jacobi", x0=x0, **tol), kt)
+
+
+@pytest.mark.parametrize("kt", ["gmres", "bcgs"])
+@pytest.mark.parametrize("side", [1, 2])
+def test_pc_side(kt, side):
+    d = nonsym_banded(80, 3)
+    ip, ix, v = dense_to_csr(d)
+    b = np.random.default_rng(12).normal(size=80)
+    pt = "jacobi" if side == 2 else "ilu"
+    tol = dict(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=500)
+    check(solve_gpu(kt, pt, ip, ix, v, b, ksp_opts={"setPCSide": side}, tol=tol),
+          oracle_solve(kt, ip, ix, v, b, pt, pc_side=side, **tol), kt)
+
+
+@pytest.mark.parametrize("normtype", [1, 3, 4])
+def test_cg_norm_types(normtype):
+    ip, ix, v = gallery.laplacian_2d(16)
+    b = np.random.default_rng(13).normal(size=256)
+    tol = dict(rtol=1e-8, atol=1e-50, divtol=1e30, max_it=300)
+    g = solve_gpu("cg", "icc", ip, ix, v, b, ksp_opts={"setNormType": normtype}, tol=tol)
+    r = oracle_solve("cg", ip, ix, v, b, "icc", normtype=normtype, **tol)
+    check(g, r, "cg")
+
+
+@pytest.mark.parametrize("cgstype", [1, 2])
+@pytest.mark.parametrize("restart", [5, 30])
+def test_gmres_refinement_and_restart(cgstype, restart):
+    ip, ix, v = gallery.laplacian_2d(11)
+    b = np.random.default_rng(3).normal(size=121)
+    opts = {"setGMRESCGSRefinementType": cgstype, "setGMRESRestart": restart}
+    tol = dict(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=2000)
+    g = solve_gpu("gmres", "none", ip, ix, v, b, ksp_opts=opts, tol=tol)
+    r = oracle_solve("gmres", ip, ix, v, b, "none", restart=restart, cgstype=cgstype, **tol)
+    check(g, r, "gmres")
+
+
+def test_max_it_reports_converged_its():
+    ip, ix, v = gallery.laplacian_2d(32)
+    b = np.random.default_rng(5).normal(size=1024)
+    for kt in KTS:
+        g = solve_gpu(kt, "none", ip, ix, v, b, tol=dict(rtol=1e-12, max_it=7))
+        assert g["reason"] == PETSc.KSP.ConvergedReason.CONVERGED_ITS
+        assert g["its"] == 7
+
+
+def test_nan_rhs_reports_nanorinf():
+    ip, ix, v = gallery.laplacian_2d(8)
+    b = np.ones(64)
+    b[5] = np.nan
+    for kt in KTS:
+        g = solve_gpu(kt, "jacobi", ip, ix, v, b)
+        assert g["reason"] == PETSc.KSP.ConvergedReason.DIVERGED_NANORINF
+
+
+def test_zero_pivot_gives_nanorinf():
+    # ILU(0) of [[1, 1], [1, 1]] has U(1,1) = 1 - 1 * 1 = 0: the inverted
+    # pivot is inf, and the solve reports a NaN/inf residual (no shift)
+    d = np.array([[1.0, 1.0, 0.0], [1.0, 1.0, 0.0], [0.0, 0.0, 2.0]])
+    ip, ix, v = dense_to_csr(d)
+    b = np.ones(3)
+    r = oracle_solve("gmres", ip, ix, v, b, "ilu", rtol=1e-10, max_it=50)
+    g = solve_gpu("gmres", "ilu", ip, ix, v, b, tol=dict(rtol=1e-10, max_it=50))
+    assert g["reason"] == r["reason"] == PETSc.KSP.ConvergedReason.DIVERGED_NANORINF
+
+
+def test_poisson3d_64_cg_jacobi_parity():
+    ip, ix, v = gallery.laplacian_3d(64)
+    b = np.random.default_rng(5).uniform(-1, 1, 64 ** 3)
+    tol = dict(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=10000)
+    check(solve_gpu("cg", "jacobi", ip, ix, v, b, tol=tol),
+          oracle_solve("cg", ip, ix, v, b, "jacobi", **tol), "cg")
+
+
+def test_repeated_solves_reuse_the_graph():
+    ip, ix, v = gallery.laplacian_2d(16)
+    n = 256
+    A = PETSc.Mat().createSeqAIJ((n, n))
+    A.setValuesCSR(ip, ix, v)
+    ksp = PETSc.KSP().create()
+    ksp.setType("cg")
+    ksp.setOperators(A)
+    ksp.getPC().setType("jacobi")
+    ksp.setTolerances(rtol=1e-10, max_it=500)
+    xs = []
+    for seed in (1, 2, 1):
+        b = PETSc.Vec().createWithArray(np.random.default_rng(seed).normal(size=n))
+        x = PETSc.Vec().createSeq(n)
+        ksp.solve(b, x)
+        xs.append(x.getArray().copy())
+    np.testing.assert_array_equal(xs[0], xs[2])

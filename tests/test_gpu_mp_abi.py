@@ -1,0 +1,246 @@
+"""The reference's host ABI (mp_*) as exported by libgpetsc.so, called exactly
+as the reference's tests call it, against the oracle's mp_* on the same
+arguments (tests/test_exported_kernels.py of the reference is the model)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import dense_to_csr, spd_dense, tridiag_dense
+from mojopetsc4py import _lib, gallery
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def G():
+    lib = ctypes.CDLL(_lib.LIB)
+    for name, (argtypes, restype) in O.SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = argtypes
+        fn.restype = restype
+    lib.mp_last_status.restype = ctypes.c_int
+    return lib
+
+
+def a(x):
+    return x.ctypes.data
+
+
+def both(G, name, *args_factory):
+    """Run `name` on both libraries with fresh copies of the arguments."""
+    outs = []
+    for lib in (G, O.lib()):
+        args = [x.copy() if isinstance(x, np.ndarray) else x for x in args_factory]
+        ret = getattr(lib, name)(*[a(x) if isinstance(x, np.ndarray) else x for x in args])
+        outs.append((ret, args))
+    assert G.mp_last_status() == 0
+    return outs
+
+
+def test_vec_entries(G):
+    rng = np.random.default_rng(0)
+    n = 1000
+    x, y, w = rng.normal(size=n), rng.normal(size=n) + 3, rng.normal(size=n)
+    for name in ("mp_vec_pointwise_mult", "mp_vec_pointwise_divide", "mp_vec_pointwise_min",
+                 "mp_vec_pointwise_max", "mp_vec_pointwise_max_abs"):
+        (_, g), (_, o) = both(G, name, w, x, y, n)
+        np.testing.assert_array_equal(g[0], o[0], err_msg=name)
+    for name, extra in (("mp_vec_axpy", (1.5,)), ("mp_vec_aypx", (-0.5,)),
+                        ("mp_vec_axpby", (2.0, 0.25))):
+        (_, g), (_, o) = both(G, name, w, *extra, x, n)
+        np.testing.assert_array_equal(g[0], o[0], err_msg=name)
+    (_, g), (_, o) = both(G, "mp_vec_axpbypcz", w, 1.0, -2.0, 0.5, x, y, n)
+    np.testing.assert_array_equal(g[0], o[0])
+    (_, g), (_, o) = both(G, "mp_vec_waxpy", w, -1.0, x, y, n)
+    np.testing.assert_array_equal(g[0], o[0])
+    for name, extra in (("mp_vec_scale", (2.5,)), ("mp_vec_shift", (1.0,)),
+                        ("mp_vec_set", (3.0,))):
+        (_, g), (_, o) = both(G, name, w, *extra, n)
+        np.testing.assert_array_equal(g[0], o[0], err_msg=name)
+    for name in ("mp_vec_reciprocal", "mp_vec_abs", "mp_vec_sqrtabs", "mp_vec_zero_entries",
+                 "mp_vec_conjugate"):
+        (_, g), (_, o) = both(G, name, w, n)
+        np.testing.assert_array_equal(g[0], o[0], err_msg=name)
+    (_, g), (_, o) = both(G, "mp_vec_exp", x, n)
+    np.testing.assert_allclose(g[0], o[0], rtol=1e-15)
+    (_, g), (_, o) = both(G, "mp_vec_log", y, n)
+    np.testing.assert_allclose(g[0], o[0], rtol=1e-15)
+    (_, g), (_, o) = both(G, "mp_vec_chop", x, n, 0.5)
+    np.testing.assert_array_equal(g[0], o[0])
+    (_, g), (_, o) = both(G, "mp_vec_copy", x, w, n)
+    np.testing.assert_array_equal(g[1], o[1])
+    (_, g), (_, o) = both(G, "mp_vec_swap", x, w, n)
+    np.testing.assert_array_equal(g[0], o[0])
+    np.testing.assert_array_equal(g[1], o[1])
+    for ntype in (0, 1, 2, 3, 4):
+        (_, g), (_, o) = both(G, "mp_vec_norm", x, ntype, np.zeros(2), n)
+        np.testing.assert_allclose(g[2], o[2], rtol=1e-13)
+    for name in ("mp_vec_dot", "mp_vec_tdot"):
+        (_, g), (_, o) = both(G, name, x, y, np.zeros(1), n)
+        np.testing.assert_allclose(g[2], o[2], rtol=1e-12)
+    (_, g), (_, o) = both(G, "mp_vec_dot_norm2", x, y, np.zeros(1), np.zeros(1), n)
+    np.testing.assert_allclose(g[2], o[2], rtol=1e-12)
+    np.testing.assert_allclose(g[3], o[3], rtol=1e-12)
+    for name in ("mp_vec_sum", "mp_vec_mean"):
+        (_, g), (_, o) = both(G, name, x, np.zeros(1), n)
+        np.testing.assert_allclose(g[1], o[1], rtol=1e-10, atol=1e-12)
+    for name in ("mp_vec_max", "mp_vec_min"):
+        (_, g), (_, o) = both(G, name, x, np.zeros(1, dtype=np.int64), np.zeros(1), n)
+        assert g[1][0] == o[1][0] and g[2][0] == o[2][0]
+    (_, g), (_, o) = both(G, "mp_vec_normalize", x, np.zeros(1), n)
+    np.testing.assert_allclose(g[0], o[0], rtol=1e-13)
+    (_, g), (_, o) = both(G, "mp_vec_max_pointwise_divide", x, y, np.zeros(1), n)
+    assert g[2][0] == o[2][0]
+    xs = [rng.normal(size=n) for _ in range(3)]
+    addrs = np.array([a(v) for v in xs], dtype=np.int64)
+    (_, g), (_, o) = both(G, "mp_vec_maxpy", w, 3, np.array([0.5, -1.0, 2.0]), addrs, n)
+    np.testing.assert_array_equal(g[0], o[0])
+
+
+def test_mat_entries(G):
+    ip, ix, v = gallery.convection_diffusion_3d(8)
+    ip, ix = O.i64(ip), O.i64(ix)
+    n = len(ip) - 1
+    x = np.random.default_rng(1).normal(size=n)
+    for name in ("mp_mat_mult", "mp_mat_mult_add"):
+        (_, g), (_, o) = both(G, name, x, np.ones(n), ip, ix, v, n)
+        np.testing.assert_array_equal(g[1], o[1], err_msg=name)
+    (_, g), (_, o) = both(G, "mp_mat_mult_transpose", x, np.ones(n), ip, ix, v, n, n)
+    np.testing.assert_array_equal(g[1], o[1])
+    (_, g), (_, o) = both(G, "mp_mat_get_diagonal", np.zeros(n), ip, ix, v, n)
+    np.testing.assert_array_equal(g[0], o[0])
+    (_, g), (_, o) = both(G, "mp_mat_scale", v, len(v), -2.0)
+    np.testing.assert_array_equal(g[0], o[0])
+    (_, g), (_, o) = both(G, "mp_mat_zero_entries", v, len(v))
+    np.testing.assert_array_equal(g[0], o[0])
+    (rg, g), (ro, o) = both(G, "mp_mat_get_diagonal_markers", ip, ix, np.zeros(n, np.int64), n)
+    assert rg == ro == 1
+    np.testing.assert_array_equal(g[2], o[2])
+
+
+def test_pc_entries(G):
+    d = spd_dense(40, 5)
+    d[np.abs(d) < 1.5] = 0
+    ip, ix, v = dense_to_csr(d)
+    n = 40
+    x = np.random.default_rng(2).normal(size=n)
+    for jt in (0, 1, 2, 3):
+        (_, g), (_, o) = both(G, "mp_pc_jacobi_setup", np.zeros(n), jt, 0, 1, 0.5, ip, ix, v, n,
+                              np.zeros(n))
+        np.testing.assert_array_equal(g[0], o[0])
+        (_, g), (_, o) = both(G, "mp_pc_jacobi_setup_symmetric", np.zeros(n), jt, ip, ix, v, n)
+        np.testing.assert_array_equal(g[0], o[0])
+    (_, g), (_, o) = both(G, "mp_pc_jacobi_apply", np.zeros(n), x, np.abs(x) + 1, n)
+    np.testing.assert_array_equal(g[0], o[0])
+    dmark = np.zeros(n, np.int64)
+    O.lib().mp_mat_get_diagonal_markers(a(ip), a(ix), a(dmark), n)
+    for omega, fshift, flag in ((1.0, 0.0, 28), (1.2, 0.1, 28), (1.0, 0.0, 17)):
+        (_, g), (_, o) = both(G, "mp_pc_sor_apply", x, np.zeros(n), ip, ix, v, dmark,
+                              np.zeros(n), np.zeros(n), np.zeros(3 * n), omega, fshift, flag, n)
+        np.testing.assert_array_equal(g[1], o[1])
+
+
+def test_factor_entries(G):
+    ip, ix, v = gallery.laplacian_2d(9)
+    ip, ix = O.i64(ip), O.i64(ix)
+    n = 81
+    b = np.random.default_rng(3).normal(size=n)
+    r = np.arange(n, dtype=np.int64)
+    adiag = np.zeros(n, np.int64)
+    O.lib().mp_mat_get_diagonal_markers(a(ip), a(ix), a(adiag), n)
+    (kg, g), (ko, o) = both(G, "mp_ilu_symbolic_ilu0", np.zeros(n + 1, np.int64),
+                            np.zeros(4 * n + 400, np.int64), np.zeros(n + 1, np.int64), adiag, ip,
+                            ix, n)
+    assert kg == ko
+    for i in range(3):
+        np.testing.assert_array_equal(g[i], o[i])
+    bi, bj, bdiag = o[0], o[1], o[2]
+    (_, g), (_, o) = both(G, "mp_pc_ilu_numeric", np.zeros(kg), np.zeros(n), ip, ix, v, bi, bj,
+                          bdiag, r, r, n)
+    np.testing.assert_array_equal(g[0], o[0])
+    ba = o[0]
+    (_, g), (_, o) = both(G, "mp_pc_ilu_apply", b, np.zeros(n), np.zeros(n), bi, bj, ba, bdiag,
+                          r, r, n)
+    np.testing.assert_array_equal(g[1], o[1])
+    # level of fill: staging layout, the contiguous pass, then numeric
+    cap = 8 * n + 100
+    args = (np.zeros(n + 1, np.int64), np.zeros(cap, np.int64), np.zeros(cap, np.int64),
+            np.zeros(n + 1, np.int64), ip, ix, r, r, 2, cap, np.zeros(7 * n + 8, np.int64), n)
+    (kg, g), (ko, o) = both(G, "mp_ilu_symbolic", *args)
+    assert kg == ko
+    for i in range(4):
+        np.testing.assert_array_equal(g[i][: kg if i in (1, 2) else n + 1],
+                                      o[i][: ko if i in (1, 2) else n + 1])
+    (_, g), (_, o) = both(G, "mp_ilu_contiguous_lu", o[1], o[0], o[3], np.zeros(cap, np.int64), n)
+    for i in (1, 2, 3):
+        np.testing.assert_array_equal(g[i], o[i])
+    # IC(1)
+    scratch = np.zeros(6 * (n + 1) + 2 * cap, np.int64)
+    args = (np.zeros(n + 1, np.int64), np.zeros(cap, np.int64), np.zeros(cap, np.int64),
+            np.zeros(n, np.int64), ip, ix, r, r, 1, cap, scratch, n, len(scratch))
+    (kg, g), (ko, o) = both(G, "mp_icc_symbolic", *args)
+    assert kg == ko
+    for i in range(4):
+        np.testing.assert_array_equal(g[i][:kg] if i in (1, 2) else g[i], o[i][:ko] if i in (1, 2) else o[i])
+    ui, uj, udiag = o[0], o[1], o[3]
+    bdg = np.zeros(n + 1, np.int64)
+    bdg[:n] = udiag
+    (_, g), (_, o) = both(G, "mp_icc_contiguous_cholesky", uj, ui, bdg, np.zeros(n + 1, np.int64),
+                          bdg, np.zeros(cap, np.int64), n)
+    for i in (3, 4, 5):
+        np.testing.assert_array_equal(g[i], o[i])
+    bi2, bd2, bj2 = o[3], o[4], o[5]
+    (_, g), (_, o) = both(G, "mp_pc_icc_numeric", np.zeros(kg), np.zeros(n), np.zeros(n, np.int64),
+                          np.zeros(n, np.int64), ip, ix, v, bi2, bj2, bd2, r, r, n)
+    np.testing.assert_array_equal(g[0], o[0])
+    ua = o[0]
+    (rg, g), (ro, o) = both(G, "mp_pc_icc_apply", b, np.zeros(n), bi2, bj2, ua, bd2, r,
+                            np.zeros(n), n)
+    assert rg == ro == 0
+    np.testing.assert_array_equal(g[1], o[1])
+    (_, g), (_, o) = both(G, "mp_ordering_rcm", np.zeros(n, np.int64), np.zeros(n, np.int64),
+                          np.zeros(n, np.int64), np.zeros(n, np.int64), ip, ix, n)
+    np.testing.assert_array_equal(g[0], o[0])
+
+
+@pytest.mark.parametrize("kt", ["cg", "bcgs", "gmres", "fgmres"])
+@pytest.mark.parametrize("pt", ["none", "jacobi", "sor", "ilu", "icc"])
+def test_ksp_entries(G, kt, pt):
+    """The raw cfg/cfgi/pci blocks, built with the oracle's PC packing."""
+    d = tridiag_dense(30)
+    ip, ix, v = dense_to_csr(d)
+    n = 30
+    b = np.random.default_rng(56).normal(size=n)
+    pc = O.OraclePC(pt, ip, ix, v)
+    max_it, mk = 200, 20
+    res = {}
+    for tag, lib in (("gpu", G), ("oracle", O.lib())):
+        cfg = np.zeros(16 + max_it + 2)
+        cfg[:5] = [1e-12, 1e-50, 1e4, 1e-30, 0.1]
+        cfgi = np.zeros(16, dtype=np.int64)
+        cfgi[:10] = [2, 0, 1, 0, -1, 0, max_it, mk, 0, 0]
+        pci, pcf, pstmp, x = pc.pci(), np.array([1.0, 0.0]), np.zeros(n), np.zeros(n)
+        if kt in ("cg", "bcgs"):
+            fn = lib.mp_ksp_solve_cg if kt == "cg" else lib.mp_ksp_solve_bcgs
+            fn(n, a(ip), a(ix), a(v), a(pci), a(pcf), a(pstmp), a(np.zeros(7 * n)), a(cfg),
+               a(cfgi), a(b), a(x))
+        else:
+            hs = np.zeros((mk + 2) * (mk + 1) + (mk + 1) ** 2 + 2 * (mk + 1) + 2 * (mk + 2))
+            vv = np.zeros((mk + 1) * n)
+            if kt == "gmres":
+                lib.mp_ksp_solve_gmres(n, a(ip), a(ix), a(v), a(pci), a(pcf), a(pstmp),
+                                       a(np.zeros(2 * n)), a(vv), a(hs), a(cfg), a(cfgi), a(b), a(x))
+            else:
+                lib.mp_ksp_solve_fgmres(n, a(ip), a(ix), a(v), a(pci), a(pcf), a(pstmp),
+                                        a(np.zeros(2 * n)), a(vv), a(np.zeros((mk + 2) * n)), a(hs),
+                                        a(cfg), a(cfgi), a(b), a(x))
+        res[tag] = (x, cfg, cfgi)
+    assert G.mp_last_status() == 0
+    xg, cg_, ig = res["gpu"]
+    xo, co, io = res["oracle"]
+    assert ig[11] == io[11]
+    assert abs(ig[10] - io[10]) <= (20 if kt == "bcgs" else 0)
+    np.testing.assert_allclose(xg, xo, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(xg, np.linalg.solve(d, b), rtol=1e-8, atol=1e-10)
