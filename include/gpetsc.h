@@ -49,6 +49,20 @@ enum {
 int gp_version(void);
 /* Message of the last failed call on this host thread. */
 const char *gp_last_error(void);
+/* Floating-point form of every kernel launched after the call (the process
+ * default comes from the environment: GPETSC_ARITHMETIC=exact selects exact,
+ * anything else FMA).
+ *   GP_ARITH_EXACT  each product and sum rounded separately, in the
+ *                   reference's order: results bit-identical to its
+ *                   sequential loops (src/ported.mojo) on the same inputs.
+ *   GP_ARITH_FMA    products folded into fused multiply-adds, same order:
+ *                   half the FP64 instructions; results differ from the
+ *                   exact form by rounding only.
+ * No counterpart in the reference (its loops are compiled one way).  Solver
+ * graphs captured in one form are re-captured when the form changes. */
+enum { GP_ARITH_EXACT = 0, GP_ARITH_FMA = 1 };
+int gp_set_arithmetic(int mode);
+int gp_get_arithmetic(void);
 /* Number of visible CUDA devices (0 when none). */
 int gp_device_count(int *count);
 int gp_set_device(int device);

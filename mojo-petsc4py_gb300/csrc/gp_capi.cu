@@ -41,6 +41,17 @@ extern "C" {
 int gp_version(void) { return 100; }
 const char* gp_last_error(void) { return gp::last_error(); }
 
+int gp_set_arithmetic(int mode) {
+  if (mode != GP_ARITH_EXACT && mode != GP_ARITH_FMA) {
+    gp::set_error("gp_set_arithmetic: mode must be GP_ARITH_EXACT (0) or GP_ARITH_FMA (1)");
+    return GP_ERR_ARG;
+  }
+  gp::set_arith_mode(mode);
+  return GP_OK;
+}
+
+int gp_get_arithmetic(void) { return gp::arith_mode(); }
+
 int gp_device_count(int* count) {
   int c = 0;
   cudaError_t e = cudaGetDeviceCount(&c);

@@ -70,6 +70,18 @@ constexpr int kRedBlock = 256;     // block for reductions
 constexpr int kMaxRedGrid = 2048;  // partials buffer size per reduction slot
 
 int num_sms();  // cached SM count of the current device
+
+// Arithmetic of the bandwidth-bound kernels (SpMV, Vec maps, reductions,
+// solver updates).  kExact: every `a*x + y` is a rounded multiply then a
+// rounded add, the operation sequence of the sequential CPU loops, so SpMV
+// and the maps are bit-identical to them.  kFma: `a*x + y` is one fused
+// multiply-add; GB300 issues FP64 at 1/64 of FP32, and the unfused form makes
+// SpMV FP64-issue-bound below the HBM roofline, while the fused form halves
+// the FP64 instructions.  Default kFma; GPETSC_ARITHMETIC=exact selects the
+// other at load, gp_set_arithmetic() at run time.
+enum Arith : int { kExact = 0, kFma = 1 };
+int arith_mode();
+void set_arith_mode(int mode);
 int red_grid(int64_t n);  // deterministic reduction grid for length n
 
 // Device error word written by kernels (spin timeouts, numeric failures).
@@ -116,6 +128,15 @@ __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, 
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double div_(double a, double b) { return __ddiv_rn(a, b); }
+
+// a * x + y in the selected arithmetic (see Arith)
+template <bool FMA>
+__device__ __forceinline__ double madd(double a, double x, double y) {
+  if constexpr (FMA)
+    return __fma_rn(a, x, y);
+  else
+    return __dadd_rn(__dmul_rn(a, x), y);
+}
 
 // ------------------------------------------------------------------ reduction
 // Deterministic block reduction of NR doubles (result valid in thread 0).

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "gp_ksp.h"
+#include "gp_spmv.cuh"
 
 namespace gp {
 
@@ -59,6 +60,15 @@ __device__ int conv_default(KspState* st, int n, double rnorm) {
   return 0;
 }
 
+// Launch a kernel templated on the arithmetic (see Arith in gp_common.cuh).
+#define FL(K, G, B, S, ...)                                   \
+  do {                                                        \
+    if (arith_mode() == kFma)                                 \
+      K<true><<<(G), (B), 0, (S)>>>(__VA_ARGS__);             \
+    else                                                      \
+      K<false><<<(G), (B), 0, (S)>>>(__VA_ARGS__);            \
+  } while (0)
+
 // ------------------------------------------------------------ vector kernels
 static int vgrid(int n) { return std::max(1, std::min((n + 255) / 256, num_sms() * 8)); }
 
@@ -79,25 +89,28 @@ __global__ void k_zero_d(const int* gate, int want, int n, DRef yr) {
 }
 
 // y = y + (sgn * a) x      (VecAXPY with a device scalar)
+template <bool FMA>
 __global__ void k_axpy_d(const int* gate, int want, int n, DRef yr, const double* a, double sgn,
                          DRef xr) {
   if (gated_off(gate, want)) return;
   double* y = yr.get();
   const double* x = xr.get();
   const double al = mul(sgn, *a);
-  GRID_LOOP(i, n) y[i] = add(y[i], mul(al, x[i]));
+  GRID_LOOP(i, n) y[i] = madd<FMA>(al, x[i], y[i]);
 }
 
 // y = x + alpha y (VecAYPX, general branch) with a host scalar
+template <bool FMA>
 __global__ void k_aypx_h(const int* gate, int want, int n, DRef yr, double alpha, DRef xr) {
   if (gated_off(gate, want)) return;
   double* y = yr.get();
   const double* x = xr.get();
-  GRID_LOOP(i, n) y[i] = add(x[i], mul(alpha, y[i]));
+  GRID_LOOP(i, n) y[i] = madd<FMA>(alpha, y[i], x[i]);
 }
 
 // VecAYPX(y, *a, x) with the reference's branch structure decided on the
 // device: a == 0 copies, a == 1 adds, otherwise x + a y.
+template <bool FMA>
 __global__ void k_aypx_d(const int* gate, int want, int n, DRef yr, const double* a, DRef xr) {
   if (gated_off(gate, want)) return;
   double* y = yr.get();
@@ -106,13 +119,14 @@ __global__ void k_aypx_d(const int* gate, int want, int n, DRef yr, const double
   if (al == 0.0) {
     GRID_LOOP(i, n) y[i] = x[i];
   } else if (al == 1.0) {
-    GRID_LOOP(i, n) y[i] = add(y[i], mul(al, x[i]));
+    GRID_LOOP(i, n) y[i] = madd<FMA>(al, x[i], y[i]);
   } else {
-    GRID_LOOP(i, n) y[i] = add(x[i], mul(al, y[i]));
+    GRID_LOOP(i, n) y[i] = madd<FMA>(al, y[i], x[i]);
   }
 }
 
 // z = a x + b y + c z      (VecAXPBYPCZ with device scalars)
+template <bool FMA>
 __global__ void k_axpbypcz_d(const int* gate, int want, int n, DRef zr, const double* a,
                              const double* b, const double* c, DRef xr, DRef yr) {
   if (gated_off(gate, want)) return;
@@ -120,10 +134,11 @@ __global__ void k_axpbypcz_d(const int* gate, int want, int n, DRef zr, const do
   const double* x = xr.get();
   const double* y = yr.get();
   const double al = *a, be = *b, ga = *c;
-  GRID_LOOP(i, n) z[i] = add(add(mul(al, x[i]), mul(be, y[i])), mul(ga, z[i]));
+  GRID_LOOP(i, n) z[i] = madd<FMA>(ga, z[i], madd<FMA>(be, y[i], mul(al, x[i])));
 }
 
 // w = (sgn * a) x + y      (VecWAXPY)
+template <bool FMA>
 __global__ void k_waxpy_d(const int* gate, int want, int n, DRef wr, const double* a, double sgn,
                           DRef xr, DRef yr) {
   if (gated_off(gate, want)) return;
@@ -131,7 +146,7 @@ __global__ void k_waxpy_d(const int* gate, int want, int n, DRef wr, const doubl
   const double* x = xr.get();
   const double* y = yr.get();
   const double al = mul(sgn, *a);
-  GRID_LOOP(i, n) w[i] = add(mul(al, x[i]), y[i]);
+  GRID_LOOP(i, n) w[i] = madd<FMA>(al, x[i], y[i]);
 }
 
 // x = x * (*a)   (VecScale)  or  x = x / (*a) when *a > 0 (VecNormalize)
@@ -149,14 +164,15 @@ __global__ void k_scale_d(const int* gate, int want, int n, DRef xr, const doubl
 }
 
 // CG update: x = x + a p; r = r + (-a) w
+template <bool FMA>
 __global__ void k_cg_xr(const int* gate, int want, int n, double* __restrict__ x,
                         double* __restrict__ r, const double* __restrict__ p,
                         const double* __restrict__ w, const double* a) {
   if (gated_off(gate, want)) return;
   const double al = *a, nal = -al;
   GRID_LOOP(i, n) {
-    x[i] = add(x[i], mul(al, p[i]));
-    r[i] = add(r[i], mul(nal, w[i]));
+    x[i] = madd<FMA>(al, p[i], x[i]);
+    r[i] = madd<FMA>(nal, w[i], r[i]);
   }
 }
 
@@ -166,7 +182,7 @@ enum DRed : int { D_DOT, D_NRM, D_DOTNRM };
 // Deterministic reduction into device scalars: out_raw receives the sum,
 // out_sqrt receives sqrt(|sum|) (the 2-norm, or sqrt|beta| for the natural
 // norm).  D_DOTNRM writes (x.y, x.x) to out_raw[0], out_raw2.
-template <int OP>
+template <int OP, bool FMA>
 __global__ void __launch_bounds__(kRedBlock) k_dred(const int* gate, int want, int n, DRef xr,
                                                     DRef yr, RedSlot slot, double* out_raw,
                                                     double* out_sqrt, double* out_raw2) {
@@ -180,10 +196,10 @@ __global__ void __launch_bounds__(kRedBlock) k_dred(const int* gate, int want, i
   GRID_LOOP(i, n) {
     const double a = x[i];
     if (OP == D_DOTNRM) {
-      v[0] = add(v[0], mul(a, y[i]));
-      v[NR - 1] = add(v[NR - 1], mul(a, a));
+      v[0] = madd<FMA>(a, y[i], v[0]);
+      v[NR - 1] = madd<FMA>(a, a, v[NR - 1]);
     } else {
-      v[0] = add(v[0], mul(a, y[i]));
+      v[0] = madd<FMA>(a, y[i], v[0]);
     }
   }
   double tot[NR];
@@ -198,6 +214,7 @@ __global__ void __launch_bounds__(kRedBlock) k_dred(const int* gate, int want, i
 // over x and the basis, per-block partial sums for every vector, last block
 // folds the partials.  Used by classical Gram-Schmidt.
 constexpr int kMaxBasis = 64;
+template <bool FMA>
 __global__ void __launch_bounds__(kRedBlock) k_mdot(const int* gate, int want, int n, DRef xr,
                                                     const double* __restrict__ basis,
                                                     const int* count, RedSlot slot,
@@ -217,7 +234,7 @@ __global__ void __launch_bounds__(kRedBlock) k_mdot(const int* gate, int want, i
       const double a = x[i];
 #pragma unroll
       for (int q = 0; q < 8; q++)
-        if (q < jn) v[q] = add(v[q], mul(a, basis[(size_t)(j0 + q) * n + i]));
+        if (q < jn) v[q] = madd<FMA>(a, basis[(size_t)(j0 + q) * n + i], v[q]);
     }
 #pragma unroll
     for (int q = 0; q < 8; q++) {
@@ -250,6 +267,7 @@ __global__ void __launch_bounds__(kRedBlock) k_mdot(const int* gate, int want, i
 
 // y = (from_zero ? 0 : y) + sum_{j < *count} coef_j basis_j, ascending j per
 // element (simdvec.maxpy, VecMAXPBY with beta = 0).
+template <bool FMA>
 __global__ void k_maxpy_dyn(const int* gate, int want, int n, DRef yr,
                             const double* __restrict__ basis, const double* __restrict__ coef,
                             const int* count, int from_zero) {
@@ -258,7 +276,7 @@ __global__ void k_maxpy_dyn(const int* gate, int want, int n, DRef yr,
   const int k = *count;
   GRID_LOOP(i, n) {
     double v = from_zero ? 0.0 : y[i];
-    for (int j = 0; j < k; j++) v = add(v, mul(coef[j], basis[(size_t)j * n + i]));
+    for (int j = 0; j < k; j++) v = madd<FMA>(coef[j], basis[(size_t)j * n + i], v);
     y[i] = v;
   }
 }
@@ -372,6 +390,167 @@ __global__ void k_cg_d(KspState* st) {
   if (st->active != 1) return;
   st->i += 1;
   if (st->i >= st->max_it) stop(st, st->dp, st->its, R_DIVITS);
+}
+
+// ================================================================== CG, fused
+// The same recurrence as KSPSolve_CG with the preconditioned norm (the
+// default), in three vector kernels per iteration instead of eight:
+//   k_cgf_p       p = z + beta/betaold p (VecAYPX's branches; a copy at i = 0)
+//   k_cgf_spmv    w = A p and dpi = p.w in one pass; the last CTA runs the
+//                 indefinite-matrix test and forms a = beta / dpi
+//   k_cgf_update  x += a p, r -= a w, then (Jacobi fused in) z = D r and
+//                 ||z||^2, z.r in the same pass; the last CTA records the
+//                 residual, runs KSPConvergedDefault, forms beta and the top
+//                 of the next iteration.
+// Every vector element is computed with the same operations as in the
+// unfused kernels; the dot products are summed in a different fixed order.
+// W shares Z's storage as in the reference (each w_i is read before z_i is
+// written, by the same thread).
+
+// Residual bookkeeping after ||z|| and z.r are known (first: the prologue).
+__device__ void cg_tail(KspState* st, double* hist, double dp, double zr, bool first) {
+  st->dp = dp;
+  int its;
+  if (first) {
+    hist[0] = dp;
+    const int reason = conv_default(st, 0, dp);
+    if (reason) {
+      stop(st, dp, 0, reason);
+      return;
+    }
+    st->i = 0;
+    st->dpi = 0.0;
+    st->betaold = 1.0;
+  } else {
+    its = st->i + 1;
+    hist[its] = dp;
+    const int reason = conv_default(st, its, dp);
+    if (reason) {
+      stop(st, dp, its, reason);
+      return;
+    }
+  }
+  st->beta = zr;
+  if (!first) {
+    st->i += 1;
+    if (st->i >= st->max_it) {
+      stop(st, dp, st->i, R_DIVITS);
+      return;
+    }
+  }
+  // top of iteration i
+  const int i = st->i;
+  st->its = i + 1;
+  const double beta = st->beta;
+  if (beta == 0.0) {
+    stop(st, dp, i + 1, R_ATOL);
+    return;
+  }
+  if (i > 0 && mul(beta, st->betaold) < 0.0) {
+    stop(st, dp, i + 1, R_INDEF_PC);
+    return;
+  }
+  st->bcoef = i == 0 ? 0.0 : div_(beta, st->betaold);
+  st->dpiold = st->dpi;
+  st->active = 1;
+  st->g[G_ON] = 1;
+}
+
+template <bool FMA>
+__global__ void k_cgf_p(KspState* st, int n, double* __restrict__ p,
+                        const double* __restrict__ z) {
+  if (st->active != 1) return;
+  const double bc = st->bcoef;
+  if (bc == 0.0) {
+    GRID_LOOP(i, n) p[i] = z[i];
+  } else if (bc == 1.0) {
+    GRID_LOOP(i, n) p[i] = madd<FMA>(bc, z[i], p[i]);
+  } else {
+    GRID_LOOP(i, n) p[i] = madd<FMA>(bc, p[i], z[i]);
+  }
+}
+
+template <bool FMA>
+__global__ void __launch_bounds__(kSpmvRows) k_cgf_spmv(KspState* st, int n,
+                                                        const int* __restrict__ rowptr,
+                                                        const int* __restrict__ colind,
+                                                        const double* __restrict__ val,
+                                                        const double* __restrict__ p,
+                                                        double* __restrict__ w, RedSlot slot) {
+  if (st->active != 1) return;
+  const int r0 = blockIdx.x * kSpmvRows;
+  const int row = r0 + threadIdx.x;
+  double s;
+  if constexpr (FMA) {
+    __shared__ SpmvSmemF<double, double, double> sm;
+    s = spmv_block_rows_fma<double, double, double>(sm, n, r0, rowptr, colind, val, p, 0.0);
+  } else {
+    __shared__ SpmvSmem<double, double, double> sm;
+    s = spmv_block_rows<double, double, double>(sm, n, r0, rowptr, colind, val, p, 0.0);
+  }
+  double v[1] = {0.0};
+  if (row < n) {
+    w[row] = s;
+    v[0] = madd<FMA>(p[row], s, 0.0);
+  }
+  double tot[1];
+  if (grid_finish<1>(v, slot, tot) && threadIdx.x == 0) {
+    const double dpi = tot[0];
+    st->dpi = dpi;
+    const int i = st->i;
+    st->betaold = st->beta;
+    if (dpi == 0.0 || (i > 0 && sgn(dpi) * sgn(st->dpiold) < 0)) {
+      stop(st, st->dp, i + 1, R_INDEF_MAT);
+      return;
+    }
+    st->a = div_(st->beta, dpi);
+  }
+}
+
+// x += a p; r -= a w; (JACOBI) z = D r with ||z||^2 and z.r; else the PC
+// follows and k_cgf_red reduces.
+template <bool FMA, bool JACOBI>
+__global__ void __launch_bounds__(kRedBlock) k_cgf_update(
+    KspState* st, double* hist, int n, double* __restrict__ x, double* __restrict__ r,
+    const double* __restrict__ p, const double* w, double* z, const double* __restrict__ d,
+    RedSlot slot) {
+  if (st->active != 1) return;
+  const double al = st->a, nal = -al;
+  double v[2] = {0.0, 0.0};
+  GRID_LOOP(i, n) {
+    x[i] = madd<FMA>(al, p[i], x[i]);
+    const double ri = madd<FMA>(nal, w[i], r[i]);
+    r[i] = ri;
+    if constexpr (JACOBI) {
+      const double zi = mul(ri, d[i]);
+      z[i] = zi;
+      v[0] = madd<FMA>(zi, zi, v[0]);
+      v[1] = madd<FMA>(zi, ri, v[1]);
+    }
+  }
+  if constexpr (JACOBI) {
+    double tot[2];
+    if (grid_finish<2>(v, slot, tot) && threadIdx.x == 0)
+      cg_tail(st, hist, __dsqrt_rn(tot[0]), tot[1], false);
+  }
+}
+
+// ||z||^2 and z.r after a separate preconditioner apply (first: prologue).
+template <bool FMA>
+__global__ void __launch_bounds__(kRedBlock) k_cgf_red(KspState* st, double* hist, int n,
+                                                       const double* __restrict__ z,
+                                                       const double* __restrict__ r,
+                                                       RedSlot slot, int first) {
+  if (!first && st->active != 1) return;
+  double v[2] = {0.0, 0.0};
+  GRID_LOOP(i, n) {
+    const double zi = z[i];
+    v[0] = madd<FMA>(zi, zi, v[0]);
+    v[1] = madd<FMA>(zi, r[i], v[1]);
+  }
+  double tot[2];
+  if (grid_finish<2>(v, slot, tot) && threadIdx.x == 0)
+    cg_tail(st, hist, __dsqrt_rn(tot[0]), tot[1], first != 0);
 }
 
 // ================================================================== BCGS
@@ -905,7 +1084,10 @@ struct Run {
   }
   template <int OP>
   int red(const int* g, DRef x, DRef y, double* raw, double* sq, double* raw2 = nullptr) const {
-    k_dred<OP><<<red_grid(n), kRedBlock, 0, s>>>(g, 1, n, x, y, k->slot, raw, sq, raw2);
+    if (arith_mode() == kFma)
+      k_dred<OP, true><<<red_grid(n), kRedBlock, 0, s>>>(g, 1, n, x, y, k->slot, raw, sq, raw2);
+    else
+      k_dred<OP, false><<<red_grid(n), kRedBlock, 0, s>>>(g, 1, n, x, y, k->slot, raw, sq, raw2);
     GP_CHECK_LAUNCH();
     return GP_OK;
   }
@@ -933,7 +1115,7 @@ struct Run {
     if (!guess_zero) {
       GP_TRY(matmult(nullptr, x, vt1));
       GP_TRY(copy(nullptr, b, vt2));
-      k_axpy_d<<<grid(), 256, 0, s>>>(nullptr, 1, n, vt2, S(&KspState::c_one), -1.0, vt1);
+      FL(k_axpy_d, grid(), 256, s, nullptr, 1, n, vt2, S(&KspState::c_one), -1.0, vt1);
       GP_CHECK_LAUNCH();
     } else {
       GP_TRY(copy(nullptr, b, vt2));
@@ -954,7 +1136,7 @@ static int cg_prologue(const Run& r, const double* b, double* x) {
   DRef R = DRef::of(k->work), Z = DRef::of(k->work + n);
   if (!o.guess_zero) {
     GP_TRY(r.matmult(nullptr, DRef::of(x), R));
-    k_aypx_h<<<r.grid(), 256, 0, r.s>>>(nullptr, 1, n, R, -1.0, DRef::of(b));
+    FL(k_aypx_h, r.grid(), 256, r.s, nullptr, 1, n, R, -1.0, DRef::of(b));
     GP_CHECK_LAUNCH();
   } else {
     GP_TRY(r.copy(nullptr, DRef::of(b), R));
@@ -987,12 +1169,12 @@ static int cg_body(const Run& r, double* x) {
   KspState* st = k->st;
   const int* on = r.G(G_ON);
   k_cg_a<<<1, 1, 0, r.s>>>(st);
-  k_aypx_d<<<r.grid(), 256, 0, r.s>>>(on, 1, n, DRef::of(P), r.S(&KspState::bcoef), DRef::of(Z));
+  FL(k_aypx_d, r.grid(), 256, r.s, on, 1, n, DRef::of(P), r.S(&KspState::bcoef), DRef::of(Z));
   GP_CHECK_LAUNCH();
   GP_TRY(r.matmult(on, DRef::of(P), DRef::of(W)));
   GP_TRY(r.red<D_DOT>(on, DRef::of(P), DRef::of(W), r.S(&KspState::dpi), nullptr));
   k_cg_b<<<1, 1, 0, r.s>>>(st);
-  k_cg_xr<<<r.grid(), 256, 0, r.s>>>(on, 1, n, x, R, P, W, r.S(&KspState::a));
+  FL(k_cg_xr, r.grid(), 256, r.s, on, 1, n, x, R, P, W, r.S(&KspState::a));
   GP_CHECK_LAUNCH();
   const int nt = k->opt.normtype;
   double* dp = r.S(&KspState::dp);
@@ -1010,6 +1192,65 @@ static int cg_body(const Run& r, double* x) {
   GP_TRY(r.pcapply(r.G(1), DRef::of(R), DRef::of(Z)));
   GP_TRY(r.red<D_DOT>(r.G(2), DRef::of(Z), DRef::of(R), beta, nullptr));
   k_cg_d<<<1, 1, 0, r.s>>>(st);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+// ------------------------------------------------------------------ CG, fused
+static bool cg_fused_ok(const Run& r) {
+  const KspOptions& o = r.k->opt;
+  return o.normtype == N_PRECOND && o.chknorm <= 1 &&
+         (int64_t)spmv_grid(r.A) <= (int64_t)kMaxBasis * kMaxRedGrid;
+}
+
+static int cg_prologue_fused(const Run& r, const double* b, double* x) {
+  Ksp* k = r.k;
+  const int n = r.n;
+  DRef R = DRef::of(k->work), Z = DRef::of(k->work + n);
+  if (!k->opt.guess_zero) {
+    GP_TRY(r.matmult(nullptr, DRef::of(x), R));
+    FL(k_aypx_h, r.grid(), 256, r.s, nullptr, 1, n, R, -1.0, DRef::of(b));
+  } else {
+    GP_TRY(r.copy(nullptr, DRef::of(b), R));
+  }
+  GP_TRY(r.pcapply(nullptr, R, Z));
+  FL(k_cgf_red, red_grid(n), kRedBlock, r.s, k->st, k->hist, n, k->work + n, k->work, k->slot,
+     1);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+static int cg_body_fused(const Run& r, double* x) {
+  Ksp* k = r.k;
+  const int n = r.n;
+  double* R = k->work;
+  double* Z = k->work + n;
+  double* P = k->work + 2 * n;
+  double* W = Z;  // the reference's W = Z aliasing
+  const Csr* A = r.A;
+  FL(k_cgf_p, r.grid(), 256, r.s, k->st, n, P, Z);
+  FL(k_cgf_spmv, spmv_grid(A), kSpmvRows, r.s, k->st, n, A->rowptr, A->colind, A->val, P, W,
+     k->slot);
+  const bool jac = r.pc->opt.type == PC_JACOBI;
+  const bool f = arith_mode() == kFma;
+  const int g = red_grid(n);
+  if (jac) {
+    if (f)
+      k_cgf_update<true, true><<<g, kRedBlock, 0, r.s>>>(k->st, k->hist, n, x, R, P, W, Z,
+                                                         r.pc->diag, k->slot);
+    else
+      k_cgf_update<false, true><<<g, kRedBlock, 0, r.s>>>(k->st, k->hist, n, x, R, P, W, Z,
+                                                          r.pc->diag, k->slot);
+  } else {
+    if (f)
+      k_cgf_update<true, false><<<g, kRedBlock, 0, r.s>>>(k->st, k->hist, n, x, R, P, W, Z,
+                                                          nullptr, k->slot);
+    else
+      k_cgf_update<false, false><<<g, kRedBlock, 0, r.s>>>(k->st, k->hist, n, x, R, P, W, Z,
+                                                           nullptr, k->slot);
+    GP_TRY(r.pcapply(r.G(G_ON), DRef::of(R), DRef::of(Z)));
+    FL(k_cgf_red, g, kRedBlock, r.s, k->st, k->hist, n, Z, R, k->slot, 0);
+  }
   GP_CHECK_LAUNCH();
   return GP_OK;
 }
@@ -1048,13 +1289,13 @@ static int bcgs_body(const Run& r, double* x) {
   const int* on = r.G(G_ON);
   GP_TRY(r.red<D_DOT>(on, R, RP, r.S(&KspState::rho), nullptr));
   k_bcgs_a<<<1, 1, 0, r.s>>>(st);
-  k_axpbypcz_d<<<r.grid(), 256, 0, r.s>>>(on, 1, n, P, r.S(&KspState::c_one),
+  FL(k_axpbypcz_d, r.grid(), 256, r.s, on, 1, n, P, r.S(&KspState::c_one),
                                            r.S(&KspState::c_omb), r.S(&KspState::bbeta), R, V);
   GP_CHECK_LAUNCH();
   GP_TRY(r.apply_ba(on, side, P, V, T));
   GP_TRY(r.red<D_DOT>(on, V, RP, r.S(&KspState::d1), nullptr));
   k_bcgs_b<<<1, 1, 0, r.s>>>(st);
-  k_waxpy_d<<<r.grid(), 256, 0, r.s>>>(on, 1, n, S, r.S(&KspState::alpha), -1.0, V, R);
+  FL(k_waxpy_d, r.grid(), 256, r.s, on, 1, n, S, r.S(&KspState::alpha), -1.0, V, R);
   GP_CHECK_LAUNCH();
   GP_TRY(r.apply_ba(on, side, S, T, R));
   // VecDotNorm2(S, T): (S.T, T.T) -- computed as (T.S, T.T), the same sums
@@ -1062,11 +1303,11 @@ static int bcgs_body(const Run& r, double* x) {
   k_bcgs_c<<<1, 1, 0, r.s>>>(st);
   GP_TRY(r.red<D_DOT>(r.G(6), S, S, r.S(&KspState::d1), nullptr));
   k_bcgs_c2<<<1, 1, 0, r.s>>>(st);
-  k_axpy_d<<<r.grid(), 256, 0, r.s>>>(r.G(6), 1, n, X, r.S(&KspState::alpha), 1.0, P);
+  FL(k_axpy_d, r.grid(), 256, r.s, r.G(6), 1, n, X, r.S(&KspState::alpha), 1.0, P);
   k_bcgs_c3<<<1, 1, 0, r.s>>>(st);
-  k_axpbypcz_d<<<r.grid(), 256, 0, r.s>>>(r.G(7), 1, n, X, r.S(&KspState::alpha),
+  FL(k_axpbypcz_d, r.grid(), 256, r.s, r.G(7), 1, n, X, r.S(&KspState::alpha),
                                            r.S(&KspState::omega), r.S(&KspState::c_one), P, S);
-  k_waxpy_d<<<r.grid(), 256, 0, r.s>>>(r.G(7), 1, n, R, r.S(&KspState::omega), -1.0, T, S);
+  FL(k_waxpy_d, r.grid(), 256, r.s, r.G(7), 1, n, R, r.S(&KspState::omega), -1.0, T, S);
   GP_CHECK_LAUNCH();
   GP_TRY(r.red<D_NRM>(r.G(0), R, R, nullptr, r.S(&KspState::dp)));
   k_bcgs_d<<<1, 1, 0, r.s>>>(st, k->hist);
@@ -1086,7 +1327,7 @@ static int bcgs_epilogue(const Run& r, double* x) {
     GP_TRY(r.copy(nullptr, T, X));
   }
   if (o.pc_side == 1 && !o.guess_zero) {
-    k_axpy_d<<<r.grid(), 256, 0, r.s>>>(nullptr, 1, n, X, r.S(&KspState::c_one), 1.0, GUESS);
+    FL(k_axpy_d, r.grid(), 256, r.s, nullptr, 1, n, X, r.S(&KspState::c_one), 1.0, GUESS);
     GP_CHECK_LAUNCH();
   }
   return GP_OK;
@@ -1099,10 +1340,10 @@ static int cgs_pass(const Run& r, int gate_idx) {
   Ksp* k = r.k;
   const int* g = r.G(gate_idx);
   DRef v1 = DRef::at(&k->st->vv_it1);
-  k_mdot<<<red_grid(r.n), kRedBlock, 0, r.s>>>(g, 1, r.n, v1, k->vv, &k->st->kcount, k->slot,
+  FL(k_mdot, red_grid(r.n), kRedBlock, r.s, g, 1, r.n, v1, k->vv, &k->st->kcount, k->slot,
                                               k->lhh);
   k_gm_cgs1<<<1, 1, 0, r.s>>>(k->st, k->hs, k->lhh, gate_idx);
-  k_maxpy_dyn<<<r.grid(), 256, 0, r.s>>>(g, 1, r.n, v1, k->vv, k->lhh, &k->st->kcount, 0);
+  FL(k_maxpy_dyn, r.grid(), 256, r.s, g, 1, r.n, v1, k->vv, k->lhh, &k->st->kcount, 0);
   GP_CHECK_LAUNCH();
   return GP_OK;
 }
@@ -1140,19 +1381,19 @@ static int gmres_body(const Run& r, const double* b, double* x) {
   k_gm_backsub<<<1, 1, 0, r.s>>>(st, k->hs);
   const int m = k->opt.restart;
   double* rs = k->hs + (size_t)(m + 2) * (m + 1) + (size_t)(m + 1) * (m + 1) + 2 * (m + 1);
-  k_maxpy_dyn<<<r.grid(), 256, 0, r.s>>>(r.G(6), 1, n, TEMP, k->vv, rs, &st->kcount, 1);
+  FL(k_maxpy_dyn, r.grid(), 256, r.s, r.G(6), 1, n, TEMP, k->vv, rs, &st->kcount, 1);
   GP_CHECK_LAUNCH();
   if (side == 1) {  // KSPUnwindPreconditioner for right preconditioning
     GP_TRY(r.pcapply(r.G(6), TEMP, TMATOP));
     GP_TRY(r.copy(r.G(6), TMATOP, TEMP));
   }
-  k_axpy_d<<<r.grid(), 256, 0, r.s>>>(r.G(6), 1, n, X, r.S(&KspState::c_one), 1.0, TEMP);
+  FL(k_axpy_d, r.grid(), 256, r.s, r.G(6), 1, n, X, r.S(&KspState::c_one), 1.0, TEMP);
   k_gm_build_ctrl<<<1, 1, 0, r.s>>>(st);
   // ---- restart: r0 = M^-1 (b - A x) (or b), normalised
   k_gm_restart_prep<<<1, 1, 0, r.s>>>(st);
   GP_TRY(r.matmult(r.G(3), X, TEMP));
   GP_TRY(r.copy(r.G(3), B, TMATOP));
-  k_axpy_d<<<r.grid(), 256, 0, r.s>>>(r.G(3), 1, n, TMATOP, r.S(&KspState::c_one), -1.0, TEMP);
+  FL(k_axpy_d, r.grid(), 256, r.s, r.G(3), 1, n, TMATOP, r.S(&KspState::c_one), -1.0, TEMP);
   GP_CHECK_LAUNCH();
   GP_TRY(r.copy(r.G(4), B, TMATOP));
   if (side == 2)
@@ -1185,7 +1426,7 @@ static int fgmres_prologue(const Run& r, const double* b, double* x) {
   DRef TEMP = DRef::of(k->work), VV0 = DRef::of(k->vv);
   if (!k->opt.guess_zero) {  // KSPFGMRESResidual, src/ksp.mojo:871-877
     GP_TRY(r.matmult(nullptr, DRef::of(x), TEMP));
-    k_waxpy_d<<<r.grid(), 256, 0, r.s>>>(nullptr, 1, n, VV0, r.S(&KspState::c_one), -1.0, TEMP,
+    FL(k_waxpy_d, r.grid(), 256, r.s, nullptr, 1, n, VV0, r.S(&KspState::c_one), -1.0, TEMP,
                                          DRef::of(b));
     GP_CHECK_LAUNCH();
   } else {
@@ -1205,12 +1446,12 @@ static int fgmres_body(const Run& r, const double* b, double* x) {
   double* rs = k->hs + (size_t)(m + 2) * (m + 1) + (size_t)(m + 1) * (m + 1) + 2 * (m + 1);
   // ---- build (KSPFGMRESBuildSoln) and the next residual
   k_fg_backsub<<<1, 1, 0, r.s>>>(st, k->hs);
-  k_maxpy_dyn<<<r.grid(), 256, 0, r.s>>>(r.G(8), 1, n, TEMP, k->prevec, rs, &st->kcount, 1);
-  k_axpy_d<<<r.grid(), 256, 0, r.s>>>(r.G(8), 1, n, X, r.S(&KspState::c_one), 1.0, TEMP);
+  FL(k_maxpy_dyn, r.grid(), 256, r.s, r.G(8), 1, n, TEMP, k->prevec, rs, &st->kcount, 1);
+  FL(k_axpy_d, r.grid(), 256, r.s, r.G(8), 1, n, X, r.S(&KspState::c_one), 1.0, TEMP);
   k_fg_build_ctrl<<<1, 1, 0, r.s>>>(st);
   GP_CHECK_LAUNCH();
   GP_TRY(r.matmult(r.G(9), X, TEMP));
-  k_waxpy_d<<<r.grid(), 256, 0, r.s>>>(r.G(9), 1, n, VV0, r.S(&KspState::c_one), -1.0, TEMP, B);
+  FL(k_waxpy_d, r.grid(), 256, r.s, r.G(9), 1, n, VV0, r.S(&KspState::c_one), -1.0, TEMP, B);
   // ---- cycle start: ||r||, convergence test, v_0 = r / ||r|| (by reciprocal)
   GP_TRY(r.red<D_NRM>(r.G(0), VV0, VV0, nullptr, r.S(&KspState::res)));
   k_fg_start_ctrl<<<1, 1, 0, r.s>>>(st, k->hs, k->hist, k->vv, k->prevec, n);
@@ -1256,7 +1497,7 @@ static int capture(const Run& r, const double* b, double* x) {
   GP_CUDA(cudaStreamBeginCapture(r.s, cudaStreamCaptureModeRelaxed));
   int st = GP_OK;
   switch (k->opt.type) {
-    case KSP_CG: st = cg_prologue(r, b, x); break;
+    case KSP_CG: st = cg_fused_ok(r) ? cg_prologue_fused(r, b, x) : cg_prologue(r, b, x); break;
     case KSP_BCGS: st = bcgs_prologue(r, b, x); break;
     case KSP_GMRES: st = gmres_prologue(r); break;
     case KSP_FGMRES: st = fgmres_prologue(r, b, x); break;
@@ -1293,7 +1534,7 @@ static int capture(const Run& r, const double* b, double* x) {
       Run rb = r;
       rb.s = k->stream2;
       switch (k->opt.type) {
-        case KSP_CG: st = cg_body(rb, x); break;
+        case KSP_CG: st = cg_fused_ok(rb) ? cg_body_fused(rb, x) : cg_body(rb, x); break;
         case KSP_BCGS: st = bcgs_body(rb, x); break;
         case KSP_GMRES: st = gmres_body(rb, b, x); break;
         case KSP_FGMRES: st = fgmres_body(rb, b, x); break;
@@ -1394,17 +1635,18 @@ int ksp_solve(Ksp* k, Csr* A, Pc* pc, const double* b, double* x, KspResult* res
   GP_CUDA(cudaMemsetAsync(k->hist, 0, (size_t)k->hist_cap * sizeof(double), s));
   Run r{k, A, pc, n, s};
   // the solve graph depends on the buffers and on every option that shapes it
-  const int key[10] = {o.type, o.normtype, o.pc_side, o.restart, o.cgstype, n, pc->opt.type,
-                       pc->opt.sor_flag, o.guess_zero, (int)(pc->epoch & 0x7fffffff)};
+  const int key[11] = {o.type,      o.normtype,    o.pc_side,          o.restart,
+                       o.cgstype,   n,             pc->opt.type,       pc->opt.sor_flag,
+                       o.guess_zero, (int)(pc->epoch & 0x7fffffff), arith_mode()};
   const bool same = !moved && k->exec && k->cap_A == A && k->cap_pc == pc &&
-                    std::equal(key, key + 10, k->cap_key) && k->cap_b == b && k->cap_x == x;
+                    std::equal(key, key + 11, k->cap_key) && k->cap_b == b && k->cap_x == x;
   if (!same) {
     GP_TRY(capture(r, b, x));
     k->cap_A = A;
     k->cap_pc = pc;
     k->cap_b = b;
     k->cap_x = x;
-    std::copy(key, key + 10, k->cap_key);
+    std::copy(key, key + 11, k->cap_key);
   }
   GP_CUDA(cudaGraphLaunch(k->exec, s));
   GP_CUDA(cudaEventRecord(ev, s));

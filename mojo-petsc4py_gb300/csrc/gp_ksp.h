@@ -83,7 +83,7 @@ struct Ksp {
   const void* cap_pc = nullptr;
   const void* cap_b = nullptr;
   const void* cap_x = nullptr;
-  int cap_key[10] = {0};
+  int cap_key[11] = {0};
   cudaStream_t stream2 = nullptr;  // body capture stream
   int64_t top_kernels = 0;         // kernels outside the loop body
   int64_t body_kernels = 0;        // kernels per loop trip

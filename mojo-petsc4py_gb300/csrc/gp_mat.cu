@@ -183,6 +183,7 @@ int csr_make_val32(Csr* A, cudaStream_t s) {
 
 // y = A x, or y = v + A x when v is given (MatMultAdd starts each row's sum
 // from v_i).  Optional gate for use inside captured solver loops.
+template <bool FMA>
 __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict__ rowptr,
                                                     const int* __restrict__ colind,
                                                     const double* __restrict__ val, DRef xr,
@@ -191,16 +192,33 @@ __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict
   if (gated_off(gate, want)) return;
   const double* __restrict__ x = xr.get();
   double* __restrict__ y = yr.get();
-  __shared__ SpmvSmem<double, double, double> sm;
   const int r0 = blockIdx.x * kSpmvRows;
   const int row = r0 + threadIdx.x;
   double init = (v != nullptr && row < n) ? v[row] : 0.0;
-  double s = spmv_block_rows<double, double, double>(sm, n, r0, rowptr, colind, val, x, init);
+  double s;
+  if constexpr (FMA) {
+    __shared__ SpmvSmemF<double, double, double> sm;
+    s = spmv_block_rows_fma<double, double, double>(sm, n, r0, rowptr, colind, val, x, init);
+  } else {
+    __shared__ SpmvSmem<double, double, double> sm;
+    s = spmv_block_rows<double, double, double>(sm, n, r0, rowptr, colind, val, x, init);
+  }
   if (row < n) y[row] = s;
+}
+
+static void launch_spmv(cudaStream_t s, const Csr* A, DRef x, const double* v, DRef y,
+                        const int* gate, int want) {
+  if (arith_mode() == kFma)
+    k_spmv<true><<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, v, y,
+                                                    gate, want);
+  else
+    k_spmv<false><<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, v,
+                                                     y, gate, want);
 }
 
 // y = A^T x over the stored transpose pattern; values gathered through the
 // source slot so a value update needs no rebuild.
+template <bool FMA>
 __global__ void __launch_bounds__(kBlock) k_spmv_t(int m, const int* __restrict__ trp,
                                                    const int* __restrict__ tcol,
                                                    const int* __restrict__ tsrc,
@@ -210,7 +228,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv_t(int m, const int* __restrict_
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m) return;
   double s = 0.0;
-  for (int k = trp[c]; k < trp[c + 1]; k++) s = add(s, mul(val[tsrc[k]], x[tcol[k]]));
+  for (int k = trp[c]; k < trp[c + 1]; k++) s = madd<FMA>(val[tsrc[k]], x[tcol[k]], s);
   y[c] = s;
 }
 
@@ -226,16 +244,14 @@ int spmv_grid(const Csr* A) { return (A->n + kSpmvRows - 1) / kSpmvRows; }
 
 int spmv(cudaStream_t s, const Csr* A, DRef x, DRef y, const int* gate, int want) {
   if (A->n == 0) return GP_OK;
-  k_spmv<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, nullptr, y,
-                                            gate, want);
+  launch_spmv(s, A, x, nullptr, y, gate, want);
   GP_CHECK_LAUNCH();
   return GP_OK;
 }
 
 int spmv_add(cudaStream_t s, const Csr* A, const double* x, const double* v, double* y) {
   if (A->n == 0) return GP_OK;
-  k_spmv<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, DRef::of(x),
-                                            v, DRef::of(y), nullptr, 0);
+  launch_spmv(s, A, DRef::of(x), v, DRef::of(y), nullptr, 0);
   GP_CHECK_LAUNCH();
   return GP_OK;
 }
@@ -243,9 +259,12 @@ int spmv_add(cudaStream_t s, const Csr* A, const double* x, const double* v, dou
 int spmv_t(cudaStream_t s, Csr* A, const double* x, double* y) {
   GP_TRY(csr_build_transpose(A, s));
   if (A->ncols == 0) return GP_OK;
-  k_spmv_t<<<(A->ncols + kBlock - 1) / kBlock, kBlock, 0, s>>>(A->ncols, A->t_rowptr,
-                                                               A->t_colind, A->t_src, A->val,
-                                                               x, y);
+  const int g = (A->ncols + kBlock - 1) / kBlock;
+  if (arith_mode() == kFma)
+    k_spmv_t<true><<<g, kBlock, 0, s>>>(A->ncols, A->t_rowptr, A->t_colind, A->t_src, A->val, x, y);
+  else
+    k_spmv_t<false><<<g, kBlock, 0, s>>>(A->ncols, A->t_rowptr, A->t_colind, A->t_src, A->val, x,
+                                         y);
   GP_CHECK_LAUNCH();
   return GP_OK;
 }

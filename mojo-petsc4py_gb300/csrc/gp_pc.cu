@@ -140,12 +140,24 @@ __global__ void k_copy_g(const int* gate, int want, int n, DRef xr, DRef yr) {
 // ------------------------------------------------------------------ SOR
 __global__ void k_sor_diag(int n, double omega, double fshift, const int* __restrict__ diagpos,
                            const double* __restrict__ val, double* __restrict__ idiag,
-                           double* __restrict__ mdiag) {
+                           double* __restrict__ mdiag, const int* gate = nullptr, int want = 0) {
+  if (gated_off(gate, want)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double a = val[diagpos[i]];
   mdiag[i] = a;
   idiag[i] = (omega == 1.0 && fshift <= 0.0) ? div_(1.0, a) : div_(omega, add(fshift, a));
+}
+
+// SOR's ELL coefficients follow A's current values (gathered each apply)
+__global__ void k_ell_refresh_g(const int* gate, int want, int n, const int* __restrict__ cnt,
+                                const int* __restrict__ cslot, const double* __restrict__ src,
+                                double* __restrict__ coef) {
+  if (gated_off(gate, want)) return;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const int c = cnt[p];
+    for (int e = 0; e < c; e++) coef[(size_t)e * n + p] = src[cslot[(size_t)e * n + p]];
+  }
 }
 
 __global__ void k_fill_pending(const int* gate, int want, int n, double* __restrict__ a,
@@ -418,6 +430,8 @@ static void free_all(Pc* pc) {
                   pc->err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  ell_free(pc->ef);
+  ell_free(pc->eb);
   PcOptions keep = pc->opt;
   *pc = Pc();
   pc->opt = keep;
@@ -436,9 +450,10 @@ int pc_destroy(Pc* pc) {
 }
 
 static int plan(SweepPlan& p, int n, const std::vector<int>& dptr, const std::vector<int>& dcol,
-                bool forward, cudaStream_t s) {
+                bool forward, cudaStream_t s, std::vector<int>* order_out = nullptr) {
   std::vector<int> order;
   level_order(n, dptr, dcol, forward, order, &p.nlevels);
+  if (order_out) *order_out = order;
   GP_TRY(upload(&p.order, order, s));
   return GP_OK;
 }
@@ -483,18 +498,27 @@ static int setup_sor(Pc* pc, cudaStream_t s) {
   GP_TRY(dalloc(&pc->t, n));
   GP_TRY(dalloc(&pc->yf, n));
   GP_TRY(dalloc(&pc->yb, n));
-  std::vector<int> lp(n + 1, 0), lc, up(n + 1, 0), uc;
+  std::vector<int> lp(n + 1, 0), lc, ls, up(n + 1, 0), uc, us;
   for (int i = 0; i < n; i++) {
     for (int j = A->h_rowptr[i]; j < A->h_rowptr[i + 1]; j++) {
       int c = A->h_colind[j];
-      if (c < i) lc.push_back(c);
-      if (c > i) uc.push_back(c);
+      if (c < i) {
+        lc.push_back(c);
+        ls.push_back(j);
+      }
+      if (c > i) {
+        uc.push_back(c);
+        us.push_back(j);
+      }
     }
     lp[i + 1] = (int)lc.size();
     up[i + 1] = (int)uc.size();
   }
-  GP_TRY(plan(pc->fwd, n, lp, lc, true, s));
-  GP_TRY(plan(pc->bwd, n, up, uc, false, s));
+  std::vector<int> of, ob, fpos, none;
+  GP_TRY(plan(pc->fwd, n, lp, lc, true, s, &of));
+  GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
+  GP_TRY(ell_build(pc->ef, n, of, lp, lc, ls, none, none, none, &fpos));
+  GP_TRY(ell_build(pc->eb, n, ob, up, uc, us, fpos, none, none, nullptr));
   if (n) {
     k_sor_diag<<<(n + 255) / 256, 256, 0, s>>>(n, pc->opt.omega, pc->opt.fshift, A->diagpos,
                                                 A->val, pc->idiag, pc->mdiag);
@@ -523,16 +547,24 @@ static int perms(Pc* pc, std::vector<int>& r, std::vector<int>& ic) {
 static int ilu_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
   const int n = pc->n;
   FactorPattern& P = pc->pat;
-  std::vector<int> lp(n + 1), lc(P.bj.begin(), P.bj.begin() + P.bi[n]);
+  std::vector<int> lp(n + 1), lc(P.bj.begin(), P.bj.begin() + P.bi[n]), ls(P.bi[n]);
   for (int i = 0; i <= n; i++) lp[i] = P.bi[i];
-  std::vector<int> up(n + 1, 0), uc;
+  for (int j = 0; j < P.bi[n]; j++) ls[j] = j;
+  std::vector<int> up(n + 1, 0), uc, us, dsl(n);
   uc.reserve(std::max(P.nnz - P.bi[n], 0));
   for (int i = 0; i < n; i++) {
-    for (int j = P.bdiag[i + 1] + 1; j < P.bdiag[i]; j++) uc.push_back(P.bj[j]);
+    for (int j = P.bdiag[i + 1] + 1; j < P.bdiag[i]; j++) {
+      uc.push_back(P.bj[j]);
+      us.push_back(j);
+    }
     up[i + 1] = (int)uc.size();
+    dsl[i] = P.bdiag[i];
   }
-  GP_TRY(plan(pc->fwd, n, lp, lc, true, s));
-  GP_TRY(plan(pc->bwd, n, up, uc, false, s));
+  std::vector<int> of, ob, fpos, none;
+  GP_TRY(plan(pc->fwd, n, lp, lc, true, s, &of));
+  GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
+  GP_TRY(ell_build(pc->ef, n, of, lp, lc, ls, P.r, none, none, &fpos));
+  GP_TRY(ell_build(pc->eb, n, ob, up, uc, us, fpos, perm_c, dsl, nullptr));
   GP_TRY(upload(&pc->bi, P.bi, s));
   GP_TRY(upload(&pc->bj, P.bj, s));
   GP_TRY(upload(&pc->bdiag, P.bdiag, s));
@@ -649,9 +681,17 @@ static int icc_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
     up[i + 1] = (int)uc.size();
   }
   std::vector<int> trow_deps(trow.begin(), trow.begin() + tptr[n]);
+  std::vector<int> tsl(tslot.begin(), tslot.begin() + tptr[n]), us, dsl(n);
+  for (int i = 0; i < n; i++) {
+    for (int j = P.bi[i]; j < P.bdiag[i]; j++) us.push_back(j);
+    dsl[i] = P.bdiag[i];
+  }
+  std::vector<int> of, ob, fpos, none;
   GP_TRY(plan(pc->num, n, cptr, crow, true, s));
-  GP_TRY(plan(pc->fwd, n, tptr, trow_deps, true, s));
-  GP_TRY(plan(pc->bwd, n, up, uc, false, s));
+  GP_TRY(plan(pc->fwd, n, tptr, trow_deps, true, s, &of));
+  GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
+  GP_TRY(ell_build(pc->ef, n, of, tptr, trow_deps, tsl, perm_c, none, dsl, &fpos));
+  GP_TRY(ell_build(pc->eb, n, ob, up, uc, us, fpos, perm_c, none, nullptr));
   GP_TRY(upload(&pc->bi, P.bi, s));
   GP_TRY(upload(&pc->bj, P.bj, s));
   GP_TRY(upload(&pc->bdiag, P.bdiag, s));
@@ -726,6 +766,8 @@ int pc_factor_numeric(Pc* pc, cudaStream_t s) {
         pc->err);
   }
   GP_CHECK_LAUNCH();
+  GP_TRY(ell_refresh(pc->ef, pc->ba, s));
+  GP_TRY(ell_refresh(pc->eb, pc->ba, s));
   return pc_check(pc, s);
 }
 
@@ -797,7 +839,24 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
       const Csr* A = pc->A;
       const int flag = pc->opt.sor_flag;
       const bool fw = flag & kSorForward, bw = flag & kSorBackward;
+      // MatInvertDiagonalForSOR_SeqAIJ runs on every apply, from the current
+      // values, as in the reference
+      k_sor_diag<<<(n + 255) / 256, 256, 0, s>>>(n, pc->opt.omega, pc->opt.fshift, A->diagpos,
+                                                  A->val, pc->idiag, pc->mdiag, gate, want);
       k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
+      if (pc->ef.ok && pc->eb.ok) {
+        k_ell_refresh_g<<<g, 256, 0, s>>>(gate, want, pc->ef.n, pc->ef.cnt, pc->ef.cslot, A->val,
+                                          pc->ef.coef);
+        k_ell_refresh_g<<<g, 256, 0, s>>>(gate, want, pc->eb.n, pc->eb.cnt, pc->eb.cslot, A->val,
+                                          pc->eb.coef);
+        if (fw)
+          GP_TRY(ell_sweep(ELL_SOR_F, pc->ef, gate, want, x, y, pc->yf, nullptr, pc->t, nullptr,
+                           pc->idiag, pc->opt.omega, 0, bw ? 0 : 1, tk0, pc->err, s));
+        if (bw)
+          GP_TRY(ell_sweep(ELL_SOR_B, pc->eb, gate, want, x, y, pc->yb, pc->yf, nullptr, pc->t,
+                           pc->idiag, pc->opt.omega, fw ? 1 : 0, 1, tk1, pc->err, s));
+        break;
+      }
       if (fw)
         k_sor_fwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->fwd.order, tk0, A->rowptr,
                                              A->colind, A->val, A->diagpos, pc->idiag, x, pc->t,
@@ -811,6 +870,13 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
     }
     case PC_ILU:
       k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
+      if (pc->ef.ok && pc->eb.ok) {
+        GP_TRY(ell_sweep(ELL_ILU_F, pc->ef, gate, want, x, y, pc->yf, nullptr, nullptr, nullptr,
+                         nullptr, 0.0, 0, 0, tk0, pc->err, s));
+        GP_TRY(ell_sweep(ELL_ILU_B, pc->eb, gate, want, x, y, pc->yb, pc->yf, nullptr, nullptr,
+                         nullptr, 0.0, 0, 1, tk1, pc->err, s));
+        break;
+      }
       k_ilu_fwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->fwd.order, tk0, pc->bi, pc->bj,
                                            pc->ba, pc->perm_r, x, pc->yf, pc->err);
       k_ilu_bwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->bwd.order, tk1, pc->bj, pc->ba,
@@ -818,6 +884,13 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
       break;
     case PC_ICC:
       k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
+      if (pc->ef.ok && pc->eb.ok) {
+        GP_TRY(ell_sweep(ELL_ICC_F, pc->ef, gate, want, x, y, pc->yf, nullptr, pc->ys, nullptr,
+                         nullptr, 0.0, 0, 0, tk0, pc->err, s));
+        GP_TRY(ell_sweep(ELL_ICC_B, pc->eb, gate, want, x, y, pc->yb, nullptr, nullptr, pc->ys,
+                         nullptr, 0.0, 0, 1, tk1, pc->err, s));
+        break;
+      }
       k_icc_fwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->fwd.order, tk0, pc->tptr,
                                            pc->trow, pc->tslot, pc->ba, pc->bdiag, pc->perm_c, x,
                                            pc->yf, pc->ys, pc->err);
@@ -867,9 +940,12 @@ int pc_import_factor(Pc* pc, int type, const FactorPattern& pat, const std::vect
     set_error("pc_import_factor: ILU or IC only");
     return GP_ERR_ARG;
   }
-  if (ba_host && pat.nnz)
+  if (ba_host && pat.nnz) {
     GP_CUDA(cudaMemcpyAsync(pc->ba, ba_host, (size_t)pat.nnz * sizeof(double),
                             cudaMemcpyHostToDevice, s));
+    GP_TRY(ell_refresh(pc->ef, pc->ba, s));
+    GP_TRY(ell_refresh(pc->eb, pc->ba, s));
+  }
   GP_CUDA(cudaStreamSynchronize(s));
   pc->ready = true;
   return GP_OK;

@@ -33,6 +33,35 @@ struct SweepPlan {
   int nlevels = 0;
 };
 
+// A sweep laid out in processing order for the ELL sweep kernels
+// (gp_sweep.cu); `ok` is false when some row has more than kEllMaxW
+// dependencies, and the CSR sweep kernels are used instead.
+constexpr int kEllMaxW = 16;
+enum EllMode : int { ELL_ILU_F, ELL_ILU_B, ELL_ICC_F, ELL_ICC_B, ELL_SOR_F, ELL_SOR_B };
+struct EllSweep {
+  int n = 0, W = 0;
+  bool ok = false;
+  int* cnt = nullptr;
+  int* dep = nullptr;
+  int* cslot = nullptr;
+  int* in_idx = nullptr;
+  int* out_idx = nullptr;
+  int* dslot = nullptr;
+  int* rowof = nullptr;
+  double* coef = nullptr;
+  double* dval = nullptr;
+};
+void ell_free(EllSweep& e);
+int ell_build(EllSweep& e, int n, const std::vector<int>& order, const std::vector<int>& dptr,
+              const std::vector<int>& dcol, const std::vector<int>& dsl,
+              const std::vector<int>& in_row, const std::vector<int>& out_row,
+              const std::vector<int>& dslot_row, std::vector<int>* pos_of_row);
+int ell_refresh(EllSweep& e, const double* src, cudaStream_t s);
+int ell_sweep(int mode, const EllSweep& e, const int* gate, int want, DRef in, DRef out,
+              double* val, const double* fval, double* aux, const double* auxin,
+              const double* idiag, double omega, int use_t, int write_out, unsigned* tickets,
+              DevErr* err, cudaStream_t s);
+
 // Host copy of a factor pattern in the reference's layout.
 struct FactorPattern {
   // ILU: L rows bi[i]..bi[i+1], U rows (reversed) ending on the diagonal at
@@ -81,6 +110,7 @@ struct Pc {
   int* amap = nullptr;       // A slot -> factor slot (or -1)
 
   SweepPlan fwd, bwd, num;
+  EllSweep ef, eb;           // ELL forms of the forward and backward sweeps
   // sweep work: value-as-flag arrays and SOR checkpoint
   double* yf = nullptr;
   double* yb = nullptr;

@@ -1,4 +1,5 @@
 // Library-wide utilities: error text, device properties, standalone scratch.
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <unordered_map>
@@ -11,6 +12,18 @@ static thread_local std::string g_err;
 
 void set_error(const std::string& msg) { g_err = msg; }
 const char* last_error() { return g_err.c_str(); }
+
+static int g_arith = -1;
+
+int arith_mode() {
+  if (g_arith < 0) {
+    const char* e = std::getenv("GPETSC_ARITHMETIC");
+    g_arith = (e && std::string(e) == "exact") ? kExact : kFma;
+  }
+  return g_arith;
+}
+
+void set_arith_mode(int mode) { g_arith = mode ? kFma : kExact; }
 
 int num_sms() {
   static int cached[64] = {0};

@@ -14,7 +14,7 @@ namespace gp {
 
 // ------------------------------------------------------------------ maps
 
-template <int OP>
+template <int OP, bool FMA>
 __global__ void __launch_bounds__(kBlock) k_map(int64_t n, double* __restrict__ y,
                                                 const double* __restrict__ x,
                                                 const double* __restrict__ w, double alpha,
@@ -36,15 +36,15 @@ __global__ void __launch_bounds__(kBlock) k_map(int64_t n, double* __restrict__ 
     } else if constexpr (OP == OP_SHIFT) {
       y[i] = add(y[i], alpha);
     } else if constexpr (OP == OP_AXPY) {  // y + alpha x
-      y[i] = add(y[i], mul(alpha, x[i]));
+      y[i] = madd<FMA>(alpha, x[i], y[i]);
     } else if constexpr (OP == OP_AYPX) {  // x + alpha y
-      y[i] = add(x[i], mul(alpha, y[i]));
+      y[i] = madd<FMA>(alpha, y[i], x[i]);
     } else if constexpr (OP == OP_AXPBY) {  // alpha x + beta y
-      y[i] = add(mul(alpha, x[i]), mul(beta, y[i]));
+      y[i] = madd<FMA>(alpha, x[i], mul(beta, y[i]));
     } else if constexpr (OP == OP_AXPBYPCZ) {  // alpha x + beta w + gamma y
-      y[i] = add(add(mul(alpha, x[i]), mul(beta, w[i])), mul(gamma, y[i]));
+      y[i] = madd<FMA>(gamma, y[i], madd<FMA>(beta, w[i], mul(alpha, x[i])));
     } else if constexpr (OP == OP_WAXPY) {  // alpha x + w
-      y[i] = add(mul(alpha, x[i]), w[i]);
+      y[i] = madd<FMA>(alpha, x[i], w[i]);
     } else if constexpr (OP == OP_PMULT) {
       y[i] = mul(x[i], w[i]);
     } else if constexpr (OP == OP_PDIV) {
@@ -94,7 +94,10 @@ template <int OP>
 static int launch_map(cudaStream_t s, int64_t n, double* y, const double* x, const double* w,
                       double a, double b, double c) {
   if (n <= 0) return GP_OK;
-  k_map<OP><<<map_grid(n), kBlock, 0, s>>>(n, y, x, w, a, b, c);
+  if (arith_mode() == kFma)
+    k_map<OP, true><<<map_grid(n), kBlock, 0, s>>>(n, y, x, w, a, b, c);
+  else
+    k_map<OP, false><<<map_grid(n), kBlock, 0, s>>>(n, y, x, w, a, b, c);
   GP_CHECK_LAUNCH();
   return GP_OK;
 }
@@ -162,11 +165,12 @@ struct MaxpyArgs {
   int nv;
 };
 
+template <bool FMA>
 __global__ void __launch_bounds__(kBlock) k_maxpy(int64_t n, double* __restrict__ y, MaxpyArgs args) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     double v = y[i];
-    for (int k = 0; k < args.nv; k++) v = add(v, mul(args.a[k], args.x[k][i]));
+    for (int k = 0; k < args.nv; k++) v = madd<FMA>(args.a[k], args.x[k][i], v);
     y[i] = v;
   }
 }
@@ -181,14 +185,17 @@ int vec_maxpy(cudaStream_t s, int64_t n, double* y, int nv, const double* alpha,
       args.x[k] = xs[k0 + k];
       args.a[k] = alpha[k0 + k];
     }
-    k_maxpy<<<map_grid(n), kBlock, 0, s>>>(n, y, args);
+    if (arith_mode() == kFma)
+      k_maxpy<true><<<map_grid(n), kBlock, 0, s>>>(n, y, args);
+    else
+      k_maxpy<false><<<map_grid(n), kBlock, 0, s>>>(n, y, args);
     GP_CHECK_LAUNCH();
   }
   return GP_OK;
 }
 
 // ------------------------------------------------------------------ reductions
-template <int OP>
+template <int OP, bool FMA>
 __global__ void __launch_bounds__(kRedBlock) k_reduce(int64_t n, const double* __restrict__ x,
                                                       const double* __restrict__ y, RedSlot slot,
                                                       double* out) {
@@ -200,16 +207,16 @@ __global__ void __launch_bounds__(kRedBlock) k_reduce(int64_t n, const double* _
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     double a = x[i];
     if constexpr (OP == RED_DOT) {
-      v[0] = add(v[0], mul(a, y[i]));
+      v[0] = madd<FMA>(a, y[i], v[0]);
     } else if constexpr (OP == RED_NORM2SQ) {
-      v[0] = add(v[0], mul(a, a));
+      v[0] = madd<FMA>(a, a, v[0]);
     } else if constexpr (OP == RED_ASUM) {
       v[0] = add(v[0], fabs(a));
     } else if constexpr (OP == RED_SUM) {
       v[0] = add(v[0], a);
     } else if constexpr (OP == RED_DOTNORM2) {
-      v[0] = add(v[0], mul(a, y[i]));
-      v[1] = add(v[1], mul(a, a));
+      v[0] = madd<FMA>(a, y[i], v[0]);
+      v[1] = madd<FMA>(a, a, v[1]);
     }
   }
   double tot[NR];
@@ -279,21 +286,24 @@ int vec_reduce(cudaStream_t s, int op, int64_t n, const double* x, const double*
     return GP_OK;
   }
   int g = red_grid(n);
+  const bool f = arith_mode() == kFma;
+#define RED_LAUNCH(OPC)                                                              \
+  if (f)                                                                             \
+    k_reduce<OPC, true><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out);        \
+  else                                                                               \
+    k_reduce<OPC, false><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out);
   switch (op) {
-    case RED_DOT: k_reduce<RED_DOT><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out); break;
-    case RED_NORM2SQ:
-      k_reduce<RED_NORM2SQ><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out);
-      break;
-    case RED_ASUM: k_reduce<RED_ASUM><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out); break;
-    case RED_SUM: k_reduce<RED_SUM><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out); break;
-    case RED_DOTNORM2:
-      k_reduce<RED_DOTNORM2><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out);
-      break;
+    case RED_DOT: RED_LAUNCH(RED_DOT); break;
+    case RED_NORM2SQ: RED_LAUNCH(RED_NORM2SQ); break;
+    case RED_ASUM: RED_LAUNCH(RED_ASUM); break;
+    case RED_SUM: RED_LAUNCH(RED_SUM); break;
+    case RED_DOTNORM2: RED_LAUNCH(RED_DOTNORM2); break;
     case RED_NORMINF:
       k_maxabs<false><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out);
       break;
     default: set_error("vec_reduce: unknown op"); return GP_ERR_ARG;
   }
+#undef RED_LAUNCH
   GP_CHECK_LAUNCH();
   GP_CUDA(cudaMemcpyAsync(sc->h_out, sc->d_out, nr * sizeof(double), cudaMemcpyDeviceToHost, s));
   GP_CUDA(cudaStreamSynchronize(s));

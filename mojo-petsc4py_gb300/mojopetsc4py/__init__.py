@@ -6,8 +6,9 @@ on the GPU through libgpetsc.so (include/gpetsc.h).
 """
 
 from . import PETSc  # noqa: F401
+from ._lib import get_arithmetic, set_arithmetic  # noqa: F401
 
 __version__ = "0.1.0"
 __upstream__ = "petsc4py 3.25.5"
 
-__all__ = ["PETSc"]
+__all__ = ["PETSc", "get_arithmetic", "set_arithmetic"]

@@ -64,6 +64,8 @@ class KspResult(ctypes.Structure):
 GP_SIGNATURES = {
     "gp_version": ([], ctypes.c_int),
     "gp_last_error": ([], ctypes.c_char_p),
+    "gp_set_arithmetic": ([ctypes.c_int], ctypes.c_int),
+    "gp_get_arithmetic": ([], ctypes.c_int),
     "gp_device_count": ([ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     "gp_set_device": ([ctypes.c_int], ctypes.c_int),
     "gp_mat_create": ([PP, I64, I64, I64, P, P, P], ctypes.c_int),
@@ -140,6 +142,22 @@ def device_count() -> int:
     c = ctypes.c_int(0)
     check(lib().gp_device_count(ctypes.byref(c)))
     return c.value
+
+
+ARITHMETIC = {"exact": 0, "fma": 1}
+
+
+def set_arithmetic(mode: str) -> None:
+    """Select the kernels' floating-point form: "exact" (every product and
+    sum rounded separately, bit-identical to the reference's loops) or "fma"
+    (fused multiply-adds, the default)."""
+    if mode not in ARITHMETIC:
+        raise ValueError(f"arithmetic must be one of {sorted(ARITHMETIC)}, got {mode!r}")
+    check(lib().gp_set_arithmetic(ARITHMETIC[mode]))
+
+
+def get_arithmetic() -> str:
+    return {v: k for k, v in ARITHMETIC.items()}[lib().gp_get_arithmetic()]
 
 
 def require_device() -> None:

@@ -116,6 +116,8 @@ def lib() -> ctypes.CDLL:
 
 
 def a(arr) -> int:
+    """The data address of `arr`.  The caller must keep `arr` referenced until
+    the call that uses the address returns (never pass a temporary)."""
     return arr.ctypes.data
 
 
@@ -289,12 +291,14 @@ class OraclePC:
                               self.omega, self.fshift, self.sor_flag(), n)
         elif self.type == "ilu":
             f = self.factor
-            L.mp_pc_ilu_apply(a(x), a(y), a(np.zeros(n)), a(f["bi"]), a(f["bj"]), a(f["ba"]),
+            tmp = np.zeros(n)
+            L.mp_pc_ilu_apply(a(x), a(y), a(tmp), a(f["bi"]), a(f["bj"]), a(f["ba"]),
                               a(f["bdiag"]), a(f["r"]), a(f["c"]), n)
         else:
             f = self.factor
+            scratch = np.zeros(n)
             L.mp_pc_icc_apply(a(x), a(y), a(f["bi"]), a(f["bj"]), a(f["ba"]), a(f["bdiag"]),
-                              a(f["r"]), a(np.zeros(n)), n)
+                              a(f["r"]), a(scratch), n)
         return y
 
 

