@@ -138,30 +138,75 @@ __device__ __forceinline__ double madd(double a, double x, double y) {
     return __dadd_rn(__dmul_rn(a, x), y);
 }
 
+// Grid-stride element loop in passes of U elements per thread: load(u, i)
+// stages a pass's loads in registers, then emit(u, i) computes and stores, so
+// U independent loads of every operand are in flight before the first store
+// (operands that may alias -- W and Z in CG -- are still read before the same
+// element is written).  Each thread visits tid, tid + stride, ... in
+// ascending order, exactly as the plain grid-stride loop does, so reductions
+// fold in the same order.
+constexpr int kVecBatch = 4;
+template <int U, typename L, typename E>
+__device__ __forceinline__ void grid_batched(int n, L&& load, E&& emit) {
+  // 32-bit unsigned indices: i0 < n < 2^31 and U * stride < 2^31
+  const unsigned st = gridDim.x * blockDim.x, un = (unsigned)n;
+  for (unsigned i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < un; i0 += U * st) {
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const unsigned i = i0 + u * st;
+      if (i < un) load(u, i);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const unsigned i = i0 + u * st;
+      if (i < un) emit(u, i);
+    }
+  }
+}
+
+// Ticket increment with acquire-release semantics at GPU scope: releases
+// this thread's earlier writes (and, cumulatively, the CTA's writes ordered
+// before it by a barrier) and acquires the writes released by earlier
+// increments.  Replaces a full fence (costly across the two dies) plus a
+// relaxed atomic.
+__device__ __forceinline__ unsigned atomic_add_acq_rel(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;"
+               : "=r"(old)
+               : "l"(p), "r"(v)
+               : "memory");
+  return old;
+}
+
 // ------------------------------------------------------------------ reduction
-// Deterministic block reduction of NR doubles (result valid in thread 0).
+// Deterministic block reduction of NR doubles (result valid in thread 0);
+// blockDim.x a power of two in [32, kRedBlock].  FP64 issue is the scarce
+// resource on this part (2 FP64 lanes per clock per SM), so the tree keeps
+// whole warps busy at every level: the halves fold in shared memory
+// (128 + 64 + 32 lanes for 256 values) and one warp finishes with five
+// shuffles -- 12 FP64 warp instructions per value instead of 45 for a
+// per-warp shuffle tree.
 template <int NR>
 __device__ __forceinline__ void block_sum(double (&v)[NR]) {
-  __shared__ double sh[NR][kRedBlock / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __shared__ double sh[NR][kRedBlock];
+  const int t = threadIdx.x;
 #pragma unroll
-  for (int r = 0; r < NR; r++) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[r] = add(v[r], __shfl_down_sync(0xffffffffu, v[r], o));
-  }
-  if (lane == 0) {
-#pragma unroll
-    for (int r = 0; r < NR; r++) sh[r][wid] = v[r];
-  }
+  for (int r = 0; r < NR; r++) sh[r][t] = v[r];
   __syncthreads();
-  if (wid == 0) {
-    const int nw = blockDim.x >> 5;
+  for (int h = blockDim.x >> 1; h >= 32; h >>= 1) {
+    if (t < h) {
+#pragma unroll
+      for (int r = 0; r < NR; r++) sh[r][t] = add(sh[r][t], sh[r][t + h]);
+    }
+    __syncthreads();
+  }
+  if (t < 32) {
 #pragma unroll
     for (int r = 0; r < NR; r++) {
-      double t = lane < nw ? sh[r][lane] : 0.0;
+      double x = sh[r][t];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) t = add(t, __shfl_down_sync(0xffffffffu, t, o));
-      v[r] = t;
+      for (int o = 16; o > 0; o >>= 1) x = add(x, __shfl_down_sync(0xffffffffu, x, o));
+      v[r] = x;
     }
   }
   __syncthreads();
@@ -185,20 +230,30 @@ __device__ __forceinline__ bool grid_finish(double (&v)[NR], RedSlot slot, doubl
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int r = 0; r < NR; r++) slot.partials[r * slot.stride + blockIdx.x] = v[r];
-    __threadfence();
-    unsigned t = atomicAdd(slot.ticket, 1u);
-    last = (t == gridDim.x - 1);
+    last = atomic_add_acq_rel(slot.ticket, 1u) == gridDim.x - 1;
   }
   __syncthreads();
   if (!last) return false;
-  __threadfence();
+  // partials are read through L2 (ld.global.cg), several in flight per
+  // thread; each thread still folds b = tid, tid + blockDim, ... in order
   double acc[NR];
 #pragma unroll
   for (int r = 0; r < NR; r++) acc[r] = 0.0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+  constexpr int U = 8;
+  const int nb = gridDim.x, bs = blockDim.x;
+  for (int b0 = threadIdx.x; b0 < nb; b0 += U * bs) {
 #pragma unroll
-    for (int r = 0; r < NR; r++)
-      acc[r] = add(acc[r], ld_relaxed(&slot.partials[r * slot.stride + b]));
+    for (int r = 0; r < NR; r++) {
+      double t[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int b = b0 + u * bs;
+        t[u] = b < nb ? __ldcg(&slot.partials[r * slot.stride + b]) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (b0 + u * bs < nb) acc[r] = add(acc[r], t[u]);
+    }
   }
   block_sum<NR>(acc);
   if (threadIdx.x == 0) {

@@ -63,6 +63,7 @@ struct Csr {
   double* val = nullptr;     // device, nnz
   float* val32 = nullptr;    // device, nnz (mixed-precision copy, lazily made)
   int* diagpos = nullptr;    // device, n: slot of a_ii or -1
+  bool stream_rows = false;  // SpMV form: false row per thread, true row stream
   // transpose (built on demand): rows of A^T in ascending original row order
   int* t_rowptr = nullptr;
   int* t_colind = nullptr;

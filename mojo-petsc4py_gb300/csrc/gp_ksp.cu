@@ -18,6 +18,7 @@
 // number of trips so the loop always ends.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -75,11 +76,31 @@ static int vgrid(int n) { return std::max(1, std::min((n + 255) / 256, num_sms()
 #define GRID_LOOP(i, n)                                                          \
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
 
+// y_i = f(a_i, b_i, c_i) over NIN inputs, in batched passes (grid_batched):
+// all loads of a pass before its stores; an input may be the output itself.
+template <int NIN, typename F>
+__device__ __forceinline__ void ew(int n, double* y, F f, const double* a,
+                                   const double* b = nullptr, const double* c = nullptr) {
+  constexpr int U = kVecBatch;
+  double av[U], bv[U] = {}, cv[U] = {};
+  grid_batched<U>(
+      n,
+      [&](int u, unsigned i) {
+        av[u] = a[i];
+        if constexpr (NIN > 1) bv[u] = b[i];
+        if constexpr (NIN > 2) cv[u] = c[i];
+      },
+      [&](int u, unsigned i) {
+        y[i] = f(av[u], bv[u], cv[u]);
+      });
+}
+
+constexpr int kBodyUnroll = 1;  // default loop-body copies per graph trip
+constexpr int kEagerPoll = 8;   // host-driven loop: trips between state polls
+
 __global__ void k_copy_d(const int* gate, int want, int n, DRef xr, DRef yr) {
   if (gated_off(gate, want)) return;
-  const double* x = xr.get();
-  double* y = yr.get();
-  GRID_LOOP(i, n) y[i] = x[i];
+  ew<1>(n, yr.get(), [](double a, double, double) { return a; }, xr.get());
 }
 
 __global__ void k_zero_d(const int* gate, int want, int n, DRef yr) {
@@ -94,9 +115,8 @@ __global__ void k_axpy_d(const int* gate, int want, int n, DRef yr, const double
                          DRef xr) {
   if (gated_off(gate, want)) return;
   double* y = yr.get();
-  const double* x = xr.get();
   const double al = mul(sgn, *a);
-  GRID_LOOP(i, n) y[i] = madd<FMA>(al, x[i], y[i]);
+  ew<2>(n, y, [=](double xv, double yv, double) { return madd<FMA>(al, xv, yv); }, xr.get(), y);
 }
 
 // y = x + alpha y (VecAYPX, general branch) with a host scalar
@@ -104,8 +124,8 @@ template <bool FMA>
 __global__ void k_aypx_h(const int* gate, int want, int n, DRef yr, double alpha, DRef xr) {
   if (gated_off(gate, want)) return;
   double* y = yr.get();
-  const double* x = xr.get();
-  GRID_LOOP(i, n) y[i] = madd<FMA>(alpha, y[i], x[i]);
+  ew<2>(n, y, [=](double yv, double xv, double) { return madd<FMA>(alpha, yv, xv); }, y,
+        xr.get());
 }
 
 // VecAYPX(y, *a, x) with the reference's branch structure decided on the
@@ -116,13 +136,12 @@ __global__ void k_aypx_d(const int* gate, int want, int n, DRef yr, const double
   double* y = yr.get();
   const double* x = xr.get();
   const double al = *a;
-  if (al == 0.0) {
-    GRID_LOOP(i, n) y[i] = x[i];
-  } else if (al == 1.0) {
-    GRID_LOOP(i, n) y[i] = madd<FMA>(al, x[i], y[i]);
-  } else {
-    GRID_LOOP(i, n) y[i] = madd<FMA>(al, y[i], x[i]);
-  }
+  if (al == 0.0)
+    ew<1>(n, y, [](double xv, double, double) { return xv; }, x);
+  else if (al == 1.0)
+    ew<2>(n, y, [=](double xv, double yv, double) { return madd<FMA>(al, xv, yv); }, x, y);
+  else
+    ew<2>(n, y, [=](double yv, double xv, double) { return madd<FMA>(al, yv, xv); }, y, x);
 }
 
 // z = a x + b y + c z      (VecAXPBYPCZ with device scalars)
@@ -131,10 +150,13 @@ __global__ void k_axpbypcz_d(const int* gate, int want, int n, DRef zr, const do
                              const double* b, const double* c, DRef xr, DRef yr) {
   if (gated_off(gate, want)) return;
   double* z = zr.get();
-  const double* x = xr.get();
-  const double* y = yr.get();
   const double al = *a, be = *b, ga = *c;
-  GRID_LOOP(i, n) z[i] = madd<FMA>(ga, z[i], madd<FMA>(be, y[i], mul(al, x[i])));
+  ew<3>(
+      n, z,
+      [=](double zv, double yv, double xv) {
+        return madd<FMA>(ga, zv, madd<FMA>(be, yv, mul(al, xv)));
+      },
+      z, yr.get(), xr.get());
 }
 
 // w = (sgn * a) x + y      (VecWAXPY)
@@ -142,11 +164,9 @@ template <bool FMA>
 __global__ void k_waxpy_d(const int* gate, int want, int n, DRef wr, const double* a, double sgn,
                           DRef xr, DRef yr) {
   if (gated_off(gate, want)) return;
-  double* w = wr.get();
-  const double* x = xr.get();
-  const double* y = yr.get();
   const double al = mul(sgn, *a);
-  GRID_LOOP(i, n) w[i] = madd<FMA>(al, x[i], y[i]);
+  ew<2>(n, wr.get(), [=](double xv, double yv, double) { return madd<FMA>(al, xv, yv); },
+        xr.get(), yr.get());
 }
 
 // x = x * (*a)   (VecScale)  or  x = x / (*a) when *a > 0 (VecNormalize)
@@ -157,9 +177,9 @@ __global__ void k_scale_d(const int* gate, int want, int n, DRef xr, const doubl
   const double al = *a;
   if (DIVIDE) {
     if (!(al > 0.0)) return;
-    GRID_LOOP(i, n) x[i] = div_(x[i], al);
+    ew<1>(n, x, [=](double xv, double, double) { return div_(xv, al); }, x);
   } else {
-    GRID_LOOP(i, n) x[i] = mul(x[i], al);
+    ew<1>(n, x, [=](double xv, double, double) { return mul(xv, al); }, x);
   }
 }
 
@@ -170,10 +190,20 @@ __global__ void k_cg_xr(const int* gate, int want, int n, double* __restrict__ x
                         const double* __restrict__ w, const double* a) {
   if (gated_off(gate, want)) return;
   const double al = *a, nal = -al;
-  GRID_LOOP(i, n) {
-    x[i] = madd<FMA>(al, p[i], x[i]);
-    r[i] = madd<FMA>(nal, w[i], r[i]);
-  }
+  constexpr int U = kVecBatch;
+  double pv[U], xv[U], wv[U], rv[U];
+  grid_batched<U>(
+      n,
+      [&](int u, unsigned i) {
+        pv[u] = p[i];
+        xv[u] = x[i];
+        wv[u] = w[i];
+        rv[u] = r[i];
+      },
+      [&](int u, unsigned i) {
+        x[i] = madd<FMA>(al, pv[u], xv[u]);
+        r[i] = madd<FMA>(nal, wv[u], rv[u]);
+      });
 }
 
 // ------------------------------------------------------------ reductions
@@ -193,15 +223,18 @@ __global__ void __launch_bounds__(kRedBlock) k_dred(const int* gate, int want, i
   double v[NR];
 #pragma unroll
   for (int r = 0; r < NR; r++) v[r] = 0.0;
-  GRID_LOOP(i, n) {
-    const double a = x[i];
-    if (OP == D_DOTNRM) {
-      v[0] = madd<FMA>(a, y[i], v[0]);
-      v[NR - 1] = madd<FMA>(a, a, v[NR - 1]);
-    } else {
-      v[0] = madd<FMA>(a, y[i], v[0]);
-    }
-  }
+  constexpr int U = kVecBatch;
+  double xv[U], yv[U];
+  grid_batched<U>(
+      n,
+      [&](int u, unsigned i) {
+        xv[u] = x[i];
+        yv[u] = OP == D_NRM ? xv[u] : y[i];
+      },
+      [&](int u, unsigned) {
+        v[0] = madd<FMA>(xv[u], yv[u], v[0]);
+        if (OP == D_DOTNRM) v[NR - 1] = madd<FMA>(xv[u], xv[u], v[NR - 1]);
+      });
   double tot[NR];
   if (grid_finish<NR>(v, slot, tot) && threadIdx.x == 0) {
     if (out_raw) *out_raw = tot[0];
@@ -249,16 +282,14 @@ __global__ void __launch_bounds__(kRedBlock) k_mdot(const int* gate, int want, i
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = add(t, sh[w][threadIdx.x]);
     slot.partials[(size_t)threadIdx.x * slot.stride + blockIdx.x] = t;
   }
-  __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(slot.ticket, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) last = atomic_add_acq_rel(slot.ticket, 1u) == gridDim.x - 1;
   __syncthreads();
   if (!last) return;
-  __threadfence();
   if (threadIdx.x < k) {
     double t = 0.0;
     for (int b = 0; b < (int)gridDim.x; b++)
-      t = add(t, ld_relaxed(&slot.partials[(size_t)threadIdx.x * slot.stride + b]));
+      t = add(t, __ldcg(&slot.partials[(size_t)threadIdx.x * slot.stride + b]));
     out[threadIdx.x] = t;
   }
   __syncthreads();
@@ -301,13 +332,20 @@ __device__ __forceinline__ void stop(KspState* st, double rnorm, int its, int re
 
 // End of the loop body: keep looping while the driver is active and under the
 // trip cap (every driver needs at most one trip per iteration, plus restarts).
-__global__ void k_loop_ctrl(cudaGraphConditionalHandle h, KspState* st) {
+__device__ __forceinline__ bool loop_trip(KspState* st) {
   st->trips += 1;
   const bool run = st->active == 1;
   const int cap = st->max_it * 2 + 64;
   if (run && st->trips >= cap) stop(st, st->rnorm, st->its, st->reason ? st->reason : R_DIVITS);
-  cudaGraphSetConditional(h, (run && st->trips < cap) ? 1u : 0u);
+  return run && st->trips < cap;
 }
+
+__global__ void k_loop_ctrl(cudaGraphConditionalHandle h, KspState* st) {
+  cudaGraphSetConditional(h, loop_trip(st) ? 1u : 0u);
+}
+
+// host-driven loop: the same bookkeeping without the graph conditional
+__global__ void k_loop_trip(KspState* st) { loop_trip(st); }
 
 // ================================================================== CG
 // gates: g[0] PC + ||z|| after the update, g[3] ||r||, g[4] natural norm,
@@ -461,16 +499,21 @@ __global__ void k_cgf_p(KspState* st, int n, double* __restrict__ p,
                         const double* __restrict__ z) {
   if (st->active != 1) return;
   const double bc = st->bcoef;
+  constexpr int U = kVecBatch;
+  double zv[U], pv[U];
   if (bc == 0.0) {
-    GRID_LOOP(i, n) p[i] = z[i];
+    grid_batched<U>(n, [&](int u, unsigned i) { zv[u] = z[i]; },
+                    [&](int u, unsigned i) { p[i] = zv[u]; });
   } else if (bc == 1.0) {
-    GRID_LOOP(i, n) p[i] = madd<FMA>(bc, z[i], p[i]);
+    grid_batched<U>(n, [&](int u, unsigned i) { zv[u] = z[i]; pv[u] = p[i]; },
+                    [&](int u, unsigned i) { p[i] = madd<FMA>(bc, zv[u], pv[u]); });
   } else {
-    GRID_LOOP(i, n) p[i] = madd<FMA>(bc, p[i], z[i]);
+    grid_batched<U>(n, [&](int u, unsigned i) { zv[u] = z[i]; pv[u] = p[i]; },
+                    [&](int u, unsigned i) { p[i] = madd<FMA>(bc, pv[u], zv[u]); });
   }
 }
 
-template <bool FMA>
+template <bool FMA, bool STREAM>
 __global__ void __launch_bounds__(kSpmvRows) k_cgf_spmv(KspState* st, int n,
                                                         const int* __restrict__ rowptr,
                                                         const int* __restrict__ colind,
@@ -478,20 +521,33 @@ __global__ void __launch_bounds__(kSpmvRows) k_cgf_spmv(KspState* st, int n,
                                                         const double* __restrict__ p,
                                                         double* __restrict__ w, RedSlot slot) {
   if (st->active != 1) return;
-  const int r0 = blockIdx.x * kSpmvRows;
-  const int row = r0 + threadIdx.x;
-  double s;
-  if constexpr (FMA) {
-    __shared__ SpmvSmemF<double, double, double> sm;
-    s = spmv_block_rows_fma<double, double, double>(sm, n, r0, rowptr, colind, val, p, 0.0);
-  } else {
-    __shared__ SpmvSmem<double, double, double> sm;
-    s = spmv_block_rows<double, double, double>(sm, n, r0, rowptr, colind, val, p, 0.0);
-  }
   double v[1] = {0.0};
-  if (row < n) {
-    w[row] = s;
-    v[0] = madd<FMA>(p[row], s, 0.0);
+  if constexpr (!STREAM) {
+    // a resident grid walks the row tiles, so each CTA pays the reduction
+    // tail once rather than once per 256 rows
+    for (int r0 = blockIdx.x * kSpmvRows; r0 < n; r0 += gridDim.x * kSpmvRows) {
+      const int row = r0 + threadIdx.x;
+      if (row < n) {
+        const double s = spmv_row<FMA>(row, rowptr, colind, val, p, 0.0);
+        w[row] = s;
+        v[0] = madd<FMA>(p[row], s, v[0]);
+      }
+    }
+  } else {
+    const int r0 = blockIdx.x * kSpmvRows;
+    const int row = r0 + threadIdx.x;
+    double s;
+    if constexpr (FMA) {
+      __shared__ SpmvSmemF<double, double, double> sm;
+      s = spmv_block_rows_fma<double, double, double>(sm, n, r0, rowptr, colind, val, p, 0.0);
+    } else {
+      __shared__ SpmvSmem<double, double, double> sm;
+      s = spmv_block_rows<double, double, double>(sm, n, r0, rowptr, colind, val, p, 0.0);
+    }
+    if (row < n) {
+      w[row] = s;
+      v[0] = madd<FMA>(p[row], s, 0.0);
+    }
   }
   double tot[1];
   if (grid_finish<1>(v, slot, tot) && threadIdx.x == 0) {
@@ -510,24 +566,35 @@ __global__ void __launch_bounds__(kSpmvRows) k_cgf_spmv(KspState* st, int n,
 // x += a p; r -= a w; (JACOBI) z = D r with ||z||^2 and z.r; else the PC
 // follows and k_cgf_red reduces.
 template <bool FMA, bool JACOBI>
-__global__ void __launch_bounds__(kRedBlock) k_cgf_update(
+__global__ void __launch_bounds__(kRedBlock, 4) k_cgf_update(
     KspState* st, double* hist, int n, double* __restrict__ x, double* __restrict__ r,
     const double* __restrict__ p, const double* w, double* z, const double* __restrict__ d,
     RedSlot slot) {
   if (st->active != 1) return;
   const double al = st->a, nal = -al;
   double v[2] = {0.0, 0.0};
-  GRID_LOOP(i, n) {
-    x[i] = madd<FMA>(al, p[i], x[i]);
-    const double ri = madd<FMA>(nal, w[i], r[i]);
-    r[i] = ri;
-    if constexpr (JACOBI) {
-      const double zi = mul(ri, d[i]);
-      z[i] = zi;
-      v[0] = madd<FMA>(zi, zi, v[0]);
-      v[1] = madd<FMA>(zi, ri, v[1]);
-    }
-  }
+  constexpr int U = kVecBatch;
+  double pv[U], xv[U], wv[U], rv[U], dv[U];
+  grid_batched<U>(
+      n,
+      [&](int u, unsigned i) {
+        pv[u] = p[i];
+        xv[u] = x[i];
+        wv[u] = w[i];
+        rv[u] = r[i];
+        if constexpr (JACOBI) dv[u] = d[i];
+      },
+      [&](int u, unsigned i) {
+        x[i] = madd<FMA>(al, pv[u], xv[u]);
+        const double ri = madd<FMA>(nal, wv[u], rv[u]);
+        r[i] = ri;
+        if constexpr (JACOBI) {
+          const double zi = mul(ri, dv[u]);
+          z[i] = zi;
+          v[0] = madd<FMA>(zi, zi, v[0]);
+          v[1] = madd<FMA>(zi, ri, v[1]);
+        }
+      });
   if constexpr (JACOBI) {
     double tot[2];
     if (grid_finish<2>(v, slot, tot) && threadIdx.x == 0)
@@ -543,11 +610,14 @@ __global__ void __launch_bounds__(kRedBlock) k_cgf_red(KspState* st, double* his
                                                        RedSlot slot, int first) {
   if (!first && st->active != 1) return;
   double v[2] = {0.0, 0.0};
-  GRID_LOOP(i, n) {
-    const double zi = z[i];
-    v[0] = madd<FMA>(zi, zi, v[0]);
-    v[1] = madd<FMA>(zi, r[i], v[1]);
-  }
+  constexpr int U = kVecBatch;
+  double zv[U], rv[U];
+  grid_batched<U>(
+      n, [&](int u, unsigned i) { zv[u] = z[i]; rv[u] = r[i]; },
+      [&](int u, unsigned) {
+        v[0] = madd<FMA>(zv[u], zv[u], v[0]);
+        v[1] = madd<FMA>(zv[u], rv[u], v[1]);
+      });
   double tot[2];
   if (grid_finish<2>(v, slot, tot) && threadIdx.x == 0)
     cg_tail(st, hist, __dsqrt_rn(tot[0]), tot[1], first != 0);
@@ -1197,6 +1267,17 @@ static int cg_body(const Run& r, double* x) {
 }
 
 // ------------------------------------------------------------------ CG, fused
+// CTAs of `kernel` that fit on the device at once (one full wave).
+static int resident_grid(const void* kernel, int block) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess ||
+      per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  return std::max(1, std::min(per_sm * num_sms(), kMaxRedGrid));
+}
+
 static bool cg_fused_ok(const Run& r) {
   const KspOptions& o = r.k->opt;
   return o.normtype == N_PRECOND && o.chknorm <= 1 &&
@@ -1229,8 +1310,14 @@ static int cg_body_fused(const Run& r, double* x) {
   double* W = Z;  // the reference's W = Z aliasing
   const Csr* A = r.A;
   FL(k_cgf_p, r.grid(), 256, r.s, k->st, n, P, Z);
-  FL(k_cgf_spmv, spmv_grid(A), kSpmvRows, r.s, k->st, n, A->rowptr, A->colind, A->val, P, W,
-     k->slot);
+  {
+    const bool f = arith_mode() == kFma;
+    auto ks = A->stream_rows ? (f ? k_cgf_spmv<true, true> : k_cgf_spmv<false, true>)
+                             : (f ? k_cgf_spmv<true, false> : k_cgf_spmv<false, false>);
+    int grid = spmv_grid(A);
+    if (!A->stream_rows) grid = std::min(grid, resident_grid((const void*)ks, kSpmvRows));
+    ks<<<grid, kSpmvRows, 0, r.s>>>(k->st, n, A->rowptr, A->colind, A->val, P, W, k->slot);
+  }
   const bool jac = r.pc->opt.type == PC_JACOBI;
   const bool f = arith_mode() == kFma;
   const int g = red_grid(n);
@@ -1490,18 +1577,73 @@ static int count_kernels(cudaGraph_t g, int64_t* out) {
   return GP_OK;
 }
 
+static int run_prologue(const Run& r, const double* b, double* x) {
+  switch (r.k->opt.type) {
+    case KSP_CG: return cg_fused_ok(r) ? cg_prologue_fused(r, b, x) : cg_prologue(r, b, x);
+    case KSP_BCGS: return bcgs_prologue(r, b, x);
+    case KSP_GMRES: return gmres_prologue(r);
+    case KSP_FGMRES: return fgmres_prologue(r, b, x);
+  }
+  return GP_OK;
+}
+
+static int run_body(const Run& r, const double* b, double* x) {
+  switch (r.k->opt.type) {
+    case KSP_CG: return cg_fused_ok(r) ? cg_body_fused(r, x) : cg_body(r, x);
+    case KSP_BCGS: return bcgs_body(r, x);
+    case KSP_GMRES: return gmres_body(r, b, x);
+    case KSP_FGMRES: return fgmres_body(r, b, x);
+  }
+  return GP_OK;
+}
+
+// Loop-body copies per conditional trip (GPETSC_KSP_UNROLL, 1..16).
+static int body_unroll() {
+  static int u = [] {
+    const char* e = std::getenv("GPETSC_KSP_UNROLL");
+    const int v = e ? std::atoi(e) : kBodyUnroll;
+    return std::max(1, std::min(16, v));
+  }();
+  return u;
+}
+
+// GPETSC_KSP_GRAPH=0: drive the loop from the host (same kernels, launched on
+// the stream, convergence polled every kEagerPoll trips) instead of one graph.
+static bool eager_mode() {
+  static bool v = [] {
+    const char* e = std::getenv("GPETSC_KSP_GRAPH");
+    return e && std::string(e) == "0";
+  }();
+  return v;
+}
+
+static int run_eager(const Run& r, const double* b, double* x) {
+  Ksp* k = r.k;
+  GP_TRY(run_prologue(r, b, x));
+  for (int64_t trip = 1;; trip++) {
+    GP_TRY(run_body(r, b, x));
+    k_loop_trip<<<1, 1, 0, r.s>>>(k->st);
+    GP_CHECK_LAUNCH();
+    if (trip % kEagerPoll == 0) {
+      int active = 0;
+      GP_CUDA(cudaMemcpyAsync(&active, &k->st->active, sizeof(int), cudaMemcpyDeviceToHost, r.s));
+      GP_CUDA(cudaStreamSynchronize(r.s));
+      if (active != 1) break;
+    }
+  }
+  if (k->opt.type == KSP_BCGS) GP_TRY(bcgs_epilogue(r, x));
+  GP_CUDA(cudaMemcpyAsync(k->h_st, k->st, sizeof(KspState), cudaMemcpyDeviceToHost, r.s));
+  k->top_kernels = -1;
+  k->body_kernels = -1;
+  return GP_OK;
+}
+
 static int capture(const Run& r, const double* b, double* x) {
   Ksp* k = r.k;
   drop_graph(k);
   if (!k->stream2) GP_CUDA(cudaStreamCreateWithFlags(&k->stream2, cudaStreamNonBlocking));
   GP_CUDA(cudaStreamBeginCapture(r.s, cudaStreamCaptureModeRelaxed));
-  int st = GP_OK;
-  switch (k->opt.type) {
-    case KSP_CG: st = cg_fused_ok(r) ? cg_prologue_fused(r, b, x) : cg_prologue(r, b, x); break;
-    case KSP_BCGS: st = bcgs_prologue(r, b, x); break;
-    case KSP_GMRES: st = gmres_prologue(r); break;
-    case KSP_FGMRES: st = fgmres_prologue(r, b, x); break;
-  }
+  int st = run_prologue(r, b, x);
   cudaGraph_t graph = nullptr;
   cudaGraph_t body = nullptr;
   cudaGraphConditionalHandle h = 0;
@@ -1533,12 +1675,9 @@ static int capture(const Run& r, const double* b, double* x) {
     } else {
       Run rb = r;
       rb.s = k->stream2;
-      switch (k->opt.type) {
-        case KSP_CG: st = cg_fused_ok(rb) ? cg_body_fused(rb, x) : cg_body(rb, x); break;
-        case KSP_BCGS: st = bcgs_body(rb, x); break;
-        case KSP_GMRES: st = gmres_body(rb, b, x); break;
-        case KSP_FGMRES: st = fgmres_body(rb, b, x); break;
-      }
+      // several gated copies of the body per conditional trip amortise the
+      // conditional node's re-launch; copies after convergence are no-ops
+      for (int u = 0; u < body_unroll() && st == GP_OK; u++) st = run_body(rb, b, x);
       if (st == GP_OK) k_loop_ctrl<<<1, 1, 0, k->stream2>>>(h, k->st);
       cudaGraph_t bout = nullptr;
       cudaError_t eb = cudaStreamEndCapture(k->stream2, &bout);
@@ -1638,6 +1777,9 @@ int ksp_solve(Ksp* k, Csr* A, Pc* pc, const double* b, double* x, KspResult* res
   const int key[11] = {o.type,      o.normtype,    o.pc_side,          o.restart,
                        o.cgstype,   n,             pc->opt.type,       pc->opt.sor_flag,
                        o.guess_zero, (int)(pc->epoch & 0x7fffffff), arith_mode()};
+  if (eager_mode()) {
+    GP_TRY(run_eager(r, b, x));
+  } else {
   const bool same = !moved && k->exec && k->cap_A == A && k->cap_pc == pc &&
                     std::equal(key, key + 11, k->cap_key) && k->cap_b == b && k->cap_x == x;
   if (!same) {
@@ -1649,6 +1791,7 @@ int ksp_solve(Ksp* k, Csr* A, Pc* pc, const double* b, double* x, KspResult* res
     std::copy(key, key + 11, k->cap_key);
   }
   GP_CUDA(cudaGraphLaunch(k->exec, s));
+  }
   GP_CUDA(cudaEventRecord(ev, s));
   GP_CUDA(cudaStreamWaitEvent(caller, ev, 0));
   GP_CUDA(cudaStreamSynchronize(s));

@@ -35,6 +35,13 @@ static int csr_finish(Csr* A, const double* h_val, cudaStream_t s) {
         diag[i] = j;
         break;
       }
+  // rows of bounded length go one per thread; a matrix with long rows (or a
+  // few rows far longer than the rest) uses the row-stream form
+  int64_t maxlen = 0;
+  for (int i = 0; i < n; i++)
+    maxlen = std::max<int64_t>(maxlen, A->h_rowptr[i + 1] - A->h_rowptr[i]);
+  const double avg = n ? (double)A->nnz / n : 0.0;
+  A->stream_rows = maxlen > kSpmvMaxRowLen || (double)maxlen > 8.0 * avg + 8.0;
   GP_TRY(dev_upload(&A->rowptr, A->h_rowptr.data(), (size_t)n + 1, s));
   GP_TRY(dev_upload(&A->colind, A->h_colind.data(), (size_t)A->nnz, s));
   GP_TRY(dev_upload(&A->val, h_val, (size_t)A->nnz, s));
@@ -183,7 +190,7 @@ int csr_make_val32(Csr* A, cudaStream_t s) {
 
 // y = A x, or y = v + A x when v is given (MatMultAdd starts each row's sum
 // from v_i).  Optional gate for use inside captured solver loops.
-template <bool FMA>
+template <bool FMA, bool STREAM>
 __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict__ rowptr,
                                                     const int* __restrict__ colind,
                                                     const double* __restrict__ val, DRef xr,
@@ -195,6 +202,10 @@ __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict
   const int r0 = blockIdx.x * kSpmvRows;
   const int row = r0 + threadIdx.x;
   double init = (v != nullptr && row < n) ? v[row] : 0.0;
+  if constexpr (!STREAM) {
+    if (row < n) y[row] = spmv_row<FMA>(row, rowptr, colind, val, x, init);
+    return;
+  }
   double s;
   if constexpr (FMA) {
     __shared__ SpmvSmemF<double, double, double> sm;
@@ -208,12 +219,10 @@ __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict
 
 static void launch_spmv(cudaStream_t s, const Csr* A, DRef x, const double* v, DRef y,
                         const int* gate, int want) {
-  if (arith_mode() == kFma)
-    k_spmv<true><<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, v, y,
-                                                    gate, want);
-  else
-    k_spmv<false><<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, v,
-                                                     y, gate, want);
+  const bool f = arith_mode() == kFma;
+  auto k = A->stream_rows ? (f ? k_spmv<true, true> : k_spmv<false, true>)
+                          : (f ? k_spmv<true, false> : k_spmv<false, false>);
+  k<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, v, y, gate, want);
 }
 
 // y = A^T x over the stored transpose pattern; values gathered through the

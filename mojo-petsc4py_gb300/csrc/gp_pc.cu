@@ -71,11 +71,10 @@ __device__ __forceinline__ void sweep_rows(int n, const int* __restrict__ order,
   }
   if (lane == 0) {
     const unsigned total = gridDim.x * (blockDim.x / 32);
-    __threadfence();
-    if (atomicAdd(&tickets[1], 1u) == total - 1) {
+    // the last warp out resets the pair for the next launch
+    if (atomic_add_acq_rel(&tickets[1], 1u) == total - 1) {
       tickets[0] = 0u;
       tickets[1] = 0u;
-      __threadfence();
     }
   }
 }
@@ -350,7 +349,6 @@ __global__ void __launch_bounds__(kSweepBlock) k_ilu_numeric(
       }
     }
     ba[bdiag[i]] = div_(1.0, ba[bdiag[i]]);
-    __threadfence();
     st_release_i32(&done[i], epoch);
   });
 }
@@ -402,7 +400,6 @@ __global__ void __launch_bounds__(kSweepBlock) k_icc_numeric(
     }
     for (int j = bi[k]; j < bdiag[k]; j++) ba[j] = orig[j];
     ba[bdiag[k]] = div_(1.0, dk);
-    __threadfence();
     st_release_i32(&done[k], epoch);
   });
 }

@@ -1,7 +1,19 @@
-// CSR SpMV building block shared by the standalone multiply and the fused
-// solver kernels.
+// CSR SpMV building blocks shared by the standalone multiply and the fused
+// solver kernels.  Two forms, chosen per matrix (Csr::stream_rows), with
+// bitwise-identical results: both fold each row from `init` in ascending slot
+// order, one rounded product (or one FMA) per slot, as MatMult_SeqAIJ does
+// (src/ported.mojo:380-391).
 //
-// One CTA owns kSpmvRows consecutive rows.  The CTA walks the contiguous slot
+// Row per thread (spmv_row): rows of bounded length (stencils, FEM, graphs).
+// Each thread loads its row's slots eight at a time, then gathers x.  A warp's
+// loads of a slot range are strided by the row length, but the 32 rows of a
+// warp cover one contiguous span of the arrays, so L1 serves the re-touched
+// lines and DRAM sees each byte once.  Matrix values and indices are read
+// once per product, with an L2 evict-first policy: the solver's vectors stay
+// resident in the 129 MB L2 while the matrix streams through.
+//
+// Row stream (spmv_block_rows*): rows of any length.  One CTA owns kSpmvRows
+// consecutive rows.  The CTA walks the contiguous slot
 // range of its rows in chunks: every thread loads values and column indices
 // with unit stride (coalesced), forms value * x[col] into shared memory, and
 // then each thread adds the products of its own row in ascending slot order.
@@ -17,6 +29,54 @@ namespace gp {
 
 constexpr int kSpmvRows = 256;    // rows per CTA == threads per CTA
 constexpr int kSpmvChunk = 2048;  // products staged per pass
+constexpr int kSpmvMaxRowLen = 64;  // longest row the row-per-thread form takes
+
+// L2 evict-first loads for data read once per product.
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ double ld_stream(const double* a, uint64_t pol) {
+  double v;
+  asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float ld_stream(const float* a, uint64_t pol) {
+  float v;
+  asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ int ld_stream(const int* a, uint64_t pol) {
+  int v;
+  asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+  return v;
+}
+
+// Row `row`'s sum, starting from `init` (caller checks row < n).
+template <bool FMA, typename VT, typename XT>
+__device__ __forceinline__ double spmv_row(int row, const int* __restrict__ rowptr,
+                                           const int* __restrict__ colind,
+                                           const VT* __restrict__ val, const XT* __restrict__ x,
+                                           double init) {
+  const uint64_t pol = l2_evict_first();
+  const int b = rowptr[row], e = rowptr[row + 1];
+  double acc = init;
+  for (int j0 = b; j0 < e; j0 += 8) {
+    int cc[8];
+    double vv[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      if (j0 + u < e) {
+        cc[u] = ld_stream(colind + j0 + u, pol);
+        vv[u] = (double)ld_stream(val + j0 + u, pol);
+      }
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      if (j0 + u < e) acc = madd<FMA>(vv[u], (double)x[cc[u]], acc);
+  }
+  return acc;
+}
 
 template <typename VT, typename XT, typename AT>
 struct SpmvSmem {

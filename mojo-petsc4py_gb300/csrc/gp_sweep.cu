@@ -139,11 +139,9 @@ __global__ void __launch_bounds__(kEllBlock) k_ell_sweep(const int* gate, int wa
   }
   if (lane == 0) {
     const unsigned total = gridDim.x * (blockDim.x / 32);
-    __threadfence();
-    if (atomicAdd(&a.tickets[1], 1u) == total - 1) {
+    if (atomic_add_acq_rel(&a.tickets[1], 1u) == total - 1) {
       a.tickets[0] = 0u;
       a.tickets[1] = 0u;
-      __threadfence();
     }
   }
 }

@@ -262,15 +262,13 @@ __global__ void __launch_bounds__(kRedBlock) k_maxabs(int64_t n, const double* _
   }
   if (threadIdx.x == 0) {
     slot.partials[blockIdx.x] = sh[0];
-    __threadfence();
-    last = atomicAdd(slot.ticket, 1u) == gridDim.x - 1;
+    last = atomic_add_acq_rel(slot.ticket, 1u) == gridDim.x - 1;
   }
   __syncthreads();
   if (!last) return;
   if (threadIdx.x == 0) {
-    __threadfence();
     double r = 0.0;
-    for (int b = 0; b < (int)gridDim.x; b++) r = comb(r, ld_relaxed(&slot.partials[b]));
+    for (int b = 0; b < (int)gridDim.x; b++) r = comb(r, __ldcg(&slot.partials[b]));
     out[0] = r;
     *slot.ticket = 0u;
   }
@@ -370,18 +368,16 @@ __global__ void __launch_bounds__(kRedBlock) k_minmax(int64_t n, const double* _
   if (threadIdx.x == 0) {
     slot.partials[blockIdx.x] = sv[0];
     slot.partials[slot.stride + blockIdx.x] = __longlong_as_double(si[0]);
-    __threadfence();
-    last = atomicAdd(slot.ticket, 1u) == gridDim.x - 1;
+    last = atomic_add_acq_rel(slot.ticket, 1u) == gridDim.x - 1;
   }
   __syncthreads();
   if (!last) return;
   if (threadIdx.x == 0) {
-    __threadfence();
     double rv = 0.0;
     long long ri = -1;
     for (int b = 0; b < (int)gridDim.x; b++) {
-      double v = ld_relaxed(&slot.partials[b]);
-      long long ii = __double_as_longlong(ld_relaxed(&slot.partials[slot.stride + b]));
+      double v = __ldcg(&slot.partials[b]);
+      long long ii = __double_as_longlong(__ldcg(&slot.partials[slot.stride + b]));
       if (better(v, ii, rv, ri)) {
         rv = v;
         ri = ii;
