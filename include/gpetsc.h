@@ -114,6 +114,22 @@ int gp_vec_maxpy(int64_t n, double *y, int64_t nv, const double *alpha,
  * reductions of src/simdvec.mojo:332-488. */
 int gp_vec_reduce(int op, int64_t n, const double *x, const double *y, double *out,
                   void *stream);
+/* gp_vec_reduce without allocation, for callers that cannot let a library
+ * allocate device memory (a host application with a fixed device-memory
+ * budget or its own allocator, a loop that must not pay an allocation's
+ * implicit synchronisation).  Same ops and the same kernels as
+ * gp_vec_reduce; the result (2 doubles for op 4, else 1) goes to `out`, a
+ * caller-owned DEVICE buffer, and the call does not synchronise.  Scratch is
+ * a fixed 16 KB area of the library's static device memory (1024 per-CTA
+ * partials per value and a ticket word, which starts at zero and which every
+ * call leaves at zero).  n must not exceed 2^31 - 1 (GP_ERR_ARG otherwise).
+ * There is one scratch area per device, so calls that overlap on a device
+ * (different streams or threads with no ordering between them) race: order
+ * them.  The first call on each device looks the area up
+ * (cudaGetSymbolAddress) and must precede any stream capture.  No counterpart
+ * in the reference (its reductions run on the host). */
+int gp_vec_reduce_static(int op, int64_t n, const double *x, const double *y, double *out,
+                         void *stream);
 /* VecMin/VecMax (src/ported.mojo:165-196): value and first index. */
 int gp_vec_minmax(int64_t n, const double *x, int is_max, int64_t *idx, double *val,
                   void *stream);

@@ -41,6 +41,8 @@ enum RedOp : int { RED_DOT, RED_NORM2SQ, RED_ASUM, RED_SUM, RED_DOTNORM2, RED_NO
 // Reductions return their result(s) to host memory (synchronous).
 int vec_reduce(cudaStream_t s, int op, int64_t n, const double* x, const double* y,
                double* out_host);
+int vec_reduce_into(cudaStream_t s, int op, int64_t n, const double* x, const double* y,
+                    RedSlot slot, int max_grid, double* out_dev);
 int vec_minmax(cudaStream_t s, int64_t n, const double* x, int is_max, long long* idx,
                double* val);
 int vec_max_pointwise_divide(cudaStream_t s, int64_t n, const double* x, const double* y,

@@ -309,6 +309,37 @@ int vec_reduce(cudaStream_t s, int op, int64_t n, const double* x, const double*
   return GP_OK;
 }
 
+// The reduction kernels of vec_reduce with caller-supplied scratch and a
+// device result (nothing allocated, nothing synchronised); grid capped at
+// max_grid partial slots per value.
+int vec_reduce_into(cudaStream_t s, int op, int64_t n, const double* x, const double* y,
+                    RedSlot slot, int max_grid, double* out_dev) {
+  const int nr = op == RED_DOTNORM2 ? 2 : 1;
+  if (n <= 0) {
+    GP_CUDA(cudaMemsetAsync(out_dev, 0, nr * sizeof(double), s));
+    return GP_OK;
+  }
+  const int g = std::min(red_grid(n), max_grid);
+  const bool f = arith_mode() == kFma;
+#define RED_LAUNCH(OPC)                                                     \
+  if (f)                                                                    \
+    k_reduce<OPC, true><<<g, kRedBlock, 0, s>>>(n, x, y, slot, out_dev);    \
+  else                                                                      \
+    k_reduce<OPC, false><<<g, kRedBlock, 0, s>>>(n, x, y, slot, out_dev);
+  switch (op) {
+    case RED_DOT: RED_LAUNCH(RED_DOT); break;
+    case RED_NORM2SQ: RED_LAUNCH(RED_NORM2SQ); break;
+    case RED_ASUM: RED_LAUNCH(RED_ASUM); break;
+    case RED_SUM: RED_LAUNCH(RED_SUM); break;
+    case RED_DOTNORM2: RED_LAUNCH(RED_DOTNORM2); break;
+    case RED_NORMINF: k_maxabs<false><<<g, kRedBlock, 0, s>>>(n, x, y, slot, out_dev); break;
+    default: set_error("vec_reduce: unknown op"); return GP_ERR_ARG;
+  }
+#undef RED_LAUNCH
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
 int vec_max_pointwise_divide(cudaStream_t s, int64_t n, const double* x, const double* y,
                              double* out_host) {
   Scratch* sc;

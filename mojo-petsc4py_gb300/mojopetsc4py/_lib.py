@@ -81,6 +81,7 @@ GP_SIGNATURES = {
     "gp_vec_map": ([ctypes.c_int, I64, P, P, P, F64, F64, F64, P], ctypes.c_int),
     "gp_vec_maxpy": ([I64, P, I64, P, P, P], ctypes.c_int),
     "gp_vec_reduce": ([ctypes.c_int, I64, P, P, P, P], ctypes.c_int),
+    "gp_vec_reduce_static": ([ctypes.c_int, I64, P, P, P, P], ctypes.c_int),
     "gp_vec_minmax": ([I64, P, ctypes.c_int, P, P, P], ctypes.c_int),
     "gp_vec_max_pointwise_divide": ([I64, P, P, P, P], ctypes.c_int),
     "gp_pc_options_default": ([ctypes.POINTER(PcOptions)], None),
