@@ -90,6 +90,19 @@ int gp_mat_mult(gp_mat A, const double *x, double *y, void *stream);
 int gp_mat_mult_add(gp_mat A, const double *x, const double *v, double *y, void *stream);
 /* y = A^T x.      Replaces MatMultTranspose_SeqAIJ (src/ported.mojo:408-431). */
 int gp_mat_mult_transpose(gp_mat A, const double *x, double *y, void *stream);
+/* MatTranspose (python/mojopetsc4py/PETSc/Mat.py:555-563, 683-746): a new
+ * device matrix holding A^T (values gathered on the device through the cached
+ * transpose pattern).  gp_mat_transpose_values refreshes At's values after A's
+ * changed (MAT_REUSE_MATRIX). */
+int gp_mat_transpose(gp_mat A, gp_mat *out, void *stream);
+int gp_mat_transpose_values(gp_mat A, gp_mat At, void *stream);
+/* out[k] = alpha * u[i] * v[j] for every stored nonzero k = (i, j) of A: the
+ * gradient of a loss through A x = b with respect to A's stored values is
+ * gp_mat_outer_on_pattern(A, lambda, x, -1, ...) with lambda = A^-T dL/dx.
+ * No counterpart in the reference (its adjoint is not on the device). */
+int gp_mat_outer_on_pattern(gp_mat A, const double *u, const double *v, double alpha,
+                            double *out, void *stream);
+
 /* d = diag(A).    Replaces MatGetDiagonal_SeqAIJ (src/ported.mojo:434-447). */
 int gp_mat_get_diagonal(gp_mat A, double *d, void *stream);
 
@@ -165,6 +178,10 @@ int gp_pc_set_options(gp_pc pc, const gp_pc_options *o);
  * Replaces PC.setUp (python/mojopetsc4py/PETSc/PC.py:315-492). */
 int gp_pc_setup(gp_pc pc, gp_mat A, void *stream);
 /* y = M^-1 x.  Replaces KSP_PCApply (src/ksp.mojo:155-198). */
+/* Same pattern, new operator values: redo only the numeric phase (ILU/IC factor
+ * values on the device, Jacobi diagonals) in the arrays of the last set-up;
+ * solver graphs captured with this PC stay valid. */
+int gp_pc_update_values(gp_pc pc, void *stream);
 int gp_pc_apply(gp_pc pc, const double *x, double *y, void *stream);
 /* Jacobi's symmetric half (src/ksp.mojo:201-208); other types apply M^-1. */
 int gp_pc_apply_symmetric(gp_pc pc, const double *x, double *y, void *stream);
@@ -205,8 +222,9 @@ void gp_ksp_options_default(gp_ksp_options *o);
 int gp_ksp_create(gp_ksp *out);
 int gp_ksp_destroy(gp_ksp ksp);
 int gp_ksp_set_options(gp_ksp ksp, const gp_ksp_options *o);
-/* Solve A x = b with preconditioner pc; b and x are device vectors.  The
- * residual history (its+1 norms) goes to hist (host, may be NULL).
+/* Solve A x = b with preconditioner pc; b and x are device vectors (with the
+ * default zero initial guess, x is zeroed first).  The residual history
+ * (its+1 norms) goes to hist (host, may be NULL).
  * Replaces mp_ksp_solve_{cg,bcgs,gmres,fgmres} (src/capi.mojo:383-424)
  * behind KSP.solve (python/mojopetsc4py/PETSc/KSP.py:367-449). */
 int gp_ksp_solve(gp_ksp ksp, gp_mat A, gp_pc pc, const double *b, double *x,

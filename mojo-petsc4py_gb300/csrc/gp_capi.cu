@@ -137,6 +137,28 @@ int gp_mat_mult_transpose(gp_mat A, const double* x, double* y, void* stream) {
   GUARD(gp::spmv_t(S(stream), A->A, x, y));
 }
 
+int gp_mat_transpose(gp_mat A, gp_mat* out, void* stream) {
+  if (!A || !out) return bad("gp_mat_transpose: null argument");
+  GUARD(([&]() {
+    gp::Csr* T = nullptr;
+    int st = gp::csr_create_transpose(A->A, &T, S(stream));
+    if (st) return st;
+    *out = new gp_mat_s{T};
+    return (int)GP_OK;
+  })());
+}
+
+int gp_mat_transpose_values(gp_mat A, gp_mat At, void* stream) {
+  if (!A || !At) return bad("gp_mat_transpose_values: null argument");
+  GUARD(gp::csr_transpose_values(A->A, At->A, S(stream)));
+}
+
+int gp_mat_outer_on_pattern(gp_mat A, const double* u, const double* v, double alpha,
+                            double* out, void* stream) {
+  if (!A || !out || (A->A->n && (!u || !v))) return bad("gp_mat_outer_on_pattern: null argument");
+  GUARD(gp::csr_outer_on_pattern(A->A, u, v, alpha, out, S(stream)));
+}
+
 int gp_mat_get_diagonal(gp_mat A, double* d, void* stream) {
   if (!A || !d) return bad("gp_mat_get_diagonal: null argument");
   GUARD(gp::mat_diagonal(S(stream), A->A, d));
@@ -234,6 +256,11 @@ int gp_pc_set_options(gp_pc pc, const gp_pc_options* o) {
 int gp_pc_setup(gp_pc pc, gp_mat A, void* stream) {
   if (!pc || !A) return bad("gp_pc_setup: null argument");
   GUARD(gp::pc_setup(pc->pc, A->A, S(stream)));
+}
+
+int gp_pc_update_values(gp_pc pc, void* stream) {
+  if (!pc) return bad("gp_pc_update_values: null argument");
+  GUARD(gp::pc_update_values(pc->pc, S(stream)));
 }
 
 int gp_pc_apply(gp_pc pc, const double* x, double* y, void* stream) {

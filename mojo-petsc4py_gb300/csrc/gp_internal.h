@@ -83,6 +83,10 @@ int csr_create_i32(Csr** out, int64_t nrows, int64_t ncols, int64_t nnz,
                    cudaStream_t s);
 int csr_set_values(Csr* A, const double* val, int on_device, cudaStream_t s);
 int csr_destroy(Csr* A);
+int csr_create_transpose(Csr* A, Csr** out, cudaStream_t s);
+int csr_transpose_values(Csr* A, Csr* T, cudaStream_t s);
+int csr_outer_on_pattern(const Csr* A, const double* u, const double* v, double alpha,
+                         double* out, cudaStream_t s);
 int csr_build_transpose(Csr* A, cudaStream_t s);
 int csr_make_val32(Csr* A, cudaStream_t s);
 

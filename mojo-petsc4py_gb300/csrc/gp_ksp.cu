@@ -1772,11 +1772,14 @@ int ksp_solve(Ksp* k, Csr* A, Pc* pc, const double* b, double* x, KspResult* res
   h.prev_rnorm = -1.0;
   GP_CUDA(cudaMemcpyAsync(k->st, &h, sizeof(KspState), cudaMemcpyHostToDevice, s));
   GP_CUDA(cudaMemsetAsync(k->hist, 0, (size_t)k->hist_cap * sizeof(double), s));
+  // a zero initial guess means x = 0 on entry (KSP.solve zeroes x first,
+  // python/mojopetsc4py/PETSc/KSP.py:367-449): done here for every caller
+  if (o.guess_zero && n) GP_CUDA(cudaMemsetAsync(x, 0, (size_t)n * sizeof(double), s));
   Run r{k, A, pc, n, s};
   // the solve graph depends on the buffers and on every option that shapes it
   const int key[11] = {o.type,      o.normtype,    o.pc_side,          o.restart,
                        o.cgstype,   n,             pc->opt.type,       pc->opt.sor_flag,
-                       o.guess_zero, (int)(pc->epoch & 0x7fffffff), arith_mode()};
+                       o.guess_zero, pc->generation,      arith_mode()};
   if (eager_mode()) {
     GP_TRY(run_eager(r, b, x));
   } else {

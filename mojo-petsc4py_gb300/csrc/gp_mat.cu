@@ -170,6 +170,76 @@ int csr_build_transpose(Csr* A, cudaStream_t s) {
   return GP_OK;
 }
 
+// At.val[k] = A.val[t_src[k]]: the values of A^T in its row order.
+__global__ void k_gather_values(int64_t nnz, const int* __restrict__ src,
+                                const double* __restrict__ a, double* __restrict__ out) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz;
+       k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = a[src[k]];
+}
+
+// MatTranspose (python/mojopetsc4py/PETSc/Mat.py:555-563, 683-746): a new CSR
+// holding A^T, built from the cached transpose pattern; values gathered on the
+// device.  The pattern has no duplicates (A's has none), so no summing.
+int csr_create_transpose(Csr* A, Csr** out, cudaStream_t s) {
+  GP_TRY(csr_build_transpose(A, s));
+  const int m = A->ncols;
+  std::vector<int> trp(m + 1), tcol(std::max<int64_t>(A->nnz, 1));
+  GP_CUDA(cudaMemcpy(trp.data(), A->t_rowptr, (m + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+  if (A->nnz)
+    GP_CUDA(cudaMemcpy(tcol.data(), A->t_colind, A->nnz * sizeof(int), cudaMemcpyDeviceToHost));
+  std::vector<double> zeros(std::max<int64_t>(A->nnz, 1), 0.0);
+  Csr* T = nullptr;
+  GP_TRY(csr_create_i32(&T, m, A->n, A->nnz, trp.data(), tcol.data(), zeros.data(), s));
+  int st = csr_transpose_values(A, T, s);
+  if (st != GP_OK) {
+    csr_destroy(T);
+    return st;
+  }
+  *out = T;
+  return GP_OK;
+}
+
+// Refresh T = A^T's values after A's changed (same pattern).
+int csr_transpose_values(Csr* A, Csr* T, cudaStream_t s) {
+  GP_TRY(csr_build_transpose(A, s));
+  if (T->n != A->ncols || T->ncols != A->n || T->nnz != A->nnz) {
+    set_error("transpose: the target does not have the transposed shape");
+    return GP_ERR_ARG;
+  }
+  if (A->nnz) {
+    const int g = (int)std::min<int64_t>((A->nnz + 255) / 256, (int64_t)num_sms() * 8);
+    k_gather_values<<<g, 256, 0, s>>>(A->nnz, A->t_src, A->val, T->val);
+    GP_CHECK_LAUNCH();
+  }
+  if (T->val32) {
+    cudaFree(T->val32);
+    T->val32 = nullptr;
+  }
+  return GP_OK;
+}
+
+// out[k] = alpha * u[row(k)] * v[col(k)] over A's nonzeros: the gradient of a
+// loss through A x = b with respect to the stored values (u = -lambda, v = x).
+__global__ void k_outer_on_pattern(int n, const int* __restrict__ rowptr,
+                                   const int* __restrict__ colind, const double* __restrict__ u,
+                                   const double* __restrict__ v, double alpha,
+                                   double* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double ui = mul(alpha, u[i]);
+    for (int k = rowptr[i]; k < rowptr[i + 1]; k++) out[k] = mul(ui, v[colind[k]]);
+  }
+}
+
+int csr_outer_on_pattern(const Csr* A, const double* u, const double* v, double alpha,
+                         double* out, cudaStream_t s) {
+  if (A->n == 0) return GP_OK;
+  const int g = std::max(1, std::min((A->n + 255) / 256, num_sms() * 8));
+  k_outer_on_pattern<<<g, 256, 0, s>>>(A->n, A->rowptr, A->colind, u, v, alpha, out);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
 __global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)

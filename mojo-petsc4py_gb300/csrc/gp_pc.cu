@@ -768,8 +768,35 @@ int pc_factor_numeric(Pc* pc, cudaStream_t s) {
   return pc_check(pc, s);
 }
 
+int pc_update_values(Pc* pc, cudaStream_t s) {
+  if (!pc->ready || !pc->A) {
+    set_error("PC values updated before set-up");
+    return GP_ERR_NOT_SETUP;
+  }
+  const Csr* A = pc->A;
+  const int n = A->n;
+  switch (pc->opt.type) {
+    case PC_JACOBI:
+      if (n) {
+        const PcOptions& o = pc->opt;
+        k_jacobi_fill<<<(n + 255) / 256, 256, 0, s>>>(n, o.jacobi_type, 0, o.use_abs,
+                                                      o.fix_diag, o.rowl1_scale, A->rowptr,
+                                                      A->val, A->diagpos, pc->diag);
+        k_jacobi_fill<<<(n + 255) / 256, 256, 0, s>>>(n, o.jacobi_type, 1, 0, 0, 1.0,
+                                                      A->rowptr, A->val, A->diagpos,
+                                                      pc->diagsqrt);
+        GP_CHECK_LAUNCH();
+      }
+      return GP_OK;
+    case PC_ILU:
+    case PC_ICC: return pc_factor_numeric(pc, s);
+    default: return GP_OK;  // none; SOR reads A's values on every apply
+  }
+}
+
 int pc_setup(Pc* pc, Csr* A, cudaStream_t s) {
   free_all(pc);
+  pc->generation += 1;
   pc->A = A;
   pc->n = A->n;
   GP_CUDA(cudaGetDevice(&pc->device));

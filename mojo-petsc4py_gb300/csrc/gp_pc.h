@@ -79,6 +79,7 @@ struct Pc {
   int device = -1;
   bool ready = false;
   int epoch = 0;
+  int generation = 0;   // bumped by every set-up (device arrays reallocated)
 
   // Jacobi
   double* diag = nullptr;
@@ -132,6 +133,9 @@ int pc_apply_symmetric(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate =
 int pc_check(Pc* pc, cudaStream_t s);
 
 int pc_factor_numeric(Pc* pc, cudaStream_t s);
+// Same operator pattern, new values: redo only the numeric phase (factor
+// values, Jacobi diagonals) in the arrays of the last set-up.
+int pc_update_values(Pc* pc, cudaStream_t s);
 int pc_import_factor(Pc* pc, int type, const FactorPattern& pat, const std::vector<int>& perm_c,
                      const double* ba_host, Csr* A, cudaStream_t s);
 int pc_import_jacobi(Pc* pc, int n, const double* diag, const double* diagsqrt, cudaStream_t s);

@@ -337,8 +337,6 @@ class KSP:
         if not self._setupcalled:
             self.setUp()
         self._pc.setUp()
-        if self._guess_zero:
-            x.zeroEntries()
         self._rhs, self._sol = b, x
         self._resolve_normtype()
         rhs = 0.0 if self._guess_zero else self._rhs_norm(b)
@@ -351,7 +349,8 @@ class KSP:
         hist = np.zeros(max(self._histlen, 0), dtype=np.float64)
         res = KspResult()
         bp = b._dptr() if n else 0
-        xp = x._wptr() if n else 0
+        # a zero guess ignores x on entry (the solver zeroes it): no upload
+        xp = (x._optr() if self._guess_zero else x._wptr()) if n else 0
         check(lib().gp_ksp_solve(self._gp, A._device(), self._pc._handle(), bp, xp,
                                  ctypes.byref(res), hist.ctypes.data if len(hist) else None,
                                  len(hist), dev.stream_ptr()))

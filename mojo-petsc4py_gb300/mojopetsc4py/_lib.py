@@ -77,6 +77,9 @@ GP_SIGNATURES = {
     "gp_mat_mult": ([P, P, P, P], ctypes.c_int),
     "gp_mat_mult_add": ([P, P, P, P, P], ctypes.c_int),
     "gp_mat_mult_transpose": ([P, P, P, P], ctypes.c_int),
+    "gp_mat_transpose": ([P, PP, P], ctypes.c_int),
+    "gp_mat_transpose_values": ([P, P, P], ctypes.c_int),
+    "gp_mat_outer_on_pattern": ([P, P, P, ctypes.c_double, P, P], ctypes.c_int),
     "gp_mat_get_diagonal": ([P, P, P], ctypes.c_int),
     "gp_vec_map": ([ctypes.c_int, I64, P, P, P, F64, F64, F64, P], ctypes.c_int),
     "gp_vec_maxpy": ([I64, P, I64, P, P, P], ctypes.c_int),
@@ -89,6 +92,7 @@ GP_SIGNATURES = {
     "gp_pc_destroy": ([P], ctypes.c_int),
     "gp_pc_set_options": ([P, ctypes.POINTER(PcOptions)], ctypes.c_int),
     "gp_pc_setup": ([P, P, P], ctypes.c_int),
+    "gp_pc_update_values": ([P, P], ctypes.c_int),
     "gp_pc_apply": ([P, P, P, P], ctypes.c_int),
     "gp_pc_apply_symmetric": ([P, P, P, P], ctypes.c_int),
     "gp_pc_factor_info": ([P, P, P], ctypes.c_int),
