@@ -235,6 +235,47 @@ int gp_ksp_solve(gp_ksp ksp, gp_mat A, gp_pc pc, const double *b, double *x,
  * top_kernels + trips * body_kernels. */
 int gp_ksp_stats(gp_ksp ksp, int64_t *trips, int64_t *top_kernels, int64_t *body_kernels);
 
+
+/* ------------------------------------------------------------ batched CG
+ * Many independent SPD systems with nrhs right-hand sides each, solved
+ * together: one block-diagonal CSR (system s owns rows sys_rows[s] ..
+ * sys_rows[s+1]-1 and may only couple to them; int64 host arrays as in
+ * gp_mat_create) and row-major multi-vectors (entry (row, r) at
+ * row * nrhs + r, device memory).  Every (system, column) pair runs its own
+ * PETSc CG recurrence (src/ksp.mojo:271-389, preconditioned norm) with its own
+ * stopping test; pairs that stop are frozen and finished systems drop out.
+ * precision 0: FP64 CG.  precision 1: FP32 inner CG (FP32 values, vectors and
+ * dot accumulation) to inner_rtol inside FP64 iterative refinement, stopping
+ * when the true residual ||b - A x|| <= rtol ||b|| per pair (max_it then
+ * caps the inner iterations of each pass, max_outer the passes).
+ * nrhs must be 1, 2, 4, 8 or 16; pc_type 0 (none) or 2 (Jacobi).
+ * gp_batch_autotune times the sparse pass for every (CTA size, columns per
+ * thread, tile rows) and keeps the fastest; gp_batch_tuning reports it.
+ * Outputs (host, nsys * nrhs entries, each may be NULL): iterations (total
+ * inner iterations for precision 1), converged reason, and the final true
+ * relative residual ||b - A x|| / ||b|| computed in FP64.
+ * No counterpart in the reference (its solves are one system at a time). */
+typedef struct gp_batch_s *gp_batch;
+typedef struct {
+  int32_t pc_type;     /* 0 none, 2 jacobi */
+  int32_t precision;   /* 0 FP64, 1 FP32 inner + FP64 refinement */
+  int32_t max_it;
+  int32_t max_outer;
+  double rtol, atol, divtol;
+  double inner_rtol;
+} gp_batch_options;
+void gp_batch_options_default(gp_batch_options *o);
+int gp_batch_create(gp_batch *out, int64_t nsys, const int64_t *sys_rows,
+                    const int64_t *indptr, const int64_t *indices, const double *values,
+                    int32_t nrhs, void *stream);
+int gp_batch_destroy(gp_batch b);
+int gp_batch_autotune(gp_batch b, void *stream);
+int gp_batch_tuning(gp_batch b, int32_t *block, int32_t *vector_width, int32_t *tile_rows,
+                    double *spmm_us);
+int gp_batch_solve_cg(gp_batch b, const gp_batch_options *o, const double *B, double *X,
+                      int64_t *its, int32_t *reason, double *relres, int32_t *passes,
+                      void *stream);
+
 /* ------------------------------------------------------------ mp_* (reference host ABI) */
 /* Mat (src/capi.mojo:32-65) */
 void mp_mat_mult(const double *x, double *y, const int64_t *irow, const int64_t *icol,

@@ -68,6 +68,12 @@ GP_SIGNATURES = {
     "gp_get_arithmetic": ([], ctypes.c_int),
     "gp_device_count": ([ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     "gp_set_device": ([ctypes.c_int], ctypes.c_int),
+    "gp_batch_create": ([PP, I64, P, P, P, P, ctypes.c_int32, P], ctypes.c_int),
+    "gp_batch_destroy": ([P], ctypes.c_int),
+    "gp_batch_options_default": ([P], None),
+    "gp_batch_autotune": ([P, P], ctypes.c_int),
+    "gp_batch_tuning": ([P, P, P, P, P], ctypes.c_int),
+    "gp_batch_solve_cg": ([P, P, P, P, P, P, P, P, P], ctypes.c_int),
     "gp_mat_create": ([PP, I64, I64, I64, P, P, P], ctypes.c_int),
     "gp_mat_create_i32": ([PP, I64, I64, I64, P, P, P], ctypes.c_int),
     "gp_mat_destroy": ([P], ctypes.c_int),

@@ -1,0 +1,133 @@
+"""Batched CG: hundreds of independent SPD systems with several right-hand
+sides each, solved together on the GPU (include/gpetsc.h, gp_batch_*).
+
+    solver = BatchedCG([(indptr, indices, data), ...], nrhs=16)
+    X, info = solver.solve(B, pc="jacobi", precision="fp64", rtol=1e-8)
+
+`B` stacks the systems' right-hand sides row-wise: an (sum n_s, nrhs) FP64
+array (numpy on the host or a CUDA tensor); `X` has the same shape and
+placement.  Each (system, column) pair follows the CG recurrence of
+KSPSolve_CG (src/ksp.mojo:271-389) with its own stopping test.
+precision="fp32" solves each pair with an FP32 inner CG inside FP64
+iterative refinement until the true FP64 residual meets rtol.
+
+`shard_systems` splits a batch across ranks (one GPU each) by a greedy
+balance of nnz * nrhs; the systems are independent, so a sharded run needs
+no collective beyond gathering the results.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _device as dev
+from ._lib import check, lib
+
+_PC = {"none": 0, "jacobi": 2}
+_PREC = {"fp64": 0, "fp32": 1}
+
+
+class BatchOptions(ctypes.Structure):
+    _fields_ = [("pc_type", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("max_it", ctypes.c_int32), ("max_outer", ctypes.c_int32),
+                ("rtol", ctypes.c_double), ("atol", ctypes.c_double),
+                ("divtol", ctypes.c_double), ("inner_rtol", ctypes.c_double)]
+
+
+def stack_systems(systems):
+    """Concatenate (indptr, indices, data) triples into one block-diagonal CSR.
+    Returns (sys_rows, indptr, indices, data) as int64/float64 arrays."""
+    sizes = [len(ip) - 1 for ip, _, _ in systems]
+    sys_rows = np.zeros(len(systems) + 1, dtype=np.int64)
+    sys_rows[1:] = np.cumsum(sizes)
+    nnz = [int(ip[-1]) for ip, _, _ in systems]
+    offs = np.concatenate([[0], np.cumsum(nnz)]).astype(np.int64)
+    indptr = np.zeros(int(sys_rows[-1]) + 1, dtype=np.int64)
+    indices = np.empty(int(offs[-1]), dtype=np.int64)
+    data = np.empty(int(offs[-1]), dtype=np.float64)
+    for s, (ip, ix, v) in enumerate(systems):
+        r0, r1 = int(sys_rows[s]), int(sys_rows[s + 1])
+        indptr[r0 + 1:r1 + 1] = np.asarray(ip[1:], dtype=np.int64) + offs[s]
+        indices[offs[s]:offs[s + 1]] = np.asarray(ix, dtype=np.int64) + r0
+        data[offs[s]:offs[s + 1]] = v
+    return sys_rows, indptr, indices, data
+
+
+def shard_systems(costs, world: int):
+    """Greedy longest-processing-time split of systems (cost = nnz * nrhs)
+    over `world` ranks: returns one sorted list of system indices per rank."""
+    order = sorted(range(len(costs)), key=lambda s: (-costs[s], s))
+    load = [0.0] * world
+    out = [[] for _ in range(world)]
+    for s in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        out[r].append(s)
+        load[r] += costs[s]
+    return [sorted(x) for x in out]
+
+
+class BatchedCG:
+    def __init__(self, systems, nrhs: int = 16, autotune: bool = True):
+        if nrhs not in (1, 2, 4, 8, 16):
+            raise ValueError("nrhs must be 1, 2, 4, 8 or 16")
+        torch = dev.torch()
+        self.nrhs = nrhs
+        self.sys_rows, indptr, indices, data = stack_systems(systems)
+        self.nsys = len(systems)
+        self.n = int(self.sys_rows[-1])
+        h = ctypes.c_void_p()
+        check(lib().gp_batch_create(ctypes.byref(h), self.nsys, self.sys_rows.ctypes.data,
+                                    indptr.ctypes.data, indices.ctypes.data,
+                                    data.ctypes.data if len(data) else None, nrhs,
+                                    dev.stream_ptr()))
+        self._h = h.value
+        self._torch = torch
+        if autotune:
+            check(lib().gp_batch_autotune(self._h, dev.stream_ptr()))
+
+    def __del__(self):
+        try:
+            lib().gp_batch_destroy(self._h)
+        except Exception:
+            pass
+
+    @property
+    def tuning(self):
+        bl, vr, tr = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        us = ctypes.c_double()
+        check(lib().gp_batch_tuning(self._h, ctypes.byref(bl), ctypes.byref(vr),
+                                    ctypes.byref(tr), ctypes.byref(us)))
+        return {"block": bl.value, "columns_per_thread": vr.value, "tile_rows": tr.value,
+                "spmm_us": us.value}
+
+    def solve(self, B, pc: str = "jacobi", precision: str = "fp64", rtol: float = 1e-8,
+              atol: float = 1e-50, divtol: float = 1e4, max_it: int = 10000,
+              max_outer: int = 20, inner_rtol: float = 1e-4, out=None):
+        torch = self._torch
+        if pc not in _PC or precision not in _PREC:
+            raise NotImplementedError(f"batched CG supports pc {sorted(_PC)} and precision "
+                                      f"{sorted(_PREC)}")
+        host = not isinstance(B, torch.Tensor)
+        Bt = torch.as_tensor(np.ascontiguousarray(B, dtype=np.float64)) if host else B
+        if tuple(Bt.shape) != (self.n, self.nrhs) or Bt.dtype != torch.float64:
+            raise ValueError(f"B must be float64 of shape ({self.n}, {self.nrhs})")
+        Bd = Bt.to("cuda").contiguous()
+        X = out if out is not None else torch.empty_like(Bd)
+        o = BatchOptions()
+        lib().gp_batch_options_default(ctypes.byref(o))
+        o.pc_type, o.precision = _PC[pc], _PREC[precision]
+        o.max_it, o.max_outer = int(max_it), int(max_outer)
+        o.rtol, o.atol, o.divtol, o.inner_rtol = rtol, atol, divtol, inner_rtol
+        npairs = self.nsys * self.nrhs
+        its = np.zeros(npairs, dtype=np.int64)
+        reason = np.zeros(npairs, dtype=np.int32)
+        relres = np.zeros(npairs, dtype=np.float64)
+        passes = ctypes.c_int32()
+        check(lib().gp_batch_solve_cg(self._h, ctypes.byref(o), dev.ptr(Bd), dev.ptr(X),
+                                      its.ctypes.data, reason.ctypes.data, relres.ctypes.data,
+                                      ctypes.byref(passes), dev.stream_ptr()))
+        shape = (self.nsys, self.nrhs)
+        info = {"its": its.reshape(shape), "reason": reason.reshape(shape),
+                "relres": relres.reshape(shape), "passes": passes.value}
+        return (X.cpu().numpy() if host else X), info

@@ -1,0 +1,110 @@
+"""Batched CG (mojopetsc4py.batch): every (system, column) pair against the
+single-system device CG on the same matrix and right-hand side, the reported
+residuals against an FP64 residual computed here, the FP32-inner refinement
+form against rtol on the true residual, and run-to-run determinism."""
+import numpy as np
+import pytest
+
+from mojopetsc4py import PETSc, gallery
+
+pytestmark = pytest.mark.gpu
+
+
+def systems(sizes, seed=11):
+    rng = np.random.default_rng(seed)
+    return [gallery.rgg_laplacian(n, rng) for n in sizes]
+
+
+def residual(sysm, X, B):
+    """||b - A x|| / ||b|| per pair, in FP64 on the host."""
+    out = []
+    r0 = 0
+    for ip, ix, v in sysm:
+        n = len(ip) - 1
+        rows = np.repeat(np.arange(n), np.diff(ip))
+        x = X[r0:r0 + n]
+        ax = np.zeros_like(x)
+        np.add.at(ax, rows, v[:, None] * x[ix])
+        b = B[r0:r0 + n]
+        out.append(np.linalg.norm(b - ax, axis=0) / np.maximum(np.linalg.norm(b, axis=0), 1e-300))
+        r0 += n
+    return np.array(out)
+
+
+def single_cg(ip, ix, v, b, pc, rtol):
+    n = len(ip) - 1
+    A = PETSc.Mat().createSeqAIJ((n, n))
+    A.setValuesCSR(ip, ix, v)
+    A.assemble()
+    ksp = PETSc.KSP().create()
+    ksp.setOperators(A)
+    ksp.setType("cg")
+    ksp.getPC().setType(pc)
+    ksp.setTolerances(rtol=rtol, atol=1e-50, max_it=10000)
+    x = PETSc.Vec().createSeq(n)
+    ksp.solve(PETSc.Vec().createWithArray(b), x)
+    return x.getArray().copy(), ksp.getIterationNumber(), ksp.getConvergedReason()
+
+
+@pytest.mark.parametrize("nrhs,pc", [(4, "jacobi"), (1, "none"), (16, "jacobi")])
+def test_each_pair_follows_the_single_system_cg(nrhs, pc):
+    from mojopetsc4py.batch import BatchedCG
+
+    sysm = systems([300, 1200, 57, 2500, 800])
+    solver = BatchedCG(sysm, nrhs=nrhs)
+    n = sum(len(ip) - 1 for ip, _, _ in sysm)
+    B = np.random.default_rng(5).normal(size=(n, nrhs))
+    X, info = solver.solve(B, pc=pc, rtol=1e-10)
+    r0 = 0
+    for s, (ip, ix, v) in enumerate(sysm):
+        m = len(ip) - 1
+        for c in range(nrhs):
+            x1, its1, reason1 = single_cg(ip, ix, v, B[r0:r0 + m, c].copy(), pc, 1e-10)
+            assert info["reason"][s, c] == reason1 == 2
+            # same recurrence; the batched kernels fuse multiply-adds and sum
+            # in another order, so the count moves by rounding on the
+            # ill-conditioned graphs (a few iterations in hundreds)
+            slack = max(2, int(0.02 * its1))
+            assert abs(int(info["its"][s, c]) - its1) <= slack, (s, c, info["its"][s, c], its1)
+            xb = X[r0:r0 + m, c]
+            assert np.linalg.norm(xb - x1) <= 1e-7 * np.linalg.norm(x1)
+        r0 += m
+    # the residual of a converged iterate is itself evaluated to ~1e-15
+    np.testing.assert_allclose(info["relres"], residual(sysm, X, B), rtol=1e-4, atol=1e-14)
+
+
+def test_fp32_inner_refinement_meets_rtol_on_the_true_residual():
+    from mojopetsc4py.batch import BatchedCG
+
+    sysm = systems([700, 4000, 1500, 90, 2600, 3100], seed=3)
+    n = sum(len(ip) - 1 for ip, _, _ in sysm)
+    solver = BatchedCG(sysm, nrhs=16)
+    B = np.random.default_rng(9).normal(size=(n, 16))
+    B[:, 3] = 0.0  # a zero right-hand side converges at once with x = 0
+    X, info = solver.solve(B, pc="jacobi", precision="fp32", rtol=1e-10)
+    true = residual(sysm, X, B)
+    mask = np.ones_like(true, dtype=bool)
+    mask[:, 3] = False
+    assert np.all(true[mask] <= 1e-10 * 1.01), true.max()
+    assert np.all(info["reason"] == 2)
+    assert np.all(X[:, 3] == 0.0)
+    assert info["passes"] >= 2
+    np.testing.assert_allclose(info["relres"][mask], true[mask], rtol=1e-4, atol=1e-14)
+
+
+def test_solves_are_deterministic_and_the_tuner_reports_its_choice():
+    import torch
+    from mojopetsc4py.batch import BatchedCG
+
+    sysm = systems([1000, 2000, 3000], seed=7)
+    n = sum(len(ip) - 1 for ip, _, _ in sysm)
+    solver = BatchedCG(sysm, nrhs=8)
+    t = solver.tuning
+    assert t["block"] in (128, 256, 512) and t["columns_per_thread"] in (1, 2, 4)
+    assert t["tile_rows"] in (128, 512) and t["spmm_us"] > 0
+    B = torch.randn(n, 8, dtype=torch.float64, device="cuda")
+    X1, i1 = solver.solve(B, rtol=1e-9)
+    X1 = X1.clone()
+    X2, i2 = solver.solve(B, rtol=1e-9)
+    assert torch.equal(X1, X2)
+    assert np.array_equal(i1["its"], i2["its"])
