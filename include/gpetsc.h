@@ -250,7 +250,8 @@ int gp_ksp_stats(gp_ksp ksp, int64_t *trips, int64_t *top_kernels, int64_t *body
  * caps the inner iterations of each pass, max_outer the passes).
  * nrhs must be 1, 2, 4, 8 or 16; pc_type 0 (none) or 2 (Jacobi).
  * gp_batch_autotune times the sparse pass for every (CTA size, columns per
- * thread, tile rows) and keeps the fastest; gp_batch_tuning reports it.
+ * thread, tile rows) and keeps the fastest, separately for the FP64 and the
+ * FP32 pass; gp_batch_tuning reports the choice for a precision (0 / 1).
  * Outputs (host, nsys * nrhs entries, each may be NULL): iterations (total
  * inner iterations for precision 1), converged reason, and the final true
  * relative residual ||b - A x|| / ||b|| computed in FP64.
@@ -270,8 +271,8 @@ int gp_batch_create(gp_batch *out, int64_t nsys, const int64_t *sys_rows,
                     int32_t nrhs, void *stream);
 int gp_batch_destroy(gp_batch b);
 int gp_batch_autotune(gp_batch b, void *stream);
-int gp_batch_tuning(gp_batch b, int32_t *block, int32_t *vector_width, int32_t *tile_rows,
-                    double *spmm_us);
+int gp_batch_tuning(gp_batch b, int32_t precision, int32_t *block, int32_t *vector_width,
+                    int32_t *tile_rows, double *spmm_us);
 int gp_batch_solve_cg(gp_batch b, const gp_batch_options *o, const double *B, double *X,
                       int64_t *its, int32_t *reason, double *relres, int32_t *passes,
                       void *stream);

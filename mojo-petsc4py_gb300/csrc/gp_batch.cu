@@ -191,12 +191,26 @@ __device__ __forceinline__ bool system_last(BatchDev& b, int s) {
   return last;
 }
 
-// Sum system s's partials (tile order) for column r, value k.
-__device__ __forceinline__ double system_sum(const BatchDev& b, int s, int r, int k, int R) {
-  double acc = 0.0;
+// Sum system s's partials for every (column, value) pair: warp w folds sums
+// j = w, w + nwarps, ... (j = column * NV + value); its lanes take tiles
+// lane, lane + 32, ... in order and a shuffle tree combines them -- a fixed
+// order, many loads in flight.  All threads call it; the totals are in the
+// returned shared array (index j) afterwards.
+__device__ __forceinline__ const double* system_sums(const BatchDev& b, int s, int R, int NV) {
+  __shared__ double tot[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int t0 = b.sys_tile0[s], nt = b.sys_ntiles[s];
-  for (int t = 0; t < nt; t++) acc += __ldcg(&b.partials[((size_t)(t0 + t) * R + r) * 2 + k]);
-  return acc;
+  for (int j = w; j < R * NV; j += nw) {
+    const int col = j / NV, k = j % NV;
+    double acc = 0.0;
+    for (int tt = lane; tt < nt; tt += 32)
+      acc += __ldcg(&b.partials[((size_t)(t0 + tt) * R + col) * 2 + k]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) tot[j] = acc;
+  }
+  __syncthreads();
+  return tot;
 }
 
 // ------------------------------------------------------------------ kernels
@@ -256,7 +270,8 @@ __global__ void k_bspmm(BatchDev b, const T* __restrict__ val, const T* __restri
     }
     tile_partials<T, R, VR, 1>(b, tile, dot, sh);
     if (system_last(b, s)) {
-      if (t < R) pair_after_spmm(b, s, s * R + t, system_sum(b, s, t, 0, R));
+      const double* tot = system_sums(b, s, R, 1);
+      if (t < R) pair_after_spmm(b, s, s * R + t, tot[t]);
       __syncthreads();
       if (t == 0) b.sys_ticket[s] = 0u;
     }
@@ -307,9 +322,8 @@ __global__ void k_bupdate(BatchDev b, const T* __restrict__ dinv, T* __restrict_
     }
     tile_partials<T, R, VR, 2>(b, tile, acc, sh);
     if (system_last(b, s)) {
-      if (t < R)
-        pair_after_update(b, s, s * R + t, system_sum(b, s, t, 0, R), system_sum(b, s, t, 1, R),
-                          FIRST);
+      const double* tot = system_sums(b, s, R, 2);
+      if (t < R) pair_after_update(b, s, s * R + t, tot[2 * t], tot[2 * t + 1], FIRST);
       __syncthreads();
       if (t == 0) b.sys_ticket[s] = 0u;
     }
@@ -321,6 +335,9 @@ __global__ void k_bctrl(cudaGraphConditionalHandle h, int* active_systems, int* 
   *trips += 1;
   cudaGraphSetConditional(h, (*active_systems > 0 && *trips < cap) ? 1u : 0u);
 }
+
+// host-driven loop: the trip count without the graph conditional
+__global__ void k_btrip(int* trips) { *trips += 1; }
 
 // residual of the FP64 system for the refinement form: r = b - A x (FP64),
 // per pair ||r||^2; the last tile stores rn = ||r|| and freezes pairs whose
@@ -362,9 +379,10 @@ __global__ void k_bresid(BatchDev b, const double* __restrict__ bb, const double
     }
     tile_partials<double, R, VR, 1>(b, tile, acc, sh);
     if (system_last(b, s)) {
+      const double* tot = system_sums(b, s, R, 1);
       if (t < R) {
         const int q = s * R + t;
-        const double nrm = sqrt(system_sum(b, s, t, 0, R));
+        const double nrm = sqrt(tot[t]);
         rn[q] = nrm;
         if (freeze && b.active[q] && !(nrm > b.rtol * bnorm[q])) pair_stop(b, s, q, BR_RTOL);
       }
@@ -390,7 +408,8 @@ __global__ void k_bnorm(BatchDev b, const double* __restrict__ bb, double* __res
     }
     tile_partials<double, R, 1, 1>(b, tile, acc, sh);
     if (system_last(b, s)) {
-      if (t < R) out[s * R + t] = sqrt(system_sum(b, s, t, 0, R));
+      const double* tot = system_sums(b, s, R, 1);
+      if (t < R) out[s * R + t] = sqrt(tot[t]);
       __syncthreads();
       if (t == 0) b.sys_ticket[s] = 0u;
     }
@@ -496,7 +515,8 @@ struct Batch {
   double *r = nullptr, *p = nullptr, *z = nullptr;
   float *x32 = nullptr, *r32 = nullptr, *p32 = nullptr, *z32 = nullptr;
   double *bnorm = nullptr, *rn = nullptr;
-  Tuning tune;
+  Tuning tune, tune32;          // FP64 and FP32 sparse-pass choices
+  const Tuning* cur = &tune;    // the one the current solve launches with
   bool tuned = false;
   cudaStream_t cap_stream = nullptr;
   // captured solves: [0] FP64 CG between (cap_b, cap_x), [1] FP32 inner CG
@@ -589,7 +609,7 @@ struct Launch {
 template <typename T, int R, int VR, int NV>
 static Launch shape_of(const Batch& B, const void* k) {
   Launch l;
-  l.block = B.tune.block;
+  l.block = B.cur->block;
   l.smem = (size_t)NV * VR * l.block * sizeof(T);
   l.grid = std::max(1, std::min(B.ntiles, resident(k, l.block, l.smem)));
   return l;
@@ -614,8 +634,8 @@ static void launch_update(const Batch& B, const BatchDev& d, const T* dinv, T* x
 template <typename T, int R>
 static void launch_p(const Batch& B, const BatchDev& d, T* p, const T* z, cudaStream_t s) {
   auto k = k_bp<T, R>;
-  const int g = std::max(1, std::min(B.ntiles, resident((const void*)k, B.tune.block, 0)));
-  k<<<g, B.tune.block, 0, s>>>(d, p, z);
+  const int g = std::max(1, std::min(B.ntiles, resident((const void*)k, B.cur->block, 0)));
+  k<<<g, B.cur->block, 0, s>>>(d, p, z);
 }
 
 template <int R, int VR>
@@ -826,55 +846,84 @@ struct BatchOptions {
   double inner_rtol = 1e-4;
 };
 
-// Time the FP64 sparse pass for every (block, vector width, tile rows) and
-// keep the fastest.  State is reset before each timing (all systems active).
+// Time the sparse pass for every (CTA size, columns per thread, tile rows)
+// and keep the fastest: tile rows from the FP64 pass, then the FP64 and the
+// FP32 pass each get their own CTA size and width.  State is reset before
+// each timing (all systems active).
+template <typename T>
+static int time_spmm(Batch* B, Tuning* t, int bl, int vr, cudaEvent_t e0, cudaEvent_t e1,
+                     cudaStream_t s, float* best_ms) {
+  t->block = bl;
+  t->vr = vr;
+  B->cur = t;
+  BatchDev d = dev_view(*B, 1e-8, 1e-50, 1e4, 1, 0);
+  *best_ms = 1e30f;
+  const T* val = sizeof(T) == 8 ? (const T*)B->val : (const T*)B->val32;
+  T* pv = sizeof(T) == 8 ? (T*)B->p : (T*)B->p32;
+  T* zv = sizeof(T) == 8 ? (T*)B->z : (T*)B->z32;
+  if (sizeof(T) == 4) GP_CUDA(cudaMemsetAsync(B->p32, 0, (size_t)B->n * B->R * sizeof(float), s));
+  int st = with_shape(B->R, vr, [&](auto RR, auto VV) {
+    for (int rep = 0; rep < 6; rep++) {
+      launch_state(*B, d, nullptr, s);
+      cudaEventRecord(e0, s);
+      launch_spmm<T, decltype(RR)::value, decltype(VV)::value>(*B, d, val, pv, zv, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep >= 2) *best_ms = std::min(*best_ms, ms);
+    }
+  });
+  GP_TRY(st);
+  GP_CUDA(cudaGetLastError());
+  return GP_OK;
+}
+
 int batch_autotune(Batch* B, cudaStream_t s) {
   drop_graphs(*B);
   const int blocks[] = {128, 256, 512};
   const int widths[] = {1, 2, 4};
   const int tiles[] = {128, 512};
-  Tuning best;
-  best.spmm_us = 1e30;
+  auto ok = [&](int bl, int vr) { return vr <= B->R && B->R % vr == 0 && bl / (B->R / vr) >= 1; };
   cudaEvent_t e0, e1;
   GP_CUDA(cudaEventCreate(&e0));
   GP_CUDA(cudaEventCreate(&e1));
+  Tuning best, t;
+  best.spmm_us = 1e30;
   for (int tr : tiles) {
     GP_TRY(build_tiles(*B, tr, s));
     for (int bl : blocks)
       for (int vr : widths) {
-        if (vr > B->R || B->R % vr || bl / (B->R / vr) < 1) continue;
-        B->tune.block = bl;
-        B->tune.vr = vr;
-        BatchDev d = dev_view(*B, 1e-8, 1e-50, 1e4, 1, 0);
-        float best_ms = 1e30f;
-        int st = with_shape(B->R, vr, [&](auto RR, auto VV) {
-          for (int rep = 0; rep < 6; rep++) {
-            launch_state(*B, d, nullptr, s);
-            cudaEventRecord(e0, s);
-            launch_spmm<double, decltype(RR)::value, decltype(VV)::value>(*B, d, B->val, B->p,
-                                                                          B->z, s);
-            cudaEventRecord(e1, s);
-            cudaEventSynchronize(e1);
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (rep >= 2) best_ms = std::min(best_ms, ms);
-          }
-        });
-        GP_TRY(st);
-        GP_CUDA(cudaGetLastError());
-        if (best_ms * 1e3 < best.spmm_us) {
+        if (!ok(bl, vr)) continue;
+        float ms;
+        GP_TRY(time_spmm<double>(B, &t, bl, vr, e0, e1, s, &ms));
+        if (ms * 1e3 < best.spmm_us) {
           best.block = bl;
           best.vr = vr;
           best.tile_rows = tr;
-          best.spmm_us = best_ms * 1e3;
+          best.spmm_us = ms * 1e3;
         }
       }
   }
+  GP_TRY(build_tiles(*B, best.tile_rows, s));
+  Tuning best32 = best;
+  best32.spmm_us = 1e30;
+  for (int bl : blocks)
+    for (int vr : widths) {
+      if (!ok(bl, vr)) continue;
+      float ms;
+      GP_TRY(time_spmm<float>(B, &t, bl, vr, e0, e1, s, &ms));
+      if (ms * 1e3 < best32.spmm_us) {
+        best32.block = bl;
+        best32.vr = vr;
+        best32.spmm_us = ms * 1e3;
+      }
+    }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   B->tune = best;
-  GP_TRY(build_tiles(*B, best.tile_rows, s));
-  B->tune = best;
+  B->tune32 = best32;
+  B->cur = &B->tune;
   B->tuned = true;
   return GP_OK;
 }
@@ -930,6 +979,58 @@ static int capture_loop(Batch& B, cudaStream_t s2, int cap, P&& prologue, Bd&& b
   return GP_OK;
 }
 
+// GPETSC_KSP_GRAPH=0: the same prologue / body / epilogue launched from the
+// host, the loop polled every 8 trips (the form ncu profiles kernel by kernel).
+static bool batch_eager() {
+  static bool v = [] {
+    const char* e = std::getenv("GPETSC_KSP_GRAPH");
+    return e && std::string(e) == "0";
+  }();
+  return v;
+}
+
+template <typename P, typename Bd, typename E>
+static int run_eager_loop(Batch& B, cudaStream_t s, int cap, P&& prologue, Bd&& body,
+                          E&& epilogue) {
+  prologue(s);
+  for (int trip = 1;; trip++) {
+    body(s);
+    k_btrip<<<1, 1, 0, s>>>(B.counters + 1);
+    if (trip % 8 == 0 || trip >= cap) {
+      int c[2] = {0, 0};
+      GP_CUDA(cudaMemcpyAsync(c, B.counters, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+      GP_CUDA(cudaStreamSynchronize(s));
+      if (c[0] == 0 || c[1] >= cap) break;
+    }
+  }
+  epilogue(s);
+  GP_CUDA(cudaGetLastError());
+  return GP_OK;
+}
+
+// Run the loop: re-use the captured graph in `slot` when its key matches,
+// else capture it (or, in the host-driven mode, launch everything directly).
+template <typename P, typename Bd, typename E>
+static int run_loop(Batch& B, int slot, cudaStream_t s2, const double* b, double* x,
+                    const double (&key)[10], int cap, P&& prologue, Bd&& body, E&& epilogue) {
+  cudaStream_t s = B.cap_stream;
+  if (batch_eager()) return run_eager_loop(B, s, cap, prologue, body, epilogue);
+  const bool same = B.exec[slot] && B.cap_b[slot] == b && B.cap_x[slot] == x &&
+                    std::equal(key, key + 10, B.cap_key[slot]);
+  if (!same) {
+    if (B.exec[slot]) cudaGraphExecDestroy(B.exec[slot]);
+    if (B.graph[slot]) cudaGraphDestroy(B.graph[slot]);
+    B.exec[slot] = nullptr;
+    B.graph[slot] = nullptr;
+    GP_TRY(capture_loop(B, s2, cap, prologue, body, epilogue, &B.graph[slot], &B.exec[slot]));
+    B.cap_b[slot] = b;
+    B.cap_x[slot] = x;
+    std::copy(key, key + 10, B.cap_key[slot]);
+  }
+  GP_CUDA(cudaGraphLaunch(B.exec[slot], s));
+  return GP_OK;
+}
+
 struct BatchResult {
   std::vector<int> its, reason;
   std::vector<double> relres;
@@ -954,7 +1055,7 @@ static int solve_shape(Batch& B, const BatchOptions& o, const double* b, double*
   // every value a captured kernel received by value
   const double key[10] = {(double)o.pc,      (double)o.max_it,     o.rtol,
                           o.atol,            o.divtol,             o.inner_rtol,
-                          (double)B.tune.block, (double)B.tune.vr, (double)B.tune.tile_rows,
+                          (double)B.cur->block, (double)B.cur->vr, (double)B.tune.tile_rows,
                           (double)B.ntiles};
   int* refined = refined_of(B);
   int* its_total = its_total_of(B);
@@ -964,15 +1065,8 @@ static int solve_shape(Batch& B, const BatchOptions& o, const double* b, double*
     k<<<l.grid, l.block, l.smem, st>>>(d64, b, B.bnorm);
   };
   if (o.precision == 0) {
-    const bool same = B.exec[0] && B.cap_b[0] == b && B.cap_x[0] == x &&
-                      std::equal(key, key + 10, B.cap_key[0]);
-    if (!same) {
-      if (B.exec[0]) cudaGraphExecDestroy(B.exec[0]);
-      if (B.graph[0]) cudaGraphDestroy(B.graph[0]);
-      B.exec[0] = nullptr;
-      B.graph[0] = nullptr;
-      GP_TRY(capture_loop(
-          B, s2, o.max_it + 8,
+    GP_TRY(run_loop(
+          B, 0, s2, b, x, key, o.max_it + 8,
           [&](cudaStream_t st) {
             cudaMemsetAsync(B.counters, 0, 2 * sizeof(int), st);
             cudaMemsetAsync(x, 0, nv * sizeof(double), st);
@@ -986,31 +1080,19 @@ static int solve_shape(Batch& B, const BatchOptions& o, const double* b, double*
             launch_spmm<double, R, VR>(B, d64, B.val, B.p, B.z, st);  // W shares Z's storage
             launch_update<double, R, VR, false>(B, d64, dinv, x, B.r, B.p, B.z, B.z, st);
           },
-          [&](cudaStream_t st) { launch_resid<R, VR>(B, d64, b, x, 0, st); }, &B.graph[0],
-          &B.exec[0]));
-      B.cap_b[0] = b;
-      B.cap_x[0] = x;
-      std::copy(key, key + 10, B.cap_key[0]);
-    }
-    GP_CUDA(cudaGraphLaunch(B.exec[0], s));
+          [&](cudaStream_t st) { launch_resid<R, VR>(B, d64, b, x, 0, st); }));
   } else {
     // FP32 inner CG on A d = r / ||r||, x += ||r|| d, until ||b - A x|| <= rtol ||b||
     const BatchDev d32 = dev_view(B, o.inner_rtol, 1e-30, 1e30, o.max_it, o.pc);
-    const bool same = B.exec[1] && B.cap_b[1] == b && B.cap_x[1] == x &&
-                      std::equal(key, key + 10, B.cap_key[1]);
-    if (!same) {
-      if (B.exec[1]) cudaGraphExecDestroy(B.exec[1]);
-      if (B.graph[1]) cudaGraphDestroy(B.graph[1]);
-      B.exec[1] = nullptr;
-      B.graph[1] = nullptr;
-      GP_TRY(capture_loop(
-          B, s2, o.max_it + 8,
+    auto pass = [&]() {
+      return run_loop(
+          B, 1, s2, b, x, key, o.max_it + 8,
           [&](cudaStream_t st) {
             cudaMemsetAsync(B.counters, 0, 2 * sizeof(int), st);
             launch_state(B, d32, refined, st);
             auto ks = k_bscale_in<R>;
-            const int g = std::max(1, std::min(B.ntiles, resident((const void*)ks, B.tune.block, 0)));
-            ks<<<g, B.tune.block, 0, st>>>(d32, B.r, B.rn, B.r32, B.x32);
+            const int g = std::max(1, std::min(B.ntiles, resident((const void*)ks, B.cur->block, 0)));
+            ks<<<g, B.cur->block, 0, st>>>(d32, B.r, B.rn, B.r32, B.x32);
             launch_update<float, R, VR, true>(B, d32, dinv32, B.x32, B.r32, B.p32, B.z32, B.z32,
                                               st);
           },
@@ -1025,16 +1107,12 @@ static int solve_shape(Batch& B, const BatchOptions& o, const double* b, double*
                 (int)np, d32.its, its_total);
             launch_state(B, d64, refined, st);
             auto ka = k_bacc<R>;
-            const int g = std::max(1, std::min(B.ntiles, resident((const void*)ka, B.tune.block, 0)));
-            ka<<<g, B.tune.block, 0, st>>>(d64, refined, B.rn, B.x32, x);
+            const int g = std::max(1, std::min(B.ntiles, resident((const void*)ka, B.cur->block, 0)));
+            ka<<<g, B.cur->block, 0, st>>>(d64, refined, B.rn, B.x32, x);
             launch_resid<R, VR>(B, d64, b, x, 1, st);
             cudaMemcpyAsync(refined, d64.active, np * sizeof(int), cudaMemcpyDeviceToDevice, st);
-          },
-          &B.graph[1], &B.exec[1]));
-      B.cap_b[1] = b;
-      B.cap_x[1] = x;
-      std::copy(key, key + 10, B.cap_key[1]);
-    }
+          });
+    };
     // first pass: r = b, rn = ||b||, pairs with b = 0 frozen
     GP_CUDA(cudaMemsetAsync(x, 0, nv * sizeof(double), s));
     GP_CUDA(cudaMemsetAsync(its_total, 0, np * sizeof(int), s));
@@ -1048,7 +1126,7 @@ static int solve_shape(Batch& B, const BatchOptions& o, const double* b, double*
       GP_CUDA(cudaMemcpyAsync(&left, B.counters, sizeof(int), cudaMemcpyDeviceToHost, s));
       GP_CUDA(cudaStreamSynchronize(s));
       if (left == 0) break;
-      GP_CUDA(cudaGraphLaunch(B.exec[1], s));
+      GP_TRY(pass());
     }
     launch_resid<R, VR>(B, d64, b, x, 0, s);
   }
@@ -1086,7 +1164,8 @@ int batch_solve(Batch* B, const BatchOptions& o, const double* b, double* x, cud
     return GP_ERR_ARG;
   }
   int st = GP_OK;
-  int r = with_shape(B->R, B->tune.vr, [&](auto RR, auto VV) {
+  B->cur = o.precision ? &B->tune32 : &B->tune;
+  int r = with_shape(B->R, B->cur->vr, [&](auto RR, auto VV) {
     st = solve_shape<decltype(RR)::value, decltype(VV)::value>(*B, o, b, x, s, res);
   });
   GP_TRY(r);
@@ -1154,13 +1233,13 @@ int gp_batch_autotune(gp_batch b, void* stream) {
   }
 }
 
-int gp_batch_tuning(gp_batch b, int32_t* block, int32_t* vector_width, int32_t* tile_rows,
-                    double* spmm_us) {
+int gp_batch_tuning(gp_batch b, int32_t precision, int32_t* block, int32_t* vector_width,
+                    int32_t* tile_rows, double* spmm_us) {
   if (!b) {
     gp::set_error("gp_batch_tuning: null argument");
     return GP_ERR_ARG;
   }
-  const gp::Tuning& t = b->B->tune;
+  const gp::Tuning& t = precision ? b->B->tune32 : b->B->tune;
   if (block) *block = t.block;
   if (vector_width) *vector_width = t.vr;
   if (tile_rows) *tile_rows = t.tile_rows;

@@ -72,7 +72,7 @@ GP_SIGNATURES = {
     "gp_batch_destroy": ([P], ctypes.c_int),
     "gp_batch_options_default": ([P], None),
     "gp_batch_autotune": ([P, P], ctypes.c_int),
-    "gp_batch_tuning": ([P, P, P, P, P], ctypes.c_int),
+    "gp_batch_tuning": ([P, ctypes.c_int32, P, P, P, P], ctypes.c_int),
     "gp_batch_solve_cg": ([P, P, P, P, P, P, P, P, P], ctypes.c_int),
     "gp_mat_create": ([PP, I64, I64, I64, P, P, P], ctypes.c_int),
     "gp_mat_create_i32": ([PP, I64, I64, I64, P, P, P], ctypes.c_int),

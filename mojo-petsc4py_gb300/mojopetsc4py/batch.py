@@ -92,14 +92,23 @@ class BatchedCG:
         except Exception:
             pass
 
-    @property
-    def tuning(self):
+    def _tuning(self, precision: int):
         bl, vr, tr = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
         us = ctypes.c_double()
-        check(lib().gp_batch_tuning(self._h, ctypes.byref(bl), ctypes.byref(vr),
+        check(lib().gp_batch_tuning(self._h, precision, ctypes.byref(bl), ctypes.byref(vr),
                                     ctypes.byref(tr), ctypes.byref(us)))
         return {"block": bl.value, "columns_per_thread": vr.value, "tile_rows": tr.value,
                 "spmm_us": us.value}
+
+    @property
+    def tuning(self):
+        """The autotuner's choice for the FP64 sparse pass."""
+        return self._tuning(0)
+
+    @property
+    def tuning32(self):
+        """The autotuner's choice for the FP32 sparse pass."""
+        return self._tuning(1)
 
     def solve(self, B, pc: str = "jacobi", precision: str = "fp64", rtol: float = 1e-8,
               atol: float = 1e-50, divtol: float = 1e4, max_it: int = 10000,
