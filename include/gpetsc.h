@@ -178,6 +178,14 @@ int gp_pc_set_options(gp_pc pc, const gp_pc_options *o);
  * Replaces PC.setUp (python/mojopetsc4py/PETSc/PC.py:315-492). */
 int gp_pc_setup(gp_pc pc, gp_mat A, void *stream);
 /* y = M^-1 x.  Replaces KSP_PCApply (src/ksp.mojo:155-198). */
+/* Failure detection: every device wait of the triangular sweeps and the
+ * numeric factorisation has an iteration budget; when it runs out the kernel
+ * records GP_ERR_TIMEOUT, returns, and the call that launched it reports
+ * GP_ERR_TIMEOUT (the context stays usable).  gp_wait_probe runs that wait
+ * once, on a flag that nothing sets (set = 0: returns GP_ERR_TIMEOUT after
+ * `spins` polls) or on a ready one (set = 1: GP_OK).  No counterpart in the
+ * reference (its sweeps are sequential host loops). */
+int gp_wait_probe(int32_t spins, int32_t set, void *stream);
 /* Same pattern, new operator values: redo only the numeric phase (ILU/IC factor
  * values on the device, Jacobi diagonals) in the arrays of the last set-up;
  * solver graphs captured with this PC stay valid. */

@@ -258,6 +258,11 @@ int gp_pc_setup(gp_pc pc, gp_mat A, void* stream) {
   GUARD(gp::pc_setup(pc->pc, A->A, S(stream)));
 }
 
+int gp_wait_probe(int32_t spins, int32_t set, void* stream) {
+  if (spins < 0) return bad("gp_wait_probe: spins must be >= 0");
+  GUARD(gp::sweep_wait_probe(spins, set, S(stream)));
+}
+
 int gp_pc_update_values(gp_pc pc, void* stream) {
   if (!pc) return bad("gp_pc_update_values: null argument");
   GUARD(gp::pc_update_values(pc->pc, S(stream)));

@@ -57,6 +57,7 @@ int ell_build(EllSweep& e, int n, const std::vector<int>& order, const std::vect
               const std::vector<int>& in_row, const std::vector<int>& out_row,
               const std::vector<int>& dslot_row, std::vector<int>* pos_of_row);
 int ell_refresh(EllSweep& e, const double* src, cudaStream_t s);
+int sweep_wait_probe(int budget, int set, cudaStream_t s);
 int ell_sweep(int mode, const EllSweep& e, const int* gate, int want, DRef in, DRef out,
               double* val, const double* fval, double* aux, const double* auxin,
               const double* idiag, double omega, int use_t, int write_out, unsigned* tickets,

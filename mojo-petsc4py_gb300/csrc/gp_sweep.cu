@@ -13,6 +13,7 @@
 // reference's slot order with rounded multiplies and adds, so the result is
 // bit-identical to the sequential loop.
 #include <algorithm>
+#include <string>
 #include <vector>
 
 #include "gp_pc.h"
@@ -22,10 +23,11 @@ namespace gp {
 constexpr int kEllBlock = 256;
 constexpr int kEllSpin = 1 << 22;
 
-__device__ __forceinline__ double ell_wait(const double* p, DevErr* err, int where) {
+__device__ __forceinline__ double ell_wait(const double* p, DevErr* err, int where,
+                                           int budget = kEllSpin) {
   unsigned long long b = ld_relaxed_bits(p);
   if (b != kPending) return __longlong_as_double((long long)b);
-  for (int spins = 0; spins < kEllSpin; spins++) {
+  for (int spins = 0; spins < budget; spins++) {
     if (spins > 64) __nanosleep(20);
     b = ld_relaxed_bits(p);
     if (b != kPending) return __longlong_as_double((long long)b);
@@ -146,6 +148,14 @@ __global__ void __launch_bounds__(kEllBlock) k_ell_sweep(const int* gate, int wa
   }
 }
 
+// The sweeps' wait, on its own: one thread waits for `flag` with the given
+// budget.  With a flag that nothing sets, the wait runs out, records
+// GP_ERR_TIMEOUT in `err` and returns -- the failure path every sweep takes
+// when a dependency never arrives, exercised without faulting anything.
+__global__ void k_wait_probe(const double* flag, int budget, DevErr* err, double* out) {
+  out[0] = ell_wait(flag, err, 99, budget);
+}
+
 // coefficient (and diagonal) refresh from the factor or matrix values
 __global__ void k_ell_refresh(int n, int W, const int* __restrict__ cnt,
                               const int* __restrict__ cslot, const double* __restrict__ src,
@@ -214,6 +224,45 @@ int ell_build(EllSweep& e, int n, const std::vector<int>& order, const std::vect
   if (pos_of_row) *pos_of_row = pos;
   e.ok = true;
   return GP_OK;
+}
+
+// Run the wait once on a pending flag (set = 0) or a ready one (set = 1) and
+// report the status the host reads after a sweep.
+int sweep_wait_probe(int budget, int set, cudaStream_t s) {
+  double* buf = nullptr;
+  DevErr* err = nullptr;
+  GP_CUDA(cudaMalloc(&buf, 2 * sizeof(double)));
+  cudaError_t e = cudaMalloc(&err, sizeof(DevErr));
+  if (e != cudaSuccess) {
+    cudaFree(buf);
+    return GP_ERR_CUDA;
+  }
+  const unsigned long long pending = kPending;
+  const double ready = 1.5;
+  int st = GP_OK;
+  if (cudaMemcpyAsync(buf, set ? (const void*)&ready : (const void*)&pending, sizeof(double),
+                      cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemsetAsync(err, 0, sizeof(DevErr), s) != cudaSuccess) {
+    st = GP_ERR_CUDA;
+  } else {
+    k_wait_probe<<<1, 1, 0, s>>>(buf, budget, err, buf + 1);
+    DevErr h{};
+    double got = 0.0;
+    if (cudaMemcpyAsync(&h, err, sizeof(DevErr), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(&got, buf + 1, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      st = GP_ERR_CUDA;
+    } else if (h.code) {
+      set_error("device wait ran out of its budget (site " + std::to_string(h.where) + ")");
+      st = h.code;
+    } else if (got != ready) {
+      set_error("device wait returned a wrong value");
+      st = GP_ERR_INTERNAL;
+    }
+  }
+  cudaFree(buf);
+  cudaFree(err);
+  return st;
 }
 
 int ell_refresh(EllSweep& e, const double* src, cudaStream_t s) {

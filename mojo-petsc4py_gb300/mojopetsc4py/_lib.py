@@ -99,6 +99,7 @@ GP_SIGNATURES = {
     "gp_pc_set_options": ([P, ctypes.POINTER(PcOptions)], ctypes.c_int),
     "gp_pc_setup": ([P, P, P], ctypes.c_int),
     "gp_pc_update_values": ([P, P], ctypes.c_int),
+    "gp_wait_probe": ([ctypes.c_int32, ctypes.c_int32, P], ctypes.c_int),
     "gp_pc_apply": ([P, P, P, P], ctypes.c_int),
     "gp_pc_apply_symmetric": ([P, P, P, P], ctypes.c_int),
     "gp_pc_factor_info": ([P, P, P], ctypes.c_int),
