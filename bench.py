@@ -351,7 +351,8 @@ def run_ours(args, world, rank, local, pg):
     forms = None
     if rank == 0 and world == 1 and not args.quick and not args.no_forms:
         forms = {}
-        for name, fn in (("batched", form_batched), ("adjoint", form_adjoint)):
+        for name, fn in (("mixed", form_mixed), ("batched", form_batched),
+                         ("adjoint", form_adjoint)):
             try:
                 forms[name] = fn(torch, PETSc)
             except Exception as e:  # reported, never hidden
@@ -467,6 +468,55 @@ def form_batched(torch, PETSc):
     return out
 
 
+def form_mixed(torch, PETSc):
+    """3-D upwind convection-diffusion 96^3 (cell Peclet 10): plain FP64
+    GMRES(30) + ILU(0) against FP32 inner FGMRES(30) + ILU(0) in FP64
+    refinement, both judged on the true FP64 residual (target 1e-10)."""
+    from mojopetsc4py import gallery
+    from mojopetsc4py.mixed import MixedSolver
+
+    ip, ix, v = gallery.convection_diffusion_3d(96)
+    n = len(ip) - 1
+    b = np.random.default_rng(7).uniform(-1.0, 1.0, n)
+    A = PETSc.Mat().createSeqAIJ((n, n))
+    A.setValuesCSR(ip, ix, v)
+    A.assemble()
+    bv = PETSc.Vec().createWithArray(b)
+    out = {"config": "3-D upwind convection-diffusion 96^3, v = (1, 0.5, 0.25), cell Peclet 10, "
+                     "b U[-1,1] seed 7; target ||b - A x|| <= 1e-10 ||b||",
+           "n": n, "nnz": int(ip[-1])}
+
+    def true_rel(x):
+        return float(np.linalg.norm(b - _csr_matvec(ip, ix, v, x)) / np.linalg.norm(b))
+
+    ksp = build_solver(PETSc, A, "gmres", "ilu")
+    ksp.setTolerances(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=MAX_IT)
+    xv = PETSc.Vec().createSeq(n)
+    ksp.solve(bv, xv)
+    ms = _sync_ms(torch, lambda: ksp.solve(bv, xv), 1)
+    out["plain_fp64_gmres30_ilu0"] = {"ms": round(ms, 2), "its": ksp.getIterationNumber(),
+                                      "reason": ksp.getConvergedReason(),
+                                      "true_rel_residual": true_rel(xv.getArray())}
+    solver = MixedSolver(A)
+    for key, sweeps in (("mixed_fp32_fgmres30_ilu0_jacobi4", 4),
+                        ("mixed_fp32_fgmres30_ilu0_exact", 0)):
+        xm = PETSc.Vec().createSeq(n)
+        solver.solve(bv, xm, rtol=1e-10, tri_sweeps=sweeps)
+        info = {}
+
+        def run():
+            info.update(solver.solve(bv, xm, rtol=1e-10, tri_sweeps=sweeps))
+
+        ms = _sync_ms(torch, run, 2)
+        out[key] = {"ms": round(ms, 2), "passes": info["passes"],
+                    "inner_its": info["inner_its"], "converged": info["converged"],
+                    "true_rel_residual": true_rel(xm.getArray())}
+    p = out["plain_fp64_gmres30_ilu0"]["ms"]
+    out["speedup_vs_plain"] = {k: round(p / out[k]["ms"], 2) for k in out
+                               if k.startswith("mixed_")}
+    return out
+
+
 def form_adjoint(torch, PETSc):
     """Gradient of ||u - u_obs||^2 through A(kappa) u = b, 2-D advection-
     diffusion 256^2 (Peclet 2), GMRES(30) + ILU(0) to rtol 1e-10: forward and
@@ -534,7 +584,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--spmv-only", action="store_true", help="SpMV launches only")
     ap.add_argument("--no-forms", action="store_true",
-                    help="skip the batched and adjoint forms")
+                    help="skip the mixed, batched and adjoint forms")
     ap.add_argument("--max-it", type=int, default=None,
                     help="cap the iterations (profiling runs only; not a bench value)")
     args = ap.parse_args()

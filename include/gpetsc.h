@@ -244,6 +244,37 @@ int gp_ksp_solve(gp_ksp ksp, gp_mat A, gp_pc pc, const double *b, double *x,
 int gp_ksp_stats(gp_ksp ksp, int64_t *trips, int64_t *top_kernels, int64_t *body_kernels);
 
 
+/* ------------------------------------------------------------ mixed precision
+ * A x = b to rtol on the true FP64 residual (||b - A x|| <= rtol ||b||) by
+ * FP64 iterative refinement around an FP32 inner FGMRES(restart) cycle
+ * preconditioned with the ILU(0) factor of `pc` (an ILU gp_pc set up on A)
+ * in FP32.  tri_sweeps > 0 applies each triangle of the factor with that many
+ * Jacobi passes (bandwidth-bound, inexact, tolerated by the flexible method);
+ * 0 applies it exactly with the level-scheduled FP64 sweeps.  Each pass runs
+ * one inner cycle to inner_rtol; max_outer caps the passes.  x (device) is
+ * overwritten (zero initial guess).  No counterpart in the reference. */
+typedef struct gp_mixed_s *gp_mixed;
+typedef struct {
+  int32_t restart;
+  int32_t max_outer;
+  int32_t tri_sweeps;
+  int32_t reserved;
+  double rtol;
+  double inner_rtol;
+} gp_mixed_options;
+typedef struct {
+  int32_t passes;      /* refinement passes (inner cycles) run */
+  int32_t inner_its;   /* FGMRES steps in total */
+  int32_t converged;   /* 1 when the true residual met rtol */
+  int32_t reserved;
+  double relres;       /* final ||b - A x|| / ||b|| (FP64) */
+} gp_mixed_result;
+void gp_mixed_options_default(gp_mixed_options *o);
+int gp_mixed_create(gp_mixed *out);
+int gp_mixed_destroy(gp_mixed m);
+int gp_mixed_solve(gp_mixed m, gp_mat A, gp_pc pc, const gp_mixed_options *o, const double *b,
+                   double *x, gp_mixed_result *result, void *stream);
+
 /* ------------------------------------------------------------ batched CG
  * Many independent SPD systems with nrhs right-hand sides each, solved
  * together: one block-diagonal CSR (system s owns rows sys_rows[s] ..

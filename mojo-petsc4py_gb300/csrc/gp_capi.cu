@@ -6,15 +6,7 @@
 #include "../../include/gpetsc.h"
 #include "gp_ksp.h"
 
-struct gp_mat_s {
-  gp::Csr* A;
-};
-struct gp_pc_s {
-  gp::Pc* pc;
-};
-struct gp_ksp_s {
-  gp::Ksp* k;
-};
+#include "gp_handles.h"
 
 
 

@@ -1,0 +1,571 @@
+// Mixed precision: FP32 inner FGMRES(m) with the ILU(0) factors in FP32, inside
+// FP64 iterative refinement.
+//
+//   repeat:  r = b - A x (FP64 SpMV),  stop when ||r|| <= rtol ||b||
+//            solve A d = r / ||r|| with one FGMRES(m) cycle in FP32
+//            x += ||r|| d (FP64)
+//
+// FP64 is kept for the outer residual, the convergence norms and GMRES's
+// Hessenberg / Givens least-squares (host side, per cycle); everything else --
+// matrix values, Krylov and preconditioned vectors, dot-product accumulation
+// inside a CTA -- is FP32 (cross-CTA sums in FP64).
+//
+// The preconditioner is the ILU(0) factor of the plain path (same symbolic and
+// numeric phase, values rounded to FP32).  Its triangular solves are applied
+// with `tri_sweeps` Jacobi iterations per triangle (y <- Pb - L_strict y;
+// x <- D^-1 (y - U_strict x)) instead of level-scheduled substitution: each
+// iteration is one fully parallel, bandwidth-bound pass, where the exact
+// substitution is a chain of dependency levels (hundreds on a 3-D grid) whose
+// cost is latency.  FGMRES tolerates the inexact, fixed-count application
+// (its basis stores the preconditioned vectors), and the FP64 refinement
+// makes the result independent of it.  tri_sweeps = 0 applies the factors
+// exactly with the level-scheduled FP64 sweeps instead.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/gpetsc.h"
+#include "gp_ksp.h"
+#include "gp_handles.h"
+#include "gp_spmv.cuh"
+
+namespace gp {
+
+constexpr int kMixBlock = 256;
+constexpr int kMixMaxM = 64;
+
+// ------------------------------------------------------------------ kernels
+static int mix_grid(int64_t n) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + kMixBlock - 1) / kMixBlock,
+                                                     (int64_t)num_sms() * 8));
+}
+
+// y = A x in FP32 (row per thread, matrix streamed with L2 evict-first)
+__global__ void __launch_bounds__(kMixBlock) k_spmv32(int n, const int* __restrict__ rp,
+                                                      const int* __restrict__ ci,
+                                                      const float* __restrict__ val,
+                                                      const float* __restrict__ x,
+                                                      float* __restrict__ y) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  const uint64_t pol = l2_evict_first();
+  const int b = rp[row], e = rp[row + 1];
+  float acc = 0.f;
+  for (int j0 = b; j0 < e; j0 += 8) {
+    int cc[8];
+    float vv[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      if (j0 + u < e) {
+        cc[u] = ld_stream(ci + j0 + u, pol);
+        vv[u] = ld_stream(val + j0 + u, pol);
+      }
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      if (j0 + u < e) acc = __fmaf_rn(vv[u], x[cc[u]], acc);
+  }
+  y[row] = acc;
+}
+
+// One Jacobi pass of a triangular solve with a strict triangle T (CSR):
+//   out_i = s_i (rhs_i - sum_j T_ij in_j),  s = dinv (or 1 when dinv is null)
+__global__ void __launch_bounds__(kMixBlock) k_tri_pass(int n, const int* __restrict__ rp,
+                                                        const int* __restrict__ ci,
+                                                        const float* __restrict__ val,
+                                                        const float* __restrict__ dinv,
+                                                        const float* __restrict__ rhs,
+                                                        const float* __restrict__ in,
+                                                        float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float acc = rhs[i];
+  for (int j = rp[i]; j < rp[i + 1]; j++) acc = __fmaf_rn(-val[j], in[ci[j]], acc);
+  out[i] = dinv ? acc * dinv[i] : acc;
+}
+
+__global__ void k_gather32(int n, const int* __restrict__ idx, const float* __restrict__ in,
+                           float* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = in[idx[i]];
+}
+
+__global__ void k_scatter32(int n, const int* __restrict__ idx, const float* __restrict__ in,
+                            float* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[idx[i]] = in[i];
+}
+
+__global__ void k_mul32(int n, const float* __restrict__ a, const float* __restrict__ b,
+                        float* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = a[i] * b[i];
+}
+
+// values of a factor triangle, FP64 factor slots -> FP32 CSR
+__global__ void k_slot_gather(int64_t m, const int* __restrict__ slot,
+                              const double* __restrict__ ba, float* __restrict__ out) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m;
+       k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = __double2float_rn(ba[slot[k]]);
+}
+
+// Dots of w against basis rows 0..k-1 (rows of V, leading dimension n), or
+// ||w||^2 when V is null: FP32 per thread and per CTA, per-CTA partials in
+// FP64; the last CTA folds them (FP64) into out[0..k-1].
+__global__ void __launch_bounds__(kMixBlock) k_mdot32(int n, const float* __restrict__ V,
+                                                      int k, const float* __restrict__ w,
+                                                      double* __restrict__ partials,
+                                                      unsigned* ticket, double* out) {
+  __shared__ float sh[kMixBlock / 32][kMixMaxM + 1];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int kk = V ? k : 1;
+  for (int j0 = 0; j0 < kk; j0 += 8) {
+    float acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) acc[q] = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      const float wi = w[i];
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if (j0 + q < kk) acc[q] = __fmaf_rn(V ? V[(size_t)(j0 + q) * n + i] : wi, wi, acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+      if (lane == 0 && j0 + q < kk) sh[wid][j0 + q] = acc[q];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < kk; j++) {
+      float t = 0.f;
+      for (int ww = 0; ww < (int)(blockDim.x >> 5); ww++) t += sh[ww][j];
+      partials[(size_t)j * gridDim.x + blockIdx.x] = (double)t;
+    }
+    last = atomic_add_acq_rel(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  for (int j = threadIdx.x; j < kk; j += blockDim.x) {
+    double t = 0.0;
+    for (int bb = 0; bb < (int)gridDim.x; bb++) t += __ldcg(&partials[(size_t)j * gridDim.x + bb]);
+    out[j] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *ticket = 0u;
+}
+
+// w -= sum_{j<k} h_j V_j   (h in FP64 on the device, applied in FP32)
+__global__ void k_maxpy32(int n, const float* __restrict__ V, int k, const double* __restrict__ h,
+                          float* __restrict__ w) {
+  __shared__ float hs[kMixMaxM + 1];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = (float)h[j];
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float v = w[i];
+    for (int j = 0; j < k; j++) v = __fmaf_rn(-hs[j], V[(size_t)j * n + i], v);
+    w[i] = v;
+  }
+}
+
+// out = sum_{j<k} c_j Z_j   (c in FP64 on the device)
+__global__ void k_lincomb32(int n, const float* __restrict__ Z, int k, const double* __restrict__ c,
+                            float* __restrict__ out) {
+  __shared__ float cs[kMixMaxM + 1];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) cs[j] = (float)c[j];
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float v = 0.f;
+    for (int j = 0; j < k; j++) v = __fmaf_rn(cs[j], Z[(size_t)j * n + i], v);
+    out[i] = v;
+  }
+}
+
+__global__ void k_scale32(int n, const float* in, float s, float* out) {  // in may be out
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = in[i] * s;
+}
+
+// r = b - y (FP64) and r32 = r * inv (FP32)
+__global__ void k_resid_parts(int n, const double* __restrict__ b, const double* __restrict__ y,
+                              double* __restrict__ r) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    r[i] = b[i] - y[i];
+}
+
+__global__ void k_to32_scaled(int n, const double* __restrict__ r, double inv,
+                              float* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = __double2float_rn(r[i] * inv);
+}
+
+// x += a d  (FP64 accumulate of the FP32 correction)
+__global__ void k_axpy64_32(int n, double a, const float* __restrict__ d, double* __restrict__ x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    x[i] = fma(a, (double)d[i], x[i]);
+}
+
+// ---------------------------------------------------------------- host side
+struct MixedOptions {
+  int restart = 30;
+  int max_outer = 200;      // FGMRES cycles (one per refinement pass)
+  int tri_sweeps = 4;       // Jacobi passes per triangle; 0 = exact FP64 sweeps
+  double rtol = 1e-10;      // on the true FP64 residual, relative to ||b||
+  double inner_rtol = 1e-4; // per cycle, relative to the cycle's start
+};
+
+struct MixedResult {
+  int passes = 0, inner_its = 0, converged = 0;
+  double relres = 0.0;
+};
+
+struct Mixed {
+  int n = 0, m = 0, device = -1;
+  const Csr* A = nullptr;
+  const Pc* pc = nullptr;
+  int pc_generation = -1, pc_epoch = -1;
+  // FP32 factor triangles (CSR) and permutations
+  int *lrp = nullptr, *lci = nullptr, *lslot = nullptr;
+  int *urp = nullptr, *uci = nullptr, *uslot = nullptr, *dslot = nullptr;
+  float *lval = nullptr, *uval = nullptr, *udinv = nullptr;
+  int64_t lnnz = 0, unnz = 0;
+  // work
+  float *V = nullptr, *Z = nullptr, *w = nullptr, *t0 = nullptr, *t1 = nullptr, *t2 = nullptr;
+  float *t3 = nullptr, *t4 = nullptr;
+  double *r = nullptr, *y = nullptr, *d64 = nullptr, *h_dev = nullptr, *partials = nullptr;
+  double* x64tmp = nullptr;
+  unsigned* ticket = nullptr;
+  double* h_pinned = nullptr;
+};
+
+static void mixed_free(Mixed* M) {
+  void* ptrs[] = {M->lrp, M->lci, M->lslot, M->urp, M->uci, M->uslot, M->dslot, M->lval,
+                  M->uval, M->udinv, M->V, M->Z, M->w, M->t0, M->t1, M->t2, M->t3, M->t4,
+                  M->r, M->y,
+                  M->d64, M->h_dev, M->partials, M->x64tmp, M->ticket};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (M->h_pinned) cudaFreeHost(M->h_pinned);
+  *M = Mixed();
+}
+
+template <typename V>
+static int up_mixed(V** d, const std::vector<V>& h) {
+  GP_CUDA(cudaMalloc(d, std::max<size_t>(h.size(), 1) * sizeof(V)));
+  if (!h.empty()) GP_CUDA(cudaMemcpy(*d, h.data(), h.size() * sizeof(V), cudaMemcpyHostToDevice));
+  return GP_OK;
+}
+
+// (Re)build the FP32 factor triangles from the PC's factor.
+static int mixed_factors(Mixed* M, cudaStream_t s) {
+  const Pc* pc = M->pc;
+  const FactorPattern& P = pc->pat;
+  const int n = M->n;
+  if (M->pc_generation != pc->generation) {
+    for (void** p : {(void**)&M->lrp, (void**)&M->lci, (void**)&M->lslot, (void**)&M->urp,
+                     (void**)&M->uci, (void**)&M->uslot, (void**)&M->dslot, (void**)&M->lval,
+                     (void**)&M->uval, (void**)&M->udinv})
+      if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+      }
+    std::vector<int> lrp(n + 1, 0), lci, lsl, urp(n + 1, 0), uci, usl, dsl(n);
+    for (int i = 0; i < n; i++) {
+      for (int j = P.bi[i]; j < P.bi[i + 1]; j++) {
+        lci.push_back(P.bj[j]);
+        lsl.push_back(j);
+      }
+      lrp[i + 1] = (int)lci.size();
+      for (int j = P.bdiag[i + 1] + 1; j < P.bdiag[i]; j++) {
+        uci.push_back(P.bj[j]);
+        usl.push_back(j);
+      }
+      urp[i + 1] = (int)uci.size();
+      dsl[i] = P.bdiag[i];
+    }
+    M->lnnz = (int64_t)lci.size();
+    M->unnz = (int64_t)uci.size();
+    GP_TRY(up_mixed(&M->lrp, lrp));
+    GP_TRY(up_mixed(&M->lci, lci));
+    GP_TRY(up_mixed(&M->lslot, lsl));
+    GP_TRY(up_mixed(&M->urp, urp));
+    GP_TRY(up_mixed(&M->uci, uci));
+    GP_TRY(up_mixed(&M->uslot, usl));
+    GP_TRY(up_mixed(&M->dslot, dsl));
+    GP_CUDA(cudaMalloc(&M->lval, std::max<int64_t>(M->lnnz, 1) * sizeof(float)));
+    GP_CUDA(cudaMalloc(&M->uval, std::max<int64_t>(M->unnz, 1) * sizeof(float)));
+    GP_CUDA(cudaMalloc(&M->udinv, std::max(n, 1) * sizeof(float)));
+    M->pc_generation = pc->generation;
+    M->pc_epoch = -1;
+  }
+  if (M->pc_epoch != pc->epoch) {
+    const int g = num_sms() * 8;
+    if (M->lnnz) k_slot_gather<<<g, 256, 0, s>>>(M->lnnz, M->lslot, pc->ba, M->lval);
+    if (M->unnz) k_slot_gather<<<g, 256, 0, s>>>(M->unnz, M->uslot, pc->ba, M->uval);
+    k_slot_gather<<<g, 256, 0, s>>>(n, M->dslot, pc->ba, M->udinv);
+    GP_CHECK_LAUNCH();
+    M->pc_epoch = pc->epoch;
+  }
+  return GP_OK;
+}
+
+static int mixed_buffers(Mixed* M, int n, int m) {
+  if (M->n == n && M->m == m && M->V) return GP_OK;
+  for (void** p : {(void**)&M->V, (void**)&M->Z, (void**)&M->w, (void**)&M->t0, (void**)&M->t1,
+                   (void**)&M->t2, (void**)&M->t3, (void**)&M->t4, (void**)&M->r, (void**)&M->y,
+                   (void**)&M->h_dev, (void**)&M->partials, (void**)&M->ticket})
+    if (*p) {
+      cudaFree(*p);
+      *p = nullptr;
+    }
+  if (M->h_pinned) cudaFreeHost(M->h_pinned);
+  M->h_pinned = nullptr;
+  const size_t nn = std::max(n, 1);
+  GP_CUDA(cudaMalloc(&M->V, (size_t)(m + 1) * nn * sizeof(float)));
+  GP_CUDA(cudaMalloc(&M->Z, (size_t)m * nn * sizeof(float)));
+  for (float** p : {&M->w, &M->t0, &M->t1, &M->t2, &M->t3, &M->t4})
+    GP_CUDA(cudaMalloc(p, nn * sizeof(float)));
+  GP_CUDA(cudaMalloc(&M->r, nn * sizeof(double)));
+  GP_CUDA(cudaMalloc(&M->y, nn * sizeof(double)));
+  GP_CUDA(cudaMalloc(&M->h_dev, (m + 2) * sizeof(double)));
+  GP_CUDA(cudaMalloc(&M->partials, (size_t)(m + 2) * mix_grid(n) * sizeof(double)));
+  GP_CUDA(cudaMalloc(&M->ticket, sizeof(unsigned)));
+  GP_CUDA(cudaMemset(M->ticket, 0, sizeof(unsigned)));
+  GP_CUDA(cudaMallocHost(&M->h_pinned, (m + 2) * sizeof(double)));
+  M->n = n;
+  M->m = m;
+  return GP_OK;
+}
+
+// k dots of w against V's first k rows (or ||w||^2 with V null) into host h
+static int mdot_host(Mixed* M, const float* V, int k, const float* w, double* h, cudaStream_t s) {
+  const int n = M->n, g = mix_grid(n);
+  k_mdot32<<<g, kMixBlock, 0, s>>>(n, V, k, w, M->partials, M->ticket, M->h_dev);
+  GP_CHECK_LAUNCH();
+  const int kk = V ? k : 1;
+  GP_CUDA(cudaMemcpyAsync(M->h_pinned, M->h_dev, kk * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GP_CUDA(cudaStreamSynchronize(s));
+  std::memcpy(h, M->h_pinned, kk * sizeof(double));
+  return GP_OK;
+}
+
+// z = M^-1 v with the FP32 factors (tri_sweeps Jacobi passes per triangle), or
+// with the exact FP64 sweeps of the plain path when tri_sweeps == 0.
+static int mixed_pc(Mixed* M, int tri_sweeps, const float* v, float* z, cudaStream_t s) {
+  const int n = M->n;
+  const int g = mix_grid(n), gr = (n + kMixBlock - 1) / kMixBlock;
+  if (tri_sweeps <= 0) {
+    // exact: through the FP64 level-scheduled sweeps
+    GP_CUDA(cudaMemsetAsync(M->y, 0, n * sizeof(double), s));
+    k_axpy64_32<<<g, kMixBlock, 0, s>>>(n, 1.0, v, M->y);
+    GP_TRY(pc_apply(const_cast<Pc*>(M->pc), DRef::of(M->y), DRef::of(M->r), s));
+    k_to32_scaled<<<g, kMixBlock, 0, s>>>(n, M->r, 1.0, z);
+    GP_CHECK_LAUNCH();
+    return GP_OK;
+  }
+  const Pc* pc = M->pc;
+  float* bp = M->t0;
+  k_gather32<<<g, kMixBlock, 0, s>>>(n, pc->perm_r, v, bp);
+  // forward, unit lower: y <- bp - L y, from y = bp
+  float* ya = M->t1;
+  float* yb = M->t2;
+  const float* yin = bp;
+  for (int k = 0; k < tri_sweeps; k++) {
+    k_tri_pass<<<gr, kMixBlock, 0, s>>>(n, M->lrp, M->lci, M->lval, nullptr, bp, yin, ya);
+    yin = ya;
+    std::swap(ya, yb);
+  }
+  // backward: x <- D^-1 (y - U x), from x = D^-1 y
+  float* xa = M->t3;
+  float* xb = M->t4;
+  k_mul32<<<g, kMixBlock, 0, s>>>(n, M->udinv, yin, xa);
+  const float* xin = xa;
+  std::swap(xa, xb);
+  for (int k = 0; k < tri_sweeps; k++) {
+    k_tri_pass<<<gr, kMixBlock, 0, s>>>(n, M->urp, M->uci, M->uval, M->udinv, yin, xin, xa);
+    xin = xa;
+    std::swap(xa, xb);
+  }
+  k_scatter32<<<g, kMixBlock, 0, s>>>(n, pc->perm_c, xin, z);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+int mixed_solve(Mixed* M, Csr* A, Pc* pc, const double* b, double* x, const MixedOptions& o,
+                MixedResult& res, cudaStream_t s) {
+  if (pc->opt.type != PC_ILU || !pc->ready || pc->n != A->n) {
+    set_error("mixed solve: needs an ILU preconditioner set up on the operator");
+    return GP_ERR_NOT_SETUP;
+  }
+  if (o.restart < 1 || o.restart > kMixMaxM || o.max_outer < 1 || o.tri_sweeps < 0) {
+    set_error("mixed solve: restart must be 1..64, max_outer >= 1, tri_sweeps >= 0");
+    return GP_ERR_ARG;
+  }
+  const int n = A->n, m = o.restart;
+  M->A = A;
+  M->pc = pc;
+  res = MixedResult();
+  if (n == 0) {
+    res.converged = 1;
+    return GP_OK;
+  }
+  GP_TRY(mixed_buffers(M, n, m));
+  GP_TRY(csr_make_val32(A, s));
+  GP_TRY(mixed_factors(M, s));
+  const int g = mix_grid(n), gr = (n + kMixBlock - 1) / kMixBlock;
+  double bb = 0.0;
+  GP_TRY(vec_reduce(s, RED_NORM2SQ, n, b, nullptr, &bb));
+  const double bnorm = std::sqrt(bb);
+  GP_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+  std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), gv(m + 1), h(m + 1), yv(m);
+  for (int pass = 0;; pass++) {
+    // FP64 residual
+    GP_TRY(spmv(s, A, DRef::of(x), DRef::of(M->y)));
+    k_resid_parts<<<g, kMixBlock, 0, s>>>(n, b, M->y, M->r);
+    double rr = 0.0;
+    GP_TRY(vec_reduce(s, RED_NORM2SQ, n, M->r, nullptr, &rr));
+    const double rn = std::sqrt(rr);
+    res.relres = bnorm > 0.0 ? rn / bnorm : rn;
+    if (!(rn > o.rtol * bnorm)) {
+      res.converged = 1;
+      break;
+    }
+    if (pass >= o.max_outer || !std::isfinite(rn)) break;
+    res.passes = pass + 1;
+    // one FP32 FGMRES(m) cycle on A d = r / ||r||
+    k_to32_scaled<<<g, kMixBlock, 0, s>>>(n, M->r, 1.0 / rn, M->V);
+    double beta2 = 0.0;
+    GP_TRY(mdot_host(M, nullptr, 1, M->V, &beta2, s));
+    const double beta = std::sqrt(beta2);
+    if (!(beta > 0.0)) break;
+    k_scale32<<<g, kMixBlock, 0, s>>>(n, M->V, (float)(1.0 / beta), M->V);
+    std::fill(gv.begin(), gv.end(), 0.0);
+    gv[0] = beta;
+    int kdim = 0;
+    for (int j = 0; j < m; j++) {
+      float* vj = M->V + (size_t)j * n;
+      float* zj = M->Z + (size_t)j * n;
+      GP_TRY(mixed_pc(M, o.tri_sweeps, vj, zj, s));
+      k_spmv32<<<gr, kMixBlock, 0, s>>>(n, A->rowptr, A->colind, A->val32, zj, M->w);
+      // classical Gram-Schmidt against v_0..v_j
+      GP_TRY(mdot_host(M, M->V, j + 1, M->w, h.data(), s));
+      k_maxpy32<<<g, kMixBlock, 0, s>>>(n, M->V, j + 1, M->h_dev, M->w);
+      double hn2 = 0.0;
+      GP_TRY(mdot_host(M, nullptr, 1, M->w, &hn2, s));
+      const double hn = std::sqrt(hn2);
+      res.inner_its += 1;
+      // Hessenberg column j, previous rotations, new rotation (FP64, host)
+      for (int i = 0; i <= j; i++) H[(size_t)i * m + j] = h[i];
+      for (int i = 0; i < j; i++) {
+        const double a = H[(size_t)i * m + j], c = H[(size_t)(i + 1) * m + j];
+        H[(size_t)i * m + j] = cs[i] * a + sn[i] * c;
+        H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * c;
+      }
+      const double hjj = H[(size_t)j * m + j];
+      const double den = std::hypot(hjj, hn);
+      cs[j] = den > 0.0 ? hjj / den : 1.0;
+      sn[j] = den > 0.0 ? hn / den : 0.0;
+      H[(size_t)j * m + j] = den;
+      gv[j + 1] = -sn[j] * gv[j];
+      gv[j] = cs[j] * gv[j];
+      kdim = j + 1;
+      if (!(hn > 0.0) || std::fabs(gv[j + 1]) <= o.inner_rtol * beta) break;
+      if (j + 1 < m)
+        k_scale32<<<g, kMixBlock, 0, s>>>(n, M->w, (float)(1.0 / hn), M->V + (size_t)(j + 1) * n);
+    }
+    // y = H^-1 g (upper triangular), d = Z y, x += ||r|| d
+    for (int i = kdim - 1; i >= 0; i--) {
+      double t = gv[i];
+      for (int k = i + 1; k < kdim; k++) t -= H[(size_t)i * m + k] * yv[k];
+      yv[i] = H[(size_t)i * m + i] != 0.0 ? t / H[(size_t)i * m + i] : 0.0;
+    }
+    std::memcpy(M->h_pinned, yv.data(), kdim * sizeof(double));
+    GP_CUDA(cudaMemcpyAsync(M->h_dev, M->h_pinned, kdim * sizeof(double), cudaMemcpyHostToDevice,
+                            s));
+    k_lincomb32<<<g, kMixBlock, 0, s>>>(n, M->Z, kdim, M->h_dev, M->w);
+    k_axpy64_32<<<g, kMixBlock, 0, s>>>(n, rn, M->w, x);
+    GP_CHECK_LAUNCH();
+  }
+  GP_CUDA(cudaStreamSynchronize(s));
+  return GP_OK;
+}
+
+Mixed* mixed_create() { return new Mixed(); }
+void mixed_destroy(Mixed* M) {
+  if (!M) return;
+  mixed_free(M);
+  delete M;
+}
+
+}  // namespace gp
+
+// ------------------------------------------------------------------- C ABI
+struct gp_mixed_s {
+  gp::Mixed* M;
+};
+
+extern "C" {
+
+void gp_mixed_options_default(gp_mixed_options* o) {
+  gp::MixedOptions d;
+  std::memset(o, 0, sizeof(*o));
+  o->restart = d.restart;
+  o->max_outer = d.max_outer;
+  o->tri_sweeps = d.tri_sweeps;
+  o->rtol = d.rtol;
+  o->inner_rtol = d.inner_rtol;
+}
+
+int gp_mixed_create(gp_mixed* out) {
+  if (!out) {
+    gp::set_error("gp_mixed_create: null argument");
+    return GP_ERR_ARG;
+  }
+  *out = new gp_mixed_s{gp::mixed_create()};
+  return GP_OK;
+}
+
+int gp_mixed_destroy(gp_mixed m) {
+  if (!m) return GP_OK;
+  gp::mixed_destroy(m->M);
+  delete m;
+  return GP_OK;
+}
+
+int gp_mixed_solve(gp_mixed m, gp_mat A, gp_pc pc, const gp_mixed_options* o, const double* b,
+                   double* x, gp_mixed_result* result, void* stream) {
+  if (!m || !A || !pc || !o || (A->A->n && (!b || !x))) {
+    gp::set_error("gp_mixed_solve: null argument");
+    return GP_ERR_ARG;
+  }
+  if (b == x) {
+    gp::set_error("gp_mixed_solve: x may not alias b");
+    return GP_ERR_ARG;
+  }
+  try {
+    gp::MixedOptions mo;
+    mo.restart = o->restart;
+    mo.max_outer = o->max_outer;
+    mo.tri_sweeps = o->tri_sweeps;
+    mo.rtol = o->rtol;
+    mo.inner_rtol = o->inner_rtol;
+    gp::MixedResult r;
+    int st = gp::mixed_solve(m->M, A->A, pc->pc, b, x, mo, r, static_cast<cudaStream_t>(stream));
+    if (st) return st;
+    if (result) {
+      result->passes = r.passes;
+      result->inner_its = r.inner_its;
+      result->converged = r.converged;
+      result->relres = r.relres;
+    }
+    return GP_OK;
+  } catch (const std::exception& e) {
+    gp::set_error(std::string("gp_mixed_solve: ") + e.what());
+    return GP_ERR_INTERNAL;
+  }
+}
+
+}  // extern "C"

@@ -68,6 +68,10 @@ GP_SIGNATURES = {
     "gp_get_arithmetic": ([], ctypes.c_int),
     "gp_device_count": ([ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     "gp_set_device": ([ctypes.c_int], ctypes.c_int),
+    "gp_mixed_options_default": ([P], None),
+    "gp_mixed_create": ([PP], ctypes.c_int),
+    "gp_mixed_destroy": ([P], ctypes.c_int),
+    "gp_mixed_solve": ([P, P, P, P, P, P, P, P], ctypes.c_int),
     "gp_batch_create": ([PP, I64, P, P, P, P, ctypes.c_int32, P], ctypes.c_int),
     "gp_batch_destroy": ([P], ctypes.c_int),
     "gp_batch_options_default": ([P], None),
