@@ -13,6 +13,7 @@
 // reference's slot order with rounded multiplies and adds, so the result is
 // bit-identical to the sequential loop.
 #include <algorithm>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -24,11 +25,12 @@ constexpr int kEllBlock = 256;
 constexpr int kEllSpin = 1 << 22;
 
 __device__ __forceinline__ double ell_wait(const double* p, DevErr* err, int where,
-                                           int budget = kEllSpin) {
+                                           int budget = kEllSpin, int sleep_after = 64,
+                                           int sleep_ns = 20) {
   unsigned long long b = ld_relaxed_bits(p);
   if (b != kPending) return __longlong_as_double((long long)b);
   for (int spins = 0; spins < budget; spins++) {
-    if (spins > 64) __nanosleep(20);
+    if (spins >= sleep_after && sleep_ns > 0) __nanosleep(sleep_ns);
     b = ld_relaxed_bits(p);
     if (b != kPending) return __longlong_as_double((long long)b);
   }
@@ -55,7 +57,28 @@ struct EllArgs {
   int use_t;           // SOR_B
   unsigned* tickets;
   DevErr* err;
+  int sleep_after, sleep_ns;  // polling back-off of the waits
 };
+
+// Launch shape and polling back-off of the sweeps (GPETSC_SWEEP_CTAS_PER_SM,
+// GPETSC_SWEEP_SLEEP_AFTER, GPETSC_SWEEP_SLEEP_NS override the defaults).
+struct SweepTuning {
+  int ctas_per_sm = 2, sleep_after = 8, sleep_ns = 20;  // best of a scan on ICC(0), 128^3
+};
+static const SweepTuning& sweep_tuning() {
+  static SweepTuning t = [] {
+    SweepTuning v;
+    auto env = [](const char* k, int d) {
+      const char* e = std::getenv(k);
+      return e ? std::atoi(e) : d;
+    };
+    v.ctas_per_sm = std::max(1, std::min(8, env("GPETSC_SWEEP_CTAS_PER_SM", v.ctas_per_sm)));
+    v.sleep_after = std::max(0, env("GPETSC_SWEEP_SLEEP_AFTER", v.sleep_after));
+    v.sleep_ns = std::max(0, std::min(1000, env("GPETSC_SWEEP_SLEEP_NS", v.sleep_ns)));
+    return v;
+  }();
+  return t;
+}
 
 template <int MODE, int WMAX>
 __global__ void __launch_bounds__(kEllBlock) k_ell_sweep(const int* gate, int want, EllArgs a,
@@ -106,7 +129,8 @@ __global__ void __launch_bounds__(kEllBlock) k_ell_sweep(const int* gate, int wa
 #pragma unroll
       for (int e = 0; e < WMAX; e++) {
         if (e < c) {
-          const double v = ell_wait(&a.val[dp[e]], a.err, 20 + MODE);
+          const double v =
+              ell_wait(&a.val[dp[e]], a.err, 20 + MODE, kEllSpin, a.sleep_after, a.sleep_ns);
           if constexpr (MODE == ELL_ICC_F || MODE == ELL_ICC_B)
             sum = add(sum, mul(cf[e], v));
           else
@@ -276,7 +300,7 @@ int ell_refresh(EllSweep& e, const double* src, cudaStream_t s) {
 template <int MODE>
 static void launch_mode(const EllSweep& e, const int* gate, int want, EllArgs a, DRef in,
                         DRef out, cudaStream_t s) {
-  const int g = num_sms() * 4;
+  const int g = num_sms() * sweep_tuning().ctas_per_sm;
   if (e.W <= 4)
     k_ell_sweep<MODE, 4><<<g, kEllBlock, 0, s>>>(gate, want, a, in, out);
   else if (e.W <= 8)
@@ -307,6 +331,8 @@ int ell_sweep(int mode, const EllSweep& e, const int* gate, int want, DRef in, D
   a.use_t = use_t;
   a.tickets = tickets;
   a.err = err;
+  a.sleep_after = sweep_tuning().sleep_after;
+  a.sleep_ns = sweep_tuning().sleep_ns;
   switch (mode) {
     case ELL_ILU_F: launch_mode<ELL_ILU_F>(e, gate, want, a, in, out, s); break;
     case ELL_ILU_B: launch_mode<ELL_ILU_B>(e, gate, want, a, in, out, s); break;
