@@ -286,11 +286,19 @@ __global__ void __launch_bounds__(kRedBlock) k_mdot(const int* gate, int want, i
   if (threadIdx.x == 0) last = atomic_add_acq_rel(slot.ticket, 1u) == gridDim.x - 1;
   __syncthreads();
   if (!last) return;
-  if (threadIdx.x < k) {
-    double t = 0.0;
-    for (int b = 0; b < (int)gridDim.x; b++)
-      t = add(t, __ldcg(&slot.partials[(size_t)threadIdx.x * slot.stride + b]));
-    out[threadIdx.x] = t;
+  // warp w folds dots w, w + nwarps, ...: lanes take blocks lane, lane + 32,
+  // ... in order (many loads in flight), then a shuffle tree -- a fixed order
+  // without a serial chain over every block
+  {
+    const int nw = blockDim.x >> 5;
+    for (int j = wid; j < k; j += nw) {
+      double t = 0.0;
+      for (int b = lane; b < (int)gridDim.x; b += 32)
+        t = add(t, __ldcg(&slot.partials[(size_t)j * slot.stride + b]));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t = add(t, __shfl_down_sync(0xffffffffu, t, o));
+      if (lane == 0) out[j] = t;
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0) *slot.ticket = 0u;

@@ -21,6 +21,8 @@
 // makes the result independent of it.  tri_sweeps = 0 applies the factors
 // exactly with the level-scheduled FP64 sweeps instead.
 #include <algorithm>
+#include <cstddef>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -36,6 +38,11 @@ constexpr int kMixBlock = 256;
 constexpr int kMixMaxM = 64;
 
 // ------------------------------------------------------------------ kernels
+// CTAs of the multi-dot kernels: two per SM keeps the last CTA's fold short
+static int mdot_grid(int64_t n) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 2));
+}
+
 static int mix_grid(int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>((n + kMixBlock - 1) / kMixBlock,
                                                      (int64_t)num_sms() * 8));
@@ -110,6 +117,21 @@ __global__ void k_slot_gather(int64_t m, const int* __restrict__ slot,
     out[k] = __double2float_rn(ba[slot[k]]);
 }
 
+// out[j] = sum over the grid's per-CTA partials of value j (j < kk), in the
+// last CTA: warp w folds values w, w + nwarps, ...; its lanes take CTAs
+// lane, lane + 32, ... (many loads in flight) and a shuffle tree combines them.
+__device__ __forceinline__ void fold_partials(const double* partials, int kk, double* out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = wid; j < kk; j += nw) {
+    double t = 0.0;
+    for (int bb = lane; bb < (int)gridDim.x; bb += 32)
+      t += __ldcg(&partials[(size_t)j * gridDim.x + bb]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) out[j] = t;
+  }
+}
+
 // Dots of w against basis rows 0..k-1 (rows of V, leading dimension n), or
 // ||w||^2 when V is null: FP32 per thread and per CTA, per-CTA partials in
 // FP64; the last CTA folds them (FP64) into out[0..k-1].
@@ -149,11 +171,7 @@ __global__ void __launch_bounds__(kMixBlock) k_mdot32(int n, const float* __rest
   }
   __syncthreads();
   if (!last) return;
-  for (int j = threadIdx.x; j < kk; j += blockDim.x) {
-    double t = 0.0;
-    for (int bb = 0; bb < (int)gridDim.x; bb++) t += __ldcg(&partials[(size_t)j * gridDim.x + bb]);
-    out[j] = t;
-  }
+  fold_partials(partials, kk, out);
   __syncthreads();
   if (threadIdx.x == 0) *ticket = 0u;
 }
@@ -239,6 +257,16 @@ struct Mixed {
   double* x64tmp = nullptr;
   unsigned* ticket = nullptr;
   double* h_pinned = nullptr;
+  // the captured refinement pass
+  struct MixDev* st = nullptr;       // device state
+  struct MixDev* h_st = nullptr;     // pinned host copy of its head
+  double* part64 = nullptr;
+  unsigned* ticket64 = nullptr;
+  cudaStream_t cap_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const void* cap_key[6] = {};
+  int cap_ikey[4] = {};
 };
 
 static void mixed_free(Mixed* M) {
@@ -249,6 +277,13 @@ static void mixed_free(Mixed* M) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (M->h_pinned) cudaFreeHost(M->h_pinned);
+  if (M->st) cudaFree(M->st);
+  if (M->h_st) cudaFreeHost(M->h_st);
+  if (M->part64) cudaFree(M->part64);
+  if (M->ticket64) cudaFree(M->ticket64);
+  if (M->exec) cudaGraphExecDestroy(M->exec);
+  if (M->graph) cudaGraphDestroy(M->graph);
+  if (M->cap_stream) cudaStreamDestroy(M->cap_stream);
   *M = Mixed();
 }
 
@@ -343,7 +378,7 @@ static int mixed_buffers(Mixed* M, int n, int m) {
 // k dots of w against V's first k rows (or ||w||^2 with V null) into host h
 static int mdot_host(Mixed* M, const float* V, int k, const float* w, double* h, cudaStream_t s) {
   const int n = M->n, g = mix_grid(n);
-  k_mdot32<<<g, kMixBlock, 0, s>>>(n, V, k, w, M->partials, M->ticket, M->h_dev);
+  k_mdot32<<<mdot_grid(n), kMixBlock, 0, s>>>(n, V, k, w, M->partials, M->ticket, M->h_dev);
   GP_CHECK_LAUNCH();
   const int kk = V ? k : 1;
   GP_CUDA(cudaMemcpyAsync(M->h_pinned, M->h_dev, kk * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -394,6 +429,18 @@ static int mixed_pc(Mixed* M, int tri_sweeps, const float* v, float* z, cudaStre
   return GP_OK;
 }
 
+int mixed_solve_graph(Mixed* M, Csr* A, Pc* pc, const double* b, double* x,
+                      const MixedOptions& o, MixedResult& res, cudaStream_t caller);
+
+// GPETSC_KSP_GRAPH=0: the host-driven form (one sync per reduction)
+static bool mixed_host_mode() {
+  static bool v = [] {
+    const char* e = std::getenv("GPETSC_KSP_GRAPH");
+    return e && std::string(e) == "0";
+  }();
+  return v;
+}
+
 int mixed_solve(Mixed* M, Csr* A, Pc* pc, const double* b, double* x, const MixedOptions& o,
                 MixedResult& res, cudaStream_t s) {
   if (pc->opt.type != PC_ILU || !pc->ready || pc->n != A->n) {
@@ -413,6 +460,7 @@ int mixed_solve(Mixed* M, Csr* A, Pc* pc, const double* b, double* x, const Mixe
     return GP_OK;
   }
   GP_TRY(mixed_buffers(M, n, m));
+  if (!mixed_host_mode()) return mixed_solve_graph(M, A, pc, b, x, o, res, s);
   GP_TRY(csr_make_val32(A, s));
   GP_TRY(mixed_factors(M, s));
   const int g = mix_grid(n), gr = (n + kMixBlock - 1) / kMixBlock;
@@ -490,6 +538,375 @@ int mixed_solve(Mixed* M, Csr* A, Pc* pc, const double* b, double* x, const Mixe
     GP_CHECK_LAUNCH();
   }
   GP_CUDA(cudaStreamSynchronize(s));
+  return GP_OK;
+}
+
+// ---------------------------------------------------- captured refinement pass
+// One refinement pass as one CUDA graph: FP64 residual and its norm, then an
+// FP32 FGMRES(m) cycle with every scalar on the device (Hessenberg column,
+// Givens rotations, least-squares in FP64 by one thread), each step gated on
+// `active` so the steps after the cycle converged are no-ops, then the
+// correction.  The host launches passes and reads one status word per pass.
+struct MixDev {
+  int pass_on, active, kdim, its, passes, pad_;
+  double rn, rtol_bnorm, beta2, beta, tol, inner_rtol, hn2;
+  double H[(kMixMaxM + 1) * kMixMaxM];
+  double cs[kMixMaxM], sn[kMixMaxM], g[kMixMaxM + 1], y[kMixMaxM];
+};
+
+__global__ void __launch_bounds__(kRedBlock) k_mx_resid(int n, const double* __restrict__ b,
+                                                        const double* __restrict__ y,
+                                                        double* __restrict__ r, RedSlot slot,
+                                                        MixDev* st) {
+  double v[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double ri = b[i] - y[i];
+    r[i] = ri;
+    v[0] = fma(ri, ri, v[0]);
+  }
+  double tot[1];
+  if (grid_finish<1>(v, slot, tot) && threadIdx.x == 0) {
+    const double rn = sqrt(tot[0]);
+    st->rn = rn;
+    const int on = (rn > st->rtol_bnorm) && isfinite(rn);
+    st->pass_on = on;
+    st->active = on;
+    st->kdim = 0;
+    if (on) st->passes += 1;
+  }
+}
+
+__global__ void k_mx_v0(int n, const double* __restrict__ r, const MixDev* st,
+                        float* __restrict__ v0) {
+  if (!st->pass_on) return;
+  const double inv = 1.0 / st->rn;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    v0[i] = __double2float_rn(r[i] * inv);
+}
+
+__global__ void k_mx_beta(MixDev* st, int m) {
+  if (!st->pass_on) return;
+  const double beta = sqrt(st->beta2);
+  st->beta = beta;
+  for (int i = 0; i <= m; i++) st->g[i] = 0.0;
+  st->g[0] = beta;
+  st->tol = st->inner_rtol * beta;
+  if (!(beta > 0.0)) st->active = 0;
+}
+
+// out = in / beta (which = 0) or in / sqrt(hn2) (which = 1), while active
+__global__ void k_mx_scale(int n, const float* in, float* out, const MixDev* st, int which) {
+  if (!st->active) return;
+  const float s = (float)(1.0 / (which == 0 ? st->beta : sqrt(st->hn2)));
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = in[i] * s;
+}
+
+// One Jacobi pass of a factor triangle, gated; rhs and in may be read through
+// a permutation, `in` scaled by in_scale, the output scattered through a
+// permutation (first / last passes of the permuted factor solve).
+__global__ void __launch_bounds__(kMixBlock) k_mx_tri(
+    const int* gate, int n, const int* __restrict__ rp, const int* __restrict__ ci,
+    const float* __restrict__ val, const float* __restrict__ dinv, const float* __restrict__ rhs,
+    const int* __restrict__ rhs_perm, const float* __restrict__ in, const int* __restrict__ in_perm,
+    const float* __restrict__ in_scale, float* __restrict__ out, const int* __restrict__ out_perm) {
+  if (gated_off(gate, 1)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float acc = rhs[rhs_perm ? rhs_perm[i] : i];
+  for (int j = rp[i]; j < rp[i + 1]; j++) {
+    const int c = ci[j];
+    float xin = in[in_perm ? in_perm[c] : c];
+    if (in_scale) xin *= in_scale[c];
+    acc = __fmaf_rn(-val[j], xin, acc);
+  }
+  const float o = dinv ? acc * dinv[i] : acc;
+  out[out_perm ? out_perm[i] : i] = o;
+}
+
+__global__ void __launch_bounds__(kMixBlock) k_mx_spmv32(const int* gate, int n,
+                                                         const int* __restrict__ rp,
+                                                         const int* __restrict__ ci,
+                                                         const float* __restrict__ val,
+                                                         const float* __restrict__ x,
+                                                         float* __restrict__ y) {
+  if (gated_off(gate, 1)) return;
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  const uint64_t pol = l2_evict_first();
+  float acc = 0.f;
+  for (int j = rp[row]; j < rp[row + 1]; j++)
+    acc = __fmaf_rn(ld_stream(val + j, pol), x[ld_stream(ci + j, pol)], acc);
+  y[row] = acc;
+}
+
+__global__ void k_mx_maxpy(const int* gate, int n, const float* __restrict__ V, int k,
+                           const double* __restrict__ h, float* __restrict__ w) {
+  if (gated_off(gate, 1)) return;
+  __shared__ float hs[kMixMaxM + 1];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = (float)h[j];
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float v = w[i];
+    for (int j = 0; j < k; j++) v = __fmaf_rn(-hs[j], V[(size_t)j * n + i], v);
+    w[i] = v;
+  }
+}
+
+// Hessenberg column j, rotations and the residual estimate (one thread, FP64)
+__global__ void k_mx_givens(MixDev* st, const double* __restrict__ h, int j, int m) {
+  if (!st->active) return;
+  double* H = st->H;
+  const double hn = sqrt(st->hn2);
+  for (int i = 0; i <= j; i++) H[i * m + j] = h[i];
+  for (int i = 0; i < j; i++) {
+    const double a = H[i * m + j], c = H[(i + 1) * m + j];
+    H[i * m + j] = st->cs[i] * a + st->sn[i] * c;
+    H[(i + 1) * m + j] = -st->sn[i] * a + st->cs[i] * c;
+  }
+  const double hjj = H[j * m + j];
+  const double den = hypot(hjj, hn);
+  st->cs[j] = den > 0.0 ? hjj / den : 1.0;
+  st->sn[j] = den > 0.0 ? hn / den : 0.0;
+  H[j * m + j] = den;
+  st->g[j + 1] = -st->sn[j] * st->g[j];
+  st->g[j] = st->cs[j] * st->g[j];
+  st->kdim = j + 1;
+  st->its += 1;
+  if (!(hn > 0.0) || fabs(st->g[j + 1]) <= st->tol || j + 1 == m) st->active = 0;
+}
+
+__global__ void k_mx_backsub(MixDev* st, int m) {
+  if (!st->pass_on) return;
+  const int k = st->kdim;
+  for (int i = k - 1; i >= 0; i--) {
+    double t = st->g[i];
+    for (int c = i + 1; c < k; c++) t -= st->H[i * m + c] * st->y[c];
+    st->y[i] = st->H[i * m + i] != 0.0 ? t / st->H[i * m + i] : 0.0;
+  }
+}
+
+// x += rn * sum_{j < kdim} y_j Z_j
+__global__ void k_mx_correct(int n, const float* __restrict__ Z, const MixDev* st,
+                             double* __restrict__ x) {
+  if (!st->pass_on) return;
+  __shared__ float ys[kMixMaxM];
+  const int k = st->kdim;
+  for (int j = threadIdx.x; j < k; j += blockDim.x) ys[j] = (float)st->y[j];
+  __syncthreads();
+  const double rn = st->rn;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float d = 0.f;
+    for (int j = 0; j < k; j++) d = __fmaf_rn(ys[j], Z[(size_t)j * n + i], d);
+    x[i] = fma(rn, (double)d, x[i]);
+  }
+}
+
+// the mdot of the host-driven form, gated on `*gate == 1`
+__global__ void __launch_bounds__(kMixBlock) k_mx_mdot(const int* gate, int n,
+                                                       const float* __restrict__ V, int k,
+                                                       const float* __restrict__ w,
+                                                       double* __restrict__ partials,
+                                                       unsigned* ticket, double* out) {
+  if (gated_off(gate, 1)) return;
+  __shared__ float sh[kMixBlock / 32][kMixMaxM + 1];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int kk = V ? k : 1;
+  for (int j0 = 0; j0 < kk; j0 += 8) {
+    float acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) acc[q] = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      const float wi = w[i];
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if (j0 + q < kk) acc[q] = __fmaf_rn(V ? V[(size_t)(j0 + q) * n + i] : wi, wi, acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+      if (lane == 0 && j0 + q < kk) sh[wid][j0 + q] = acc[q];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < kk; j++) {
+      float t = 0.f;
+      for (int ww = 0; ww < (int)(blockDim.x >> 5); ww++) t += sh[ww][j];
+      partials[(size_t)j * gridDim.x + blockIdx.x] = (double)t;
+    }
+    last = atomic_add_acq_rel(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  fold_partials(partials, kk, out);
+  __syncthreads();
+  if (threadIdx.x == 0) *ticket = 0u;
+}
+
+__global__ void k_mx_cast64(const int* gate, int n, const float* __restrict__ a,
+                            double* __restrict__ b) {
+  if (gated_off(gate, 1)) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+
+__global__ void k_mx_cast32(const int* gate, int n, const double* __restrict__ a,
+                            float* __restrict__ b) {
+  if (gated_off(gate, 1)) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    b[i] = __double2float_rn(a[i]);
+}
+
+// Record one refinement pass into the current capture on stream s.
+static int record_pass(Mixed* M, const Csr* A, const Pc* pc, const double* b, double* x,
+                       int tri_sweeps, cudaStream_t s) {
+  const int n = M->n, m = M->m, g = mix_grid(n), gr = (n + kMixBlock - 1) / kMixBlock;
+  MixDev* st = M->st;
+  const int* on = &st->pass_on;
+  const int* act = &st->active;
+  RedSlot slot{};
+  slot.partials = M->part64;
+  slot.ticket = M->ticket64;
+  slot.stride = kMaxRedGrid;
+  GP_TRY(spmv(s, A, DRef::of(x), DRef::of(M->y)));
+  k_mx_resid<<<red_grid(n), kRedBlock, 0, s>>>(n, b, M->y, M->r, slot, st);
+  k_mx_v0<<<g, kMixBlock, 0, s>>>(n, M->r, st, M->V);
+  k_mx_mdot<<<mdot_grid(n), kMixBlock, 0, s>>>(on, n, nullptr, 1, M->V, M->partials, M->ticket,
+                                     &st->beta2);
+  k_mx_beta<<<1, 1, 0, s>>>(st, m);
+  k_mx_scale<<<g, kMixBlock, 0, s>>>(n, M->V, M->V, st, 0);
+  for (int j = 0; j < m; j++) {
+    float* vj = M->V + (size_t)j * n;
+    float* zj = M->Z + (size_t)j * n;
+    if (tri_sweeps > 0) {
+      // L: y <- Pv - L y from y = Pv;  U: x <- D^-1 (y - U x) from x = D^-1 y
+      float* ya = M->t1;
+      float* yb = M->t2;
+      const float* yin = vj;
+      const int* yperm = pc->perm_r;
+      for (int k = 0; k < tri_sweeps; k++) {
+        k_mx_tri<<<gr, kMixBlock, 0, s>>>(act, n, M->lrp, M->lci, M->lval, nullptr, vj,
+                                          pc->perm_r, yin, yperm, nullptr, ya, nullptr);
+        yin = ya;
+        yperm = nullptr;
+        std::swap(ya, yb);
+      }
+      float* xa = M->t3;
+      float* xb = M->t4;
+      const float* xin = yin;
+      const float* xscale = M->udinv;
+      for (int k = 0; k < tri_sweeps; k++) {
+        const bool lastp = k + 1 == tri_sweeps;
+        k_mx_tri<<<gr, kMixBlock, 0, s>>>(act, n, M->urp, M->uci, M->uval, M->udinv, yin,
+                                          nullptr, xin, nullptr, xscale, lastp ? zj : xa,
+                                          lastp ? pc->perm_c : nullptr);
+        xin = xa;
+        xscale = nullptr;
+        std::swap(xa, xb);
+      }
+    } else {
+      // exact: the FP64 level-scheduled sweeps of the plain path, gated
+      k_mx_cast64<<<g, kMixBlock, 0, s>>>(act, n, vj, M->y);
+      GP_TRY(pc_apply(const_cast<Pc*>(pc), DRef::of(M->y), DRef::of(M->r), s, act, 1));
+      k_mx_cast32<<<g, kMixBlock, 0, s>>>(act, n, M->r, zj);
+    }
+    k_mx_spmv32<<<gr, kMixBlock, 0, s>>>(act, n, A->rowptr, A->colind, A->val32, zj, M->w);
+    k_mx_mdot<<<mdot_grid(n), kMixBlock, 0, s>>>(act, n, M->V, j + 1, M->w, M->partials, M->ticket,
+                                       M->h_dev);
+    k_mx_maxpy<<<g, kMixBlock, 0, s>>>(act, n, M->V, j + 1, M->h_dev, M->w);
+    k_mx_mdot<<<mdot_grid(n), kMixBlock, 0, s>>>(act, n, nullptr, 1, M->w, M->partials, M->ticket,
+                                       &st->hn2);
+    k_mx_givens<<<1, 1, 0, s>>>(st, M->h_dev, j, m);
+    if (j + 1 < m) k_mx_scale<<<g, kMixBlock, 0, s>>>(n, M->w, M->V + (size_t)(j + 1) * n, st, 1);
+  }
+  k_mx_backsub<<<1, 1, 0, s>>>(st, m);
+  k_mx_correct<<<g, kMixBlock, 0, s>>>(n, M->Z, st, x);
+  GP_CUDA(cudaMemcpyAsync(M->h_st, st, offsetof(MixDev, H), cudaMemcpyDeviceToHost, s));
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+int mixed_solve_graph(Mixed* M, Csr* A, Pc* pc, const double* b, double* x,
+                      const MixedOptions& o, MixedResult& res, cudaStream_t caller) {
+  const int n = A->n, m = o.restart;
+  if (!M->st) {
+    GP_CUDA(cudaMalloc(&M->st, sizeof(MixDev)));
+    GP_CUDA(cudaMallocHost(&M->h_st, sizeof(MixDev)));
+    GP_CUDA(cudaMalloc(&M->part64, kMaxRedGrid * sizeof(double)));
+    GP_CUDA(cudaMalloc(&M->ticket64, sizeof(unsigned)));
+    GP_CUDA(cudaMemset(M->ticket64, 0, sizeof(unsigned)));
+    GP_CUDA(cudaStreamCreateWithFlags(&M->cap_stream, cudaStreamNonBlocking));
+  }
+  cudaStream_t s = M->cap_stream;
+  cudaEvent_t ev;
+  GP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  GP_CUDA(cudaEventRecord(ev, caller));
+  GP_CUDA(cudaStreamWaitEvent(s, ev, 0));
+  GP_TRY(csr_make_val32(A, s));
+  GP_TRY(mixed_factors(M, s));
+  double bb = 0.0;
+  GP_TRY(vec_reduce(s, RED_NORM2SQ, n, b, nullptr, &bb));
+  const double bnorm = std::sqrt(bb);
+  // device state for this solve
+  MixDev h{};
+  h.rtol_bnorm = o.rtol * bnorm;
+  h.inner_rtol = o.inner_rtol;
+  std::memcpy(M->h_st, &h, offsetof(MixDev, H));
+  GP_CUDA(cudaMemcpyAsync(M->st, M->h_st, offsetof(MixDev, H), cudaMemcpyHostToDevice, s));
+  GP_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+  const void* key[6] = {A, pc, b, x, pc->ba, A->val32};
+  const int ikey[4] = {n, m, o.tri_sweeps, pc->generation};
+  const bool same = M->exec && std::equal(key, key + 6, M->cap_key) &&
+                    std::equal(ikey, ikey + 4, M->cap_ikey);
+  if (!same) {
+    if (M->exec) cudaGraphExecDestroy(M->exec);
+    if (M->graph) cudaGraphDestroy(M->graph);
+    M->exec = nullptr;
+    M->graph = nullptr;
+    GP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+    int st = record_pass(M, A, pc, b, x, o.tri_sweeps, s);
+    cudaGraph_t gph = nullptr;
+    cudaError_t ec = cudaStreamEndCapture(s, &gph);
+    if (st != GP_OK) {
+      if (gph) cudaGraphDestroy(gph);
+      return st;
+    }
+    if (ec != cudaSuccess) {
+      set_error(std::string("mixed solve capture: ") + cudaGetErrorString(ec));
+      return GP_ERR_CUDA;
+    }
+    M->graph = gph;
+    GP_CUDA(cudaGraphInstantiate(&M->exec, gph, 0));
+    std::copy(key, key + 6, M->cap_key);
+    std::copy(ikey, ikey + 4, M->cap_ikey);
+  }
+  res = MixedResult();
+  for (int pass = 0; pass <= o.max_outer; pass++) {
+    GP_CUDA(cudaGraphLaunch(M->exec, s));
+    GP_CUDA(cudaStreamSynchronize(s));
+    const MixDev& hs = *M->h_st;
+    res.relres = bnorm > 0.0 ? hs.rn / bnorm : hs.rn;
+    res.inner_its = hs.its;
+    res.passes = hs.passes;
+    if (!hs.pass_on) {
+      res.converged = hs.rn <= o.rtol * bnorm;
+      break;
+    }
+  }
+  if (!res.converged) {  // the last pass corrected x after its residual: measure again
+    GP_TRY(spmv(s, A, DRef::of(x), DRef::of(M->y)));
+    k_resid_parts<<<mix_grid(n), kMixBlock, 0, s>>>(n, b, M->y, M->r);
+    double rr = 0.0;
+    GP_TRY(vec_reduce(s, RED_NORM2SQ, n, M->r, nullptr, &rr));
+    res.relres = bnorm > 0.0 ? std::sqrt(rr) / bnorm : std::sqrt(rr);
+    res.converged = res.relres <= o.rtol;
+  }
+  GP_CUDA(cudaEventRecord(ev, s));
+  GP_CUDA(cudaStreamWaitEvent(caller, ev, 0));
+  cudaEventDestroy(ev);
   return GP_OK;
 }
 
