@@ -1456,6 +1456,40 @@ static int cgs(const Run& r) {
   return GP_OK;
 }
 
+// modified Gram-Schmidt (KSPGMRESModifiedGramSchmidtOrthogonalization,
+// src/ksp.mojo:511-530): for k = 0..it, d = v_{it+1} . v_k, HH(k, it) =
+// HES(k, it) = d, v_{it+1} -= d v_k.  The captured body holds `restart`
+// (dot, store, axpy) triples; triple k runs while k <= it.
+static_assert(kMaxBasis <= 64, "mgs_on holds one gate per basis vector");
+__global__ void k_gm_mgs_prep(KspState* st) {
+  const int on = st->g[1];
+  for (int k = 0; k < kMaxBasis; k++) st->mgs_on[k] = on && k <= st->it ? 1 : 0;
+}
+
+__global__ void k_gm_mgs_store(KspState* st, double* hs, int k) {
+  if (!st->mgs_on[k]) return;
+  Hs H(hs, st->m);
+  const int it = st->it, m = st->m;
+  H.hh[it * (m + 2) + k] = st->mgs_d;
+  H.hes[it * (m + 1) + k] = st->mgs_d;
+}
+
+static int mgs(const Run& r) {
+  Ksp* k = r.k;
+  KspState* st = k->st;
+  DRef v1 = DRef::at(&st->vv_it1);
+  k_gm_mgs_prep<<<1, 1, 0, r.s>>>(st);
+  for (int kk = 0; kk < k->opt.restart; kk++) {
+    const int* gate = &st->mgs_on[kk];
+    DRef vk = DRef::of(k->vv + (size_t)kk * r.n);
+    GP_TRY(r.red<D_DOT>(gate, v1, vk, &st->mgs_d, nullptr));
+    k_gm_mgs_store<<<1, 1, 0, r.s>>>(st, k->hs, kk);
+    FL(k_axpy_d, r.grid(), 256, r.s, gate, 1, r.n, v1, &st->mgs_d, -1.0, vk);
+  }
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
 // the first cycle starts with a restart (no solution to build yet)
 __global__ void k_first_restart(KspState* st) { gm_set_phase(st, PH_RESTART); }
 
@@ -1504,7 +1538,7 @@ static int gmres_body(const Run& r, const double* b, double* x) {
   // ---- one Arnoldi step
   DRef vit = DRef::at(&st->vv_it), vit1 = DRef::at(&st->vv_it1);
   GP_TRY(r.apply_ba(r.G(1), side, vit, vit1, TMATOP));
-  GP_TRY(cgs(r));
+  GP_TRY(k->opt.orthog ? mgs(r) : cgs(r));
   GP_TRY(r.red<D_NRM>(r.G(1), vit1, vit1, nullptr, r.S(&KspState::tt)));
   k_scale_d<true><<<r.grid(), 256, 0, r.s>>>(r.G(1), 1, n, vit1, r.S(&KspState::tt));
   k_gm_step_ctrl<<<1, 1, 0, r.s>>>(st, k->hs, k->hist, k->vv, n);
@@ -1556,7 +1590,7 @@ static int fgmres_body(const Run& r, const double* b, double* x) {
   DRef vit = DRef::at(&st->vv_it), vit1 = DRef::at(&st->vv_it1), pit = DRef::at(&st->pv_it);
   GP_TRY(r.pcapply(r.G(1), vit, pit));
   GP_TRY(r.matmult(r.G(1), pit, vit1));
-  GP_TRY(cgs(r));
+  GP_TRY(k->opt.orthog ? mgs(r) : cgs(r));
   GP_TRY(r.red<D_NRM>(r.G(1), vit1, vit1, nullptr, r.S(&KspState::tt)));
   k_fg_step_ctrl<<<1, 1, 0, r.s>>>(st, k->hs, k->hist, k->vv, k->prevec, n);
   k_scale_d<false><<<r.grid(), 256, 0, r.s>>>(r.G(10), 1, n, DRef::at(&st->vv_scale),
@@ -1743,10 +1777,6 @@ int ksp_solve(Ksp* k, Csr* A, Pc* pc, const double* b, double* x, KspResult* res
     set_error("GMRES restart must be between 1 and " + std::to_string(kMaxBasis - 1));
     return GP_ERR_UNSUPPORTED;
   }
-  if (gm && o.orthog != 0) {
-    set_error("modified Gram-Schmidt is not available on the device path");
-    return GP_ERR_UNSUPPORTED;
-  }
   if (o.max_it < 0) o.max_it = 0;
   const int n = A->n;
   k->n = n;
@@ -1785,21 +1815,21 @@ int ksp_solve(Ksp* k, Csr* A, Pc* pc, const double* b, double* x, KspResult* res
   if (o.guess_zero && n) GP_CUDA(cudaMemsetAsync(x, 0, (size_t)n * sizeof(double), s));
   Run r{k, A, pc, n, s};
   // the solve graph depends on the buffers and on every option that shapes it
-  const int key[11] = {o.type,      o.normtype,    o.pc_side,          o.restart,
+  const int key[12] = {o.type,      o.normtype,    o.pc_side,          o.restart,
                        o.cgstype,   n,             pc->opt.type,       pc->opt.sor_flag,
-                       o.guess_zero, pc->generation,      arith_mode()};
+                       o.guess_zero, pc->generation, arith_mode(),    o.orthog};
   if (eager_mode()) {
     GP_TRY(run_eager(r, b, x));
   } else {
   const bool same = !moved && k->exec && k->cap_A == A && k->cap_pc == pc &&
-                    std::equal(key, key + 11, k->cap_key) && k->cap_b == b && k->cap_x == x;
+                    std::equal(key, key + 12, k->cap_key) && k->cap_b == b && k->cap_x == x;
   if (!same) {
     GP_TRY(capture(r, b, x));
     k->cap_A = A;
     k->cap_pc = pc;
     k->cap_b = b;
     k->cap_x = x;
-    std::copy(key, key + 11, k->cap_key);
+    std::copy(key, key + 12, k->cap_key);
   }
   GP_CUDA(cudaGraphLaunch(k->exec, s));
   }

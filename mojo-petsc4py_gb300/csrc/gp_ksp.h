@@ -56,6 +56,8 @@ struct KspState {
   double* pv_it;    // FGMRES prevec `it`
   double* vv_scale; // FGMRES: the vector the step's scale applies to
   double red[4];
+  int mgs_on[64];    // modified Gram-Schmidt: projection k runs while k <= it
+  double mgs_d;      // the current projection
 };
 
 struct Ksp {
@@ -83,7 +85,7 @@ struct Ksp {
   const void* cap_pc = nullptr;
   const void* cap_b = nullptr;
   const void* cap_x = nullptr;
-  int cap_key[11] = {0};
+  int cap_key[12] = {0};
   cudaStream_t stream2 = nullptr;  // body capture stream
   int64_t top_kernels = 0;         // kernels outside the loop body
   int64_t body_kernels = 0;        // kernels per loop trip

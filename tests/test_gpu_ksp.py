@@ -148,6 +148,19 @@ def test_cg_norm_types(normtype):
     check(g, r, "cg")
 
 
+@pytest.mark.parametrize("kt,pt", [("gmres", "none"), ("gmres", "ilu"), ("fgmres", "jacobi")])
+@pytest.mark.parametrize("restart", [5, 30])
+def test_modified_gram_schmidt(kt, pt, restart):
+    """KSPGMRESModifiedGramSchmidtOrthogonalization (src/ksp.mojo:511-530)."""
+    ip, ix, v = gallery.laplacian_2d(12)
+    b = np.random.default_rng(21).normal(size=144)
+    tol = dict(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=2000)
+    opts = {"setGMRESRestart": restart, "setGMRESOrthogonalization": 1}
+    g = solve_gpu(kt, pt, ip, ix, v, b, ksp_opts=opts, tol=tol)
+    r = oracle_solve(kt, ip, ix, v, b, pt, restart=restart, orthog=1, **tol)
+    check(g, r, kt)
+
+
 @pytest.mark.parametrize("cgstype", [1, 2])
 @pytest.mark.parametrize("restart", [5, 30])
 def test_gmres_refinement_and_restart(cgstype, restart):
