@@ -406,6 +406,9 @@ def _sync_ms(torch, fn, reps):
     return float(np.mean(out))
 
 
+BATCH_SYSTEMS = 512
+
+
 def form_batched(torch, PETSc):
     """Batched CG on 512 RGG Laplacians x 16 right-hand sides (rtol 1e-8,
     Jacobi): FP64 and FP32-inner-refined forms in one captured solve each,
@@ -414,7 +417,7 @@ def form_batched(torch, PETSc):
     from mojopetsc4py.batch import BatchedCG
 
     t0 = time.perf_counter()
-    systems = gallery.rgg_batch(512, seed=11)
+    systems = gallery.rgg_batch(BATCH_SYSTEMS, seed=11)
     sizes = np.array([len(ip) - 1 for ip, _, _ in systems])
     n = int(sizes.sum())
     nnz = int(sum(int(ip[-1]) for ip, _, _ in systems))
@@ -457,7 +460,7 @@ def form_batched(torch, PETSc):
         ksp.solve(bv, xv)
         per.append(_sync_ms(torch, lambda: ksp.solve(bv, xv), 1))
     # the sample spans the size range evenly: scale its mean to all pairs
-    est = float(np.mean(per)) * 512 * 16
+    est = float(np.mean(per)) * BATCH_SYSTEMS * 16
     out["plain_fp64_single_system"] = {
         "sample_pairs": len(per), "sample_ms": [round(p, 2) for p in per],
         "estimated_ms_all_pairs": round(est, 1),
@@ -583,6 +586,11 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline solve only")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--spmv-only", action="store_true", help="SpMV launches only")
+    ap.add_argument("--form", choices=["mixed", "batched", "adjoint"], default=None,
+                    help="run one of the further forms alone (profiling)")
+    ap.add_argument("--batch-systems", type=int, default=512,
+                    help="systems in the batched form (512 is the benchmark; fewer "
+                         "only for profiling)")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the mixed, batched and adjoint forms")
     ap.add_argument("--max-it", type=int, default=None,
@@ -592,7 +600,16 @@ def main():
         global MAX_IT
         MAX_IT = args.max_it
     world, rank, local, pg = dist_setup()
-    if args.spmv_only:
+    if args.form:
+        import torch
+
+        from mojopetsc4py import PETSc
+
+        global BATCH_SYSTEMS
+        BATCH_SYSTEMS = args.batch_systems
+        fn = {"mixed": form_mixed, "batched": form_batched, "adjoint": form_adjoint}[args.form]
+        print(json.dumps({"form": args.form, **fn(torch, PETSc)}), flush=True)
+    elif args.spmv_only:
         run_spmv_only(args)
     elif args.impl == "reference":
         run_reference(args, world, rank, pg)
