@@ -255,11 +255,30 @@ __global__ void k_bspmm(BatchDev b, const T* __restrict__ val, const T* __restri
       T acc[VR];
 #pragma unroll
       for (int v = 0; v < VR; v++) acc[v] = (T)0;
-      for (int j = j0; j < j1; j++) {
-        const T a = val[j];
-        const T* xp = p + (size_t)b.colind[j] * R + g * VR;
+      // four slots per batch: their values, columns and gathers are all in
+      // flight before the first multiply-add (the chain column -> gather is
+      // otherwise paid once per nonzero)
+      for (int j = j0; j < j1; j += 4) {
+        T a[4], xv[4][VR];
+        int c[4];
 #pragma unroll
-        for (int v = 0; v < VR; v++) acc[v] = fmadd<T>(a, xp[v], acc[v]);
+        for (int u = 0; u < 4; u++)
+          if (j + u < j1) {
+            a[u] = val[j + u];
+            c[u] = b.colind[j + u];
+          }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (j + u < j1) {
+#pragma unroll
+            for (int v = 0; v < VR; v++) xv[u][v] = p[(size_t)c[u] * R + g * VR + v];
+          }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (j + u < j1) {
+#pragma unroll
+            for (int v = 0; v < VR; v++) acc[v] = fmadd<T>(a[u], xv[u][v], acc[v]);
+          }
       }
       const size_t o = (size_t)row * R + g * VR;
 #pragma unroll
@@ -363,11 +382,27 @@ __global__ void k_bresid(BatchDev b, const double* __restrict__ bb, const double
       double ax[VR];
 #pragma unroll
       for (int v = 0; v < VR; v++) ax[v] = 0.0;
-      for (int j = j0; j < j1; j++) {
-        const double a = b.val[j];
-        const double* xp = x + (size_t)b.colind[j] * R + g * VR;
+      for (int j = j0; j < j1; j += 4) {
+        double a[4], xv[4][VR];
+        int c[4];
 #pragma unroll
-        for (int v = 0; v < VR; v++) ax[v] = fma(a, xp[v], ax[v]);
+        for (int u = 0; u < 4; u++)
+          if (j + u < j1) {
+            a[u] = b.val[j + u];
+            c[u] = b.colind[j + u];
+          }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (j + u < j1) {
+#pragma unroll
+            for (int v = 0; v < VR; v++) xv[u][v] = x[(size_t)c[u] * R + g * VR + v];
+          }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (j + u < j1) {
+#pragma unroll
+            for (int v = 0; v < VR; v++) ax[v] = fma(a[u], xv[u][v], ax[v]);
+          }
       }
       const size_t o = (size_t)row * R + g * VR;
 #pragma unroll

@@ -5,7 +5,7 @@
 // (src/ported.mojo:380-391).
 //
 // Row per thread (spmv_row): rows of bounded length (stencils, FEM, graphs).
-// Each thread loads its row's slots eight at a time, then gathers x.  A warp's
+// Each thread loads its row's slots four at a time, then gathers x.  A warp's
 // loads of a slot range are strided by the row length, but the 32 rows of a
 // warp cover one contiguous span of the arrays, so L1 serves the re-touched
 // lines and DRAM sees each byte once.  Matrix values and indices are read
@@ -62,17 +62,19 @@ __device__ __forceinline__ double spmv_row(int row, const int* __restrict__ rowp
   const uint64_t pol = l2_evict_first();
   const int b = rowptr[row], e = rowptr[row + 1];
   double acc = init;
-  for (int j0 = b; j0 < e; j0 += 8) {
-    int cc[8];
-    double vv[8];
+  // four slots per batch: 32 registers, full occupancy (a GB300 scan of
+  // 2/4/7/8-slot batches on the 7-point stencil put 4 first)
+  for (int j0 = b; j0 < e; j0 += 4) {
+    int cc[4];
+    double vv[4];
 #pragma unroll
-    for (int u = 0; u < 8; u++)
+    for (int u = 0; u < 4; u++)
       if (j0 + u < e) {
         cc[u] = ld_stream(colind + j0 + u, pol);
         vv[u] = (double)ld_stream(val + j0 + u, pol);
       }
 #pragma unroll
-    for (int u = 0; u < 8; u++)
+    for (int u = 0; u < 4; u++)
       if (j0 + u < e) acc = madd<FMA>(vv[u], (double)x[cc[u]], acc);
   }
   return acc;
