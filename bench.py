@@ -432,12 +432,15 @@ def form_batched(torch, PETSc):
            "tuning_fp32": solver.tuning32,
            "setup_s": round(setup_s, 1)}
     X = torch.empty_like(B)
-    for prec in ("fp64", "fp32"):
-        solver.solve(B, pc="jacobi", precision=prec, rtol=1e-8, out=X)  # capture + warm
-        ms = _sync_ms(torch, lambda: solver.solve(B, pc="jacobi", precision=prec, rtol=1e-8,
+    # fp64 at rtol 1e-8 stops on the preconditioned norm (its true residual is
+    # larger); fp64 at 1e-10 reaches the true 1e-8 the refined fp32 form meets
+    for key, prec, rt in (("fp64", "fp64", 1e-8), ("fp64_rtol_1e-10", "fp64", 1e-10),
+                          ("fp32_inner_fp64_refined", "fp32", 1e-8)):
+        solver.solve(B, pc="jacobi", precision=prec, rtol=rt, out=X)  # capture + warm
+        ms = _sync_ms(torch, lambda: solver.solve(B, pc="jacobi", precision=prec, rtol=rt,
                                                    out=X), 2)
-        _, info = solver.solve(B, pc="jacobi", precision=prec, rtol=1e-8, out=X)
-        out[prec if prec == "fp64" else "fp32_inner_fp64_refined"] = {
+        _, info = solver.solve(B, pc="jacobi", precision=prec, rtol=rt, out=X)
+        out[key] = {
             "ms": round(ms, 2), "max_its": int(info["its"].max()),
             "mean_its": round(float(info["its"].mean()), 1),
             "max_true_rel_residual": float(info["relres"].max()),

@@ -223,13 +223,18 @@ __global__ void k_bp(BatchDev b, T* __restrict__ p, const T* __restrict__ z) {
   TILE_LOOP(tile) {
     const int s = b.tile_sys[tile];
     if (!b.sys_active[s]) continue;
+    // blockDim is a multiple of R: a thread keeps one column for the tile
+    const int q = s * R + threadIdx.x % R;
+    if (!b.active[q]) continue;
+    const double bc = b.bcoef[q];
+    const T tb = (T)bc;
     const int r0 = b.tile_row0[tile], ne = b.tile_nrows[tile] * R;
-    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
-      const int c = e % R, q = s * R + c;
-      if (!b.active[q]) continue;
-      const size_t i = (size_t)r0 * R + e;
-      const double bc = b.bcoef[q];
-      p[i] = bc == 0.0 ? z[i] : fmadd<T>((T)bc, p[i], z[i]);
+    T* pp = p + (size_t)r0 * R;
+    const T* zz = z + (size_t)r0 * R;
+    if (bc == 0.0) {
+      for (int e = threadIdx.x; e < ne; e += blockDim.x) pp[e] = zz[e];
+    } else {
+      for (int e = threadIdx.x; e < ne; e += blockDim.x) pp[e] = fmadd<T>(tb, pp[e], zz[e]);
     }
   }
 }
@@ -258,23 +263,24 @@ __global__ void k_bspmm(BatchDev b, const T* __restrict__ val, const T* __restri
       // four slots per batch: their values, columns and gathers are all in
       // flight before the first multiply-add (the chain column -> gather is
       // otherwise paid once per nonzero)
-      for (int j = j0; j < j1; j += 4) {
-        T a[4], xv[4][VR];
-        int c[4];
+      constexpr int S = 4;  // slots per batch (2 measured slower for 4-wide FP32 rows)
+      for (int j = j0; j < j1; j += S) {
+        T a[S], xv[S][VR];
+        int c[S];
 #pragma unroll
-        for (int u = 0; u < 4; u++)
+        for (int u = 0; u < S; u++)
           if (j + u < j1) {
             a[u] = val[j + u];
             c[u] = b.colind[j + u];
           }
 #pragma unroll
-        for (int u = 0; u < 4; u++)
+        for (int u = 0; u < S; u++)
           if (j + u < j1) {
 #pragma unroll
             for (int v = 0; v < VR; v++) xv[u][v] = p[(size_t)c[u] * R + g * VR + v];
           }
 #pragma unroll
-        for (int u = 0; u < 4; u++)
+        for (int u = 0; u < S; u++)
           if (j + u < j1) {
 #pragma unroll
             for (int v = 0; v < VR; v++) acc[v] = fmadd<T>(a[u], xv[u][v], acc[v]);
@@ -1108,12 +1114,12 @@ static int solve_shape(Batch& B, const BatchOptions& o, const double* b, double*
             cudaMemcpyAsync(B.r, b, nv * sizeof(double), cudaMemcpyDeviceToDevice, st);
             norms(st);
             launch_state(B, d64, nullptr, st);
-            launch_update<double, R, VR, true>(B, d64, dinv, x, B.r, B.p, B.z, B.z, st);
+            launch_update<double, R, 1, true>(B, d64, dinv, x, B.r, B.p, B.z, B.z, st);
           },
           [&](cudaStream_t st) {
             launch_p<double, R>(B, d64, B.p, B.z, st);
             launch_spmm<double, R, VR>(B, d64, B.val, B.p, B.z, st);  // W shares Z's storage
-            launch_update<double, R, VR, false>(B, d64, dinv, x, B.r, B.p, B.z, B.z, st);
+            launch_update<double, R, 1, false>(B, d64, dinv, x, B.r, B.p, B.z, B.z, st);
           },
           [&](cudaStream_t st) { launch_resid<R, VR>(B, d64, b, x, 0, st); }));
   } else {
@@ -1128,13 +1134,13 @@ static int solve_shape(Batch& B, const BatchOptions& o, const double* b, double*
             auto ks = k_bscale_in<R>;
             const int g = std::max(1, std::min(B.ntiles, resident((const void*)ks, B.cur->block, 0)));
             ks<<<g, B.cur->block, 0, st>>>(d32, B.r, B.rn, B.r32, B.x32);
-            launch_update<float, R, VR, true>(B, d32, dinv32, B.x32, B.r32, B.p32, B.z32, B.z32,
+            launch_update<float, R, 1, true>(B, d32, dinv32, B.x32, B.r32, B.p32, B.z32, B.z32,
                                               st);
           },
           [&](cudaStream_t st) {
             launch_p<float, R>(B, d32, B.p32, B.z32, st);
             launch_spmm<float, R, VR>(B, d32, B.val32, B.p32, B.z32, st);
-            launch_update<float, R, VR, false>(B, d32, dinv32, B.x32, B.r32, B.p32, B.z32,
+            launch_update<float, R, 1, false>(B, d32, dinv32, B.x32, B.r32, B.p32, B.z32,
                                                B.z32, st);
           },
           [&](cudaStream_t st) {
