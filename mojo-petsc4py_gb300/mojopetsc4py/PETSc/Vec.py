@@ -116,7 +116,7 @@ class Vec:
         if self._loc == _DEVICE:
             if len(self._h):
                 dev.torch().cuda.current_stream().synchronize()
-                self._h[:] = self._d.cpu().numpy()
+                dev.torch().from_numpy(self._h).copy_(self._d)
             self._loc = _BOTH
 
     def _tensor(self):
@@ -138,12 +138,14 @@ class Vec:
             raise ValueError(f"invalid block size {bs}")
         if n % bs:
             raise ValueError(f"global size {n} not divisible by block size {bs}")
-        self._init_storage(np.zeros(n, dtype=np.float64))
+        self._init_storage(dev.host_zeros(n))
         self._bsize = bs
         return self
 
     def createWithArray(self, array, bsize=None, comm=None) -> "Vec":
-        arr = _f64(array, copy=True)
+        src = _f64(array)
+        arr = dev.host_zeros(len(src))
+        arr[:] = src
         bs = 1 if bsize is None else int(bsize)
         if len(arr) % bs:
             raise ValueError(
@@ -157,9 +159,11 @@ class Vec:
         out = Vec()
         out._bsize = self._bsize
         if array is None:
-            out._init_storage(np.zeros(self._size(), dtype=np.float64))
+            out._init_storage(dev.host_zeros(self._size()))
         else:
-            arr = _f64(array, copy=True)
+            src = _f64(array)
+            arr = dev.host_zeros(len(src))
+            arr[:] = src
             if len(arr) != self._size():
                 raise ValueError(f"incompatible array size: {len(arr)} != {self._size()}")
             out._init_storage(arr)

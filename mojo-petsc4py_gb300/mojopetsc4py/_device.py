@@ -39,5 +39,22 @@ def from_host(a: np.ndarray):
     return t.from_numpy(np.ascontiguousarray(a)).to("cuda", non_blocking=False)
 
 
+PINNED_MIN = 1 << 15  # entries; smaller host arrays stay ordinary numpy arrays
+
+
+def host_zeros(n: int) -> np.ndarray:
+    """A zeroed float64 host array; page-locked (pinned) when large and a CUDA
+    device is present, so copies to and from the device run at the full link
+    rate.  The array keeps its pinned buffer alive."""
+    n = max(int(n), 0)
+    if n >= PINNED_MIN:
+        try:
+            t = torch()
+            return t.zeros(n, dtype=t.float64, pin_memory=True).numpy()
+        except Exception:
+            pass
+    return np.zeros(n, dtype=np.float64)
+
+
 def ptr(tensor) -> int:
     return int(tensor.data_ptr()) if tensor is not None and tensor.numel() else 0
