@@ -544,36 +544,58 @@ def form_adjoint(torch, PETSc):
     obs.set_values(torch.tensor(v_obs, device="cuda"))
     u_obs = obs.solve(b)
     vals = torch.tensor(v, device="cuda", requires_grad=True)
-
-    def forward():
-        return sparse_solve(vals, b, sysm)
-
-    def both():
-        vals.grad = None
-        u = forward()
-        ((u - u_obs) ** 2).sum().backward()
-
-    both()  # set-up, capture and warm-up of both solvers
-    fwd_ms = _sync_ms(torch, forward, 3)
-    tot_ms = _sync_ms(torch, both, 3)
-    # the adjoint residual ||A^T lam - g|| / ||g|| in FP64 on the host
-    u = forward()
-    g = 2 * (u - u_obs)
-    lam = sysm.solve_transpose(g).cpu().numpy()
     rows = np.repeat(np.arange(n), np.diff(ip))
-    atl = np.bincount(ix, weights=v * lam[rows], minlength=n)
-    gh = g.detach().cpu().numpy()
-    adj_res = float(np.linalg.norm(atl - gh) / np.linalg.norm(gh))
+    bh = b.cpu().numpy()
+
+    def measure(system):
+        """Times and FP64 residuals of one system's forward and adjoint solves."""
+        def forward():
+            return sparse_solve(vals, b, system)
+
+        def both():
+            vals.grad = None
+            u = forward()
+            ((u - u_obs) ** 2).sum().backward()
+
+        both()  # set-up, capture and warm-up of both solvers
+        fwd_ms = _sync_ms(torch, forward, 3)
+        tot_ms = _sync_ms(torch, both, 3)
+        grad = vals.grad.detach().cpu().numpy()
+        # residuals ||A u - b|| / ||b|| and ||A^T lam - g|| / ||g|| in FP64 on the host
+        u = forward()
+        uh = u.detach().cpu().numpy()
+        fwd_res = float(np.linalg.norm(_csr_matvec(ip, ix, v, uh) - bh) / np.linalg.norm(bh))
+        g = 2 * (u - u_obs)
+        lam = system.solve_transpose(g).cpu().numpy()
+        atl = np.bincount(ix, weights=v * lam[rows], minlength=n)
+        gh = g.detach().cpu().numpy()
+        adj_res = float(np.linalg.norm(atl - gh) / np.linalg.norm(gh))
+        fs, ad = system.forward_solver, system.adjoint_solver
+        out = {"forward_ms": round(fwd_ms, 2),
+               "forward_plus_gradient_ms": round(tot_ms, 2),
+               "gradient_over_forward": round(tot_ms / fwd_ms, 2),
+               "forward_its": fs.its, "adjoint_its": ad.its,
+               "forward_true_rel_residual": fwd_res,
+               "adjoint_true_rel_residual": adj_res}
+        if system.precision == "mixed":
+            out["forward_passes"], out["adjoint_passes"] = fs.passes, ad.passes
+        return out, grad
+
+    plain, g64 = measure(sysm)
+    mixed_sys = SparseSystem(ip, ix, rtol=1e-10, precision="mixed")
+    mixed, gmx = measure(mixed_sys)
+    mixed["gradient_rel_diff_vs_fp64"] = float(np.linalg.norm(gmx - g64) / np.linalg.norm(g64))
     return {"config": "2-D advection-diffusion 256^2, kappa = exp(GRF, corr 16 cells), "
-                      "Peclet 2, upwind; loss ||u - u_obs||^2; gmres(30)+ilu(0) rtol 1e-10",
+                      "Peclet 2, upwind; loss ||u - u_obs||^2; forward and adjoint solves to "
+                      "rtol 1e-10",
             "n": n, "nnz": int(ip[-1]),
-            "forward_ms": round(fwd_ms, 2),
-            "forward_plus_gradient_ms": round(tot_ms, 2),
-            "gradient_over_forward": round(tot_ms / fwd_ms, 2),
-            "forward_its": sysm.forward_solver.its,
-            "adjoint_its": sysm.adjoint_solver.its,
-            "adjoint_true_rel_residual": adj_res,
-            "finite_difference_equivalent_ms": round(2 * int(ip[-1]) * fwd_ms, 0)}
+            "plain_fp64_gmres30_ilu0": plain,
+            "mixed_fp32_fgmres30_ilu0_refined": mixed,
+            "speedup_mixed_gradient_vs_plain_gradient": round(
+                plain["forward_plus_gradient_ms"] / mixed["forward_plus_gradient_ms"], 2),
+            "speedup_mixed_gradient_vs_plain_forward": round(
+                plain["forward_ms"] / mixed["forward_plus_gradient_ms"], 2),
+            "finite_difference_equivalent_ms": round(2 * int(ip[-1]) * plain["forward_ms"], 0)}
 
 
 def _csr_matvec(ip, ix, v, x):

@@ -64,6 +64,7 @@ struct Csr {
   int* colind = nullptr;     // device, nnz
   double* val = nullptr;     // device, nnz
   float* val32 = nullptr;    // device, nnz (mixed-precision copy, lazily made)
+  bool val32_stale = false;  // values changed since val32 was converted
   int* diagpos = nullptr;    // device, n: slot of a_ii or -1
   bool stream_rows = false;  // SpMV form: false row per thread, true row stream
   // transpose (built on demand): rows of A^T in ascending original row order

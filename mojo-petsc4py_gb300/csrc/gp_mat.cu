@@ -128,10 +128,7 @@ int csr_set_values(Csr* A, const double* val, int on_device, cudaStream_t s) {
   if (A->nnz == 0) return GP_OK;
   GP_CUDA(cudaMemcpyAsync(A->val, val, (size_t)A->nnz * sizeof(double),
                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
-  if (A->val32) {
-    cudaFree(A->val32);
-    A->val32 = nullptr;
-  }
+  A->val32_stale = true;  // converted again, in place, by the next csr_make_val32
   return GP_OK;
 }
 
@@ -212,10 +209,7 @@ int csr_transpose_values(Csr* A, Csr* T, cudaStream_t s) {
     k_gather_values<<<g, 256, 0, s>>>(A->nnz, A->t_src, A->val, T->val);
     GP_CHECK_LAUNCH();
   }
-  if (T->val32) {
-    cudaFree(T->val32);
-    T->val32 = nullptr;
-  }
+  T->val32_stale = true;
   return GP_OK;
 }
 
@@ -246,9 +240,12 @@ __global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restr
     b[i] = __double2float_rn(a[i]);
 }
 
+// FP32 copy of the values, kept at one address (captured solve graphs of the
+// mixed form read it there) and converted again after every value change.
 int csr_make_val32(Csr* A, cudaStream_t s) {
-  if (A->val32) return GP_OK;
-  GP_CUDA(cudaMalloc(&A->val32, std::max<int64_t>(A->nnz, 1) * sizeof(float)));
+  if (A->val32 && !A->val32_stale) return GP_OK;
+  if (!A->val32) GP_CUDA(cudaMalloc(&A->val32, std::max<int64_t>(A->nnz, 1) * sizeof(float)));
+  A->val32_stale = false;
   if (A->nnz) {
     k_to_f32<<<num_sms() * 8, 256, 0, s>>>(A->nnz, A->val, A->val32);
     GP_CHECK_LAUNCH();

@@ -514,8 +514,8 @@ static int setup_sor(Pc* pc, cudaStream_t s) {
   std::vector<int> of, ob, fpos, none;
   GP_TRY(plan(pc->fwd, n, lp, lc, true, s, &of));
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
-  GP_TRY(ell_build(pc->ef, n, of, lp, lc, ls, none, none, none, &fpos));
-  GP_TRY(ell_build(pc->eb, n, ob, up, uc, us, fpos, none, none, nullptr));
+  GP_TRY(ell_build(pc->ef, n, true, of, lp, lc, ls, none, none, none, &fpos));
+  GP_TRY(ell_build(pc->eb, n, false, ob, up, uc, us, fpos, none, none, nullptr));
   if (n) {
     k_sor_diag<<<(n + 255) / 256, 256, 0, s>>>(n, pc->opt.omega, pc->opt.fshift, A->diagpos,
                                                 A->val, pc->idiag, pc->mdiag);
@@ -560,8 +560,8 @@ static int ilu_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
   std::vector<int> of, ob, fpos, none;
   GP_TRY(plan(pc->fwd, n, lp, lc, true, s, &of));
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
-  GP_TRY(ell_build(pc->ef, n, of, lp, lc, ls, P.r, none, none, &fpos));
-  GP_TRY(ell_build(pc->eb, n, ob, up, uc, us, fpos, perm_c, dsl, nullptr));
+  GP_TRY(ell_build(pc->ef, n, true, of, lp, lc, ls, P.r, none, none, &fpos));
+  GP_TRY(ell_build(pc->eb, n, false, ob, up, uc, us, fpos, perm_c, dsl, nullptr));
   GP_TRY(upload(&pc->bi, P.bi, s));
   GP_TRY(upload(&pc->bj, P.bj, s));
   GP_TRY(upload(&pc->bdiag, P.bdiag, s));
@@ -687,8 +687,8 @@ static int icc_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
   GP_TRY(plan(pc->num, n, cptr, crow, true, s));
   GP_TRY(plan(pc->fwd, n, tptr, trow_deps, true, s, &of));
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
-  GP_TRY(ell_build(pc->ef, n, of, tptr, trow_deps, tsl, perm_c, none, dsl, &fpos));
-  GP_TRY(ell_build(pc->eb, n, ob, up, uc, us, fpos, perm_c, none, nullptr));
+  GP_TRY(ell_build(pc->ef, n, true, of, tptr, trow_deps, tsl, perm_c, none, dsl, &fpos));
+  GP_TRY(ell_build(pc->eb, n, false, ob, up, uc, us, fpos, perm_c, none, nullptr));
   GP_TRY(upload(&pc->bi, P.bi, s));
   GP_TRY(upload(&pc->bj, P.bj, s));
   GP_TRY(upload(&pc->bdiag, P.bdiag, s));
@@ -869,16 +869,18 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
                                                   A->val, pc->idiag, pc->mdiag, gate, want);
       k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
       if (pc->ef.ok && pc->eb.ok) {
-        k_ell_refresh_g<<<g, 256, 0, s>>>(gate, want, pc->ef.n, pc->ef.cnt, pc->ef.cslot, A->val,
-                                          pc->ef.coef);
-        k_ell_refresh_g<<<g, 256, 0, s>>>(gate, want, pc->eb.n, pc->eb.cnt, pc->eb.cslot, A->val,
-                                          pc->eb.coef);
+        if (!pc->ef.tiled)
+          k_ell_refresh_g<<<g, 256, 0, s>>>(gate, want, pc->ef.n, pc->ef.cnt, pc->ef.cslot,
+                                            A->val, pc->ef.coef);
+        if (!pc->eb.tiled)
+          k_ell_refresh_g<<<g, 256, 0, s>>>(gate, want, pc->eb.n, pc->eb.cnt, pc->eb.cslot,
+                                            A->val, pc->eb.coef);
         if (fw)
           GP_TRY(ell_sweep(ELL_SOR_F, pc->ef, gate, want, x, y, pc->yf, nullptr, pc->t, nullptr,
-                           pc->idiag, pc->opt.omega, 0, bw ? 0 : 1, tk0, pc->err, s));
+                           pc->idiag, pc->opt.omega, 0, bw ? 0 : 1, tk0, pc->err, A->val, s));
         if (bw)
           GP_TRY(ell_sweep(ELL_SOR_B, pc->eb, gate, want, x, y, pc->yb, pc->yf, nullptr, pc->t,
-                           pc->idiag, pc->opt.omega, fw ? 1 : 0, 1, tk1, pc->err, s));
+                           pc->idiag, pc->opt.omega, fw ? 1 : 0, 1, tk1, pc->err, A->val, s));
         break;
       }
       if (fw)
@@ -896,9 +898,9 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
       k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
       if (pc->ef.ok && pc->eb.ok) {
         GP_TRY(ell_sweep(ELL_ILU_F, pc->ef, gate, want, x, y, pc->yf, nullptr, nullptr, nullptr,
-                         nullptr, 0.0, 0, 0, tk0, pc->err, s));
+                         nullptr, 0.0, 0, 0, tk0, pc->err, pc->ba, s));
         GP_TRY(ell_sweep(ELL_ILU_B, pc->eb, gate, want, x, y, pc->yb, pc->yf, nullptr, nullptr,
-                         nullptr, 0.0, 0, 1, tk1, pc->err, s));
+                         nullptr, 0.0, 0, 1, tk1, pc->err, pc->ba, s));
         break;
       }
       k_ilu_fwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->fwd.order, tk0, pc->bi, pc->bj,
@@ -910,9 +912,9 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
       k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
       if (pc->ef.ok && pc->eb.ok) {
         GP_TRY(ell_sweep(ELL_ICC_F, pc->ef, gate, want, x, y, pc->yf, nullptr, pc->ys, nullptr,
-                         nullptr, 0.0, 0, 0, tk0, pc->err, s));
+                         nullptr, 0.0, 0, 0, tk0, pc->err, pc->ba, s));
         GP_TRY(ell_sweep(ELL_ICC_B, pc->eb, gate, want, x, y, pc->yb, nullptr, nullptr, pc->ys,
-                         nullptr, 0.0, 0, 1, tk1, pc->err, s));
+                         nullptr, 0.0, 0, 1, tk1, pc->err, pc->ba, s));
         break;
       }
       k_icc_fwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->fwd.order, tk0, pc->tptr,

@@ -50,18 +50,36 @@ struct EllSweep {
   int* rowof = nullptr;
   double* coef = nullptr;
   double* dval = nullptr;
+  // Tiled form (gp_sweep.cu, k_tile_sweep): positions grouped in chunks of
+  // consecutive rows of the sweep's natural sequence, each chunk sorted by
+  // the dependency level among its own rows and processed by one warp that
+  // stages the chunk's metadata in shared memory with one bulk copy.  When
+  // `tiled` is set the ELL column arrays above are not allocated.
+  bool tiled = false;
+  int nchunks = 0, C = 0, max_blob = 0, grid = 0;
+  size_t smem = 0;
+  unsigned char* blob = nullptr;  // per chunk: header, level offsets, columns
+  long long* blob_off = nullptr;  // [nchunks + 1] byte offsets into blob
+  int* cstart = nullptr;          // [nchunks + 1] first position of each chunk
+  int internal_pct = 0;           // share of dependencies inside their chunk
 };
 void ell_free(EllSweep& e);
-int ell_build(EllSweep& e, int n, const std::vector<int>& order, const std::vector<int>& dptr,
-              const std::vector<int>& dcol, const std::vector<int>& dsl,
-              const std::vector<int>& in_row, const std::vector<int>& out_row,
-              const std::vector<int>& dslot_row, std::vector<int>* pos_of_row);
+// Lay out one sweep.  forward: dependencies precede each row (ascending
+// processing); otherwise they follow it.  `order` is the level order, used
+// when the sweep is not tiled.
+int ell_build(EllSweep& e, int n, bool forward, const std::vector<int>& order,
+              const std::vector<int>& dptr, const std::vector<int>& dcol,
+              const std::vector<int>& dsl, const std::vector<int>& in_row,
+              const std::vector<int>& out_row, const std::vector<int>& dslot_row,
+              std::vector<int>* pos_of_row);
 int ell_refresh(EllSweep& e, const double* src, cudaStream_t s);
 int sweep_wait_probe(int budget, int set, cudaStream_t s);
+// coefsrc: the array the sweep's coefficient slots index (the factor values
+// for ILU/IC, the matrix values for SOR); the tiled form gathers from it.
 int ell_sweep(int mode, const EllSweep& e, const int* gate, int want, DRef in, DRef out,
               double* val, const double* fval, double* aux, const double* auxin,
               const double* idiag, double omega, int use_t, int write_out, unsigned* tickets,
-              DevErr* err, cudaStream_t s);
+              DevErr* err, const double* coefsrc, cudaStream_t s);
 
 // Host copy of a factor pattern in the reference's layout.
 struct FactorPattern {

@@ -24,6 +24,13 @@ factorisation of A^T is the transpose of that of A in exact arithmetic (the
 ILU(0) conditions -- M = LU with L, U on the pattern and M = A there -- are
 invariant under transposition), so this is the transposed preconditioner.
 
+With `precision="mixed"` both solves are the library's mixed-precision form
+(`gp_mixed_solve`): FP32 FGMRES(restart) preconditioned with the ILU(0) factor
+rounded to FP32, inside FP64 iterative refinement that stops on the true FP64
+residual ||b - A x|| <= rtol ||b||.  The forward solve runs on A and the
+adjoint solve on the device-built A^T with its own ILU(0), so the gradient has
+the accuracy of two FP64 solves to rtol.
+
 torch is plumbing here: tensors hold device memory, the autograd engine calls
 backward; every kernel is the library's.
 """
@@ -113,6 +120,76 @@ class _Solver:
         self.ksp = self.pc = None
 
 
+class _MixedSolver:
+    """One matrix handle with an ILU(0) PC and a mixed-precision solver
+    handle; same interface as `_Solver`."""
+
+    def __init__(self, mat: int, rtol: float, max_outer: int, restart: int,
+                 inner_rtol: float = 1e-4, tri_sweeps: int = 4):
+        self.mat = mat
+        self.pc = None
+        self.h = None
+        self.ksp_type, self.pc_type = "mixed-fgmres", "ilu"
+        self.rtol, self.max_outer, self.restart = rtol, max_outer, restart
+        self.inner_rtol, self.tri_sweeps = inner_rtol, tri_sweeps
+        self.its = 0         # inner FP32 iterations
+        self.passes = 0      # FP64 refinement passes
+        self.reason = 0
+        self.rnorm = 0.0     # true relative residual
+
+    def setup(self, fresh_pattern: bool):
+        st = dev.stream_ptr()
+        if self.pc is None:
+            h = ctypes.c_void_p()
+            check(lib().gp_pc_create(ctypes.byref(h)))
+            self.pc = h.value
+            o = PcOptions()
+            lib().gp_pc_options_default(ctypes.byref(o))
+            o.type = _PC["ilu"]
+            check(lib().gp_pc_set_options(self.pc, ctypes.byref(o)))
+            fresh_pattern = True
+        if fresh_pattern:
+            check(lib().gp_pc_setup(self.pc, self.mat, st))
+        else:
+            check(lib().gp_pc_update_values(self.pc, st))
+        if self.h is None:
+            h = ctypes.c_void_p()
+            check(lib().gp_mixed_create(ctypes.byref(h)))
+            self.h = h.value
+
+    def solve(self, b, x):
+        from .mixed import MixedOptions, MixedResult
+
+        # the refinement pass graph is keyed on the vector addresses
+        if getattr(self, "_bbuf", None) is None or self._bbuf.numel() != b.numel():
+            self._bbuf = b.clone()
+            self._xbuf = b.new_empty(b.shape)
+        else:
+            self._bbuf.copy_(b)
+        o = MixedOptions()
+        lib().gp_mixed_options_default(ctypes.byref(o))
+        o.restart, o.max_outer, o.tri_sweeps = self.restart, self.max_outer, self.tri_sweeps
+        o.rtol, o.inner_rtol = self.rtol, self.inner_rtol
+        res = MixedResult()
+        check(lib().gp_mixed_solve(self.h, self.mat, self.pc, ctypes.byref(o),
+                                   dev.ptr(self._bbuf), dev.ptr(self._xbuf), ctypes.byref(res),
+                                   dev.stream_ptr()))
+        x.copy_(self._xbuf)
+        self.its, self.passes, self.rnorm = int(res.inner_its), int(res.passes), float(res.relres)
+        self.reason = 2 if res.converged else -3
+        if not res.converged:
+            raise SolveError(f"mixed-precision solve stopped after {self.passes} passes "
+                             f"({self.its} inner iterations) at relative residual "
+                             f"{self.rnorm:.3e} > {self.rtol:.1e}")
+
+    def close(self):
+        if self.h is not None:
+            lib().gp_mixed_destroy(self.h)
+        if self.pc is not None:
+            lib().gp_pc_destroy(self.pc)
+        self.h = self.pc = None
+
+
 class SparseSystem:
     """A x = b for a square CSR pattern that stays fixed while its values
     change: the forward solver on A and, built on first use, the adjoint
@@ -120,8 +197,12 @@ class SparseSystem:
 
     def __init__(self, indptr, indices, ksp_type: str = "gmres", pc_type: str = "ilu",
                  rtol: float = 1e-10, atol: float = 1e-50, max_it: int = 10000,
-                 restart: int = 30):
+                 restart: int = 30, precision: str = "fp64"):
         torch = dev.torch()
+        if precision not in ("fp64", "mixed"):
+            raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
+        if precision == "mixed" and pc_type != "ilu":
+            raise NotImplementedError("the mixed-precision solve is preconditioned with ilu")
         self.indptr = np.ascontiguousarray(indptr, dtype=np.int64)
         self.indices = np.ascontiguousarray(indices, dtype=np.int64)
         self.n = len(self.indptr) - 1
@@ -135,10 +216,14 @@ class SparseSystem:
                                   zeros.ctypes.data))
         self._mat = h.value
         self._matT = None
-        cfg = (ksp_type, pc_type, rtol, atol, max_it, restart)
-        self.forward_solver = _Solver(self._mat, *cfg)
+        if precision == "mixed":
+            self._make = lambda mat: _MixedSolver(mat, rtol, max(1, max_it // restart), restart)
+        else:
+            cfg = (ksp_type, pc_type, rtol, atol, max_it, restart)
+            self._make = lambda mat: _Solver(mat, *cfg)
+        self.precision = precision
+        self.forward_solver = self._make(self._mat)
         self.adjoint_solver = None
-        self._cfg = cfg
         self._version = 0          # bumped by every set_values
         self._adjoint_version = -1
         self._fwd_version = -1
@@ -192,7 +277,7 @@ class SparseSystem:
             h = ctypes.c_void_p()
             check(lib().gp_mat_transpose(self._mat, ctypes.byref(h), st))
             self._matT = h.value
-            self.adjoint_solver = _Solver(self._matT, *self._cfg)
+            self.adjoint_solver = self._make(self._matT)
             fresh = True
         elif self._adjoint_version != self._version:
             check(lib().gp_mat_transpose_values(self._mat, self._matT, st))

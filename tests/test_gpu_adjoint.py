@@ -44,15 +44,16 @@ def test_transpose_matrix_on_the_device():
     np.testing.assert_allclose(a.T @ lam.cpu().numpy(), g.cpu().numpy(), rtol=0, atol=1e-8)
 
 
-@pytest.mark.parametrize("kt,pt,rtol,tol", [("gmres", "ilu", 1e-13, 1e-8),
-                                            ("bcgs", "jacobi", 1e-12, 1e-6)])
-def test_gradient_matches_the_dense_fp64_gradient(kt, pt, rtol, tol):
+@pytest.mark.parametrize("kt,pt,rtol,tol,prec", [("gmres", "ilu", 1e-13, 1e-8, "fp64"),
+                                                 ("bcgs", "jacobi", 1e-12, 1e-6, "fp64"),
+                                                 ("gmres", "ilu", 1e-13, 1e-8, "mixed")])
+def test_gradient_matches_the_dense_fp64_gradient(kt, pt, rtol, tol, prec):
     import torch
     from mojopetsc4py.adjoint import SparseSystem, sparse_solve
 
     ip, ix, v, b, u_obs = case()
     n = len(b)
-    sysm = SparseSystem(ip, ix, ksp_type=kt, pc_type=pt, rtol=rtol)
+    sysm = SparseSystem(ip, ix, ksp_type=kt, pc_type=pt, rtol=rtol, precision=prec)
     vals = torch.tensor(v, device="cuda", requires_grad=True)
     bt = torch.tensor(b, device="cuda", requires_grad=True)
     uo = torch.tensor(u_obs, device="cuda")
@@ -110,3 +111,27 @@ def test_gradient_matches_central_finite_differences():
         fd = (loss_of(v, torch.tensor(bp, device="cuda"))
               - loss_of(v, torch.tensor(bm, device="cuda"))) / (2 * h)
         assert abs(fd - gb[i]) <= 1e-4 * abs(gb[i]) + 1e-9, (i, fd, gb[i])
+
+
+def test_mixed_precision_solves_follow_value_changes():
+    """The mixed form keeps its FP32 values, factor and captured pass at fixed
+    addresses: after every value change both the forward and the adjoint
+    solve must meet rtol on the true FP64 residual of the new matrix."""
+    import torch
+    from mojopetsc4py.adjoint import SparseSystem
+
+    ip, ix, v, b, _ = case(k=24)
+    n = len(b)
+    sysm = SparseSystem(ip, ix, rtol=1e-11, precision="mixed")
+    bt = torch.tensor(b, device="cuda")
+    g = torch.tensor(np.random.default_rng(2).normal(size=n), device="cuda")
+    for scale in (1.0, 1.7, 0.6):
+        vs = v * scale * (1.0 + 0.05 * np.sin(np.arange(len(v))))
+        sysm.set_values(torch.tensor(vs, device="cuda"))
+        a = dense(ip, ix, vs, n)
+        u = sysm.solve(bt).cpu().numpy()
+        assert np.linalg.norm(a @ u - b) <= 1e-11 * np.linalg.norm(b) * 1.01
+        lam = sysm.solve_transpose(g).cpu().numpy()
+        gh = g.cpu().numpy()
+        assert np.linalg.norm(a.T @ lam - gh) <= 1e-11 * np.linalg.norm(gh) * 1.01
+        assert sysm.forward_solver.passes >= 1 and sysm.adjoint_solver.passes >= 1
