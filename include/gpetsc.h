@@ -186,6 +186,26 @@ int gp_pc_setup(gp_pc pc, gp_mat A, void *stream);
  * `spins` polls) or on a ready one (set = 1: GP_OK).  No counterpart in the
  * reference (its sweeps are sequential host loops). */
 int gp_wait_probe(int32_t spins, int32_t set, void *stream);
+/* Form of the ILU/IC/SOR triangular sweeps laid out by later PC set-ups.
+ *   tiles = 0       the level-ordered form: rows in dependency-level order,
+ *                   32 rows a warp, each value passed through L2.
+ *   tiles = 1       (default) the chunked form where a simulated schedule
+ *                   of it beats the level-ordered form: runs of consecutive
+ *                   rows, each chunk walked level by level by one warp with
+ *                   in-chunk values in shared memory.
+ *   tile_rows > 0   force the chunked form with this many rows a chunk (it
+ *                   still falls back when the chunk does not fit in shared
+ *                   memory); 0 lets the set-up choose.
+ * Both forms give bit-identical results.  Default from GPETSC_SWEEP_TILES
+ * and GPETSC_TILE_ROWS.  No counterpart in the reference (its sweeps are
+ * sequential host loops). */
+int gp_set_sweep_form(int32_t tiles, int32_t tile_rows);
+/* Which form a set-up PC's sweeps got: for the forward (which = 0) and the
+ * backward (which = 1) sweep, tiled (0/1), rows per chunk and chunks (0 when
+ * not tiled), and the number of dependency levels.  No counterpart in the
+ * reference. */
+int gp_pc_sweep_form(gp_pc pc, int32_t which, int32_t *tiled, int32_t *rows_per_chunk,
+                     int32_t *chunks);
 /* Same pattern, new operator values: redo only the numeric phase (ILU/IC factor
  * values on the device, Jacobi diagonals) in the arrays of the last set-up;
  * solver graphs captured with this PC stay valid. */

@@ -255,6 +255,24 @@ int gp_wait_probe(int32_t spins, int32_t set, void* stream) {
   GUARD(gp::sweep_wait_probe(spins, set, S(stream)));
 }
 
+int gp_set_sweep_form(int32_t tiles, int32_t tile_rows) {
+  if (tiles < 0 || tiles > 1 || tile_rows < 0 || tile_rows > 8192)
+    return bad("gp_set_sweep_form: tiles must be 0 or 1 and tile_rows in [0, 8192]");
+  gp::set_sweep_form(tiles, tile_rows);
+  return GP_OK;
+}
+
+int gp_pc_sweep_form(gp_pc pc, int32_t which, int32_t* tiled, int32_t* rows_per_chunk,
+                     int32_t* chunks) {
+  if (!pc || !tiled || !rows_per_chunk || !chunks || (which != 0 && which != 1))
+    return bad("gp_pc_sweep_form: null argument or which not 0/1");
+  const gp::EllSweep& e = which == 0 ? pc->pc->ef : pc->pc->eb;
+  *tiled = e.tiled ? 1 : 0;
+  *rows_per_chunk = e.tiled ? e.rows_per_chunk : 0;
+  *chunks = e.tiled ? e.nchunks : 0;
+  return GP_OK;
+}
+
 int gp_pc_update_values(gp_pc pc, void* stream) {
   if (!pc) return bad("gp_pc_update_values: null argument");
   GUARD(gp::pc_update_values(pc->pc, S(stream)));

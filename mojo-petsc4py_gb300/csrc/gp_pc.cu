@@ -514,8 +514,8 @@ static int setup_sor(Pc* pc, cudaStream_t s) {
   std::vector<int> of, ob, fpos, none;
   GP_TRY(plan(pc->fwd, n, lp, lc, true, s, &of));
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
-  GP_TRY(ell_build(pc->ef, n, true, of, lp, lc, ls, none, none, none, &fpos));
-  GP_TRY(ell_build(pc->eb, n, false, ob, up, uc, us, fpos, none, none, nullptr));
+  GP_TRY(ell_build(pc->ef, ELL_SOR_F, n, true, of, lp, lc, ls, none, none, none, &fpos));
+  GP_TRY(ell_build(pc->eb, ELL_SOR_B, n, false, ob, up, uc, us, fpos, none, none, nullptr));
   if (n) {
     k_sor_diag<<<(n + 255) / 256, 256, 0, s>>>(n, pc->opt.omega, pc->opt.fshift, A->diagpos,
                                                 A->val, pc->idiag, pc->mdiag);
@@ -560,8 +560,8 @@ static int ilu_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
   std::vector<int> of, ob, fpos, none;
   GP_TRY(plan(pc->fwd, n, lp, lc, true, s, &of));
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
-  GP_TRY(ell_build(pc->ef, n, true, of, lp, lc, ls, P.r, none, none, &fpos));
-  GP_TRY(ell_build(pc->eb, n, false, ob, up, uc, us, fpos, perm_c, dsl, nullptr));
+  GP_TRY(ell_build(pc->ef, ELL_ILU_F, n, true, of, lp, lc, ls, P.r, none, none, &fpos));
+  GP_TRY(ell_build(pc->eb, ELL_ILU_B, n, false, ob, up, uc, us, fpos, perm_c, dsl, nullptr));
   GP_TRY(upload(&pc->bi, P.bi, s));
   GP_TRY(upload(&pc->bj, P.bj, s));
   GP_TRY(upload(&pc->bdiag, P.bdiag, s));
@@ -687,8 +687,8 @@ static int icc_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
   GP_TRY(plan(pc->num, n, cptr, crow, true, s));
   GP_TRY(plan(pc->fwd, n, tptr, trow_deps, true, s, &of));
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
-  GP_TRY(ell_build(pc->ef, n, true, of, tptr, trow_deps, tsl, perm_c, none, dsl, &fpos));
-  GP_TRY(ell_build(pc->eb, n, false, ob, up, uc, us, fpos, perm_c, none, nullptr));
+  GP_TRY(ell_build(pc->ef, ELL_ICC_F, n, true, of, tptr, trow_deps, tsl, perm_c, none, dsl, &fpos));
+  GP_TRY(ell_build(pc->eb, ELL_ICC_B, n, false, ob, up, uc, us, fpos, perm_c, none, nullptr));
   GP_TRY(upload(&pc->bi, P.bi, s));
   GP_TRY(upload(&pc->bj, P.bj, s));
   GP_TRY(upload(&pc->bdiag, P.bdiag, s));

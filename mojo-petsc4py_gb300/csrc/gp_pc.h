@@ -54,26 +54,31 @@ struct EllSweep {
   // consecutive rows of the sweep's natural sequence, each chunk sorted by
   // the dependency level among its own rows and processed by one warp that
   // stages the chunk's metadata in shared memory with one bulk copy.  When
-  // `tiled` is set the ELL column arrays above are not allocated.
+  // `tiled` is set the ELL columns above are not allocated: every index the
+  // tiled kernel reads is in the blob.
   bool tiled = false;
   int nchunks = 0, C = 0, max_blob = 0, grid = 0;
   size_t smem = 0;
   unsigned char* blob = nullptr;  // per chunk: header, level offsets, columns
   long long* blob_off = nullptr;  // [nchunks + 1] byte offsets into blob
   int* cstart = nullptr;          // [nchunks + 1] first position of each chunk
-  int internal_pct = 0;           // share of dependencies inside their chunk
+  double est_us = 0.0;            // simulated duration of one tiled sweep
+  int rows_per_chunk = 0;         // chunk size of the tiled layout
 };
 void ell_free(EllSweep& e);
 // Lay out one sweep.  forward: dependencies precede each row (ascending
 // processing); otherwise they follow it.  `order` is the level order, used
 // when the sweep is not tiled.
-int ell_build(EllSweep& e, int n, bool forward, const std::vector<int>& order,
+// mode: the EllMode of the kernel that will run the sweep.
+int ell_build(EllSweep& e, int mode, int n, bool forward, const std::vector<int>& order,
               const std::vector<int>& dptr, const std::vector<int>& dcol,
               const std::vector<int>& dsl, const std::vector<int>& in_row,
               const std::vector<int>& out_row, const std::vector<int>& dslot_row,
               std::vector<int>* pos_of_row);
 int ell_refresh(EllSweep& e, const double* src, cudaStream_t s);
 int sweep_wait_probe(int budget, int set, cudaStream_t s);
+// Sweep form of later set-ups (gp_set_sweep_form).
+void set_sweep_form(int tiles, int tile_rows);
 // coefsrc: the array the sweep's coefficient slots index (the factor values
 // for ILU/IC, the matrix values for SOR); the tiled form gathers from it.
 int ell_sweep(int mode, const EllSweep& e, const int* gate, int want, DRef in, DRef out,

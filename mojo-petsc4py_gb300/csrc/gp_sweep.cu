@@ -13,7 +13,12 @@
 // reference's slot order with rounded multiplies and adds, so the result is
 // bit-identical to the sequential loop.
 #include <algorithm>
+#include <cstdint>
+#include <cstdio>
 #include <cstdlib>
+#include <functional>
+#include <map>
+#include <queue>
 #include <string>
 #include <vector>
 
@@ -25,7 +30,7 @@ constexpr int kEllBlock = 256;
 constexpr int kEllSpin = 1 << 22;
 constexpr int kTileSmemMax = 227 * 1024;  // dynamic shared memory limit of one CTA
 constexpr int kTileBulkPiece = 16384;     // bytes per bulk copy instruction
-constexpr int kTileHeader = 4;            // ints: levels, rows, padded levels+1, padded rows
+constexpr int kTileHeader = 8;  // ints: levels, rows, Lp, Cp, external entries, Ep, Cp8, 0
 
 __device__ __forceinline__ double ell_wait(const double* p, DevErr* err, int where,
                                            int budget = kEllSpin, int sleep_after = 64,
@@ -41,6 +46,17 @@ __device__ __forceinline__ double ell_wait(const double* p, DevErr* err, int whe
   return __longlong_as_double(0x7FF8000000000000LL);
 }
 
+
+// One dependency term of a sweep row: sum - c*v (ILU, SOR) or sum + c*v (IC),
+// rounded after the product and after the sum (the reference's arithmetic),
+// or fused into one rounding in the FMA arithmetic.
+template <int MODE, bool FMA>
+__device__ __forceinline__ double sweep_term(double sum, double c, double v) {
+  if constexpr (MODE == ELL_ICC_F || MODE == ELL_ICC_B)
+    return FMA ? __fma_rn(c, v, sum) : add(sum, mul(c, v));
+  else
+    return FMA ? __fma_rn(-c, v, sum) : sub(sum, mul(c, v));
+}
 
 struct EllArgs {
   int n;
@@ -68,11 +84,11 @@ struct EllArgs {
 // GPETSC_SWEEP_SLEEP_AFTER, GPETSC_SWEEP_SLEEP_NS override the defaults).
 struct SweepTuning {
   int ctas_per_sm = 2, sleep_after = 8, sleep_ns = 20;  // best of a scan on ICC(0), 128^3
-  int tiles = 0;                // GPETSC_SWEEP_TILES=1: chunked form where it applies
-  int tile_smem = 110 * 1024;   // GPETSC_TILE_SMEM: shared memory budget of one chunk
-  int tile_rows = 0;            // GPETSC_TILE_ROWS: rows per chunk (0: from the budget)
+  int tiles = 1;                // GPETSC_SWEEP_TILES=0: always the level-ordered ELL form
+  int tile_smem = kTileSmemMax;  // GPETSC_TILE_SMEM: shared memory cap of one chunk
+  int tile_rows = 0;            // GPETSC_TILE_ROWS: force this chunk size (0: chosen)
 };
-static const SweepTuning& sweep_tuning() {
+static SweepTuning& sweep_tuning_mut() {
   static SweepTuning t = [] {
     SweepTuning v;
     auto env = [](const char* k, int d) {
@@ -89,8 +105,14 @@ static const SweepTuning& sweep_tuning() {
   }();
   return t;
 }
+static const SweepTuning& sweep_tuning() { return sweep_tuning_mut(); }
 
-template <int MODE, int WMAX>
+void set_sweep_form(int tiles, int tile_rows) {
+  sweep_tuning_mut().tiles = tiles != 0;
+  sweep_tuning_mut().tile_rows = std::max(0, std::min(8192, tile_rows));
+}
+
+template <int MODE, int WMAX, bool FMA>
 __global__ void __launch_bounds__(kEllBlock) k_ell_sweep(const int* gate, int want, EllArgs a,
                                                          DRef inr, DRef outr) {
   if (gated_off(gate, want)) return;
@@ -104,11 +126,13 @@ __global__ void __launch_bounds__(kEllBlock) k_ell_sweep(const int* gate, int wa
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= (unsigned)n) break;
     const int p = (int)base + lane;
+    // ---- everything that does not wait
+    int c = 0;
+    int dp[WMAX];
+    double cf[WMAX];
+    double sum = 0.0, dv = 0.0, yf = 0.0;
     if (p < n) {
-      // ---- everything that does not wait
-      const int c = a.cnt[p];
-      int dp[WMAX];
-      double cf[WMAX];
+      c = a.cnt[p];
 #pragma unroll
       for (int e = 0; e < WMAX; e++) {
         if (e < c) {
@@ -116,8 +140,6 @@ __global__ void __launch_bounds__(kEllBlock) k_ell_sweep(const int* gate, int wa
           cf[e] = a.coef[(size_t)e * n + p];
         }
       }
-      double sum;
-      double dv = 0.0, yf = 0.0;
       if constexpr (MODE == ELL_ILU_F || MODE == ELL_ICC_F) {
         sum = in[a.in_idx[p]];
         if (MODE == ELL_ICC_F) dv = a.dval[p];
@@ -135,52 +157,69 @@ __global__ void __launch_bounds__(kEllBlock) k_ell_sweep(const int* gate, int wa
         yf = a.use_t ? a.fval[fp] : 0.0;
         dv = a.idiag[a.rowof[p]];
       }
-      // ---- the dependency chain, in the reference's slot order.  Every
-      // dependency is loaded once up front (independent loads, one L2 round
-      // trip for all of them); only those still pending are polled.
-      unsigned long long bits[WMAX];
+    }
+    // ---- the dependency chain, in the reference's slot order.  Every
+    // dependency is loaded up front (independent loads).  Then the warp
+    // polls in lock step, but each lane folds its dependencies in order as
+    // they arrive and stores its result in the same step as its last one:
+    // no lane waits for the slowest of its warp before publishing.
+    unsigned long long bits[WMAX];
 #pragma unroll
-      for (int e = 0; e < WMAX; e++)
-        if (e < c) bits[e] = ld_relaxed_bits(&a.val[dp[e]]);
+    for (int e = 0; e < WMAX; e++)
+      if (e < c) bits[e] = ld_relaxed_bits(&a.val[dp[e]]);
+    int ecur = 0;
+    bool fin = p >= n;
+    for (int spins = 0;; spins++) {
+      if (!fin) {
 #pragma unroll
-      for (int e = 0; e < WMAX; e++) {
-        if (e < c) {
-          const double v =
-              bits[e] != kPending
-                  ? __longlong_as_double((long long)bits[e])
-                  : ell_wait(&a.val[dp[e]], a.err, 20 + MODE, kEllSpin, a.sleep_after,
-                             a.sleep_ns);
-          if constexpr (MODE == ELL_ICC_F || MODE == ELL_ICC_B)
-            sum = add(sum, mul(cf[e], v));
-          else
-            sum = sub(sum, mul(cf[e], v));
+        for (int e = 0; e < WMAX; e++) {
+          if (e < c && e == ecur && bits[e] != kPending) {
+            sum = sweep_term<MODE, FMA>(sum, cf[e], __longlong_as_double((long long)bits[e]));
+            ecur++;
+          }
+        }
+        if (ecur >= c) {
+          if constexpr (MODE == ELL_ILU_F) {
+            st_relaxed(&a.val[p], sum);
+          } else if constexpr (MODE == ELL_ILU_B) {
+            const double y = mul(sum, dv);
+            out[a.out_idx[p]] = y;
+            st_relaxed(&a.val[p], y);
+          } else if constexpr (MODE == ELL_ICC_F) {
+            a.aux[p] = mul(sum, dv);
+            st_relaxed(&a.val[p], sum);
+          } else if constexpr (MODE == ELL_ICC_B) {
+            out[a.out_idx[p]] = sum;
+            st_relaxed(&a.val[p], sum);
+          } else if constexpr (MODE == ELL_SOR_F) {
+            a.aux[p] = sum;
+            const double y = mul(sum, dv);
+            if (a.out_idx) out[a.rowof[p]] = y;
+            st_relaxed(&a.val[p], y);
+          } else {
+            const double y = a.use_t ? add(mul(a.om1, yf), mul(sum, dv)) : mul(sum, dv);
+            out[a.rowof[p]] = y;
+            st_relaxed(&a.val[p], y);
+          }
+          fin = true;
         }
       }
-      // ---- results
-      if constexpr (MODE == ELL_ILU_F) {
-        st_relaxed(&a.val[p], sum);
-      } else if constexpr (MODE == ELL_ILU_B) {
-        const double y = mul(sum, dv);
-        out[a.out_idx[p]] = y;
-        st_relaxed(&a.val[p], y);
-      } else if constexpr (MODE == ELL_ICC_F) {
-        a.aux[p] = mul(sum, dv);
-        st_relaxed(&a.val[p], sum);
-      } else if constexpr (MODE == ELL_ICC_B) {
-        out[a.out_idx[p]] = sum;
-        st_relaxed(&a.val[p], sum);
-      } else if constexpr (MODE == ELL_SOR_F) {
-        a.aux[p] = sum;
-        const double y = mul(sum, dv);
-        if (a.out_idx) out[a.rowof[p]] = y;
-        st_relaxed(&a.val[p], y);
-      } else {
-        const double y = a.use_t ? add(mul(a.om1, yf), mul(sum, dv)) : mul(sum, dv);
-        out[a.rowof[p]] = y;
-        st_relaxed(&a.val[p], y);
+      if (__all_sync(0xffffffffu, fin)) break;
+      if (!fin) {
+        if (spins >= kEllSpin) {
+          // a dependency never arrived: record it and fold quiet NaNs
+          if (atomicCAS(&a.err->code, 0, GP_ERR_TIMEOUT) == 0) a.err->where = 20 + MODE;
+#pragma unroll
+          for (int e = 0; e < WMAX; e++)
+            if (e < c && bits[e] == kPending) bits[e] = 0x7FF8000000000000ULL;
+        } else {
+          if (spins >= a.sleep_after && a.sleep_ns > 0) __nanosleep(a.sleep_ns);
+#pragma unroll
+          for (int e = 0; e < WMAX; e++)
+            if (e < c && e >= ecur && bits[e] == kPending) bits[e] = ld_relaxed_bits(&a.val[dp[e]]);
+        }
       }
     }
-    __syncwarp();
   }
   if (lane == 0) {
     const unsigned total = gridDim.x * (blockDim.x / 32);
@@ -195,20 +234,37 @@ __global__ void __launch_bounds__(kEllBlock) k_ell_sweep(const int* gate, int wa
 //
 // A chunk is a run of consecutive rows of the sweep's natural sequence
 // (ascending rows forward, descending backward).  Inside a chunk its rows are
-// sorted by their dependency level counted over the chunk's own rows, so one
-// warp can walk the chunk level by level: dependencies inside the chunk are
-// read from shared memory (one __syncwarp between levels), dependencies in
-// earlier chunks are polled in the global value-as-flag array.  On a grid
+// sorted by their dependency level counted over the chunk's own rows.  One
+// CTA of two warps takes a chunk: the compute warp walks it level by level,
+// reading dependencies inside the chunk from shared memory (one __syncwarp
+// between levels), while the fetch warp polls the chunk's dependencies in
+// earlier chunks (the global value-as-flag array) in level order, several in
+// flight per lane, and drops each into a shared-memory value-as-flag slot.
+// The compute warp therefore pays an L2 round trip only where a value from
+// another chunk arrives just in time, not on every level.  On a grid
 // numbered in natural order most dependencies are neighbours inside the same
-// chunk, so the global round trip is paid once per chunk boundary instead of
-// once per level.  Each chunk's metadata (level offsets, dependency counts,
-// positions, coefficient slots, input/output indices) is one contiguous blob
-// staged with cp.async.bulk on an mbarrier; coefficients, diagonals and
-// right-hand sides are then gathered by the warp.  Chunks are handed out by a
-// ticket in order, and a chunk waits only on earlier chunks, which running
+// chunk; the chunk size is chosen on the host by simulating the schedule
+// (tile_choose), so chunk boundaries fall where the dependency chains break.
+// Each chunk's level offsets, dependency counts, encoded dependencies,
+// output indices and external positions form one contiguous blob staged
+// with cp.async.bulk on an mbarrier; coefficients, diagonals and right-hand
+// sides are gathered from global memory meanwhile.  Chunks are handed out by
+// a ticket in order and a chunk waits only on earlier chunks, which running
 // CTAs already hold, so the sweep cannot deadlock on CTAs that are not yet
 // resident.  Per row the arithmetic and the dependency order are those of
 // k_ell_sweep, so the results are bit-identical.
+
+constexpr int kTileThreads = 128;  // warp 0 computes, warps 1-3 fetch; all gather
+constexpr int kTileNoDep = -32768;  // int16 dependency code of an absent slot
+
+// Per-row shared-memory columns a mode needs beyond coefficients, values and
+// sums: a diagonal factor, and for the SOR backward half the forward value.
+__host__ __device__ constexpr bool tile_has_dv(int mode) {
+  return mode == ELL_ILU_B || mode == ELL_ICC_F || mode == ELL_SOR_F || mode == ELL_SOR_B;
+}
+__host__ __device__ constexpr int tile_extra_cols(int mode) {
+  return (tile_has_dv(mode) ? 1 : 0) + (mode == ELL_SOR_B ? 1 : 0);
+}
 
 struct TileArgs {
   int nchunks, W, C, max_blob;
@@ -261,33 +317,57 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
       : "memory");
 }
 
-template <int MODE, int WMAX>
-__global__ void __launch_bounds__(32) k_tile_sweep(const int* gate, int want, EllArgs a,
-                                                   TileArgs t, DRef inr, DRef outr) {
+__device__ __forceinline__ void st_shared_volatile(double* p, double v) {
+  *reinterpret_cast<volatile double*>(p) = v;
+}
+
+// Wait for a shared-memory value-as-flag slot written by the fetch warp.  The
+// fetch warp's own waits are bounded and write a NaN when they give up, so
+// this budget only guards against a slot that is never written.
+__device__ __forceinline__ double smem_wait(const double* p, DevErr* err, int where) {
+  volatile const unsigned long long* q = reinterpret_cast<volatile const unsigned long long*>(p);
+  unsigned long long b = *q;
+  for (int i = 0; b == kPending && i < (1 << 26); i++) {
+    if (i >= 64) __nanosleep(32);
+    b = *q;
+  }
+  if (b == kPending) {
+    if (atomicCAS(&err->code, 0, GP_ERR_TIMEOUT) == 0) err->where = where;
+    return __longlong_as_double(0x7FF8000000000000LL);
+  }
+  return __longlong_as_double((long long)b);
+}
+
+template <int MODE, int WMAX, bool FMA>
+__global__ void __launch_bounds__(kTileThreads, 1) k_tile_sweep(const int* gate, int want,
+                                                                EllArgs a, TileArgs t, DRef inr,
+                                                                DRef outr) {
   if (gated_off(gate, want)) return;
   extern __shared__ __align__(16) unsigned char sm[];
   unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm);
+  unsigned* s_chunk = reinterpret_cast<unsigned*>(sm + 8);
   int* blob = reinterpret_cast<int*>(sm + 16);
   const int W = t.W, C = t.C;
   double* s_cf = reinterpret_cast<double*>(sm + 16 + t.max_blob);  // [W][C]
   double* s_val = s_cf + (size_t)(W > 0 ? W : 1) * C;
   double* s_sum = s_val + C;
-  double* s_dv = s_sum + C;
-  double* s_yf = s_dv + C;
+  double* s_dv = s_sum + C;                            // modes with a diagonal
+  double* s_yf = s_dv + (tile_has_dv(MODE) ? C : 0);   // SOR backward only
+  double* s_ext = s_yf + (MODE == ELL_SOR_B ? C : 0);  // external values, value-as-flag
   const double* __restrict__ in = inr.get();
   double* __restrict__ out = outr.get();
-  const int lane = threadIdx.x;
-  if (lane == 0) mbar_init(bar, 1);
-  __syncwarp();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) mbar_init(bar, 1);
+  __syncthreads();
   unsigned parity = 0;
   for (;;) {
-    unsigned c = 0;
-    if (lane == 0) c = atomicAdd(&a.tickets[0], 1u);
-    c = __shfl_sync(0xffffffffu, c, 0);
+    if (tid == 0) *s_chunk = atomicAdd(&a.tickets[0], 1u);
+    __syncthreads();
+    const unsigned c = *s_chunk;
     if (c >= (unsigned)t.nchunks) break;
     const int cs = t.cstart[c];
-    // ---- stage the chunk's blob (one elected lane issues the bulk copies)
-    if (lane == 0) {
+    // ---- stage the chunk's blob (one elected thread issues the bulk copies)
+    if (tid == 0) {
       const long long b0 = t.blob_off[c];
       const unsigned bytes = (unsigned)(t.blob_off[c + 1] - b0);
       // earlier generic reads of the blob area come before the async writes
@@ -297,109 +377,154 @@ __global__ void __launch_bounds__(32) k_tile_sweep(const int* gate, int want, El
         bulk_g2s(sm + 16 + off, t.blob + b0 + off, min((unsigned)kTileBulkPiece, bytes - off),
                  bar);
     }
-    if (!mbar_wait(bar, parity, kEllSpin)) {
-      if (lane == 0 && atomicCAS(&a.err->code, 0, GP_ERR_TIMEOUT) == 0) a.err->where = 30 + MODE;
-      // let the copies in flight land before the CTA leaves
-      mbar_wait(bar, parity, kEllSpin);
-      break;
+    const bool staged = mbar_wait(bar, parity, kEllSpin);
+    if (!staged) {
+      if (lane == 0 && atomicCAS(&a.err->code, 0, GP_ERR_TIMEOUT) == 0) a.err->where = 40 + MODE;
+      mbar_wait(bar, parity, kEllSpin);  // let the copies in flight land before leaving
     }
     parity ^= 1u;
-    const int nl = blob[0], Cc = blob[1], Lp = blob[2], Cp = blob[3];
+    if (__syncthreads_or(!staged)) break;
+    const int nl = blob[0], Cc = blob[1], Lp = blob[2], Cp = blob[3], Ne = blob[4];
+    const int Ep = blob[5], Cp8 = blob[6];
     const int* lo = blob + kTileHeader;
-    const int* cnt = lo + Lp;
-    const int* dep = cnt + Cp;
-    const int* csl = dep + (size_t)W * Cp;
-    const int* iidx = csl + (size_t)W * Cp;
-    const int* oidx = iidx + Cp;
-    const int* rowof = oidx + Cp;
-    const int* dsl = rowof + Cp;
+    const int* oidx = lo + Lp;
+    const int* iidx = oidx + Cp;
+    const int* gidx = iidx + Cp;
+    const int* csl = gidx + Cp;
+    const int* epos = csl + (size_t)W * Cp;
+    const short* dep = reinterpret_cast<const short*>(epos + Ep);  // [W][Cp8]
     // ---- gathers that do not wait: coefficients, initial sums, diagonals
 #pragma unroll 4
-    for (int r = lane; r < Cc; r += 32) {
-      const int cn = cnt[r];
+    for (int r = tid; r < Cc; r += kTileThreads) {
 #pragma unroll
-      for (int e = 0; e < WMAX; e++)
-        if (e < cn) s_cf[(size_t)e * C + r] = t.coefsrc[csl[(size_t)e * Cp + r]];
+      for (int e = 0; e < WMAX; e++) {
+        if (e < W) {
+          const int slot = csl[(size_t)e * Cp + r];
+          if (slot >= 0) s_cf[(size_t)e * C + r] = t.coefsrc[slot];
+        }
+      }
       if constexpr (MODE == ELL_ILU_F) {
         s_sum[r] = in[iidx[r]];
       } else if constexpr (MODE == ELL_ICC_F) {
         s_sum[r] = in[iidx[r]];
-        s_dv[r] = t.coefsrc[dsl[r]];
+        s_dv[r] = t.coefsrc[gidx[r]];
       } else if constexpr (MODE == ELL_ILU_B) {
         s_sum[r] = a.fval[iidx[r]];
-        s_dv[r] = t.coefsrc[dsl[r]];
+        s_dv[r] = t.coefsrc[gidx[r]];
       } else if constexpr (MODE == ELL_ICC_B) {
         s_sum[r] = a.auxin[iidx[r]];
       } else if constexpr (MODE == ELL_SOR_F) {
-        s_sum[r] = in[rowof[r]];
-        s_dv[r] = a.idiag[rowof[r]];
+        s_sum[r] = in[gidx[r]];
+        s_dv[r] = a.idiag[gidx[r]];
       } else {  // ELL_SOR_B
         const int fp = iidx[r];
-        s_sum[r] = a.use_t ? a.auxin[fp] : in[rowof[r]];
+        s_sum[r] = a.use_t ? a.auxin[fp] : in[gidx[r]];
         s_yf[r] = a.use_t ? a.fval[fp] : 0.0;
-        s_dv[r] = a.idiag[rowof[r]];
+        s_dv[r] = a.idiag[gidx[r]];
       }
     }
-    __syncwarp();
-    // ---- the chunk's levels
-    for (int l = 0; l < nl; l++) {
-      const int r1 = lo[l + 1];
-      for (int r = lo[l] + lane; r < r1; r += 32) {
-        const int p = cs + r;
-        const int cn = cnt[r];
-        int dp[WMAX];
-        unsigned long long bits[WMAX];
-#pragma unroll
-        for (int e = 0; e < WMAX; e++) {
-          if (e < cn) {
-            dp[e] = dep[(size_t)e * Cp + r];
-            bits[e] = dp[e] < cs ? ld_relaxed_bits(&a.val[dp[e]]) : 0ull;
+    const double pend = __longlong_as_double((long long)kPending);
+    for (int k = tid; k < Ne; k += kTileThreads) s_ext[k] = pend;
+    __syncthreads();
+    if (warp > 0) {
+      // ---- fetch: external dependencies in level order.  Each lane follows
+      // two strided streams of the list and stores each value the moment it
+      // sees it, so no value waits for another lane's.
+      const int f = tid - 32, nf = kTileThreads - 32;
+      int k1 = f, k2 = f + nf;
+      int sp1 = 0, sp2 = 0;
+      for (;;) {
+        const bool a1 = k1 < Ne, a2 = k2 < Ne;
+        if (!__any_sync(0xffffffffu, a1 || a2)) break;
+        const unsigned long long b1 = a1 ? ld_relaxed_bits(&a.val[epos[k1]]) : 0ull;
+        const unsigned long long b2 = a2 ? ld_relaxed_bits(&a.val[epos[k2]]) : 0ull;
+        bool idle = true;
+        if (a1) {
+          if (b1 != kPending || ++sp1 > kEllSpin) {
+            if (b1 == kPending && atomicCAS(&a.err->code, 0, GP_ERR_TIMEOUT) == 0)
+              a.err->where = 30 + MODE;
+            st_shared_volatile(&s_ext[k1], b1 != kPending ? __longlong_as_double((long long)b1)
+                                                          : __longlong_as_double(0x7FF8000000000000LL));
+            k1 += 2 * nf;
+            sp1 = 0;
+            idle = false;
           }
         }
-        double sum = s_sum[r];
-#pragma unroll
-        for (int e = 0; e < WMAX; e++) {
-          if (e < cn) {
-            double v;
-            if (dp[e] >= cs)
-              v = s_val[dp[e] - cs];
-            else if (bits[e] != kPending)
-              v = __longlong_as_double((long long)bits[e]);
-            else
-              v = ell_wait(&a.val[dp[e]], a.err, 30 + MODE, kEllSpin, a.sleep_after, a.sleep_ns);
-            if constexpr (MODE == ELL_ICC_F || MODE == ELL_ICC_B)
-              sum = add(sum, mul(s_cf[(size_t)e * C + r], v));
-            else
-              sum = sub(sum, mul(s_cf[(size_t)e * C + r], v));
+        if (a2) {
+          if (b2 != kPending || ++sp2 > kEllSpin) {
+            if (b2 == kPending && atomicCAS(&a.err->code, 0, GP_ERR_TIMEOUT) == 0)
+              a.err->where = 30 + MODE;
+            st_shared_volatile(&s_ext[k2], b2 != kPending ? __longlong_as_double((long long)b2)
+                                                          : __longlong_as_double(0x7FF8000000000000LL));
+            k2 += 2 * nf;
+            sp2 = 0;
+            idle = false;
           }
         }
-        double res;
-        if constexpr (MODE == ELL_ILU_F) {
-          res = sum;
-        } else if constexpr (MODE == ELL_ILU_B) {
-          res = mul(sum, s_dv[r]);
-          out[oidx[r]] = res;
-        } else if constexpr (MODE == ELL_ICC_F) {
-          a.aux[p] = mul(sum, s_dv[r]);
-          res = sum;
-        } else if constexpr (MODE == ELL_ICC_B) {
-          res = sum;
-          out[oidx[r]] = res;
-        } else if constexpr (MODE == ELL_SOR_F) {
-          a.aux[p] = sum;
-          res = mul(sum, s_dv[r]);
-          if (a.write_out) out[rowof[r]] = res;
-        } else {
-          res = a.use_t ? add(mul(a.om1, s_yf[r]), mul(sum, s_dv[r])) : mul(sum, s_dv[r]);
-          out[rowof[r]] = res;
-        }
-        s_val[r] = res;
-        st_relaxed(&a.val[p], res);
+        if (idle && a.sleep_ns > 0 && (sp1 >= a.sleep_after || sp2 >= a.sleep_after))
+          __nanosleep(a.sleep_ns);
       }
-      __syncwarp();
+    } else {
+      // ---- compute: the chunk's levels; the next level's bounds are read
+      // one level ahead, and each row loads all its operands before the sum
+      int b0 = lo[0], b1 = nl > 0 ? lo[1] : 0;
+      for (int l = 0; l < nl; l++) {
+        const int b2 = l + 2 <= nl ? lo[l + 2] : 0;
+        for (int r = b0 + lane; r < b1; r += 32) {
+          int dd[WMAX];
+          double cf[WMAX], v[WMAX];
+#pragma unroll
+          for (int e = 0; e < WMAX; e++) dd[e] = e < W ? dep[(size_t)e * Cp8 + r] : kTileNoDep;
+#pragma unroll
+          for (int e = 0; e < WMAX; e++) {
+            if (dd[e] != kTileNoDep) {
+              cf[e] = s_cf[(size_t)e * C + r];
+              v[e] = dd[e] >= 0
+                         ? s_val[dd[e]]
+                         : *reinterpret_cast<volatile const double*>(&s_ext[-dd[e] - 1]);
+            }
+          }
+          double sum = s_sum[r];
+#pragma unroll
+          for (int e = 0; e < WMAX; e++) {
+            if (dd[e] != kTileNoDep) {
+              if (dd[e] < 0 && __double_as_longlong(v[e]) == (long long)kPending)
+                v[e] = smem_wait(&s_ext[-dd[e] - 1], a.err, 50 + MODE);
+              sum = sweep_term<MODE, FMA>(sum, cf[e], v[e]);
+            }
+          }
+          const int p = cs + r;
+          double res;
+          if constexpr (MODE == ELL_ILU_F) {
+            res = sum;
+          } else if constexpr (MODE == ELL_ILU_B) {
+            res = mul(sum, s_dv[r]);
+            out[oidx[r]] = res;
+          } else if constexpr (MODE == ELL_ICC_F) {
+            a.aux[p] = mul(sum, s_dv[r]);
+            res = sum;
+          } else if constexpr (MODE == ELL_ICC_B) {
+            res = sum;
+            out[oidx[r]] = res;
+          } else if constexpr (MODE == ELL_SOR_F) {
+            a.aux[p] = sum;
+            res = mul(sum, s_dv[r]);
+            if (a.write_out) out[oidx[r]] = res;
+          } else {
+            res = a.use_t ? add(mul(a.om1, s_yf[r]), mul(sum, s_dv[r])) : mul(sum, s_dv[r]);
+            out[oidx[r]] = res;
+          }
+          s_val[r] = res;
+          st_relaxed(&a.val[p], res);
+        }
+        __syncwarp();
+        b0 = b1;
+        b1 = b2;
+      }
     }
+    __syncthreads();
   }
-  if (lane == 0) {
+  if (tid == 0) {
     if (atomic_add_acq_rel(&a.tickets[1], 1u) == gridDim.x - 1) {
       a.tickets[0] = 0u;
       a.tickets[1] = 0u;
@@ -448,40 +573,47 @@ void ell_free(EllSweep& e) {
 // rows (backward).  Chunk c holds sequence entries [c*C, (c+1)*C); inside it,
 // rows are sorted (stably) by their level over dependencies inside the chunk.
 struct TilePlan {
+  int C = 0;
   std::vector<int> order;    // position -> row
   std::vector<int> cstart;   // [nchunks + 1]
   std::vector<int> lvl_ptr;  // [nchunks + 1] into lvl_off
   std::vector<int> lvl_off;  // per chunk: level offsets relative to its start (levels + 1)
-  long long internal = 0, total = 0;
+  int max_ext = 0, max_levels = 0;
+  size_t smem = 0;
+  double est_us = 0.0;
 };
+
+static int round4(int v) { return (v + 3) & ~3; }
 
 static void tile_order(int n, const std::vector<int>& dptr, const std::vector<int>& dcol,
                        bool forward, int C, TilePlan& tp) {
   const int nch = (n + C - 1) / C;
+  tp.C = C;
   tp.order.assign(n, 0);
   tp.cstart.assign(nch + 1, 0);
   tp.lvl_ptr.assign(nch + 1, 0);
   tp.lvl_off.clear();
-  tp.internal = tp.total = 0;
+  tp.max_ext = tp.max_levels = 0;
   std::vector<int> lev(C), cnt;
   auto row_of = [&](int q) { return forward ? q : n - 1 - q; };
   for (int c = 0; c < nch; c++) {
     const int q0 = c * C, q1 = std::min(n, q0 + C);
-    int maxl = 0;
+    int maxl = 0, next = 0;
     for (int q = q0; q < q1; q++) {
       const int i = row_of(q);
       int l = 0;
       for (int e = dptr[i]; e < dptr[i + 1]; e++) {
         const int qj = forward ? dcol[e] : n - 1 - dcol[e];
-        tp.total++;
-        if (qj >= q0) {
-          tp.internal++;
+        if (qj >= q0)
           l = std::max(l, lev[qj - q0] + 1);
-        }
+        else
+          next++;
       }
       lev[q - q0] = l;
       maxl = std::max(maxl, l);
     }
+    tp.max_ext = std::max(tp.max_ext, next);
+    tp.max_levels = std::max(tp.max_levels, maxl + 1);
     cnt.assign(maxl + 2, 0);
     for (int q = q0; q < q1; q++) cnt[lev[q - q0] + 1]++;
     for (int l = 0; l <= maxl; l++) cnt[l + 1] += cnt[l];
@@ -494,59 +626,199 @@ static void tile_order(int n, const std::vector<int>& dptr, const std::vector<in
   tp.lvl_ptr[nch] = (int)tp.lvl_off.size();
 }
 
-static int round4(int v) { return (v + 3) & ~3; }
+static int round8(int v) { return (v + 7) & ~7; }
 
-// The per-chunk blobs of a tiled sweep (layout read by k_tile_sweep):
-// header {levels, rows, Lp, Cp}, level offsets [Lp], then [Cp] columns:
-// count, dependency positions x W, coefficient slots x W, input index,
-// output index, row, diagonal slot.
-static int tile_upload(EllSweep& e, const TilePlan& tp, int W, const std::vector<int>& cnt,
-                       const std::vector<int>& dep, const std::vector<int>& cs,
-                       const std::vector<int>& in, const std::vector<int>& out,
-                       const std::vector<int>& ds, const std::vector<int>& rowof) {
+// Bytes of one chunk's blob: header, level offsets, then int32 columns
+// (output index, input index, diagonal or row index, W coefficient slots),
+// the external positions, and the W int16 dependency columns.
+static int tile_blob_bytes(int levels, int rows, int ext, int W) {
+  return 4 * (kTileHeader + round4(levels + 1) + round4(rows) * (3 + W) + round4(ext)) +
+         2 * W * round8(rows);
+}
+
+static size_t tile_smem_bytes(int mode, int C, int max_levels, int max_ext, int W) {
+  const int C4 = round4(C);
+  return 16 + (size_t)tile_blob_bytes(max_levels, C, max_ext, W) +
+         8 * ((size_t)(std::max(W, 1) + 2 + tile_extra_cols(mode)) * C4 + (size_t)max_ext);
+}
+
+// Schedule model of the two sweep forms, in microseconds, fitted to GB300
+// measurements of ILU(0)/IC(0)/SOR sweeps on 2-D and 3-D grids (128^3,
+// 96^3, 256^2; within ~12%): one level of a chunk on the compute warp (its
+// FP64 chain is ~64 cycles an operation), the hand-off of a value between
+// CTAs through L2, the staging of a chunk, and one dependency level of the
+// level-ordered ELL form.  Tiles are used when the simulated schedule is
+// below 0.8 of the level-ordered estimate.
+struct TileModel {
+  double level = 0.4, handoff = 0.8, stage = 20.0, ell_level = 1.25;
+};
+
+// Simulated duration of a tiled sweep: chunks are taken in order by the
+// first of `resident` CTAs to become free; a level of a chunk ends one level
+// time after the later of the previous level and the arrival of its rows'
+// values from earlier chunks.
+static double tile_estimate(int n, const std::vector<int>& dptr, const std::vector<int>& dcol,
+                            bool forward, const TilePlan& tp, int resident,
+                            std::vector<double>& trow) {
+  const TileModel m;
+  const int nch = (int)tp.cstart.size() - 1;
+  trow.assign(n, 0.0);
+  std::priority_queue<double, std::vector<double>, std::greater<double>> freeq;
+  for (int r = 0; r < std::max(1, std::min(resident, nch)); r++) freeq.push(0.0);
+  double end = 0.0;
+  for (int c = 0; c < nch; c++) {
+    double t = freeq.top() + m.stage;
+    freeq.pop();
+    const int p0 = tp.cstart[c];
+    const int* lo = tp.lvl_off.data() + tp.lvl_ptr[c];
+    const int nl = tp.lvl_ptr[c + 1] - tp.lvl_ptr[c] - 1;
+    for (int l = 0; l < nl; l++) {
+      double ready = t;
+      for (int r = lo[l]; r < lo[l + 1]; r++) {
+        const int i = tp.order[p0 + r];
+        for (int e = dptr[i]; e < dptr[i + 1]; e++) {
+          const int qj = forward ? dcol[e] : n - 1 - dcol[e];
+          if (qj < p0) ready = std::max(ready, trow[dcol[e]] + m.handoff);
+        }
+      }
+      t = ready + m.level * ((lo[l + 1] - lo[l] + 31) / 32);
+      for (int r = lo[l]; r < lo[l + 1]; r++) trow[tp.order[p0 + r]] = t;
+    }
+    freeq.push(t);
+    end = std::max(end, t);
+  }
+  return end;
+}
+
+static int tile_blocks_per_sm(size_t smem) {
+  const size_t per_sm = 228 * 1024;  // shared memory of one SM, 1 KB reserved per CTA
+  return (int)std::min<size_t>(2048 / kTileThreads, per_sm / (smem + 1024));
+}
+
+// Pick the chunk size whose simulated schedule is shortest, or none when the
+// level-ordered form is expected to be faster.  Candidates: powers of two and
+// multiples of the most frequent dependency distances (a grid's line and
+// plane lengths), within the shared-memory budget.
+static bool tile_choose(int mode, int n, int W, const std::vector<int>& dptr,
+                        const std::vector<int>& dcol, bool forward, int nlevels,
+                        const SweepTuning& tu, TilePlan& best, int* considered) {
+  std::vector<int> cands;
+  if (tu.tile_rows) {
+    cands.push_back(tu.tile_rows);
+  } else {
+    for (int c = 64; c <= 8192; c *= 2) cands.push_back(c);
+    std::map<int, long long> hist;
+    const int scan = std::min(n, 1 << 18);
+    for (int i = 0; i < scan; i++)
+      for (int e = dptr[i]; e < dptr[i + 1]; e++) {
+        const int d = std::abs(i - dcol[e]);
+        if (d >= 8) hist[d]++;
+      }
+    std::vector<std::pair<long long, int>> top;
+    for (auto& kv : hist) top.push_back({kv.second, kv.first});
+    std::sort(top.rbegin(), top.rend());
+    for (size_t k = 0; k < top.size() && k < 2; k++)
+      for (int mlt : {1, 2, 3, 4, 6, 8, 12, 16})
+        if ((long long)top[k].second * mlt <= 8192) cands.push_back(top[k].second * mlt);
+    std::sort(cands.begin(), cands.end());
+    cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
+  }
+  const TileModel m;
+  const double ell_us = m.ell_level * std::max(nlevels, 1);
+  std::vector<double> trow;
+  bool found = false;
+  *considered = 0;
+  for (int C : cands) {
+    if (C < 8 || C > n * 2) continue;
+    TilePlan tp;
+    tile_order(n, dptr, dcol, forward, std::min(C, n), tp);
+    tp.smem = tile_smem_bytes(mode, tp.C, tp.max_levels, tp.max_ext, W);
+    if (tp.smem > (size_t)tu.tile_smem) continue;
+    const int bps = tile_blocks_per_sm(tp.smem);
+    if (bps < 1) continue;
+    tp.est_us = tile_estimate(n, dptr, dcol, forward, tp, bps * num_sms(), trow);
+    (*considered)++;
+    if (!found || tp.est_us < best.est_us) {
+      best = std::move(tp);
+      found = true;
+    }
+  }
+  return found && (tu.tile_rows || best.est_us < 0.8 * ell_us);
+}
+
+// The per-chunk blobs of a tiled sweep (layout read by k_tile_sweep).
+// Dependencies inside the chunk are encoded as the local index of the row,
+// those in earlier chunks as -(k + 1), k the slot of the chunk's external list.
+static int tile_upload(EllSweep& e, int mode, const TilePlan& tp, int W,
+                       const std::vector<int>& cnt, const std::vector<int>& dep,
+                       const std::vector<int>& cs, const std::vector<int>& in,
+                       const std::vector<int>& out, const std::vector<int>& ds,
+                       bool has_ds, const std::vector<int>& rowof) {
   const int n = e.n;
   const int nch = (int)tp.cstart.size() - 1;
   std::vector<long long> off(nch + 1, 0);
-  int maxC = 0, max_blob = 0;
+  std::vector<int> next(nch, 0);
+  int maxC = 0, max_blob = 0, max_ext = 0;
   for (int c = 0; c < nch; c++) {
-    const int Cc = tp.cstart[c + 1] - tp.cstart[c];
+    const int p0 = tp.cstart[c], Cc = tp.cstart[c + 1] - p0;
     const int nl = tp.lvl_ptr[c + 1] - tp.lvl_ptr[c] - 1;
-    const int ints = kTileHeader + round4(nl + 1) + round4(Cc) * (5 + 2 * W);
-    off[c + 1] = off[c] + (long long)ints * 4;
+    for (int r = 0; r < Cc; r++)
+      for (int q = 0; q < cnt[p0 + r]; q++) next[c] += dep[(size_t)q * n + p0 + r] < p0;
+    const int bytes = tile_blob_bytes(nl, Cc, next[c], W);
+    off[c + 1] = off[c] + bytes;
     maxC = std::max(maxC, Cc);
-    max_blob = std::max(max_blob, ints * 4);
+    max_blob = std::max(max_blob, bytes);
+    max_ext = std::max(max_ext, next[c]);
   }
   std::vector<int> blob((size_t)(off[nch] / 4), 0);
   for (int c = 0; c < nch; c++) {
     int* b = blob.data() + off[c] / 4;
     const int p0 = tp.cstart[c], Cc = tp.cstart[c + 1] - p0;
     const int nl = tp.lvl_ptr[c + 1] - tp.lvl_ptr[c] - 1;
-    const int Lp = round4(nl + 1), Cp = round4(Cc);
+    const int Lp = round4(nl + 1), Cp = round4(Cc), Ne = next[c], Ep = round4(Ne);
+    const int Cp8 = round8(Cc);
     b[0] = nl;
     b[1] = Cc;
     b[2] = Lp;
     b[3] = Cp;
+    b[4] = Ne;
+    b[5] = Ep;
+    b[6] = Cp8;
     int* lo = b + kTileHeader;
     for (int l = 0; l <= nl; l++) lo[l] = tp.lvl_off[tp.lvl_ptr[c] + l];
-    int* col = lo + Lp;
+    int* oidx = lo + Lp;
+    int* iidx = oidx + Cp;
+    int* gidx = iidx + Cp;
+    int* csl = gidx + Cp;
+    int* epos = csl + (size_t)W * Cp;
+    int16_t* depc = reinterpret_cast<int16_t*>(epos + Ep);
+    for (size_t q = 0; q < (size_t)W * Cp8; q++) depc[q] = (int16_t)kTileNoDep;
+    for (size_t q = 0; q < (size_t)W * Cp; q++) csl[q] = -1;
+    int k = 0;
     for (int r = 0; r < Cc; r++) {
       const int p = p0 + r;
-      col[r] = cnt[p];
+      iidx[r] = in[p];
+      gidx[r] = has_ds ? ds[p] : rowof[p];
       for (int q = 0; q < cnt[p]; q++) {
-        col[(size_t)(1 + q) * Cp + r] = dep[(size_t)q * n + p];
-        col[(size_t)(1 + W + q) * Cp + r] = cs[(size_t)q * n + p];
+        csl[(size_t)q * Cp + r] = cs[(size_t)q * n + p];
+        const int dp = dep[(size_t)q * n + p];
+        if (dp >= p0) {
+          depc[(size_t)q * Cp8 + r] = (int16_t)(dp - p0);
+        } else {
+          epos[k] = dp;
+          depc[(size_t)q * Cp8 + r] = (int16_t)(-(k + 1));
+          k++;
+        }
       }
-      col[(size_t)(1 + 2 * W) * Cp + r] = in[p];
-      col[(size_t)(2 + 2 * W) * Cp + r] = out[p];
-      col[(size_t)(3 + 2 * W) * Cp + r] = rowof[p];
-      col[(size_t)(4 + 2 * W) * Cp + r] = ds[p];
+      oidx[r] = out[p] >= 0 ? out[p] : rowof[p];
     }
   }
   e.nchunks = nch;
   e.C = round4(maxC);
   e.max_blob = max_blob;
-  e.smem = 16 + (size_t)max_blob + (size_t)(std::max(W, 1) + 4) * e.C * sizeof(double);
-  if (e.smem > (size_t)kTileSmemMax) return GP_ERR_UNSUPPORTED;
+  e.smem = 16 + (size_t)max_blob +
+           8 * ((size_t)(std::max(W, 1) + 2 + tile_extra_cols(mode)) * e.C + (size_t)max_ext);
+  if (e.smem > (size_t)kTileSmemMax || maxC > 32767 || max_ext > 32767) return GP_ERR_UNSUPPORTED;
   GP_TRY(up(&e.blob, std::vector<unsigned char>((unsigned char*)blob.data(),
                                                 (unsigned char*)(blob.data() + blob.size()))));
   GP_TRY(up(&e.blob_off, off));
@@ -554,16 +826,29 @@ static int tile_upload(EllSweep& e, const TilePlan& tp, int W, const std::vector
   return GP_OK;
 }
 
-// Shared memory per chunk row of a tiled sweep with W dependencies a row.
-static int tile_row_bytes(int W) { return 4 * (5 + 2 * W) + 8 * (std::max(W, 1) + 4) + 4; }
-
 static void tile_kernel_attrs(int W, const EllSweep& e, int* blocks_per_sm);
+
+// Number of dependency levels of a sweep (the level-ordered form's depth).
+static int sweep_levels(int n, const std::vector<int>& dptr, const std::vector<int>& dcol,
+                        bool forward) {
+  std::vector<int> lev(n, 0);
+  int maxl = 0;
+  for (int s = 0; s < n; s++) {
+    const int i = forward ? s : n - 1 - s;
+    int l = 0;
+    for (int e = dptr[i]; e < dptr[i + 1]; e++) l = std::max(l, lev[dcol[e]] + 1);
+    lev[i] = l;
+    maxl = std::max(maxl, l);
+  }
+  return n ? maxl + 1 : 0;
+}
 
 // Lay out one sweep.  dptr/dcol/dsl: each row's dependencies (rows) and their
 // coefficient slots, in the reference's order.  The positions follow the
-// chunked order of the tiled form when most dependencies fall inside their
-// chunk, else `order` (dependency levels).
-static int ell_build_impl(EllSweep& e, int n, bool forward, const std::vector<int>& order_in,
+// chunked order of the tiled form when its simulated schedule beats the
+// level-ordered form, else `order` (dependency levels).
+static int ell_build_impl(EllSweep& e, int mode, int n, bool forward,
+                          const std::vector<int>& order_in,
                           const std::vector<int>& dptr, const std::vector<int>& dcol,
                           const std::vector<int>& dsl, const std::vector<int>& in_row,
                           const std::vector<int>& out_row, const std::vector<int>& dslot_row,
@@ -577,12 +862,10 @@ static int ell_build_impl(EllSweep& e, int n, bool forward, const std::vector<in
   const SweepTuning& tu = sweep_tuning();
   TilePlan tp;
   bool tiled = false;
+  int considered = 0, nlev = 0;
   if (tu.tiles && allow_tiles && n > 0) {
-    int C = tu.tile_rows ? tu.tile_rows : (tu.tile_smem / tile_row_bytes(W)) / 32 * 32;
-    C = std::max(32, std::min(C, 8192));
-    tile_order(n, dptr, dcol, forward, C, tp);
-    tiled = tp.total == 0 || 2 * tp.internal >= tp.total;
-    e.internal_pct = tp.total ? (int)(100 * tp.internal / tp.total) : 100;
+    nlev = sweep_levels(n, dptr, dcol, forward);
+    tiled = tile_choose(mode, n, W, dptr, dcol, forward, nlev, tu, tp, &considered);
   }
   const std::vector<int>& order = tiled ? tp.order : order_in;
   std::vector<int> pos(n);
@@ -603,29 +886,33 @@ static int ell_build_impl(EllSweep& e, int n, bool forward, const std::vector<in
     if (!dslot_row.empty()) ds[p] = dslot_row[i];
   }
   if (tiled) {
-    int st = tile_upload(e, tp, W, cnt, dep, cs, in, out, ds, rowof);
-    if (st == GP_OK) {
-      int bps = 0;
-      tile_kernel_attrs(W, e, &bps);
-      if (bps > 0) {
-        e.grid = std::min(e.nchunks, bps * num_sms());
-        e.tiled = true;
-        if (pos_of_row) *pos_of_row = pos;
-        e.ok = true;
-        return GP_OK;
-      }
-    } else if (st != GP_ERR_UNSUPPORTED) {
-      return st;
+    int st = tile_upload(e, mode, tp, W, cnt, dep, cs, in, out, ds, !dslot_row.empty(), rowof);
+    int bps = 0;
+    if (st == GP_OK) tile_kernel_attrs(W, e, &bps);
+    if (st == GP_OK && bps > 0) {
+      e.grid = std::min(e.nchunks, bps * num_sms());
+      e.tiled = true;
+      e.est_us = tp.est_us;
+      e.rows_per_chunk = tp.C;
+      if (std::getenv("GPETSC_SWEEP_VERBOSE"))
+        std::fprintf(stderr,
+                     "gpetsc sweep: n=%d W=%d levels=%d tiled rows/chunk=%d chunks=%d "
+                     "smem=%zu ctas/sm=%d grid=%d est=%.0fus (level order %.0fus, %d sizes)\n",
+                     n, W, nlev, tp.C, e.nchunks, e.smem, bps, e.grid, tp.est_us,
+                     TileModel().ell_level * nlev, considered);
+      if (pos_of_row) *pos_of_row = pos;
+      e.ok = true;
+      return GP_OK;
     }
+    if (st != GP_OK && st != GP_ERR_UNSUPPORTED) return st;
     // the tiled form does not fit: fall back to the level order
-    for (void* q : {(void*)e.blob, (void*)e.blob_off, (void*)e.cstart})
-      if (q) cudaFree(q);
-    e.blob = nullptr;
-    e.blob_off = nullptr;
-    e.cstart = nullptr;
-    return ell_build_impl(e, n, forward, order_in, dptr, dcol, dsl, in_row, out_row,
+    ell_free(e);
+    return ell_build_impl(e, mode, n, forward, order_in, dptr, dcol, dsl, in_row, out_row,
                           dslot_row, pos_of_row, false);
   }
+  if (std::getenv("GPETSC_SWEEP_VERBOSE") && tu.tiles && allow_tiles && n > 0)
+    std::fprintf(stderr, "gpetsc sweep: n=%d W=%d levels=%d level order (%d chunk sizes tried)\n",
+                 n, W, nlev, considered);
   GP_TRY(up(&e.cnt, cnt));
   GP_TRY(up(&e.dep, dep));
   GP_TRY(up(&e.cslot, cs));
@@ -640,13 +927,13 @@ static int ell_build_impl(EllSweep& e, int n, bool forward, const std::vector<in
   return GP_OK;
 }
 
-int ell_build(EllSweep& e, int n, bool forward, const std::vector<int>& order,
+int ell_build(EllSweep& e, int mode, int n, bool forward, const std::vector<int>& order,
               const std::vector<int>& dptr, const std::vector<int>& dcol,
               const std::vector<int>& dsl, const std::vector<int>& in_row,
               const std::vector<int>& out_row, const std::vector<int>& dslot_row,
               std::vector<int>* pos_of_row) {
-  return ell_build_impl(e, n, forward, order, dptr, dcol, dsl, in_row, out_row, dslot_row,
-                        pos_of_row, true);
+  return ell_build_impl(e, mode, n, forward, order, dptr, dcol, dsl, in_row, out_row,
+                        dslot_row, pos_of_row, true);
 }
 
 // Run the wait once on a pending flag (set = 0) or a ready one (set = 1) and
@@ -696,26 +983,32 @@ int ell_refresh(EllSweep& e, const double* src, cudaStream_t s) {
   return GP_OK;
 }
 
+template <int WMAX, bool FMA>
+static void tile_set_attrs() {
+  auto set = [](const void* f) {
+    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmemMax);
+  };
+  set((const void*)k_tile_sweep<ELL_ILU_F, WMAX, FMA>);
+  set((const void*)k_tile_sweep<ELL_ILU_B, WMAX, FMA>);
+  set((const void*)k_tile_sweep<ELL_ICC_F, WMAX, FMA>);
+  set((const void*)k_tile_sweep<ELL_ICC_B, WMAX, FMA>);
+  set((const void*)k_tile_sweep<ELL_SOR_F, WMAX, FMA>);
+  set((const void*)k_tile_sweep<ELL_SOR_B, WMAX, FMA>);
+}
+
 template <int WMAX>
 static void tile_attrs_w(const EllSweep& e, int* bps) {
   static unsigned long long done = 0;  // one bit per device
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 64 && !(done >> dev & 1ull)) {
-    auto set = [](const void* f) {
-      cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmemMax);
-    };
-    set((const void*)k_tile_sweep<ELL_ILU_F, WMAX>);
-    set((const void*)k_tile_sweep<ELL_ILU_B, WMAX>);
-    set((const void*)k_tile_sweep<ELL_ICC_F, WMAX>);
-    set((const void*)k_tile_sweep<ELL_ICC_B, WMAX>);
-    set((const void*)k_tile_sweep<ELL_SOR_F, WMAX>);
-    set((const void*)k_tile_sweep<ELL_SOR_B, WMAX>);
+    tile_set_attrs<WMAX, false>();
+    tile_set_attrs<WMAX, true>();
     done |= 1ull << dev;
   }
   *bps = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_tile_sweep<ELL_SOR_B, WMAX>, 32,
-                                                    e.smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_tile_sweep<ELL_SOR_B, WMAX, false>,
+                                                    kTileThreads, e.smem) != cudaSuccess)
     *bps = 0;
   cudaGetLastError();
 }
@@ -729,28 +1022,46 @@ static void tile_kernel_attrs(int W, const EllSweep& e, int* bps) {
     tile_attrs_w<kEllMaxW>(e, bps);
 }
 
+template <int MODE, bool FMA>
+static void launch_tile_a(const EllSweep& e, const int* gate, int want, EllArgs a, TileArgs t,
+                          DRef in, DRef out, cudaStream_t s) {
+  const int g = std::max(1, e.grid);
+  if (e.W <= 4)
+    k_tile_sweep<MODE, 4, FMA><<<g, kTileThreads, e.smem, s>>>(gate, want, a, t, in, out);
+  else if (e.W <= 8)
+    k_tile_sweep<MODE, 8, FMA><<<g, kTileThreads, e.smem, s>>>(gate, want, a, t, in, out);
+  else
+    k_tile_sweep<MODE, kEllMaxW, FMA><<<g, kTileThreads, e.smem, s>>>(gate, want, a, t, in, out);
+}
+
 template <int MODE>
 static void launch_tile(const EllSweep& e, const int* gate, int want, EllArgs a, TileArgs t,
                         DRef in, DRef out, cudaStream_t s) {
-  const int g = std::max(1, e.grid);
-  if (e.W <= 4)
-    k_tile_sweep<MODE, 4><<<g, 32, e.smem, s>>>(gate, want, a, t, in, out);
-  else if (e.W <= 8)
-    k_tile_sweep<MODE, 8><<<g, 32, e.smem, s>>>(gate, want, a, t, in, out);
+  if (arith_mode() == kFma)
+    launch_tile_a<MODE, true>(e, gate, want, a, t, in, out, s);
   else
-    k_tile_sweep<MODE, kEllMaxW><<<g, 32, e.smem, s>>>(gate, want, a, t, in, out);
+    launch_tile_a<MODE, false>(e, gate, want, a, t, in, out, s);
+}
+
+template <int MODE, bool FMA>
+static void launch_mode_a(const EllSweep& e, const int* gate, int want, EllArgs a, DRef in,
+                          DRef out, cudaStream_t s) {
+  const int g = num_sms() * sweep_tuning().ctas_per_sm;
+  if (e.W <= 4)
+    k_ell_sweep<MODE, 4, FMA><<<g, kEllBlock, 0, s>>>(gate, want, a, in, out);
+  else if (e.W <= 8)
+    k_ell_sweep<MODE, 8, FMA><<<g, kEllBlock, 0, s>>>(gate, want, a, in, out);
+  else
+    k_ell_sweep<MODE, kEllMaxW, FMA><<<g, kEllBlock, 0, s>>>(gate, want, a, in, out);
 }
 
 template <int MODE>
 static void launch_mode(const EllSweep& e, const int* gate, int want, EllArgs a, DRef in,
                         DRef out, cudaStream_t s) {
-  const int g = num_sms() * sweep_tuning().ctas_per_sm;
-  if (e.W <= 4)
-    k_ell_sweep<MODE, 4><<<g, kEllBlock, 0, s>>>(gate, want, a, in, out);
-  else if (e.W <= 8)
-    k_ell_sweep<MODE, 8><<<g, kEllBlock, 0, s>>>(gate, want, a, in, out);
+  if (arith_mode() == kFma)
+    launch_mode_a<MODE, true>(e, gate, want, a, in, out, s);
   else
-    k_ell_sweep<MODE, kEllMaxW><<<g, kEllBlock, 0, s>>>(gate, want, a, in, out);
+    launch_mode_a<MODE, false>(e, gate, want, a, in, out, s);
 }
 
 int ell_sweep(int mode, const EllSweep& e, const int* gate, int want, DRef in, DRef out,

@@ -104,6 +104,8 @@ GP_SIGNATURES = {
     "gp_pc_setup": ([P, P, P], ctypes.c_int),
     "gp_pc_update_values": ([P, P], ctypes.c_int),
     "gp_wait_probe": ([ctypes.c_int32, ctypes.c_int32, P], ctypes.c_int),
+    "gp_set_sweep_form": ([ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+    "gp_pc_sweep_form": ([P, ctypes.c_int32, P, P, P], ctypes.c_int),
     "gp_pc_apply": ([P, P, P, P], ctypes.c_int),
     "gp_pc_apply_symmetric": ([P, P, P, P], ctypes.c_int),
     "gp_pc_factor_info": ([P, P, P], ctypes.c_int),
@@ -174,6 +176,26 @@ def set_arithmetic(mode: str) -> None:
 
 def get_arithmetic() -> str:
     return {v: k for k, v in ARITHMETIC.items()}[lib().gp_get_arithmetic()]
+
+
+def set_sweep_form(tiles: bool = True, tile_rows: int = 0) -> None:
+    """Form of the ILU/IC/SOR triangular sweeps of later PC set-ups:
+    `tiles=False` keeps the level-ordered form; `tiles=True` (the default)
+    takes the chunked form where its simulated schedule is faster, or with
+    `tile_rows` > 0 forces chunks of that many rows.  Both are bit-identical."""
+    check(lib().gp_set_sweep_form(1 if tiles else 0, int(tile_rows)))
+
+
+def sweep_form(pc_handle) -> dict:
+    """The sweep layout a set-up PC got: per sweep, tiled or not, rows per
+    chunk and chunk count."""
+    out = {}
+    for which, name in ((0, "forward"), (1, "backward")):
+        t, r, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        check(lib().gp_pc_sweep_form(pc_handle, which, ctypes.byref(t), ctypes.byref(r),
+                                     ctypes.byref(c)))
+        out[name] = {"tiled": bool(t.value), "rows_per_chunk": r.value, "chunks": c.value}
+    return out
 
 
 def require_device() -> None:

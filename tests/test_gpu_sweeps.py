@@ -1,0 +1,145 @@
+"""The two forms of the ILU / IC / SOR triangular sweeps against the oracle.
+
+The level-ordered form hands out rows in dependency-level order, 32 to a
+warp; the chunked form gives runs of consecutive rows to one CTA, whose
+compute warp walks the chunk level by level with in-chunk values in shared
+memory while its fetch warps poll the values of earlier chunks.  Both must
+reproduce the reference's sequential sweeps bit for bit in the exact
+arithmetic, whatever the chunk size: chunk sizes that cut grid lines (so a
+dependency chain runs across chunks), tiny chunks, and one chunk holding a
+whole sweep.  In the fused arithmetic both forms fold the same terms with the
+same fused operations, so they agree with each other bit for bit too.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from mojopetsc4py import PETSc, _lib, gallery
+
+pytestmark = pytest.mark.gpu
+
+MATRICES = {
+    "poisson2d_24": lambda: gallery.laplacian_2d(24),
+    "poisson3d_10": lambda: gallery.laplacian_3d(10),
+    "convdiff_9": lambda: gallery.convection_diffusion_3d(9),
+}
+
+# (name, tiles, rows per chunk); 0 rows lets the set-up choose
+FORMS = [
+    ("level-order", False, 0),
+    ("chosen", True, 0),
+    ("chunks-32", True, 32),
+    ("chunks-100", True, 100),   # cuts 24-row lines and 100-row planes
+    ("chunks-777", True, 777),
+    ("one-chunk", True, 1024),
+]
+
+PCS = [
+    ("ilu", {}, {}),
+    ("ilu", {"setFactorLevels": 1}, {"levels": 1}),
+    ("ilu", {"setFactorOrdering": "rcm"}, {"ordering": "rcm"}),
+    ("icc", {}, {}),
+    ("sor", {}, {}),
+    ("sor", {"setSOROmega": 1.2}, {"omega": 1.2}),
+    ("sor", {"setSORSymmetric": False}, {"symmetric": False}),
+]
+
+
+@pytest.fixture(autouse=True)
+def _restore_form():
+    yield
+    _lib.set_sweep_form(True, 0)
+
+
+def _mat(ip, ix, v):
+    n = len(ip) - 1
+    A = PETSc.Mat().createSeqAIJ((n, n))
+    A.setValuesCSR(ip, ix, v)
+    A.assemble()
+    return A
+
+
+def _pc(pt, A, opts):
+    pc = PETSc.PC().create()
+    pc.setType(pt)
+    for k, val in opts.items():
+        getattr(pc, k)(val)
+    pc.setOperators(A)
+    pc.setUp()
+    return pc
+
+
+def _apply(pc, x):
+    y = PETSc.Vec().createSeq(len(x))
+    pc.apply(PETSc.Vec().createWithArray(np.asarray(x, dtype=np.float64)), y)
+    return y.getArray().copy()
+
+
+@pytest.mark.parametrize("form,tiles,rows", FORMS, ids=[f[0] for f in FORMS])
+@pytest.mark.parametrize("pt,gopts,oopts", PCS)
+@pytest.mark.parametrize("name", sorted(MATRICES))
+def test_sweep_forms_bit_exact(name, pt, gopts, oopts, form, tiles, rows):
+    if pt == "icc" and name == "convdiff_9":
+        pytest.skip("IC is for symmetric operators")
+    ip, ix, v = MATRICES[name]()
+    n = len(ip) - 1
+    _lib.set_sweep_form(tiles, rows)
+    pc = _pc(pt, _mat(ip, ix, v), gopts)
+    got = _lib.sweep_form(pc._handle())
+    if rows:
+        # a forced chunk size is taken whenever the chunk fits in shared memory
+        assert got["forward"]["tiled"] and got["backward"]["tiled"], got
+        assert got["forward"]["rows_per_chunk"] == min(rows, n)
+    elif not tiles:
+        assert not got["forward"]["tiled"] and not got["backward"]["tiled"], got
+    x = np.random.default_rng(5).normal(size=n)
+    want = O.OraclePC(pt, ip, ix, v, **oopts).apply(x)
+    np.testing.assert_array_equal(_apply(pc, x), want)
+    # a second apply reuses the sweeps' ticket and flag state
+    x2 = np.random.default_rng(6).normal(size=n)
+    np.testing.assert_array_equal(_apply(pc, x2), O.OraclePC(pt, ip, ix, v, **oopts).apply(x2))
+
+
+@pytest.mark.fma
+@pytest.mark.parametrize("pt", ["ilu", "icc", "sor"])
+def test_fused_forms_agree(pt):
+    ip, ix, v = gallery.laplacian_2d(40)
+    n = len(ip) - 1
+    x = np.random.default_rng(8).normal(size=n)
+    out = []
+    for tiles, rows in ((False, 0), (True, 160), (True, 333)):
+        _lib.set_sweep_form(tiles, rows)
+        out.append(_apply(_pc(pt, _mat(ip, ix, v), {}), x))
+    np.testing.assert_array_equal(out[0], out[1])
+    np.testing.assert_array_equal(out[0], out[2])
+    # and the fused sweeps stay within rounding of the reference's
+    want = O.OraclePC(pt, ip, ix, v).apply(x)
+    np.testing.assert_allclose(out[0], want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
+
+
+@pytest.mark.parametrize("tiles,rows", [(False, 0), (True, 64)])
+def test_solves_match_the_oracle_in_both_forms(tiles, rows):
+    """A whole captured CG+ICC and GMRES+ILU solve on each form: same
+    iteration count and reason as the oracle, iterate to 1e-10."""
+    ip, ix, v = gallery.laplacian_2d(32)
+    n = len(ip) - 1
+    b = np.random.default_rng(5).normal(size=n)
+    _lib.set_sweep_form(tiles, rows)
+    for kt, pt in (("cg", "icc"), ("gmres", "ilu")):
+        A = _mat(ip, ix, v)
+        pc = PETSc.PC().create()
+        pc.setType(pt)
+        pc.setOperators(A)
+        ksp = PETSc.KSP().create()
+        ksp.setPC(pc)
+        ksp.setType(kt)
+        ksp.setOperators(A)
+        ksp.setTolerances(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=2000)
+        x = PETSc.Vec().createSeq(n)
+        ksp.solve(PETSc.Vec().createWithArray(b), x)
+        o = O.solve(kt, ip, ix, v, b, pc_type=pt, rtol=1e-10, atol=1e-50, divtol=1e30,
+                    max_it=2000)
+        assert ksp.getIterationNumber() == o["its"], (kt, pt)
+        assert int(ksp.getConvergedReason()) == o["reason"], (kt, pt)
+        xs = x.getArray()
+        assert np.linalg.norm(xs - o["x"]) <= 1e-10 * np.linalg.norm(o["x"])
