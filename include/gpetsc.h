@@ -165,7 +165,8 @@ typedef struct {
   double fshift;
   int32_t sor_flag;    /* MatSORType bits, default 12|16 */
   int32_t levels;      /* factor levels of fill */
-  int32_t ordering;    /* 0 natural, 1 rcm */
+  int32_t ordering;    /* 0 natural, 1 rcm, 2 multicolour (greedy colouring; not
+                          in the reference, which has natural and rcm) */
   int32_t reserved;
 } gp_pc_options;
 
@@ -269,8 +270,12 @@ int gp_ksp_stats(gp_ksp ksp, int64_t *trips, int64_t *top_kernels, int64_t *body
  * FP64 iterative refinement around an FP32 inner FGMRES(restart) cycle
  * preconditioned with the ILU(0) factor of `pc` (an ILU gp_pc set up on A)
  * in FP32.  tri_sweeps > 0 applies each triangle of the factor with that many
- * Jacobi passes (bandwidth-bound, inexact, tolerated by the flexible method);
- * 0 applies it exactly with the level-scheduled FP64 sweeps.  Each pass runs
+ * passes (inexact, tolerated by the flexible method): with tri_block = 0
+ * point-Jacobi passes (bandwidth-bound); with tri_block != 0 block passes,
+ * each solving runs of tri_block consecutive rows exactly (level by level in
+ * shared memory, -1: length chosen from the matrix) with the couplings between
+ * runs from the previous pass.  tri_sweeps = 0 applies the triangles exactly
+ * with the level-scheduled FP64 sweeps.  Each pass runs
  * one inner cycle to inner_rtol; max_outer caps the passes.  x (device) is
  * overwritten (zero initial guess).  No counterpart in the reference. */
 typedef struct gp_mixed_s *gp_mixed;
@@ -278,7 +283,7 @@ typedef struct {
   int32_t restart;
   int32_t max_outer;
   int32_t tri_sweeps;
-  int32_t reserved;
+  int32_t tri_block;
   double rtol;
   double inner_rtol;
 } gp_mixed_options;

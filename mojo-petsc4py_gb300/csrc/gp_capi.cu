@@ -230,6 +230,8 @@ int gp_pc_set_options(gp_pc pc, const gp_pc_options* o) {
   if (o->type != 0 && o->type != 2 && o->type != 4 && o->type != 5 && o->type != 6)
     return bad("gp_pc_set_options: unknown PC type");
   if (o->levels < 0) return bad("gp_pc_set_options: negative levels");
+  if (o->ordering < 0 || o->ordering > 2)
+    return bad("gp_pc_set_options: ordering must be 0 (natural), 1 (rcm) or 2 (multicolour)");
   gp::PcOptions& d = pc->pc->opt;
   d.type = o->type;
   d.jacobi_type = o->jacobi_type;

@@ -529,6 +529,8 @@ static int perms(Pc* pc, std::vector<int>& r, std::vector<int>& ic) {
   const int n = A->n;
   if (pc->opt.ordering == 1)
     GP_TRY(rcm_order(A->h_rowptr, A->h_colind, n, r));
+  else if (pc->opt.ordering == 2)
+    GP_TRY(color_order(A->h_rowptr, A->h_colind, n, r, nullptr));
   else {
     r.resize(n);
     for (int i = 0; i < n; i++) r[i] = i;

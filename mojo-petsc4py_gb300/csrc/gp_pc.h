@@ -23,7 +23,7 @@ struct PcOptions {
   double fshift = 0.0;
   int sor_flag = 12 | 16;  // LOCAL_SYMMETRIC | ZERO_INITIAL_GUESS
   int levels = 0;
-  int ordering = 0;      // 0 natural, 1 rcm
+  int ordering = 0;      // 0 natural, 1 rcm, 2 multicolour
 };
 
 // Processing plan of one sync-free sweep: rows in dependency-level order and
@@ -170,6 +170,8 @@ int sor_diagonals(Pc* pc, cudaStream_t s);
 // host analysis (gp_pcsetup.cu)
 int rcm_order(const std::vector<int>& rowptr, const std::vector<int>& colind, int n,
               std::vector<int>& perm);
+int color_order(const std::vector<int>& rowptr, const std::vector<int>& colind, int n,
+                std::vector<int>& perm, int* ncolors);
 int ilu_symbolic_rows(const Csr* A, int levels, const std::vector<int>& r,
                       const std::vector<int>& ic,
                       std::vector<std::vector<std::pair<int, int>>>& rows, std::vector<int>& nL);

@@ -52,6 +52,47 @@ int rcm_order(const std::vector<int>& rowptr, const std::vector<int>& colind, in
   return GP_OK;
 }
 
+// Multicolour ordering: greedy colouring of the symmetrised graph in index
+// order (each row takes the smallest colour none of its neighbours has), then
+// the rows colour by colour, ascending within a colour.  A factor in this
+// ordering has one dependency level per colour in each triangular solve (two
+// for a 5- or 7-point stencil), which is what the mixed-precision form's
+// bandwidth-bound triangle passes want: with as many passes as colours they
+// apply the triangles exactly.  No counterpart in the reference (it offers
+// natural and RCM orderings).
+int color_order(const std::vector<int>& rowptr, const std::vector<int>& colind, int n,
+                std::vector<int>& perm, int* ncolors) {
+  std::vector<int> tp(n + 1, 0), tc(rowptr[n]);
+  for (int k = 0; k < rowptr[n]; k++) tp[colind[k] + 1]++;
+  for (int i = 0; i < n; i++) tp[i + 1] += tp[i];
+  std::vector<int> fill(tp.begin(), tp.end() - 1);
+  for (int i = 0; i < n; i++)
+    for (int k = rowptr[i]; k < rowptr[i + 1]; k++) tc[fill[colind[k]]++] = i;
+  std::vector<int> color(n, -1), mark;
+  int nc = 0;
+  for (int i = 0; i < n; i++) {
+    auto see = [&](int j) {
+      if (j != i && color[j] >= 0) mark[color[j]] = i;
+    };
+    for (int k = rowptr[i]; k < rowptr[i + 1]; k++) see(colind[k]);
+    for (int k = tp[i]; k < tp[i + 1]; k++) see(tc[k]);
+    int c = 0;
+    while (c < nc && mark[c] == i) c++;
+    if (c == nc) {
+      nc++;
+      mark.push_back(-1);
+    }
+    color[i] = c;
+  }
+  std::vector<int> start(nc + 1, 0);
+  for (int i = 0; i < n; i++) start[color[i] + 1]++;
+  for (int c = 0; c < nc; c++) start[c + 1] += start[c];
+  perm.assign(n, 0);
+  for (int i = 0; i < n; i++) perm[start[color[i]]++] = i;
+  if (ncolors) *ncolors = nc;
+  return GP_OK;
+}
+
 // Rows of the ILU(levels) pattern: ascending (column, level) pairs of each
 // permuted row, and the count of strictly lower entries in nL.
 int ilu_symbolic_rows(const Csr* A, int levels, const std::vector<int>& r,

@@ -279,6 +279,8 @@ class PC:
         o.sor_flag = self._sor_flag()
         o.levels = int(self._levels)
         o.ordering = 1 if self._ordering == MatOrderingType.RCM else 0
+        if getattr(self, "_multicolor", False):
+            o.ordering = 2
         return o
 
     def setUp(self) -> "PC":

@@ -125,13 +125,13 @@ class _MixedSolver:
     handle; same interface as `_Solver`."""
 
     def __init__(self, mat: int, rtol: float, max_outer: int, restart: int,
-                 inner_rtol: float = 1e-4, tri_sweeps: int = 4):
+                 inner_rtol: float = 1e-4, tri_sweeps: int = None, tri_block: int = None):
         self.mat = mat
         self.pc = None
         self.h = None
         self.ksp_type, self.pc_type = "mixed-fgmres", "ilu"
         self.rtol, self.max_outer, self.restart = rtol, max_outer, restart
-        self.inner_rtol, self.tri_sweeps = inner_rtol, tri_sweeps
+        self.inner_rtol, self.tri_sweeps, self.tri_block = inner_rtol, tri_sweeps, tri_block
         self.its = 0         # inner FP32 iterations
         self.passes = 0      # FP64 refinement passes
         self.reason = 0
@@ -168,7 +168,11 @@ class _MixedSolver:
             self._bbuf.copy_(b)
         o = MixedOptions()
         lib().gp_mixed_options_default(ctypes.byref(o))
-        o.restart, o.max_outer, o.tri_sweeps = self.restart, self.max_outer, self.tri_sweeps
+        o.restart, o.max_outer = self.restart, self.max_outer
+        if self.tri_sweeps is not None:
+            o.tri_sweeps = self.tri_sweeps
+        if self.tri_block is not None:
+            o.tri_block = self.tri_block
         o.rtol, o.inner_rtol = self.rtol, self.inner_rtol
         res = MixedResult()
         check(lib().gp_mixed_solve(self.h, self.mat, self.pc, ctypes.byref(o),

@@ -6,8 +6,11 @@ gp_mixed_*).
     info = solver.solve(b, x, rtol=1e-10)   # b, x: PETSc.Vec
 
 The ILU(0) factor is the plain path's (PC "ilu", same symbolic and numeric
-phase), rounded to FP32; each triangle is applied with `tri_sweeps` Jacobi
-passes (0: the exact level-scheduled FP64 sweeps).
+phase), rounded to FP32; each triangle is applied with `tri_sweeps` passes:
+point-Jacobi passes (`tri_block=0`) or block passes that solve runs of
+`tri_block` consecutive rows exactly and couple the runs through the previous
+pass (`tri_block=-1` picks the run length); `tri_sweeps=0` uses the exact
+level-scheduled FP64 sweeps.
 """
 from __future__ import annotations
 
@@ -20,7 +23,7 @@ from .PETSc import PC
 
 class MixedOptions(ctypes.Structure):
     _fields_ = [("restart", ctypes.c_int32), ("max_outer", ctypes.c_int32),
-                ("tri_sweeps", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("tri_sweeps", ctypes.c_int32), ("tri_block", ctypes.c_int32),
                 ("rtol", ctypes.c_double), ("inner_rtol", ctypes.c_double)]
 
 
@@ -31,12 +34,21 @@ class MixedResult(ctypes.Structure):
 
 
 class MixedSolver:
-    def __init__(self, A, levels: int = 0):
+    """`ordering="multicolor"` factors the inner ILU in a greedy multicolour
+    ordering of the rows (a library extension; the reference has natural and
+    RCM): every triangle then has one dependency level per colour, and
+    `tri_sweeps` equal to the number of colours (two for 5- and 7-point
+    stencils) applies it exactly with bandwidth-bound passes."""
+
+    def __init__(self, A, levels: int = 0, ordering: str = "natural"):
+        if ordering not in ("natural", "multicolor"):
+            raise ValueError(f"ordering must be 'natural' or 'multicolor', not {ordering!r}")
         self.A = A
         self.pc = PC().create()
         self.pc.setType("ilu")
         if levels:
             self.pc.setFactorLevels(levels)
+        self.pc._multicolor = ordering == "multicolor"
         self.pc.setOperators(A)
         h = ctypes.c_void_p()
         check(lib().gp_mixed_create(ctypes.byref(h)))
@@ -49,7 +61,7 @@ class MixedSolver:
             pass
 
     def solve(self, b, x, rtol: float = 1e-10, restart: int = 30, inner_rtol: float = 1e-4,
-              tri_sweeps: int = 4, max_outer: int = 200):
+              tri_sweeps: int = None, max_outer: int = 200, tri_block: int = None):
         """x = A^-1 b with ||b - A x|| <= rtol ||b||; returns a dict with the
         passes, inner iterations, convergence flag and final relative
         residual."""
@@ -63,7 +75,11 @@ class MixedSolver:
         self.pc.setUp()
         o = MixedOptions()
         lib().gp_mixed_options_default(ctypes.byref(o))
-        o.restart, o.max_outer, o.tri_sweeps = int(restart), int(max_outer), int(tri_sweeps)
+        o.restart, o.max_outer = int(restart), int(max_outer)
+        if tri_sweeps is not None:
+            o.tri_sweeps = int(tri_sweeps)
+        if tri_block is not None:
+            o.tri_block = int(tri_block)
         o.rtol, o.inner_rtol = float(rtol), float(inner_rtol)
         res = MixedResult()
         bp = b._dptr() if n else 0

@@ -1,7 +1,8 @@
 """Mixed precision (mojopetsc4py.mixed): FP32 inner FGMRES + ILU(0) inside FP64
-refinement reaches rtol on the true FP64 residual, with the inexact (Jacobi
-pass) and the exact (level-scheduled) triangle application, and agrees with
-the plain FP64 GMRES + ILU(0) solution."""
+refinement reaches rtol on the true FP64 residual, with every form of the
+triangle application (point-Jacobi passes, block passes, the exact
+level-scheduled sweeps, the multicolour factor), and agrees with the plain
+FP64 GMRES + ILU(0) solution."""
 import numpy as np
 import pytest
 
@@ -24,8 +25,15 @@ def true_relres(ip, ix, v, x, b):
     return np.linalg.norm(b - ax) / np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("tri_sweeps", [4, 0])
-def test_refined_solution_meets_rtol_on_the_true_residual(tri_sweeps):
+# (passes per triangle, block rows, ordering): point-Jacobi passes, block
+# passes (chosen and forced run lengths, one cutting grid lines), the exact
+# FP64 sweeps, and the multicolour factor (one pass is exact for two colours)
+FORMS = [(4, 0, "natural"), (2, -1, "natural"), (2, 100, "natural"), (0, 0, "natural"),
+         (1, 0, "multicolor")]
+
+
+@pytest.mark.parametrize("tri_sweeps,tri_block,ordering", FORMS)
+def test_refined_solution_meets_rtol_on_the_true_residual(tri_sweeps, tri_block, ordering):
     from mojopetsc4py.mixed import MixedSolver
 
     ip, ix, v = gallery.convection_diffusion_3d(24)
@@ -33,8 +41,9 @@ def test_refined_solution_meets_rtol_on_the_true_residual(tri_sweeps):
     b = np.random.default_rng(7).uniform(-1, 1, n)
     A = mat(ip, ix, v)
     x = PETSc.Vec().createSeq(n)
-    info = MixedSolver(A).solve(PETSc.Vec().createWithArray(b), x, rtol=1e-10,
-                                tri_sweeps=tri_sweeps)
+    info = MixedSolver(A, ordering=ordering).solve(PETSc.Vec().createWithArray(b), x,
+                                                   rtol=1e-10, tri_sweeps=tri_sweeps,
+                                                   tri_block=tri_block)
     assert info["converged"] and info["relres"] <= 1e-10
     assert info["passes"] >= 2
     xs = x.getArray()
@@ -63,3 +72,20 @@ def test_zero_rhs_and_size_checks():
     assert np.all(x.getArray() == 0.0)
     with pytest.raises(ValueError):
         s.solve(PETSc.Vec().createSeq(n + 1), x)
+
+
+def test_multicolour_passes_apply_the_triangles_exactly():
+    """With two colours one pass per triangle is the exact triangular solve:
+    the inner iteration counts match those of the exact FP64 sweeps."""
+    from mojopetsc4py.mixed import MixedSolver
+
+    ip, ix, v = gallery.convection_diffusion_3d(16)
+    n = len(ip) - 1
+    b = np.random.default_rng(3).uniform(-1, 1, n)
+    A = mat(ip, ix, v)
+    s = MixedSolver(A, ordering="multicolor")
+    x = PETSc.Vec().createSeq(n)
+    one = s.solve(PETSc.Vec().createWithArray(b), x, rtol=1e-10, tri_sweeps=1)
+    exact = s.solve(PETSc.Vec().createWithArray(b), x, rtol=1e-10, tri_sweeps=0)
+    assert one["converged"] and exact["converged"]
+    assert abs(one["inner_its"] - exact["inner_its"]) <= 2
