@@ -506,6 +506,7 @@ def form_mixed(torch, PETSc):
                                       "true_rel_residual": true_rel(xv.getArray())}
     solver = MixedSolver(A)
     for key, sweeps in (("mixed_fp32_fgmres30_ilu0_jacobi4", 4),
+                        ("mixed_fp32_fgmres30_ilu0_jacobi6", 6),
                         ("mixed_fp32_fgmres30_ilu0_exact", 0)):
         xm = PETSc.Vec().createSeq(n)
         solver.solve(bv, xm, rtol=1e-10, tri_sweeps=sweeps)

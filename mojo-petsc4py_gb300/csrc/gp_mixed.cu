@@ -412,6 +412,7 @@ struct Mixed {
   BlockTri bl, bu;       // block layouts of L and U (tri_block != 0)
   int bt_rows = 0;       // their block length (0: not built)
   int bt_generation = -1, bt_epoch = -1;
+  bool ident_r = false, ident_c = false;  // factor row / solution permutations are identities
   const Csr* A = nullptr;
   const Pc* pc = nullptr;
   int pc_generation = -1, pc_epoch = -1;
@@ -505,6 +506,17 @@ static int mixed_factors(Mixed* M, cudaStream_t s) {
     GP_CUDA(cudaMalloc(&M->lval, std::max<int64_t>(M->lnnz, 1) * sizeof(float)));
     GP_CUDA(cudaMalloc(&M->uval, std::max<int64_t>(M->unnz, 1) * sizeof(float)));
     GP_CUDA(cudaMalloc(&M->udinv, std::max(n, 1) * sizeof(float)));
+    // identity permutations (natural ordering) are skipped by the passes
+    std::vector<int> pr(n), pcv(n);
+    if (n) {
+      GP_CUDA(cudaMemcpy(pr.data(), pc->perm_r, n * sizeof(int), cudaMemcpyDeviceToHost));
+      GP_CUDA(cudaMemcpy(pcv.data(), pc->perm_c, n * sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    M->ident_r = M->ident_c = true;
+    for (int i = 0; i < n; i++) {
+      M->ident_r = M->ident_r && pr[i] == i;
+      M->ident_c = M->ident_c && pcv[i] == i;
+    }
     M->pc_generation = pc->generation;
     M->pc_epoch = -1;
   }
@@ -1149,6 +1161,8 @@ static int record_pass(Mixed* M, const Csr* A, const Pc* pc, const double* b, do
   for (int j = 0; j < m; j++) {
     float* vj = M->V + (size_t)j * n;
     float* zj = M->Z + (size_t)j * n;
+    const int* perm_r = M->ident_r ? nullptr : pc->perm_r;
+    const int* perm_c = M->ident_c ? nullptr : pc->perm_c;
     if (tri_sweeps > 0 && tri_block != 0) {
       // block passes: exact inside each run of rows, couplings from the last pass
       const BtArgs tl = bt_args(M->bl, n), tu = bt_args(M->bu, n);
@@ -1167,7 +1181,7 @@ static int record_pass(Mixed* M, const Csr* A, const Pc* pc, const double* b, do
       for (int k = 0; k < tri_sweeps; k++) {
         const bool lastp = k + 1 == tri_sweeps;
         launch_btri<true>(tu, M->bu.nblocks, M->bu.smem, act, yfin, xprev, lastp ? zj : xa,
-                          lastp ? pc->perm_c : nullptr, s);
+                          lastp ? perm_c : nullptr, s);
         xprev = xa;
         std::swap(xa, xb);
       }
@@ -1176,10 +1190,10 @@ static int record_pass(Mixed* M, const Csr* A, const Pc* pc, const double* b, do
       float* ya = M->t1;
       float* yb = M->t2;
       const float* yin = vj;
-      const int* yperm = pc->perm_r;
+      const int* yperm = perm_r;
       for (int k = 0; k < tri_sweeps; k++) {
-        k_mx_tri<<<gr, kMixBlock, 0, s>>>(act, n, M->lrp, M->lci, M->lval, nullptr, vj,
-                                          pc->perm_r, yin, yperm, nullptr, ya, nullptr);
+        k_mx_tri<<<gr, kMixBlock, 0, s>>>(act, n, M->lrp, M->lci, M->lval, nullptr, vj, perm_r,
+                                          yin, yperm, nullptr, ya, nullptr);
         yin = ya;
         yperm = nullptr;
         std::swap(ya, yb);
@@ -1192,7 +1206,7 @@ static int record_pass(Mixed* M, const Csr* A, const Pc* pc, const double* b, do
         const bool lastp = k + 1 == tri_sweeps;
         k_mx_tri<<<gr, kMixBlock, 0, s>>>(act, n, M->urp, M->uci, M->uval, M->udinv, yin,
                                           nullptr, xin, nullptr, xscale, lastp ? zj : xa,
-                                          lastp ? pc->perm_c : nullptr);
+                                          lastp ? perm_c : nullptr);
         xin = xa;
         xscale = nullptr;
         std::swap(xa, xb);
