@@ -111,6 +111,14 @@ __global__ void k_mul32(int n, const float* __restrict__ a, const float* __restr
 }
 
 // values of a factor triangle, FP64 factor slots -> FP32 CSR
+// ELL coefficients from the factor values (slot -1: absent, zero)
+__global__ void k_ell32_refresh(int64_t m, const int* __restrict__ slot,
+                                const double* __restrict__ src, float* __restrict__ dst) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m;
+       k += (int64_t)gridDim.x * blockDim.x)
+    dst[k] = slot[k] >= 0 ? __double2float_rn(src[slot[k]]) : 0.f;
+}
+
 __global__ void k_slot_gather(int64_t m, const int* __restrict__ slot,
                               const double* __restrict__ ba, float* __restrict__ out) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m;
@@ -421,6 +429,10 @@ struct Mixed {
   int *urp = nullptr, *uci = nullptr, *uslot = nullptr, *dslot = nullptr;
   float *lval = nullptr, *uval = nullptr, *udinv = nullptr;
   int64_t lnnz = 0, unnz = 0;
+  // column-major ELL copies of the triangles (W slots a row; 0 when wider than 8)
+  int lW = 0, uW = 0;
+  int *lell_ci = nullptr, *lell_slot = nullptr, *uell_ci = nullptr, *uell_slot = nullptr;
+  float *lell_val = nullptr, *uell_val = nullptr;
   // work
   float *V = nullptr, *Z = nullptr, *w = nullptr, *t0 = nullptr, *t1 = nullptr, *t2 = nullptr;
   float *t3 = nullptr, *t4 = nullptr;
@@ -444,7 +456,8 @@ static void mixed_free(Mixed* M) {
   bt_free(M->bl);
   bt_free(M->bu);
   void* ptrs[] = {M->lrp, M->lci, M->lslot, M->urp, M->uci, M->uslot, M->dslot, M->lval,
-                  M->uval, M->udinv, M->V, M->Z, M->w, M->t0, M->t1, M->t2, M->t3, M->t4,
+                  M->uval, M->udinv, M->lell_ci, M->lell_slot, M->uell_ci, M->uell_slot,
+                  M->lell_val, M->uell_val, M->V, M->Z, M->w, M->t0, M->t1, M->t2, M->t3, M->t4,
                   M->r, M->y,
                   M->d64, M->h_dev, M->partials, M->x64tmp, M->ticket};
   for (void* p : ptrs)
@@ -475,7 +488,9 @@ static int mixed_factors(Mixed* M, cudaStream_t s) {
   if (M->pc_generation != pc->generation) {
     for (void** p : {(void**)&M->lrp, (void**)&M->lci, (void**)&M->lslot, (void**)&M->urp,
                      (void**)&M->uci, (void**)&M->uslot, (void**)&M->dslot, (void**)&M->lval,
-                     (void**)&M->uval, (void**)&M->udinv})
+                     (void**)&M->uval, (void**)&M->udinv, (void**)&M->lell_ci,
+                     (void**)&M->lell_slot, (void**)&M->uell_ci, (void**)&M->uell_slot,
+                     (void**)&M->lell_val, (void**)&M->uell_val})
       if (*p) {
         cudaFree(*p);
         *p = nullptr;
@@ -506,6 +521,30 @@ static int mixed_factors(Mixed* M, cudaStream_t s) {
     GP_CUDA(cudaMalloc(&M->lval, std::max<int64_t>(M->lnnz, 1) * sizeof(float)));
     GP_CUDA(cudaMalloc(&M->uval, std::max<int64_t>(M->unnz, 1) * sizeof(float)));
     GP_CUDA(cudaMalloc(&M->udinv, std::max(n, 1) * sizeof(float)));
+    // ELL copies
+    auto ell = [&](const std::vector<int>& rp, const std::vector<int>& ci,
+                   const std::vector<int>& sl, int& W, int** eci, int** esl,
+                   float** eval) -> int {
+      W = 0;
+      for (int i = 0; i < n; i++) W = std::max(W, rp[i + 1] - rp[i]);
+      if (W > 8 || W == 0) {
+        W = 0;
+        return GP_OK;
+      }
+      std::vector<int> c((size_t)W * n), t((size_t)W * n, -1);
+      for (int i = 0; i < n; i++)
+        for (int e = 0; e < W; e++) {
+          const int j = rp[i] + e;
+          c[(size_t)e * n + i] = j < rp[i + 1] ? ci[j] : i;
+          if (j < rp[i + 1]) t[(size_t)e * n + i] = sl[j];
+        }
+      GP_TRY(up_mixed(eci, c));
+      GP_TRY(up_mixed(esl, t));
+      GP_CUDA(cudaMalloc(eval, (size_t)W * n * sizeof(float)));
+      return GP_OK;
+    };
+    GP_TRY(ell(lrp, lci, lsl, M->lW, &M->lell_ci, &M->lell_slot, &M->lell_val));
+    GP_TRY(ell(urp, uci, usl, M->uW, &M->uell_ci, &M->uell_slot, &M->uell_val));
     // identity permutations (natural ordering) are skipped by the passes
     std::vector<int> pr(n), pcv(n);
     if (n) {
@@ -525,6 +564,10 @@ static int mixed_factors(Mixed* M, cudaStream_t s) {
     if (M->lnnz) k_slot_gather<<<g, 256, 0, s>>>(M->lnnz, M->lslot, pc->ba, M->lval);
     if (M->unnz) k_slot_gather<<<g, 256, 0, s>>>(M->unnz, M->uslot, pc->ba, M->uval);
     k_slot_gather<<<g, 256, 0, s>>>(n, M->dslot, pc->ba, M->udinv);
+    if (M->lW)
+      k_ell32_refresh<<<g, 256, 0, s>>>((int64_t)M->lW * n, M->lell_slot, pc->ba, M->lell_val);
+    if (M->uW)
+      k_ell32_refresh<<<g, 256, 0, s>>>((int64_t)M->uW * n, M->uell_slot, pc->ba, M->uell_val);
     GP_CHECK_LAUNCH();
     M->pc_epoch = pc->epoch;
   }
@@ -977,6 +1020,39 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_tri(
   out[out_perm ? out_perm[i] : i] = o;
 }
 
+// The same pass over a column-major ELL copy of the triangle ([e * n + i],
+// W slots a row, absent ones with a zero coefficient): no row-pointer loads,
+// every column and coefficient load coalesced and issued before the gathers.
+template <int W>
+__global__ void __launch_bounds__(kMixBlock) k_mx_tri_ell(
+    const int* gate, int n, const int* __restrict__ ci, const float* __restrict__ val,
+    const float* __restrict__ dinv, const float* __restrict__ rhs,
+    const int* __restrict__ rhs_perm, const float* __restrict__ in,
+    const int* __restrict__ in_perm, const float* __restrict__ in_scale, float* __restrict__ out,
+    const int* __restrict__ out_perm) {
+  if (gated_off(gate, 1)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c[W];
+  float a[W], x[W];
+#pragma unroll
+  for (int e = 0; e < W; e++) {
+    c[e] = ci[(size_t)e * n + i];
+    a[e] = val[(size_t)e * n + i];
+  }
+  float acc = rhs[rhs_perm ? rhs_perm[i] : i];
+#pragma unroll
+  for (int e = 0; e < W; e++) {
+    float xin = in[in_perm ? in_perm[c[e]] : c[e]];
+    if (in_scale) xin *= in_scale[c[e]];
+    x[e] = xin;
+  }
+#pragma unroll
+  for (int e = 0; e < W; e++) acc = __fmaf_rn(-a[e], x[e], acc);
+  const float o = dinv ? acc * dinv[i] : acc;
+  out[out_perm ? out_perm[i] : i] = o;
+}
+
 __global__ void __launch_bounds__(kMixBlock) k_mx_spmv32(const int* gate, int n,
                                                          const int* __restrict__ rp,
                                                          const int* __restrict__ ci,
@@ -1140,6 +1216,34 @@ __global__ void k_mx_cast32(const int* gate, int n, const double* __restrict__ a
     b[i] = __double2float_rn(a[i]);
 }
 
+// One triangle pass: the ELL form when the triangle has at most 8 slots a row.
+static void tri_pass(int W, const int* eci, const float* eval, const int* rp, const int* ci,
+                     const float* val, const int* gate, int n, const float* dinv,
+                     const float* rhs, const int* rhs_perm, const float* in, const int* in_perm,
+                     const float* in_scale, float* out, const int* out_perm, cudaStream_t s) {
+  const int gr = (n + kMixBlock - 1) / kMixBlock;
+#define GP_TRI_ELL(WW)                                                                     \
+  case WW:                                                                                 \
+    k_mx_tri_ell<WW><<<gr, kMixBlock, 0, s>>>(gate, n, eci, eval, dinv, rhs, rhs_perm, in,  \
+                                             in_perm, in_scale, out, out_perm);            \
+    return;
+  switch (W) {
+    GP_TRI_ELL(1)
+    GP_TRI_ELL(2)
+    GP_TRI_ELL(3)
+    GP_TRI_ELL(4)
+    GP_TRI_ELL(5)
+    GP_TRI_ELL(6)
+    GP_TRI_ELL(7)
+    GP_TRI_ELL(8)
+    default:
+      break;
+  }
+#undef GP_TRI_ELL
+  k_mx_tri<<<gr, kMixBlock, 0, s>>>(gate, n, rp, ci, val, dinv, rhs, rhs_perm, in, in_perm,
+                                    in_scale, out, out_perm);
+}
+
 // Record one refinement pass into the current capture on stream s.
 static int record_pass(Mixed* M, const Csr* A, const Pc* pc, const double* b, double* x,
                        int tri_sweeps, int tri_block, cudaStream_t s) {
@@ -1192,8 +1296,8 @@ static int record_pass(Mixed* M, const Csr* A, const Pc* pc, const double* b, do
       const float* yin = vj;
       const int* yperm = perm_r;
       for (int k = 0; k < tri_sweeps; k++) {
-        k_mx_tri<<<gr, kMixBlock, 0, s>>>(act, n, M->lrp, M->lci, M->lval, nullptr, vj, perm_r,
-                                          yin, yperm, nullptr, ya, nullptr);
+        tri_pass(M->lW, M->lell_ci, M->lell_val, M->lrp, M->lci, M->lval, act, n, nullptr, vj,
+                 perm_r, yin, yperm, nullptr, ya, nullptr, s);
         yin = ya;
         yperm = nullptr;
         std::swap(ya, yb);
@@ -1204,9 +1308,8 @@ static int record_pass(Mixed* M, const Csr* A, const Pc* pc, const double* b, do
       const float* xscale = M->udinv;
       for (int k = 0; k < tri_sweeps; k++) {
         const bool lastp = k + 1 == tri_sweeps;
-        k_mx_tri<<<gr, kMixBlock, 0, s>>>(act, n, M->urp, M->uci, M->uval, M->udinv, yin,
-                                          nullptr, xin, nullptr, xscale, lastp ? zj : xa,
-                                          lastp ? perm_c : nullptr);
+        tri_pass(M->uW, M->uell_ci, M->uell_val, M->urp, M->uci, M->uval, act, n, M->udinv, yin,
+                 nullptr, xin, nullptr, xscale, lastp ? zj : xa, lastp ? perm_c : nullptr, s);
         xin = xa;
         xscale = nullptr;
         std::swap(xa, xb);
