@@ -143,3 +143,46 @@ def test_solves_match_the_oracle_in_both_forms(tiles, rows):
         assert int(ksp.getConvergedReason()) == o["reason"], (kt, pt)
         xs = x.getArray()
         assert np.linalg.norm(xs - o["x"]) <= 1e-10 * np.linalg.norm(o["x"])
+
+
+def _sparse_spd(n, density, seed):
+    """A random sparse SPD matrix with ragged rows (some rows with no
+    off-diagonal entries, some with many)."""
+    rng = np.random.default_rng(seed)
+    a = np.zeros((n, n))
+    for i in range(n):
+        k = rng.integers(0, max(1, int(density * n)) + 1)
+        cols = rng.choice(n, size=k, replace=False)
+        a[i, cols] = rng.uniform(-1, 1, size=k)
+    a = a + a.T
+    np.fill_diagonal(a, 0.0)
+    np.fill_diagonal(a, np.abs(a).sum(axis=1) + 1.0)
+    rows, cols = np.nonzero(a)
+    ip = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(ip, rows + 1, 1)
+    return np.cumsum(ip), cols.astype(np.int64), a[rows, cols]
+
+
+EDGE = {
+    "one_row": lambda: (np.array([0, 1]), np.array([0]), np.array([4.0])),
+    "two_rows": lambda: (np.array([0, 2, 4]), np.array([0, 1, 0, 1]),
+                         np.array([4.0, -1.0, -1.0, 4.0])),
+    "diagonal_7": lambda: (np.arange(8), np.arange(7), np.arange(1.0, 8.0)),
+    "ragged_60": lambda: _sparse_spd(60, 0.12, 4),
+    "wide_rows_40": lambda: _sparse_spd(40, 0.6, 9),   # rows wider than 16: CSR sweeps
+}
+
+
+@pytest.mark.parametrize("form,tiles,rows", [FORMS[0], FORMS[1], FORMS[2], FORMS[3]],
+                         ids=[f[0] for f in FORMS[:4]])
+@pytest.mark.parametrize("pt", ["ilu", "icc", "sor"])
+@pytest.mark.parametrize("name", sorted(EDGE))
+def test_sweep_forms_edge_cases(name, pt, form, tiles, rows):
+    """Tiny systems, rows without dependencies, ragged and very wide rows:
+    every form stays bit-identical to the oracle."""
+    ip, ix, v = EDGE[name]()
+    n = len(ip) - 1
+    _lib.set_sweep_form(tiles, rows)
+    pc = _pc(pt, _mat(ip, ix, v), {})
+    x = np.random.default_rng(11).normal(size=n)
+    np.testing.assert_array_equal(_apply(pc, x), O.OraclePC(pt, ip, ix, v).apply(x))
