@@ -83,7 +83,9 @@ struct EllArgs {
 // Launch shape and polling back-off of the sweeps (GPETSC_SWEEP_CTAS_PER_SM,
 // GPETSC_SWEEP_SLEEP_AFTER, GPETSC_SWEEP_SLEEP_NS override the defaults).
 struct SweepTuning {
-  int ctas_per_sm = 2, sleep_after = 8, sleep_ns = 20;  // best of a scan on ICC(0), 128^3
+  // best of a scan (1-4 CTAs a SM x 0-300 ns back-off) of the level-ordered
+  // IC(0)/ILU(0)/SOR sweeps on 128^3 with the per-lane polling kernel
+  int ctas_per_sm = 1, sleep_after = 8, sleep_ns = 0;
   int tiles = 1;                // GPETSC_SWEEP_TILES=0: always the level-ordered ELL form
   int tile_smem = kTileSmemMax;  // GPETSC_TILE_SMEM: shared memory cap of one chunk
   int tile_rows = 0;            // GPETSC_TILE_ROWS: force this chunk size (0: chosen)
