@@ -39,9 +39,10 @@ constexpr int kMixBlock = 256;
 constexpr int kMixMaxM = 64;
 
 // ------------------------------------------------------------------ kernels
-// CTAs of the multi-dot kernels: two per SM keeps the last CTA's fold short
+// CTAs of the multi-dot kernels: four per SM (more loads in flight; the last
+// CTA's fold stays short)
 static int mdot_grid(int64_t n) {
-  return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 2));
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 4));
 }
 
 static int mix_grid(int64_t n) {
@@ -946,6 +947,10 @@ int mixed_solve(Mixed* M, Csr* A, Pc* pc, const double* b, double* x, const Mixe
 struct MixDev {
   int pass_on, active, kdim, its, passes, pad_;
   double rn, rtol_bnorm, beta2, beta, tol, inner_rtol, hn2;
+  // reciprocals computed once by the one thread that has the norm (a divide
+  // in every thread of a streaming kernel costs more than the stream)
+  double inv_rn;
+  float inv_beta, inv_hn;
   double H[(kMixMaxM + 1) * kMixMaxM];
   double cs[kMixMaxM], sn[kMixMaxM], g[kMixMaxM + 1], y[kMixMaxM];
 };
@@ -964,6 +969,7 @@ __global__ void __launch_bounds__(kRedBlock) k_mx_resid(int n, const double* __r
   if (grid_finish<1>(v, slot, tot) && threadIdx.x == 0) {
     const double rn = sqrt(tot[0]);
     st->rn = rn;
+    st->inv_rn = rn > 0.0 ? 1.0 / rn : 0.0;
     const int on = (rn > st->rtol_bnorm) && isfinite(rn);
     st->pass_on = on;
     st->active = on;
@@ -975,7 +981,7 @@ __global__ void __launch_bounds__(kRedBlock) k_mx_resid(int n, const double* __r
 __global__ void k_mx_v0(int n, const double* __restrict__ r, const MixDev* st,
                         float* __restrict__ v0) {
   if (!st->pass_on) return;
-  const double inv = 1.0 / st->rn;
+  const double inv = st->inv_rn;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     v0[i] = __double2float_rn(r[i] * inv);
 }
@@ -984,6 +990,7 @@ __global__ void k_mx_beta(MixDev* st, int m) {
   if (!st->pass_on) return;
   const double beta = sqrt(st->beta2);
   st->beta = beta;
+  st->inv_beta = beta > 0.0 ? (float)(1.0 / beta) : 0.f;
   for (int i = 0; i <= m; i++) st->g[i] = 0.0;
   st->g[0] = beta;
   st->tol = st->inner_rtol * beta;
@@ -993,7 +1000,7 @@ __global__ void k_mx_beta(MixDev* st, int m) {
 // out = in / beta (which = 0) or in / sqrt(hn2) (which = 1), while active
 __global__ void k_mx_scale(int n, const float* in, float* out, const MixDev* st, int which) {
   if (!st->active) return;
-  const float s = (float)(1.0 / (which == 0 ? st->beta : sqrt(st->hn2)));
+  const float s = which == 0 ? st->inv_beta : st->inv_hn;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     out[i] = in[i] * s;
 }
@@ -1110,36 +1117,71 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_maxpy_norm(const int* gate, in
 }
 
 // Hessenberg column j, rotations and the residual estimate (one thread, FP64)
+// One warp: the lanes stage the new column and the earlier rotations in
+// shared memory (independent loads), then lane 0 runs the rotations out of
+// shared memory -- the chain is the FP64 arithmetic, not a memory round trip
+// per rotation.
 __global__ void k_mx_givens(MixDev* st, const double* __restrict__ h, int j, int m) {
   if (!st->active) return;
+  __shared__ double col[kMixMaxM + 1], cs[kMixMaxM], sn[kMixMaxM];
+  for (int i = threadIdx.x; i <= j; i += blockDim.x) {
+    col[i] = h[i];
+    if (i < j) {
+      cs[i] = st->cs[i];
+      sn[i] = st->sn[i];
+    }
+  }
+  __syncwarp();
+  if (threadIdx.x != 0) return;
   double* H = st->H;
   const double hn = sqrt(st->hn2);
-  for (int i = 0; i <= j; i++) H[i * m + j] = h[i];
+  st->inv_hn = hn > 0.0 ? (float)(1.0 / hn) : 0.f;
   for (int i = 0; i < j; i++) {
-    const double a = H[i * m + j], c = H[(i + 1) * m + j];
-    H[i * m + j] = st->cs[i] * a + st->sn[i] * c;
-    H[(i + 1) * m + j] = -st->sn[i] * a + st->cs[i] * c;
+    const double a = col[i], c = col[i + 1];
+    col[i] = cs[i] * a + sn[i] * c;
+    col[i + 1] = -sn[i] * a + cs[i] * c;
   }
-  const double hjj = H[j * m + j];
-  const double den = hypot(hjj, hn);
-  st->cs[j] = den > 0.0 ? hjj / den : 1.0;
-  st->sn[j] = den > 0.0 ? hn / den : 0.0;
-  H[j * m + j] = den;
-  st->g[j + 1] = -st->sn[j] * st->g[j];
-  st->g[j] = st->cs[j] * st->g[j];
+  const double hjj = col[j];
+  // one square root and one reciprocal (FP64 divide, square root and hypot
+  // are long dependent sequences on this part; the operands are far from
+  // overflow: a normalised basis keeps them O(||A||))
+  const double den = sqrt(hjj * hjj + hn * hn);
+  const double rden = den > 0.0 ? 1.0 / den : 0.0;
+  const double cj = den > 0.0 ? hjj * rden : 1.0;
+  const double sj = den > 0.0 ? hn * rden : 0.0;
+  col[j] = den;
+  for (int i = 0; i <= j; i++) H[i * m + j] = col[i];
+  st->cs[j] = cj;
+  st->sn[j] = sj;
+  const double gj = st->g[j];
+  st->g[j + 1] = -sj * gj;
+  st->g[j] = cj * gj;
   st->kdim = j + 1;
   st->its += 1;
-  if (!(hn > 0.0) || fabs(st->g[j + 1]) <= st->tol || j + 1 == m) st->active = 0;
+  if (!(hn > 0.0) || fabs(-sj * gj) <= st->tol || j + 1 == m) st->active = 0;
 }
 
+// Back-substitution of the least-squares system: the warp stages the upper
+// triangle of H and g in shared memory, lane 0 solves out of it.
 __global__ void k_mx_backsub(MixDev* st, int m) {
   if (!st->pass_on) return;
+  __shared__ double Hs[kMixMaxM * kMixMaxM], gs[kMixMaxM], ys[kMixMaxM];
   const int k = st->kdim;
-  for (int i = k - 1; i >= 0; i--) {
-    double t = st->g[i];
-    for (int c = i + 1; c < k; c++) t -= st->H[i * m + c] * st->y[c];
-    st->y[i] = st->H[i * m + i] != 0.0 ? t / st->H[i * m + i] : 0.0;
+  for (int q = threadIdx.x; q < k * k; q += blockDim.x) {
+    const int i = q / k, c = q % k;
+    if (c >= i) Hs[i * k + c] = st->H[i * m + c];
   }
+  for (int i = threadIdx.x; i < k; i += blockDim.x) gs[i] = st->g[i];
+  __syncwarp();
+  if (threadIdx.x == 0) {
+    for (int i = k - 1; i >= 0; i--) {
+      double t = gs[i];
+      for (int c = i + 1; c < k; c++) t -= Hs[i * k + c] * ys[c];
+      ys[i] = Hs[i * k + i] != 0.0 ? t / Hs[i * k + i] : 0.0;
+    }
+  }
+  __syncwarp();
+  for (int i = threadIdx.x; i < k; i += blockDim.x) st->y[i] = ys[i];
 }
 
 // x += rn * sum_{j < kdim} y_j Z_j
@@ -1325,10 +1367,10 @@ static int record_pass(Mixed* M, const Csr* A, const Pc* pc, const double* b, do
                                        M->h_dev);
     k_mx_maxpy_norm<<<g, kMixBlock, 0, s>>>(act, n, M->V, j + 1, M->h_dev, M->w, M->partials,
                                             M->ticket, &st->hn2);
-    k_mx_givens<<<1, 1, 0, s>>>(st, M->h_dev, j, m);
+    k_mx_givens<<<1, 32, 0, s>>>(st, M->h_dev, j, m);
     if (j + 1 < m) k_mx_scale<<<g, kMixBlock, 0, s>>>(n, M->w, M->V + (size_t)(j + 1) * n, st, 1);
   }
-  k_mx_backsub<<<1, 1, 0, s>>>(st, m);
+  k_mx_backsub<<<1, 32, 0, s>>>(st, m);
   k_mx_correct<<<g, kMixBlock, 0, s>>>(n, M->Z, st, x);
   GP_CUDA(cudaMemcpyAsync(M->h_st, st, offsetof(MixDev, H), cudaMemcpyDeviceToHost, s));
   GP_CHECK_LAUNCH();
