@@ -293,35 +293,17 @@ __global__ void __launch_bounds__(kSweepBlock) k_icc_bwd(
 // Row i of the factor is accumulated in its own slots of `ba` (the reference's
 // dense `rtmp` restricted to the row's pattern; positions outside the pattern
 // are never stored or read back there either).
-__device__ __forceinline__ int ilu_find(int col, int i, const int* __restrict__ bi,
-                                        const int* __restrict__ bj,
-                                        const int* __restrict__ bdiag) {
-  if (col < i) {
-    int lo = bi[i], hi = bi[i + 1];
-    while (lo < hi) {
-      int mid = (lo + hi) >> 1;
-      int c = bj[mid];
-      if (c == col) return mid;
-      if (c < col) lo = mid + 1; else hi = mid;
-    }
-    return -1;
-  }
-  if (col == i) return bdiag[i];
-  int lo = bdiag[i + 1] + 1, hi = bdiag[i];
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    int c = bj[mid];
-    if (c == col) return mid;
-    if (c < col) lo = mid + 1; else hi = mid;
-  }
-  return -1;
-}
 
+// upd_ptr/upd_dst/upd_src: for each L slot k of row i, the updates its pivot
+// row makes to row i -- (row i's slot, pivot row's U slot) pairs in the
+// pivot row's U order -- found once on the host (the pattern is fixed), so
+// the numeric phase does no pattern searches.
 __global__ void __launch_bounds__(kSweepBlock) k_ilu_numeric(
     int n, const int* __restrict__ order, unsigned* tickets, const int* __restrict__ arow,
     const double* __restrict__ aval, const int* __restrict__ amap, const int* __restrict__ perm_r,
     const int* __restrict__ bi, const int* __restrict__ bj, const int* __restrict__ bdiag,
-    double* ba, int* done, int epoch, DevErr* err) {
+    const int* __restrict__ upd_ptr, const int* __restrict__ upd_dst,
+    const int* __restrict__ upd_src, double* ba, int* done, int epoch, DevErr* err) {
   sweep_rows(n, order, tickets, [&](int i) {
     // zero the row's slots, then load A's row r_i
     for (int j = bi[i]; j < bi[i + 1]; j++) ba[j] = 0.0;
@@ -340,11 +322,9 @@ __global__ void __launch_bounds__(kSweepBlock) k_ilu_numeric(
         const double pv = __ldcg(&ba[bdiag[row]]);
         const double m = mul(pc, pv);
         ba[k] = m;
-        const int pj = bdiag[row + 1] + 1;
-        const int nz = bdiag[row] - bdiag[row + 1] - 1;
-        for (int j = 0; j < nz; j++) {
-          const int s = ilu_find(bj[pj + j], i, bi, bj, bdiag);
-          if (s >= 0) ba[s] = sub(ba[s], mul(m, __ldcg(&ba[pj + j])));
+        for (int u = upd_ptr[k]; u < upd_ptr[k + 1]; u++) {
+          const int s = upd_dst[u];
+          ba[s] = sub(ba[s], mul(m, __ldcg(&ba[upd_src[u]])));
         }
       }
     }
@@ -424,7 +404,7 @@ static void free_all(Pc* pc) {
                   pc->perm_r, pc->perm_c, pc->perm_ic, pc->ba, pc->ba_orig, pc->done, pc->cptr, pc->crow,
                   pc->cslot, pc->tptr, pc->trow, pc->tslot, pc->amap, pc->fwd.order,
                   pc->bwd.order, pc->num.order, pc->yf, pc->yb, pc->ys, pc->t, pc->tickets,
-                  pc->err};
+                  pc->err, pc->upd_ptr, pc->upd_dst, pc->upd_src};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   ell_free(pc->ef);
@@ -564,6 +544,50 @@ static int ilu_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
   GP_TRY(ell_build(pc->ef, ELL_ILU_F, n, true, of, lp, lc, ls, P.r, none, none, &fpos));
   GP_TRY(ell_build(pc->eb, ELL_ILU_B, n, false, ob, up, uc, us, fpos, perm_c, dsl, nullptr));
+  // the numeric phase's update lists (the searches of the elimination, once);
+  // kept to the end of the function: the copies below are asynchronous
+  std::vector<int> uptr(P.bi[n] + 1, 0), udst, usrc;
+  {
+    auto find = [&](int col, int i) {
+      int lo, hi;
+      if (col < i) {
+        lo = P.bi[i];
+        hi = P.bi[i + 1];
+      } else if (col == i) {
+        return P.bdiag[i];
+      } else {
+        lo = P.bdiag[i + 1] + 1;
+        hi = P.bdiag[i];
+      }
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const int c = P.bj[mid];
+        if (c == col) return mid;
+        if (c < col)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      return -1;
+    };
+    for (int i = 0; i < n; i++)
+      for (int k = P.bi[i]; k < P.bi[i + 1]; k++) {
+        const int row = P.bj[k];
+        const int pj = P.bdiag[row + 1] + 1;
+        const int nz = P.bdiag[row] - P.bdiag[row + 1] - 1;
+        for (int j = 0; j < nz; j++) {
+          const int d = find(P.bj[pj + j], i);
+          if (d >= 0) {
+            udst.push_back(d);
+            usrc.push_back(pj + j);
+          }
+        }
+        uptr[k + 1] = (int)udst.size();
+      }
+    GP_TRY(upload(&pc->upd_ptr, uptr, s));
+    GP_TRY(upload(&pc->upd_dst, udst, s));
+    GP_TRY(upload(&pc->upd_src, usrc, s));
+  }
   GP_TRY(upload(&pc->bi, P.bi, s));
   GP_TRY(upload(&pc->bj, P.bj, s));
   GP_TRY(upload(&pc->bdiag, P.bdiag, s));
@@ -754,10 +778,9 @@ int pc_factor_numeric(Pc* pc, cudaStream_t s) {
   if (n == 0) return GP_OK;
   pc->epoch = pc->epoch == INT32_MAX ? 1 : pc->epoch + 1;
   if (pc->opt.type == PC_ILU) {
-    k_ilu_numeric<<<sweep_grid(), kSweepBlock, 0, s>>>(n, pc->fwd.order, pc->tickets,
-                                                        A->rowptr, A->val, pc->amap, pc->perm_r,
-                                                        pc->bi, pc->bj, pc->bdiag, pc->ba,
-                                                        pc->done, pc->epoch, pc->err);
+    k_ilu_numeric<<<sweep_grid(), kSweepBlock, 0, s>>>(
+        n, pc->fwd.order, pc->tickets, A->rowptr, A->val, pc->amap, pc->perm_r, pc->bi, pc->bj,
+        pc->bdiag, pc->upd_ptr, pc->upd_dst, pc->upd_src, pc->ba, pc->done, pc->epoch, pc->err);
   } else {
     k_icc_numeric<<<sweep_grid(), kSweepBlock, 0, s>>>(
         n, pc->num.order, pc->tickets, A->rowptr, A->val, pc->amap, pc->perm_r, pc->bi, pc->bj,

@@ -133,6 +133,10 @@ struct Pc {
   int* trow = nullptr;
   int* tslot = nullptr;
   int* amap = nullptr;       // A slot -> factor slot (or -1)
+  // ILU numeric: per L slot, the (row slot, pivot U slot) updates it makes
+  int* upd_ptr = nullptr;
+  int* upd_dst = nullptr;
+  int* upd_src = nullptr;
 
   SweepPlan fwd, bwd, num;
   EllSweep ef, eb;           // ELL forms of the forward and backward sweeps
