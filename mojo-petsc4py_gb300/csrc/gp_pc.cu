@@ -313,18 +313,37 @@ __global__ void __launch_bounds__(kSweepBlock) k_ilu_numeric(
       const int s = amap[j];
       if (s >= 0) ba[s] = aval[j];
     }
-    // eliminate with each L entry in ascending column order
+    // eliminate with each L entry in ascending column order; once the pivot
+    // row is done its pivot and the U values this row needs are loaded
+    // together (one L2 round trip), then applied in order
+    constexpr int kU = 8;
     for (int k = bi[i]; k < bi[i + 1]; k++) {
       const double pc = ba[k];
       if (pc != 0.0) {
         const int row = bj[k];
+        const int u0 = upd_ptr[k], u1 = upd_ptr[k + 1];
+        int dst[kU], src[kU];
+#pragma unroll
+        for (int q = 0; q < kU; q++)
+          if (u0 + q < u1) {
+            dst[q] = upd_dst[u0 + q];
+            src[q] = upd_src[u0 + q];
+          }
+        const int pslot = bdiag[row];
         wait_done(&done[row], epoch, err, 7);
-        const double pv = __ldcg(&ba[bdiag[row]]);
+        const double pv = __ldcg(&ba[pslot]);
+        double sv[kU];
+#pragma unroll
+        for (int q = 0; q < kU; q++)
+          if (u0 + q < u1) sv[q] = __ldcg(&ba[src[q]]);
         const double m = mul(pc, pv);
         ba[k] = m;
-        for (int u = upd_ptr[k]; u < upd_ptr[k + 1]; u++) {
-          const int s = upd_dst[u];
-          ba[s] = sub(ba[s], mul(m, __ldcg(&ba[upd_src[u]])));
+#pragma unroll
+        for (int q = 0; q < kU; q++)
+          if (u0 + q < u1) ba[dst[q]] = sub(ba[dst[q]], mul(m, sv[q]));
+        for (int u = u0 + kU; u < u1; u++) {  // rows with more fill
+          const int d = upd_dst[u];
+          ba[d] = sub(ba[d], mul(m, __ldcg(&ba[upd_src[u]])));
         }
       }
     }
