@@ -1030,6 +1030,12 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_tri(
 // The same pass over a column-major ELL copy of the triangle ([e * n + i],
 // W slots a row, absent ones with a zero coefficient): no row-pointer loads,
 // every column and coefficient load coalesced and issued before the gathers.
+// Each thread takes kTriRows rows a grid-width apart (coalesced) and issues
+// all their column/coefficient loads, then all their gathers, before any
+// arithmetic: two memory round trips for the whole pass instead of two per
+// row-wave.
+constexpr int kTriRows = 4;
+
 template <int W>
 __global__ void __launch_bounds__(kMixBlock) k_mx_tri_ell(
     const int* gate, int n, const int* __restrict__ ci, const float* __restrict__ val,
@@ -1038,26 +1044,45 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_tri_ell(
     const int* __restrict__ in_perm, const float* __restrict__ in_scale, float* __restrict__ out,
     const int* __restrict__ out_perm) {
   if (gated_off(gate, 1)) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int c[W];
-  float a[W], x[W];
+  const int stride = gridDim.x * blockDim.x;
+  const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  int c[kTriRows][W];
+  float a[kTriRows][W], acc[kTriRows];
 #pragma unroll
-  for (int e = 0; e < W; e++) {
-    c[e] = ci[(size_t)e * n + i];
-    a[e] = val[(size_t)e * n + i];
+  for (int q = 0; q < kTriRows; q++) {
+    const int i = i0 + q * stride;
+    if (i < n) {
+#pragma unroll
+      for (int e = 0; e < W; e++) {
+        c[q][e] = ci[(size_t)e * n + i];
+        a[q][e] = val[(size_t)e * n + i];
+      }
+      acc[q] = rhs[rhs_perm ? rhs_perm[i] : i];
+    }
   }
-  float acc = rhs[rhs_perm ? rhs_perm[i] : i];
 #pragma unroll
-  for (int e = 0; e < W; e++) {
-    float xin = in[in_perm ? in_perm[c[e]] : c[e]];
-    if (in_scale) xin *= in_scale[c[e]];
-    x[e] = xin;
+  for (int q = 0; q < kTriRows; q++) {
+    const int i = i0 + q * stride;
+    if (i < n) {
+      float x[W];
+#pragma unroll
+      for (int e = 0; e < W; e++) {
+        float xin = in[in_perm ? in_perm[c[q][e]] : c[q][e]];
+        if (in_scale) xin *= in_scale[c[q][e]];
+        x[e] = xin;
+      }
+#pragma unroll
+      for (int e = 0; e < W; e++) acc[q] = __fmaf_rn(-a[q][e], x[e], acc[q]);
+    }
   }
 #pragma unroll
-  for (int e = 0; e < W; e++) acc = __fmaf_rn(-a[e], x[e], acc);
-  const float o = dinv ? acc * dinv[i] : acc;
-  out[out_perm ? out_perm[i] : i] = o;
+  for (int q = 0; q < kTriRows; q++) {
+    const int i = i0 + q * stride;
+    if (i < n) {
+      const float o = dinv ? acc[q] * dinv[i] : acc[q];
+      out[out_perm ? out_perm[i] : i] = o;
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kMixBlock) k_mx_spmv32(const int* gate, int n,
@@ -1263,7 +1288,7 @@ static void tri_pass(int W, const int* eci, const float* eval, const int* rp, co
                      const float* val, const int* gate, int n, const float* dinv,
                      const float* rhs, const int* rhs_perm, const float* in, const int* in_perm,
                      const float* in_scale, float* out, const int* out_perm, cudaStream_t s) {
-  const int gr = (n + kMixBlock - 1) / kMixBlock;
+  const int gr = (n + kMixBlock * kTriRows - 1) / (kMixBlock * kTriRows);
 #define GP_TRI_ELL(WW)                                                                     \
   case WW:                                                                                 \
     k_mx_tri_ell<WW><<<gr, kMixBlock, 0, s>>>(gate, n, eci, eval, dinv, rhs, rhs_perm, in,  \
@@ -1282,8 +1307,8 @@ static void tri_pass(int W, const int* eci, const float* eval, const int* rp, co
       break;
   }
 #undef GP_TRI_ELL
-  k_mx_tri<<<gr, kMixBlock, 0, s>>>(gate, n, rp, ci, val, dinv, rhs, rhs_perm, in, in_perm,
-                                    in_scale, out, out_perm);
+  k_mx_tri<<<(n + kMixBlock - 1) / kMixBlock, kMixBlock, 0, s>>>(
+      gate, n, rp, ci, val, dinv, rhs, rhs_perm, in, in_perm, in_scale, out, out_perm);
 }
 
 // Record one refinement pass into the current capture on stream s.
