@@ -1117,7 +1117,36 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_maxpy_norm(const int* gate, in
   for (int j = threadIdx.x; j < k; j += blockDim.x) hs[j] = (float)h[j];
   __syncthreads();
   float acc = 0.f;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  // two rows a thread per step, eight basis loads of each in flight before
+  // their (ordered) multiply-adds
+  const int stride = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + stride < n; i += 2 * stride) {
+    float v0 = w[i], v1 = w[i + stride];
+    int j = 0;
+    for (; j + 8 <= k; j += 8) {
+      float t0[8], t1[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        t0[q] = V[(size_t)(j + q) * n + i];
+        t1[q] = V[(size_t)(j + q) * n + i + stride];
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        v0 = __fmaf_rn(-hs[j + q], t0[q], v0);
+        v1 = __fmaf_rn(-hs[j + q], t1[q], v1);
+      }
+    }
+    for (; j < k; j++) {
+      v0 = __fmaf_rn(-hs[j], V[(size_t)j * n + i], v0);
+      v1 = __fmaf_rn(-hs[j], V[(size_t)j * n + i + stride], v1);
+    }
+    w[i] = v0;
+    w[i + stride] = v1;
+    acc = __fmaf_rn(v0, v0, acc);
+    acc = __fmaf_rn(v1, v1, acc);
+  }
+  for (; i < n; i += stride) {
     float v = w[i];
     for (int j = 0; j < k; j++) v = __fmaf_rn(-hs[j], V[(size_t)j * n + i], v);
     w[i] = v;
@@ -1240,7 +1269,27 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_mdot(const int* gate, int n,
     float acc[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) acc[q] = 0.f;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    // two rows a thread per step, all their loads issued before the
+    // multiply-adds (accumulation order per thread unchanged: row by row)
+    const int stride = gridDim.x * blockDim.x;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + stride < n; i += 2 * stride) {
+      const float w0 = w[i], w1 = w[i + stride];
+      float v0[8], v1[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if (j0 + q < kk) {
+          v0[q] = V ? V[(size_t)(j0 + q) * n + i] : w0;
+          v1[q] = V ? V[(size_t)(j0 + q) * n + i + stride] : w1;
+        }
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if (j0 + q < kk) {
+          acc[q] = __fmaf_rn(v0[q], w0, acc[q]);
+          acc[q] = __fmaf_rn(v1[q], w1, acc[q]);
+        }
+    }
+    for (; i < n; i += stride) {
       const float wi = w[i];
 #pragma unroll
       for (int q = 0; q < 8; q++)
