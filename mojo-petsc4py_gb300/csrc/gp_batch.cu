@@ -23,12 +23,15 @@
 // well; the cross-tile sums, the norms and all scalars are FP64).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "../../include/gpetsc.h"
 #include "gp_common.cuh"
 #include "gp_internal.h"
+#include "gp_pc.h"
 
 namespace gp {
 
@@ -535,6 +538,12 @@ struct Tuning {
 struct Batch {
   int nsys = 0, n = 0, R = 0, ntiles = 0, device = -1;
   int64_t nnz = 0;
+  // rows of each system renumbered by reverse Cuthill-McKee so that a row's
+  // neighbours -- whose right-hand-side blocks the sparse pass gathers -- sit
+  // close to it: perm[new] = old (global rows); right-hand sides come in and
+  // solutions go out through it, in the caller's numbering
+  int* perm = nullptr;
+  double *bp = nullptr, *xp = nullptr;  // permuted B and X
   std::vector<int> sys_row;           // host, nsys + 1
   std::vector<int> h_rowptr, h_colind;
   // device matrix and preconditioner
@@ -757,11 +766,27 @@ void batch_destroy(Batch* B) {
   void* ptrs[] = {B->rowptr, B->colind, B->diagpos, B->val, B->val32, B->dinv, B->dinv32,
                   B->sys_ticket, B->sys_active, B->sys_pairs_left, B->counters, B->pair_d,
                   B->pair_i, B->r, B->p, B->z, B->x32, B->r32, B->p32, B->z32, B->bnorm,
-                  B->rn};
+                  B->rn, B->perm, B->bp, B->xp};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (B->cap_stream) cudaStreamDestroy(B->cap_stream);
   delete B;
+}
+
+// out row k = in row perm[k] (gather) or out row perm[k] = in row k (scatter),
+// R columns a row
+__global__ void k_brows_permute(int n, int R, const int* __restrict__ perm, int scatter,
+                                const double* __restrict__ in, double* __restrict__ out) {
+  const int64_t total = (int64_t)n * R;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(q / R), c = (int)(q % R);
+    const int64_t o = (int64_t)perm[k] * R + c;
+    if (scatter)
+      out[o] = in[q];
+    else
+      out[q] = in[o];
+  }
 }
 
 __global__ void k_bto_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
@@ -821,6 +846,56 @@ int batch_create(Batch** out, int64_t nsys, const int64_t* sys_rows, const int64
     return GP_ERR_ARG;
   }
   for (int64_t i = 0; i <= n; i++) B->h_rowptr[i] = (int)indptr[i];
+  // renumber each system's rows by RCM (GPETSC_BATCH_RCM=0 keeps the caller's
+  // numbering); values are permuted on the host before the upload
+  std::vector<double> pval;
+  std::vector<int> perm;
+  {
+    const char* e = std::getenv("GPETSC_BATCH_RCM");
+    if (!(e && std::string(e) == "0") && nnz > 0) {
+      perm.resize(n);
+      std::vector<int> inv(n), nrp(n + 1, 0), nci(nnz), lrp, lci, lperm;
+      std::vector<int64_t> nslot(nnz);
+      for (int sy = 0; sy < B->nsys; sy++) {
+        const int r0 = B->sys_row[sy], m = B->sys_row[sy + 1] - r0;
+        lrp.assign(m + 1, 0);
+        lci.clear();
+        for (int i = 0; i < m; i++) {
+          for (int j = B->h_rowptr[r0 + i]; j < B->h_rowptr[r0 + i + 1]; j++)
+            lci.push_back(B->h_colind[j] - r0);
+          lrp[i + 1] = (int)lci.size();
+        }
+        rcm_order(lrp, lci, m, lperm);
+        for (int k = 0; k < m; k++) {
+          perm[r0 + k] = r0 + lperm[k];
+          inv[r0 + lperm[k]] = r0 + k;
+        }
+      }
+      std::vector<std::pair<int, int64_t>> row;
+      for (int64_t k = 0; k < n; k++) {
+        const int old = perm[k];
+        row.clear();
+        for (int j = B->h_rowptr[old]; j < B->h_rowptr[old + 1]; j++)
+          row.push_back({inv[B->h_colind[j]], j});
+        std::sort(row.begin(), row.end());
+        nrp[k + 1] = nrp[k] + (int)row.size();
+        for (size_t q = 0; q < row.size(); q++) {
+          nci[nrp[k] + q] = row[q].first;
+          nslot[nrp[k] + q] = row[q].second;
+        }
+      }
+      B->h_rowptr = nrp;
+      for (int64_t j = 0; j < nnz; j++) B->h_colind[j] = nci[j];
+      std::fill(diag.begin(), diag.end(), -1);
+      for (int64_t k = 0; k < n; k++)
+        for (int j = nrp[k]; j < nrp[k + 1]; j++)
+          if (nci[j] == k) diag[k] = j;
+      if (values) {
+        pval.resize(nnz);
+        for (int64_t j = 0; j < nnz; j++) pval[j] = values[nslot[j]];
+      }
+    }
+  }
   GP_CUDA(cudaGetDevice(&B->device));
   const size_t np = (size_t)nsys * nrhs, nv = (size_t)std::max<int64_t>(n, 1) * nrhs;
   auto fail = [&](int code) {
@@ -859,9 +934,18 @@ int batch_create(Batch** out, int64_t nsys, const int64_t* sys_rows, const int64
     return fail(GP_ERR_CUDA);
   }
   if (nnz && values)
-    if (cudaMemcpyAsync(B->val, values, nnz * sizeof(double), cudaMemcpyHostToDevice, s) !=
-        cudaSuccess)
+    if (cudaMemcpyAsync(B->val, pval.empty() ? values : pval.data(), nnz * sizeof(double),
+                        cudaMemcpyHostToDevice, s) != cudaSuccess)
       return fail(GP_ERR_CUDA);
+  if (!perm.empty()) {
+    BT(upload_vec(&B->perm, perm, s));
+    if (cudaMalloc(&B->bp, nv * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&B->xp, nv * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("batched CG: out of device memory");
+      return fail(GP_ERR_CUDA);
+    }
+  }
   if (cudaMemsetAsync(B->sys_ticket, 0, nsys * sizeof(unsigned), s) != cudaSuccess ||
       cudaMemsetAsync(B->pair_i, 0, 6 * np * sizeof(int), s) != cudaSuccess ||
       cudaMemsetAsync(B->pair_d, 0, 9 * np * sizeof(double), s) != cudaSuccess)
@@ -872,6 +956,7 @@ int batch_create(Batch** out, int64_t nsys, const int64_t* sys_rows, const int64
         (int)n, B->diagpos, B->val, B->dinv, B->dinv32);
   if (cudaGetLastError() != cudaSuccess) return fail(GP_ERR_CUDA);
   BT(build_tiles(*B, B->tune.tile_rows, s));
+  if (cudaStreamSynchronize(s) != cudaSuccess) return fail(GP_ERR_CUDA);  // host copies done
 #undef BT
   *out = B;
   return GP_OK;
@@ -1206,10 +1291,24 @@ int batch_solve(Batch* B, const BatchOptions& o, const double* b, double* x, cud
   }
   int st = GP_OK;
   B->cur = o.precision ? &B->tune32 : &B->tune;
+  const double* bs = b;
+  double* xs = x;
+  const int g = std::max(1, std::min((int)(((int64_t)B->n * B->R + 255) / 256), num_sms() * 8));
+  if (B->perm && B->n) {  // into the renumbered rows
+    k_brows_permute<<<g, 256, 0, s>>>(B->n, B->R, B->perm, 0, b, B->bp);
+    k_brows_permute<<<g, 256, 0, s>>>(B->n, B->R, B->perm, 0, x, B->xp);
+    GP_CHECK_LAUNCH();
+    bs = B->bp;
+    xs = B->xp;
+  }
   int r = with_shape(B->R, B->cur->vr, [&](auto RR, auto VV) {
-    st = solve_shape<decltype(RR)::value, decltype(VV)::value>(*B, o, b, x, s, res);
+    st = solve_shape<decltype(RR)::value, decltype(VV)::value>(*B, o, bs, xs, s, res);
   });
   GP_TRY(r);
+  if (st == GP_OK && B->perm && B->n) {  // back to the caller's numbering
+    k_brows_permute<<<g, 256, 0, s>>>(B->n, B->R, B->perm, 1, B->xp, x);
+    GP_CHECK_LAUNCH();
+  }
   return st;
 }
 
