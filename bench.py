@@ -348,7 +348,7 @@ def run_ours(args, world, rank, local, pg):
             methods[name] = {"ms": round(m2, 3), "its": k2.getIterationNumber(),
                              "reason": k2.getConvergedReason()}
 
-    # ---- the benchmark spec's other forms on their own configurations (N = 1)
+    # ---- the three further forms on their own workloads (N = 1)
     forms = None
     if rank == 0 and world == 1 and not args.quick and not args.no_forms:
         forms = {}
@@ -478,7 +478,7 @@ def form_batched(torch, PETSc):
 def form_mixed(torch, PETSc):
     """3-D upwind convection-diffusion 96^3 (cell Peclet 10): plain FP64
     GMRES(30) + ILU(0) against FP32 inner FGMRES(30) + ILU(0) in FP64
-    refinement, both judged on the true FP64 residual (target 1e-10)."""
+    refinement, both held to the true FP64 residual (target 1e-10)."""
     from mojopetsc4py import gallery
     from mojopetsc4py.mixed import MixedSolver
 
