@@ -1250,7 +1250,15 @@ __global__ void k_mx_correct(int n, const float* __restrict__ Z, const MixDev* s
   const double rn = st->rn;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float d = 0.f;
-    for (int j = 0; j < k; j++) d = __fmaf_rn(ys[j], Z[(size_t)j * n + i], d);
+    int j = 0;
+    for (; j + 8 <= k; j += 8) {  // eight loads in flight before their ordered sums
+      float t[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) t[q] = Z[(size_t)(j + q) * n + i];
+#pragma unroll
+      for (int q = 0; q < 8; q++) d = __fmaf_rn(ys[j + q], t[q], d);
+    }
+    for (; j < k; j++) d = __fmaf_rn(ys[j], Z[(size_t)j * n + i], d);
     x[i] = fma(rn, (double)d, x[i]);
   }
 }

@@ -455,7 +455,9 @@ static int plan(SweepPlan& p, int n, const std::vector<int>& dptr, const std::ve
 }
 
 int pc_check(Pc* pc, cudaStream_t s) {
-  if (!pc->err) return GP_OK;
+  // none and Jacobi have no bounded waits that could set the flag: their
+  // standalone apply stays asynchronous
+  if (!pc->err || pc->opt.type == PC_NONE || pc->opt.type == PC_JACOBI) return GP_OK;
   DevErr h{};
   GP_CUDA(cudaMemcpyAsync(&h, pc->err, sizeof(DevErr), cudaMemcpyDeviceToHost, s));
   GP_CUDA(cudaStreamSynchronize(s));
