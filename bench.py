@@ -353,7 +353,7 @@ def run_ours(args, world, rank, local, pg):
     if rank == 0 and world == 1 and not args.quick and not args.no_forms:
         forms = {}
         for name, fn in (("mixed", form_mixed), ("batched", form_batched),
-                         ("adjoint", form_adjoint)):
+                         ("adjoint", form_adjoint), ("bandwidth", form_bandwidth)):
             try:
                 forms[name] = fn(torch, PETSc)
             except Exception as e:  # reported, never hidden
@@ -599,6 +599,148 @@ def form_adjoint(torch, PETSc):
             "finite_difference_equivalent_ms": round(2 * int(ip[-1]) * plain["forward_ms"], 0)}
 
 
+# GB300 FP64 issue rate, FMA counted as one operation: 152 SMs x 4
+# sub-partitions x 32 lanes per 64 cycles at the 2.07 GHz maximum clock
+# (1.26 TFLOP/s counting an FMA as two, the published FP64 figure)
+FP64_OPS_PER_S = 152 * 4 * 32 / 64 * 2.07e9
+L2_BYTES = 129e6
+
+
+def form_bandwidth(torch, PETSc):
+    """Standalone kernel sweep: the Vec kernels at n = 2^20 ... 2^26 and the
+    FP64 SpMV, its transpose and the Jacobi apply on 7-point grids 64^3,
+    128^3 and 160^3.
+
+    cold    each repetition reads a 512 MB buffer first, so L2 holds clean
+            lines of another buffer when the kernel starts (the read also
+            covers the host's launch of the kernel), then times ONE launch
+            between two CUDA events; median of the repetitions.  Vectors of
+            2^20 doubles (8 MB) sit in L2 once read, so their writes need not
+            reach HBM inside the timed launch: small sizes measure launch
+            latency as much as bandwidth.
+    stream  (launches that move more than L2 holds) the mean of 8
+            back-to-back launches after one untimed launch.
+
+    GB/s = algorithmic bytes / time.  Each kernel also has an FP64 floor, its
+    FP64 operations / FP64_OPS_PER_S: on GB300 a kernel with fewer than
+    ~11 bytes per FP64 operation is bound by FP64 issue before HBM (norm2,
+    dotNorm2, axpby, axpbypcz; scale and the SpMV come close).  `roof_frac` =
+    max(HBM floor, FP64 floor) / stream time."""
+    import ctypes
+
+    from mojopetsc4py import _device as dev
+    from mojopetsc4py import gallery
+    from mojopetsc4py._lib import check, lib
+
+    L = lib()
+    st = dev.stream_ptr()
+    peak, kind = peaks()
+    flush = torch.ones(64 * 2**20, dtype=torch.float64, device="cuda")
+    fout = torch.empty((), dtype=torch.float64, device="cuda")
+    reps, burst = 15, 8
+
+    def event():
+        e = torch.cuda.Event(enable_timing=True)
+        e.record()
+        return e
+
+    def timed(fn, nbytes):
+        fn()
+        ev = []
+        for _ in range(reps):
+            torch.sum(flush, dim=0, out=fout)
+            e0 = event()
+            fn()
+            ev.append((e0, event()))
+        stream = None
+        if nbytes > L2_BYTES:
+            fn()
+            e0 = event()
+            for _ in range(burst):
+                fn()
+            stream = (e0, event())
+        torch.cuda.synchronize()
+        cold = float(np.median([a.elapsed_time(b) for a, b in ev])) * 1e-3
+        return cold, (stream[0].elapsed_time(stream[1]) * 1e-3 / burst if stream else None)
+
+    def entry(nbytes, fp64_ops, fn):
+        cold, stream = timed(fn, nbytes)
+        out = {"cold_gbs": round(nbytes / cold / 1e9, 1)}
+        if stream:
+            floor = max(nbytes / (peak * 1e9), fp64_ops / FP64_OPS_PER_S)
+            out.update(stream_gbs=round(nbytes / stream / 1e9, 1),
+                       stream_us=round(stream * 1e6, 2),
+                       hbm_floor_us=round(nbytes / (peak * 1e9) * 1e6, 2),
+                       fp64_floor_us=round(fp64_ops / FP64_OPS_PER_S * 1e6, 2),
+                       roof_frac=round(floor / stream, 3))
+        return out
+
+    vec = {}
+    na = ctypes.c_double * 4
+    for p in (20, 22, 24, 26):
+        n = 2**p
+        g = torch.Generator(device="cuda").manual_seed(p)
+        x, w, y, u, z = (torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
+                         for _ in range(5))
+        out = torch.zeros(2, dtype=torch.float64, device="cuda")
+        X, W, Y, O = x.data_ptr(), w.data_ptr(), y.data_ptr(), out.data_ptr()
+        alphas = na(0.5, -0.25, 0.125, -0.0625)
+        xs = (ctypes.c_void_p * 4)(X, W, u.data_ptr(), z.data_ptr())
+
+        def vmap(op, yp, xp=0, wp=0, a=0.5, b=0.25, c=0.125):
+            return lambda: check(L.gp_vec_map(op, n, yp, xp, wp, a, b, c, st))
+
+        def red(op, xp, yp=0):
+            return lambda: check(L.gp_vec_reduce_static(op, n, xp, yp, O, st))
+
+        # (name, algorithmic bytes and FP64 operations per element, one
+        # launch); op codes as in gp_vec_map / gp_vec_reduce_static
+        kernels = (("copy", 16, 0, vmap(0, Y, X)), ("set", 8, 0, vmap(1, Y)),
+                   ("scale", 16, 1, vmap(2, Y, a=0.999)), ("axpy", 24, 1, vmap(4, Y, X)),
+                   ("aypx", 24, 1, vmap(5, Y, X)), ("axpby", 24, 2, vmap(6, Y, X)),
+                   ("axpbypcz", 32, 3, vmap(7, Y, X, W)), ("waxpy", 24, 1, vmap(8, Y, X, W)),
+                   ("pointwiseMult", 24, 1, vmap(9, Y, X, W)),
+                   ("maxpy4", 48, 4,
+                    lambda: check(L.gp_vec_maxpy(n, Y, 4, alphas, xs, st))),
+                   ("dot", 16, 1, red(0, X, W)), ("norm2", 8, 1, red(1, X)),
+                   ("dotNorm2", 16, 2, red(4, X, W)))
+        for name, per, ops, fn in kernels:
+            # keep y finite and of unit size whatever the updates did to it
+            y.copy_(x)
+            vec.setdefault(name, {})[f"2^{p}"] = entry(per * n, ops * n, fn)
+        del x, w, y, u, z, out
+
+    mats = {}
+    for k in (64, 128, 160):
+        ip, ix, v = gallery.laplacian_3d(k)
+        n, nnz = len(ip) - 1, int(ip[-1])
+        A = PETSc.Mat().createSeqAIJ((n, n), nnz=7)
+        A.setValuesCSR(ip, ix, v)
+        A.assemble()
+        xv = PETSc.Vec().createWithArray(np.random.default_rng(3).normal(size=n))
+        yv = PETSc.Vec().createSeq(n)
+        pc = PETSc.PC().create()
+        pc.setType("jacobi")
+        pc.setOperators(A)
+        pc.setUp()
+        h, xp, yp, hp = A._device(), xv._dptr(), yv._optr(), pc._handle()
+        mb = 12 * nnz + 4 * (n + 1) + 16 * n
+        mats[f"{k}^3"] = {
+            "n": n, "nnz": nnz,
+            "spmv": entry(mb, nnz, lambda: check(L.gp_mat_mult(h, xp, yp, st))),
+            "spmv_transpose": entry(mb, nnz, lambda: check(
+                L.gp_mat_mult_transpose(h, xp, yp, st))),
+            "jacobi_apply": entry(24 * n, n, lambda: check(L.gp_pc_apply(hp, xp, yp, st)))}
+        del A, xv, yv, pc
+    return {"peak_gbs": peak, "peak_kind": f"{kind} hbm_gbs",
+            "fp64_ops_per_s": FP64_OPS_PER_S,
+            "timing": f"cold: one launch between CUDA events after a 512 MB read, median of "
+                      f"{reps}; stream: mean of {burst} back-to-back launches (launches moving "
+                      "more than L2); algorithmic bytes = 8 per vector operand and element, "
+                      "SpMV 12 nnz + 4 (n+1) + 16 n, Jacobi 24 n",
+            "vec": vec, "sparse": mats}
+
+
 def _csr_matvec(ip, ix, v, x):
     rows = np.repeat(np.arange(len(ip) - 1), np.diff(ip))
     return np.bincount(rows, weights=v * x[ix], minlength=len(ip) - 1)
@@ -613,7 +755,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline solve only")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--spmv-only", action="store_true", help="SpMV launches only")
-    ap.add_argument("--form", choices=["mixed", "batched", "adjoint"], default=None,
+    ap.add_argument("--form", choices=["mixed", "batched", "adjoint", "bandwidth"], default=None,
                     help="run one of the further forms alone (profiling)")
     ap.add_argument("--batch-systems", type=int, default=512,
                     help="systems in the batched form (512 is the benchmark; fewer "
@@ -634,7 +776,8 @@ def main():
 
         global BATCH_SYSTEMS
         BATCH_SYSTEMS = args.batch_systems
-        fn = {"mixed": form_mixed, "batched": form_batched, "adjoint": form_adjoint}[args.form]
+        fn = {"mixed": form_mixed, "batched": form_batched, "adjoint": form_adjoint,
+              "bandwidth": form_bandwidth}[args.form]
         print(json.dumps({"form": args.form, **fn(torch, PETSc)}), flush=True)
     elif args.spmv_only:
         run_spmv_only(args)

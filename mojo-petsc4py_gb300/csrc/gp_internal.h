@@ -67,10 +67,14 @@ struct Csr {
   bool val32_stale = false;  // values changed since val32 was converted
   int* diagpos = nullptr;    // device, n: slot of a_ii or -1
   bool stream_rows = false;  // SpMV form: false row per thread, true row stream
+  int l2_evict_first = 1;    // row form: matrix loads marked L2 evict-first
   // transpose (built on demand): rows of A^T in ascending original row order
   int* t_rowptr = nullptr;
   int* t_colind = nullptr;
   int* t_src = nullptr;      // slot in A of each A^T entry
+  double* t_val = nullptr;   // A^T's values in its row order (lazily gathered)
+  bool t_val_stale = true;   // values changed since t_val was gathered
+  bool t_stream_rows = false;  // SpMV form of A^T (as stream_rows)
   // host pattern copy for set-up analysis
   std::vector<int> h_rowptr, h_colind;
   bool owns = true;

@@ -527,16 +527,18 @@ __global__ void __launch_bounds__(kSpmvRows) k_cgf_spmv(KspState* st, int n,
                                                         const int* __restrict__ colind,
                                                         const double* __restrict__ val,
                                                         const double* __restrict__ p,
-                                                        double* __restrict__ w, RedSlot slot) {
+                                                        double* __restrict__ w, RedSlot slot,
+                                                        int evict_first) {
   if (st->active != 1) return;
   double v[1] = {0.0};
   if constexpr (!STREAM) {
+    const uint64_t pol = spmv_policy(evict_first);
     // a resident grid walks the row tiles, so each CTA pays the reduction
     // tail once rather than once per 256 rows
     for (int r0 = blockIdx.x * kSpmvRows; r0 < n; r0 += gridDim.x * kSpmvRows) {
       const int row = r0 + threadIdx.x;
       if (row < n) {
-        const double s = spmv_row<FMA>(row, rowptr, colind, val, p, 0.0);
+        const double s = spmv_row<FMA>(row, rowptr, colind, val, p, 0.0, pol);
         w[row] = s;
         v[0] = madd<FMA>(p[row], s, v[0]);
       }
@@ -1324,7 +1326,8 @@ static int cg_body_fused(const Run& r, double* x) {
                              : (f ? k_cgf_spmv<true, false> : k_cgf_spmv<false, false>);
     int grid = spmv_grid(A);
     if (!A->stream_rows) grid = std::min(grid, resident_grid((const void*)ks, kSpmvRows));
-    ks<<<grid, kSpmvRows, 0, r.s>>>(k->st, n, A->rowptr, A->colind, A->val, P, W, k->slot);
+    ks<<<grid, kSpmvRows, 0, r.s>>>(k->st, n, A->rowptr, A->colind, A->val, P, W, k->slot,
+                                     A->l2_evict_first);
   }
   const bool jac = r.pc->opt.type == PC_JACOBI;
   const bool f = arith_mode() == kFma;

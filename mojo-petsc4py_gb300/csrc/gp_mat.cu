@@ -12,12 +12,36 @@
 // ascending original-row order, which is the order the reference's scatter
 // loop adds into y[c]: the gather is bit-identical to the scatter.
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 #include "gp_internal.h"
 #include "gp_spmv.cuh"
 
 namespace gp {
+
+// L2 policy of the row-per-thread SpMV's matrix loads.  Marking the matrix
+// evict-first pays when the vectors a Krylov iteration cycles through (five
+// of n doubles) fit in L2 and the matrix does not: the vectors stay resident
+// while the matrix streams (7-point 128^3 CG + Jacobi: 49.8 ms marked, 53.1
+// unmarked, on GB300).  When everything fits, the mark would only evict the
+// matrix first; when the vectors alone exceed L2, their normal-priority lines
+// fill it and leave the marked stream the spare ways, so the lines the L1
+// re-requests come back from DRAM (7-point 160^3 SpMV: 4.4 TB/s marked, 5.4
+// unmarked).  GPETSC_SPMV_EVICT_FIRST=0/1 overrides the choice.
+static int spmv_evict_first(int n, int64_t nnz) {
+  const char* e = std::getenv("GPETSC_SPMV_EVICT_FIRST");
+  if (e && *e) return std::atoi(e) != 0;
+  int dev = 0, l2 = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess || l2 <= 0) {
+    cudaGetLastError();
+    return 1;
+  }
+  const double vecs = 40.0 * n;
+  const double mat = 12.0 * (double)nnz + 4.0 * ((double)n + 1);
+  return mat + vecs > l2 && vecs <= l2;
+}
 
 template <typename T>
 static int dev_upload(T** d, const T* h, size_t count, cudaStream_t s) {
@@ -42,6 +66,7 @@ static int csr_finish(Csr* A, const double* h_val, cudaStream_t s) {
     maxlen = std::max<int64_t>(maxlen, A->h_rowptr[i + 1] - A->h_rowptr[i]);
   const double avg = n ? (double)A->nnz / n : 0.0;
   A->stream_rows = maxlen > kSpmvMaxRowLen || (double)maxlen > 8.0 * avg + 8.0;
+  A->l2_evict_first = spmv_evict_first(n, A->nnz);
   GP_TRY(dev_upload(&A->rowptr, A->h_rowptr.data(), (size_t)n + 1, s));
   GP_TRY(dev_upload(&A->colind, A->h_colind.data(), (size_t)A->nnz, s));
   GP_TRY(dev_upload(&A->val, h_val, (size_t)A->nnz, s));
@@ -126,9 +151,13 @@ int csr_create_i32(Csr** out, int64_t nrows, int64_t ncols, int64_t nnz,
 
 int csr_set_values(Csr* A, const double* val, int on_device, cudaStream_t s) {
   if (A->nnz == 0) return GP_OK;
-  GP_CUDA(cudaMemcpyAsync(A->val, val, (size_t)A->nnz * sizeof(double),
-                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  // the library's own values array (written in place through
+  // gp_mat_values_ptr) needs no copy, only the caches below marked
+  if (val != A->val)
+    GP_CUDA(cudaMemcpyAsync(A->val, val, (size_t)A->nnz * sizeof(double),
+                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
   A->val32_stale = true;  // converted again, in place, by the next csr_make_val32
+  A->t_val_stale = true;  // gathered again by the next transpose multiply
   return GP_OK;
 }
 
@@ -142,6 +171,7 @@ int csr_destroy(Csr* A) {
   cudaFree(A->t_rowptr);
   cudaFree(A->t_colind);
   cudaFree(A->t_src);
+  cudaFree(A->t_val);
   delete A;
   return GP_OK;
 }
@@ -163,6 +193,10 @@ int csr_build_transpose(Csr* A, cudaStream_t s) {
   GP_TRY(dev_upload(&A->t_rowptr, trp.data(), (size_t)m + 1, s));
   GP_TRY(dev_upload(&A->t_colind, tcol.data(), (size_t)A->nnz, s));
   GP_TRY(dev_upload(&A->t_src, tsrc.data(), (size_t)A->nnz, s));
+  int64_t maxlen = 0;
+  for (int c = 0; c < m; c++) maxlen = std::max<int64_t>(maxlen, trp[c + 1] - trp[c]);
+  const double avg = m ? (double)A->nnz / m : 0.0;
+  A->t_stream_rows = maxlen > kSpmvMaxRowLen || (double)maxlen > 8.0 * avg + 8.0;
   GP_CUDA(cudaStreamSynchronize(s));
   return GP_OK;
 }
@@ -210,6 +244,7 @@ int csr_transpose_values(Csr* A, Csr* T, cudaStream_t s) {
     GP_CHECK_LAUNCH();
   }
   T->val32_stale = true;
+  T->t_val_stale = true;
   return GP_OK;
 }
 
@@ -262,7 +297,7 @@ __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict
                                                     const int* __restrict__ colind,
                                                     const double* __restrict__ val, DRef xr,
                                                     const double* __restrict__ v, DRef yr,
-                                                    const int* gate, int want) {
+                                                    const int* gate, int want, int evict_first) {
   if (gated_off(gate, want)) return;
   const double* __restrict__ x = xr.get();
   double* __restrict__ y = yr.get();
@@ -270,7 +305,8 @@ __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict
   const int row = r0 + threadIdx.x;
   double init = (v != nullptr && row < n) ? v[row] : 0.0;
   if constexpr (!STREAM) {
-    if (row < n) y[row] = spmv_row<FMA>(row, rowptr, colind, val, x, init);
+    if (row < n)
+      y[row] = spmv_row<FMA>(row, rowptr, colind, val, x, init, spmv_policy(evict_first));
     return;
   }
   double s;
@@ -289,23 +325,8 @@ static void launch_spmv(cudaStream_t s, const Csr* A, DRef x, const double* v, D
   const bool f = arith_mode() == kFma;
   auto k = A->stream_rows ? (f ? k_spmv<true, true> : k_spmv<false, true>)
                           : (f ? k_spmv<true, false> : k_spmv<false, false>);
-  k<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, v, y, gate, want);
-}
-
-// y = A^T x over the stored transpose pattern; values gathered through the
-// source slot so a value update needs no rebuild.
-template <bool FMA>
-__global__ void __launch_bounds__(kBlock) k_spmv_t(int m, const int* __restrict__ trp,
-                                                   const int* __restrict__ tcol,
-                                                   const int* __restrict__ tsrc,
-                                                   const double* __restrict__ val,
-                                                   const double* __restrict__ x,
-                                                   double* __restrict__ y) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= m) return;
-  double s = 0.0;
-  for (int k = trp[c]; k < trp[c + 1]; k++) s = madd<FMA>(val[tsrc[k]], x[tcol[k]], s);
-  y[c] = s;
+  k<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, v, y, gate, want,
+                                       A->l2_evict_first);
 }
 
 __global__ void k_diag(int n, const int* __restrict__ diagpos, const double* __restrict__ val,
@@ -332,15 +353,29 @@ int spmv_add(cudaStream_t s, const Csr* A, const double* x, const double* v, dou
   return GP_OK;
 }
 
+// y = A^T x: the row kernels over A^T's pattern and a copy of its values
+// (gathered once per value change through the source slots).  Each row of
+// A^T folds its entries in ascending row order of A, the order in which
+// MatMultTranspose_SeqAIJ (src/ported.mojo:408-431) accumulates y_c.
 int spmv_t(cudaStream_t s, Csr* A, const double* x, double* y) {
   GP_TRY(csr_build_transpose(A, s));
   if (A->ncols == 0) return GP_OK;
-  const int g = (A->ncols + kBlock - 1) / kBlock;
-  if (arith_mode() == kFma)
-    k_spmv_t<true><<<g, kBlock, 0, s>>>(A->ncols, A->t_rowptr, A->t_colind, A->t_src, A->val, x, y);
-  else
-    k_spmv_t<false><<<g, kBlock, 0, s>>>(A->ncols, A->t_rowptr, A->t_colind, A->t_src, A->val, x,
-                                         y);
+  if (!A->t_val) {
+    GP_CUDA(cudaMalloc(&A->t_val, std::max<int64_t>(A->nnz, 1) * sizeof(double)));
+    A->t_val_stale = true;
+  }
+  if (A->t_val_stale && A->nnz) {
+    const int g = (int)std::min<int64_t>((A->nnz + kBlock - 1) / kBlock, 8LL * num_sms());
+    k_gather_values<<<g, kBlock, 0, s>>>(A->nnz, A->t_src, A->val, A->t_val);
+    GP_CHECK_LAUNCH();
+  }
+  A->t_val_stale = false;
+  const bool f = arith_mode() == kFma;
+  auto k = A->t_stream_rows ? (f ? k_spmv<true, true> : k_spmv<false, true>)
+                            : (f ? k_spmv<true, false> : k_spmv<false, false>);
+  k<<<(A->ncols + kSpmvRows - 1) / kSpmvRows, kSpmvRows, 0, s>>>(
+      A->ncols, A->t_rowptr, A->t_colind, A->t_val, DRef::of(x), nullptr, DRef::of(y), nullptr, 0,
+      A->l2_evict_first);
   GP_CHECK_LAUNCH();
   return GP_OK;
 }

@@ -9,8 +9,9 @@
 // loads of a slot range are strided by the row length, but the 32 rows of a
 // warp cover one contiguous span of the arrays, so L1 serves the re-touched
 // lines and DRAM sees each byte once.  Matrix values and indices are read
-// once per product, with an L2 evict-first policy: the solver's vectors stay
-// resident in the 129 MB L2 while the matrix streams through.
+// once per product; where the solver's vectors fit in the 129 MB L2 and the
+// matrix does not, they are loaded with an L2 evict-first policy so the
+// vectors stay resident while the matrix streams through (Csr::l2_evict_first).
 //
 // Row stream (spmv_block_rows*): rows of any length.  One CTA owns kSpmvRows
 // consecutive rows.  The CTA walks the contiguous slot
@@ -37,6 +38,16 @@ __device__ __forceinline__ uint64_t l2_evict_first() {
   asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
   return p;
 }
+__device__ __forceinline__ uint64_t l2_evict_normal() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+// The matrix stream's policy (Csr::l2_evict_first): evict-first keeps the
+// vectors resident, normal lets the stream use L2 like any other data.
+__device__ __forceinline__ uint64_t spmv_policy(int evict_first) {
+  return evict_first ? l2_evict_first() : l2_evict_normal();
+}
 __device__ __forceinline__ double ld_stream(const double* a, uint64_t pol) {
   double v;
   asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
@@ -58,8 +69,7 @@ template <bool FMA, typename VT, typename XT>
 __device__ __forceinline__ double spmv_row(int row, const int* __restrict__ rowptr,
                                            const int* __restrict__ colind,
                                            const VT* __restrict__ val, const XT* __restrict__ x,
-                                           double init) {
-  const uint64_t pol = l2_evict_first();
+                                           double init, uint64_t pol) {
   const int b = rowptr[row], e = rowptr[row + 1];
   double acc = init;
   // four slots per batch: 32 registers, full occupancy (a GB300 scan of

@@ -78,6 +78,30 @@ def test_spmv_rectangular_and_long_rows():
                                atol=1e-11)
 
 
+def test_spmv_transpose_follows_value_changes():
+    """The transpose multiply runs over a cached copy of A^T's values: it
+    must follow a change of A's values, and stay bit-identical to the
+    reference's scatter for long columns too (the row-stream form of A^T)."""
+    rng = np.random.default_rng(4)
+    n = 400
+    d = rng.normal(size=(n, n)) * (rng.random((n, n)) < 0.02)
+    d[:, 7] = rng.normal(size=n)  # a full column: a 400-entry row of A^T
+    np.fill_diagonal(d, 4.0)
+    ip, ix, v = dense_to_csr(d)
+    A = mat(ip, ix, v)
+    x = rng.normal(size=n)
+
+    def want(vals):
+        out = np.zeros(n)
+        O.lib().mp_mat_mult_transpose(a(x), a(out), a(O.i64(ip)), a(O.i64(ix)),
+                                      a(np.ascontiguousarray(vals)), n, n)
+        return out
+
+    np.testing.assert_array_equal(A.multTranspose(vec(x)).getArray(), want(v))
+    A.scale(1.5)
+    np.testing.assert_array_equal(A.multTranspose(vec(x)).getArray(), want(v * 1.5))
+
+
 def test_empty_matrix_and_vectors():
     A = mat(np.zeros(1, dtype=np.int64), np.zeros(0, dtype=np.int64), np.zeros(0))
     y = A.mult(PETSc.Vec().createSeq(0))
