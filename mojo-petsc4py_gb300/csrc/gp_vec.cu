@@ -14,64 +14,142 @@ namespace gp {
 
 // ------------------------------------------------------------------ maps
 
+// Which operands an op reads (y is always written).
+template <int OP>
+struct MapReads {
+  static constexpr bool y = OP == OP_SCALE || OP == OP_DIVS || OP == OP_SHIFT || OP == OP_AXPY ||
+                            OP == OP_AYPX || OP == OP_AXPBY || OP == OP_AXPBYPCZ ||
+                            OP == OP_RECIP || OP == OP_EXP || OP == OP_LOG ||
+                            OP == OP_SQRTABS || OP == OP_ABS;
+  static constexpr bool x = OP == OP_COPY || OP == OP_SCALESET || OP == OP_AXPY ||
+                            OP == OP_AYPX || OP == OP_AXPBY || OP == OP_AXPBYPCZ ||
+                            OP == OP_WAXPY || OP == OP_PMULT || OP == OP_PDIV ||
+                            OP == OP_PMIN || OP == OP_PMAX || OP == OP_PMAXABS;
+  static constexpr bool w = OP == OP_AXPBYPCZ || OP == OP_WAXPY || OP == OP_PMULT ||
+                            OP == OP_PDIV || OP == OP_PMIN || OP == OP_PMAX || OP == OP_PMAXABS;
+};
+
+// One element of an op from its loaded operands.
+template <int OP, bool FMA>
+__device__ __forceinline__ double map_value(double yv, double xv, double wv, double alpha,
+                                            double beta, double gamma) {
+  if constexpr (OP == OP_COPY) {
+    return xv;
+  } else if constexpr (OP == OP_SET) {
+    return alpha;
+  } else if constexpr (OP == OP_ZERO) {
+    return 0.0;
+  } else if constexpr (OP == OP_SCALE) {
+    return mul(yv, alpha);
+  } else if constexpr (OP == OP_SCALESET) {  // x alpha into y
+    return mul(xv, alpha);
+  } else if constexpr (OP == OP_DIVS) {  // y / alpha (VecNormalize)
+    return div_(yv, alpha);
+  } else if constexpr (OP == OP_SHIFT) {
+    return add(yv, alpha);
+  } else if constexpr (OP == OP_AXPY) {  // y + alpha x
+    return madd<FMA>(alpha, xv, yv);
+  } else if constexpr (OP == OP_AYPX) {  // x + alpha y
+    return madd<FMA>(alpha, yv, xv);
+  } else if constexpr (OP == OP_AXPBY) {  // alpha x + beta y
+    return madd<FMA>(alpha, xv, mul(beta, yv));
+  } else if constexpr (OP == OP_AXPBYPCZ) {  // alpha x + beta w + gamma y
+    return madd<FMA>(gamma, yv, madd<FMA>(beta, wv, mul(alpha, xv)));
+  } else if constexpr (OP == OP_WAXPY) {  // alpha x + w
+    return madd<FMA>(alpha, xv, wv);
+  } else if constexpr (OP == OP_PMULT) {
+    return mul(xv, wv);
+  } else if constexpr (OP == OP_PDIV) {
+    return div_(xv, wv);
+  } else if constexpr (OP == OP_PMIN) {
+    return (wv < xv) ? wv : xv;
+  } else if constexpr (OP == OP_PMAX) {
+    return (wv > xv) ? wv : xv;
+  } else if constexpr (OP == OP_PMAXABS) {
+    const double a = fabs(xv), b = fabs(wv);
+    return (b > a) ? b : a;
+  } else if constexpr (OP == OP_RECIP) {
+    return (yv == 0.0) ? 0.0 : div_(1.0, yv);
+  } else if constexpr (OP == OP_EXP) {
+    return exp(yv);
+  } else if constexpr (OP == OP_LOG) {
+    return log(yv);
+  } else if constexpr (OP == OP_SQRTABS) {
+    return __dsqrt_rn(fabs(yv));
+  } else {
+    static_assert(OP == OP_ABS, "map op");
+    return fabs(yv);
+  }
+}
+
+// Elements a thread takes per trip (kMapU, or 1 where noted); all their
+// loads are issued before the arithmetic.  With one element a trip a thread
+// has one load per operand in flight and then waits on its FP64 operation
+// (which holds the sub-partition's FP64 pipe ~64 cycles on GB300): scale,
+// axpby, axpbypcz, maxpy and the two-operand reductions ran 4-8% faster with
+// four, while axpy, aypx and the one-operand reductions ran 3-5% slower
+// (2^24-2^26 doubles), so those keep one.
+constexpr int kMapU = 4;
+
+template <int OP>
+__host__ __device__ constexpr int map_unroll() {
+  return (OP == OP_AXPY || OP == OP_AYPX) ? 1 : kMapU;
+}
+
+// Warp-contiguous trips: the grid's warps take chunks of 32 U consecutive
+// elements round robin (lane l of a warp owns elements c + 32 u + l of its
+// chunk c), so each trip of a warp touches one contiguous span of 256 U
+// bytes per operand; the ragged end (fewer than 32 U elements) goes one
+// element a thread.  `body(idx[U])` handles one trip, `tail(i)` one element.
+template <int U, typename Body, typename Tail>
+__device__ __forceinline__ void warp_chunks(int64_t n, Body body, Tail tail) {
+  constexpr int64_t C = 32 * U;
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t full = n / C;
+  for (int64_t c = gw; c < full; c += nw) {
+    int64_t idx[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) idx[u] = c * C + 32 * u + lane;
+    body(idx);
+  }
+  for (int64_t i = full * C + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    tail(i);
+}
+
 template <int OP, bool FMA>
 __global__ void __launch_bounds__(kBlock) k_map(int64_t n, double* __restrict__ y,
                                                 const double* __restrict__ x,
                                                 const double* __restrict__ w, double alpha,
                                                 double beta, double gamma) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    if constexpr (OP == OP_COPY) {
-      y[i] = x[i];
-    } else if constexpr (OP == OP_SET) {
-      y[i] = alpha;
-    } else if constexpr (OP == OP_ZERO) {
-      y[i] = 0.0;
-    } else if constexpr (OP == OP_SCALE) {
-      y[i] = mul(y[i], alpha);
-    } else if constexpr (OP == OP_SCALESET) {  // x alpha into y
-      y[i] = mul(x[i], alpha);
-    } else if constexpr (OP == OP_DIVS) {  // y / alpha (VecNormalize)
-      y[i] = div_(y[i], alpha);
-    } else if constexpr (OP == OP_SHIFT) {
-      y[i] = add(y[i], alpha);
-    } else if constexpr (OP == OP_AXPY) {  // y + alpha x
-      y[i] = madd<FMA>(alpha, x[i], y[i]);
-    } else if constexpr (OP == OP_AYPX) {  // x + alpha y
-      y[i] = madd<FMA>(alpha, y[i], x[i]);
-    } else if constexpr (OP == OP_AXPBY) {  // alpha x + beta y
-      y[i] = madd<FMA>(alpha, x[i], mul(beta, y[i]));
-    } else if constexpr (OP == OP_AXPBYPCZ) {  // alpha x + beta w + gamma y
-      y[i] = madd<FMA>(gamma, y[i], madd<FMA>(beta, w[i], mul(alpha, x[i])));
-    } else if constexpr (OP == OP_WAXPY) {  // alpha x + w
-      y[i] = madd<FMA>(alpha, x[i], w[i]);
-    } else if constexpr (OP == OP_PMULT) {
-      y[i] = mul(x[i], w[i]);
-    } else if constexpr (OP == OP_PDIV) {
-      y[i] = div_(x[i], w[i]);
-    } else if constexpr (OP == OP_PMIN) {
-      double a = x[i], b = w[i];
-      y[i] = (b < a) ? b : a;
-    } else if constexpr (OP == OP_PMAX) {
-      double a = x[i], b = w[i];
-      y[i] = (b > a) ? b : a;
-    } else if constexpr (OP == OP_PMAXABS) {
-      double a = fabs(x[i]), b = fabs(w[i]);
-      y[i] = (b > a) ? b : a;
-    } else if constexpr (OP == OP_RECIP) {
-      double v = y[i];
-      y[i] = (v == 0.0) ? 0.0 : div_(1.0, v);
-    } else if constexpr (OP == OP_EXP) {
-      y[i] = exp(y[i]);
-    } else if constexpr (OP == OP_LOG) {
-      y[i] = log(y[i]);
-    } else if constexpr (OP == OP_SQRTABS) {
-      y[i] = __dsqrt_rn(fabs(y[i]));
-    } else if constexpr (OP == OP_ABS) {
-      y[i] = fabs(y[i]);
-    } else if constexpr (OP == OP_CHOP) {
+  using R = MapReads<OP>;
+  if constexpr (OP == OP_CHOP) {  // writes only the entries it zeroes
+    const int64_t T = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += T)
       if (fabs(y[i]) < alpha) y[i] = 0.0;
-    }
+    return;
+  } else {
+    constexpr int U = map_unroll<OP>();
+    warp_chunks<U>(
+        n,
+        [&](const int64_t* idx) {
+          double yv[U], xv[U], wv[U];
+#pragma unroll
+          for (int u = 0; u < U; u++) {
+            yv[u] = R::y ? y[idx[u]] : 0.0;
+            xv[u] = R::x ? x[idx[u]] : 0.0;
+            wv[u] = R::w ? w[idx[u]] : 0.0;
+          }
+#pragma unroll
+          for (int u = 0; u < U; u++)
+            y[idx[u]] = map_value<OP, FMA>(yv[u], xv[u], wv[u], alpha, beta, gamma);
+        },
+        [&](int64_t j) {
+          y[j] = map_value<OP, FMA>(R::y ? y[j] : 0.0, R::x ? x[j] : 0.0, R::w ? w[j] : 0.0,
+                                    alpha, beta, gamma);
+        });
   }
 }
 
@@ -84,8 +162,8 @@ __global__ void __launch_bounds__(kBlock) k_swap(int64_t n, double* a, double* b
   }
 }
 
-static int map_grid(int64_t n) {
-  int64_t g = (n + kBlock - 1) / kBlock;
+static int map_grid(int64_t n, int unroll = kMapU) {
+  int64_t g = (n + (int64_t)kBlock * unroll - 1) / ((int64_t)kBlock * unroll);
   int64_t cap = (int64_t)num_sms() * 16;
   return (int)std::max<int64_t>(1, std::min(g, cap));
 }
@@ -95,9 +173,9 @@ static int launch_map(cudaStream_t s, int64_t n, double* y, const double* x, con
                       double a, double b, double c) {
   if (n <= 0) return GP_OK;
   if (arith_mode() == kFma)
-    k_map<OP, true><<<map_grid(n), kBlock, 0, s>>>(n, y, x, w, a, b, c);
+    k_map<OP, true><<<map_grid(n, map_unroll<OP>()), kBlock, 0, s>>>(n, y, x, w, a, b, c);
   else
-    k_map<OP, false><<<map_grid(n), kBlock, 0, s>>>(n, y, x, w, a, b, c);
+    k_map<OP, false><<<map_grid(n, map_unroll<OP>()), kBlock, 0, s>>>(n, y, x, w, a, b, c);
   GP_CHECK_LAUNCH();
   return GP_OK;
 }
@@ -146,7 +224,7 @@ int vec_map(cudaStream_t s, int op, int64_t n, double* y, const double* x, const
     case OP_CHOP: return launch_map<OP_CHOP>(s, n, y, x, w, alpha, 0, 0);
     case OP_SWAP:
       if (n <= 0) return GP_OK;
-      k_swap<<<map_grid(n), kBlock, 0, s>>>(n, y, const_cast<double*>(x));
+      k_swap<<<map_grid(n, 1), kBlock, 0, s>>>(n, y, const_cast<double*>(x));
       GP_CHECK_LAUNCH();
       return GP_OK;
   }
@@ -167,12 +245,30 @@ struct MaxpyArgs {
 
 template <bool FMA>
 __global__ void __launch_bounds__(kBlock) k_maxpy(int64_t n, double* __restrict__ y, MaxpyArgs args) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    double v = y[i];
-    for (int k = 0; k < args.nv; k++) v = madd<FMA>(args.a[k], args.x[k][i], v);
-    y[i] = v;
-  }
+  // kMapU elements a trip: their k-th loads go out together and their
+  // update chains interleave
+  warp_chunks<kMapU>(
+      n,
+      [&](const int64_t* idx) {
+        double v[kMapU];
+#pragma unroll
+        for (int u = 0; u < kMapU; u++) v[u] = y[idx[u]];
+        for (int k = 0; k < args.nv; k++) {
+          const double* __restrict__ xk = args.x[k];
+          double t[kMapU];
+#pragma unroll
+          for (int u = 0; u < kMapU; u++) t[u] = xk[idx[u]];
+#pragma unroll
+          for (int u = 0; u < kMapU; u++) v[u] = madd<FMA>(args.a[k], t[u], v[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < kMapU; u++) y[idx[u]] = v[u];
+      },
+      [&](int64_t j) {
+        double v = y[j];
+        for (int k = 0; k < args.nv; k++) v = madd<FMA>(args.a[k], args.x[k][j], v);
+        y[j] = v;
+      });
 }
 
 int vec_maxpy(cudaStream_t s, int64_t n, double* y, int nv, const double* alpha,
@@ -203,11 +299,10 @@ __global__ void __launch_bounds__(kRedBlock) k_reduce(int64_t n, const double* _
   double v[NR];
 #pragma unroll
   for (int r = 0; r < NR; r++) v[r] = 0.0;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    double a = x[i];
+  constexpr bool RY = OP == RED_DOT || OP == RED_DOTNORM2;
+  auto fold = [&](double a, double b) {
     if constexpr (OP == RED_DOT) {
-      v[0] = madd<FMA>(a, y[i], v[0]);
+      v[0] = madd<FMA>(a, b, v[0]);
     } else if constexpr (OP == RED_NORM2SQ) {
       v[0] = madd<FMA>(a, a, v[0]);
     } else if constexpr (OP == RED_ASUM) {
@@ -215,10 +310,26 @@ __global__ void __launch_bounds__(kRedBlock) k_reduce(int64_t n, const double* _
     } else if constexpr (OP == RED_SUM) {
       v[0] = add(v[0], a);
     } else if constexpr (OP == RED_DOTNORM2) {
-      v[0] = madd<FMA>(a, y[i], v[0]);
+      v[0] = madd<FMA>(a, b, v[0]);
       v[1] = madd<FMA>(a, a, v[1]);
     }
-  }
+  };
+  // each thread folds its elements in a fixed order (warp-contiguous trips,
+  // then the ragged end); the loads of a trip go out before its folds
+  constexpr int U = RY ? kMapU : 1;
+  warp_chunks<U>(
+      n,
+      [&](const int64_t* idx) {
+        double a[U], b[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          a[u] = x[idx[u]];
+          b[u] = RY ? y[idx[u]] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) fold(a[u], b[u]);
+      },
+      [&](int64_t j) { fold(x[j], RY ? y[j] : 0.0); });
   double tot[NR];
   if (grid_finish<NR>(v, slot, tot) && threadIdx.x == 0) {
 #pragma unroll
