@@ -272,12 +272,15 @@ def spmv_roofline(torch, PETSc, A, n, nnz, launches=20):
 
 
 def run_spmv_only(args):
-    """SpMV launches alone on the benchmark matrix (the profiling target)."""
+    """SpMV launches alone on the 7-point matrix of a k^3 grid (k =
+    --spmv-grid, the benchmark's 128 by default; the profiling target)."""
     import torch
 
     from mojopetsc4py import PETSc
 
-    ip, ix, v, _ = problem()
+    from mojopetsc4py import gallery
+
+    ip, ix, v = gallery.laplacian_3d(args.spmv_grid)
     n, nnz = len(ip) - 1, int(ip[-1])
     A = PETSc.Mat().createSeqAIJ((n, n), nnz=7)
     A.setValuesCSR(ip, ix, v)
@@ -599,6 +602,57 @@ def form_adjoint(torch, PETSc):
             "finite_difference_equivalent_ms": round(2 * int(ip[-1]) * plain["forward_ms"], 0)}
 
 
+def vec_kernels(torch, n, seed=0):
+    """The Vec kernels of the bandwidth sweep on vectors of n doubles:
+    (vectors, [(name, algorithmic bytes and FP64 operations per element, one
+    launch through the C ABI)]); op codes as in gp_vec_map /
+    gp_vec_reduce_static.  The vectors must outlive the launches."""
+    import ctypes
+
+    from mojopetsc4py import _device as dev
+    from mojopetsc4py._lib import check, lib
+
+    L, st = lib(), dev.stream_ptr()
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    x, w, y, u, z = (torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
+                     for _ in range(5))
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    X, W, Y, O = x.data_ptr(), w.data_ptr(), y.data_ptr(), out.data_ptr()
+    alphas = (ctypes.c_double * 4)(0.5, -0.25, 0.125, -0.0625)
+    xs = (ctypes.c_void_p * 4)(X, W, u.data_ptr(), z.data_ptr())
+
+    def vmap(op, yp, xp=0, wp=0, a=0.5, b=0.25, c=0.125):
+        return lambda: check(L.gp_vec_map(op, n, yp, xp, wp, a, b, c, st))
+
+    def red(op, xp, yp=0):
+        return lambda: check(L.gp_vec_reduce_static(op, n, xp, yp, O, st))
+
+    kernels = [("copy", 16, 0, vmap(0, Y, X)), ("set", 8, 0, vmap(1, Y)),
+               ("scale", 16, 1, vmap(2, Y, a=0.999)), ("axpy", 24, 1, vmap(4, Y, X)),
+               ("aypx", 24, 1, vmap(5, Y, X)), ("axpby", 24, 2, vmap(6, Y, X)),
+               ("axpbypcz", 32, 3, vmap(7, Y, X, W)), ("waxpy", 24, 1, vmap(8, Y, X, W)),
+               ("pointwiseMult", 24, 1, vmap(9, Y, X, W)),
+               ("maxpy4", 48, 4, lambda: check(L.gp_vec_maxpy(n, Y, 4, alphas, xs, st))),
+               ("dot", 16, 1, red(0, X, W)), ("norm2", 8, 1, red(1, X)),
+               ("dotNorm2", 16, 2, red(4, X, W))]
+    return (x, w, y, u, z, out, alphas, xs), kernels
+
+
+def run_vec_only(args):
+    """Each Vec kernel of the sweep launched twice on vectors of 2^P doubles
+    (the profiling target; no timing)."""
+    import torch
+
+    vs, kernels = vec_kernels(torch, 2**args.vec_only, seed=1)
+    for name, _, _, fn in kernels:
+        vs[2].copy_(vs[0])
+        fn()
+        fn()
+    torch.cuda.synchronize()
+    print(json.dumps({"vec_only": args.vec_only, "kernels": [k[0] for k in kernels]}),
+          flush=True)
+
+
 # GB300 FP64 issue rate, FMA counted as one operation: 152 SMs x 4
 # sub-partitions x 32 lanes per 64 cycles at the 2.07 GHz maximum clock
 # (1.26 TFLOP/s counting an FMA as two, the published FP64 figure)
@@ -626,8 +680,6 @@ def form_bandwidth(torch, PETSc):
     ~11 bytes per FP64 operation is bound by FP64 issue before HBM (norm2,
     dotNorm2, axpby, axpbypcz; scale and the SpMV come close).  `roof_frac` =
     max(HBM floor, FP64 floor) / stream time."""
-    import ctypes
-
     from mojopetsc4py import _device as dev
     from mojopetsc4py import gallery
     from mojopetsc4py._lib import check, lib
@@ -676,39 +728,14 @@ def form_bandwidth(torch, PETSc):
         return out
 
     vec = {}
-    na = ctypes.c_double * 4
     for p in (20, 22, 24, 26):
         n = 2**p
-        g = torch.Generator(device="cuda").manual_seed(p)
-        x, w, y, u, z = (torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
-                         for _ in range(5))
-        out = torch.zeros(2, dtype=torch.float64, device="cuda")
-        X, W, Y, O = x.data_ptr(), w.data_ptr(), y.data_ptr(), out.data_ptr()
-        alphas = na(0.5, -0.25, 0.125, -0.0625)
-        xs = (ctypes.c_void_p * 4)(X, W, u.data_ptr(), z.data_ptr())
-
-        def vmap(op, yp, xp=0, wp=0, a=0.5, b=0.25, c=0.125):
-            return lambda: check(L.gp_vec_map(op, n, yp, xp, wp, a, b, c, st))
-
-        def red(op, xp, yp=0):
-            return lambda: check(L.gp_vec_reduce_static(op, n, xp, yp, O, st))
-
-        # (name, algorithmic bytes and FP64 operations per element, one
-        # launch); op codes as in gp_vec_map / gp_vec_reduce_static
-        kernels = (("copy", 16, 0, vmap(0, Y, X)), ("set", 8, 0, vmap(1, Y)),
-                   ("scale", 16, 1, vmap(2, Y, a=0.999)), ("axpy", 24, 1, vmap(4, Y, X)),
-                   ("aypx", 24, 1, vmap(5, Y, X)), ("axpby", 24, 2, vmap(6, Y, X)),
-                   ("axpbypcz", 32, 3, vmap(7, Y, X, W)), ("waxpy", 24, 1, vmap(8, Y, X, W)),
-                   ("pointwiseMult", 24, 1, vmap(9, Y, X, W)),
-                   ("maxpy4", 48, 4,
-                    lambda: check(L.gp_vec_maxpy(n, Y, 4, alphas, xs, st))),
-                   ("dot", 16, 1, red(0, X, W)), ("norm2", 8, 1, red(1, X)),
-                   ("dotNorm2", 16, 2, red(4, X, W)))
+        vs, kernels = vec_kernels(torch, n, seed=p)
         for name, per, ops, fn in kernels:
             # keep y finite and of unit size whatever the updates did to it
-            y.copy_(x)
+            vs[2].copy_(vs[0])
             vec.setdefault(name, {})[f"2^{p}"] = entry(per * n, ops * n, fn)
-        del x, w, y, u, z, out
+        del vs, kernels
 
     mats = {}
     for k in (64, 128, 160):
@@ -755,6 +782,10 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline solve only")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--spmv-only", action="store_true", help="SpMV launches only")
+    ap.add_argument("--spmv-grid", type=int, default=K3,
+                    help="grid size k of the k^3 matrix for --spmv-only")
+    ap.add_argument("--vec-only", type=int, default=None, metavar="P",
+                    help="launch each Vec kernel twice on 2^P doubles (profiling)")
     ap.add_argument("--form", choices=["mixed", "batched", "adjoint", "bandwidth"], default=None,
                     help="run one of the further forms alone (profiling)")
     ap.add_argument("--batch-systems", type=int, default=512,
@@ -781,6 +812,8 @@ def main():
         print(json.dumps({"form": args.form, **fn(torch, PETSc)}), flush=True)
     elif args.spmv_only:
         run_spmv_only(args)
+    elif args.vec_only is not None:
+        run_vec_only(args)
     elif args.impl == "reference":
         run_reference(args, world, rank, pg)
     else:
