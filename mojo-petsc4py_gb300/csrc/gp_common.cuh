@@ -96,6 +96,19 @@ struct DevErr {
 // result can never equal it.
 constexpr unsigned long long kPending = 0x7FF4DEAD0BADF00DULL;
 
+// Programmatic dependent launch.  A kernel launched with the programmatic
+// stream-serialization attribute may be scheduled while its predecessor in
+// the stream drains; pdl_wait() blocks (in hardware, no polling) until that
+// predecessor has completed and its writes are visible, so it must come
+// before the first access to anything the predecessor writes, and before the
+// kernel can exit (a successor's wait covers only this grid).  pdl_trigger()
+// lets this grid's own successor be scheduled once every CTA has issued it.
+// Both are no-ops for a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ double ld_relaxed(const double* p) {
   unsigned long long v;
   asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");

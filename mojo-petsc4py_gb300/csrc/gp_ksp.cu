@@ -70,6 +70,33 @@ __device__ int conv_default(KspState* st, int n, double rnorm) {
       K<false><<<(G), (B), 0, (S)>>>(__VA_ARGS__);            \
   } while (0)
 
+// Launch with programmatic dependent launch allowed (the kernel calls
+// pdl_wait() before touching its predecessor's output).  GPETSC_PDL=0 turns
+// the attribute off: ordinary stream order, same kernels.
+static bool pdl_enabled() {
+  static bool v = [] {
+    const char* e = std::getenv("GPETSC_PDL");
+    return !(e && std::string(e) == "0");
+  }();
+  return v;
+}
+
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t s,
+                              Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // ------------------------------------------------------------ vector kernels
 static int vgrid(int n) { return std::max(1, std::min((n + 255) / 256, num_sms() * 8)); }
 
@@ -349,6 +376,7 @@ __device__ __forceinline__ bool loop_trip(KspState* st) {
 }
 
 __global__ void k_loop_ctrl(cudaGraphConditionalHandle h, KspState* st) {
+  pdl_wait();
   cudaGraphSetConditional(h, loop_trip(st) ? 1u : 0u);
 }
 
@@ -505,6 +533,7 @@ __device__ void cg_tail(KspState* st, double* hist, double dp, double zr, bool f
 template <bool FMA>
 __global__ void k_cgf_p(KspState* st, int n, double* __restrict__ p,
                         const double* __restrict__ z) {
+  pdl_trigger();
   if (st->active != 1) return;
   const double bc = st->bcoef;
   constexpr int U = kVecBatch;
@@ -529,6 +558,8 @@ __global__ void __launch_bounds__(kSpmvRows) k_cgf_spmv(KspState* st, int n,
                                                         const double* __restrict__ p,
                                                         double* __restrict__ w, RedSlot slot,
                                                         int evict_first) {
+  pdl_wait();
+  pdl_trigger();
   if (st->active != 1) return;
   double v[1] = {0.0};
   if constexpr (!STREAM) {
@@ -580,6 +611,8 @@ __global__ void __launch_bounds__(kRedBlock, 4) k_cgf_update(
     KspState* st, double* hist, int n, double* __restrict__ x, double* __restrict__ r,
     const double* __restrict__ p, const double* w, double* z, const double* __restrict__ d,
     RedSlot slot) {
+  pdl_wait();
+  pdl_trigger();
   if (st->active != 1) return;
   const double al = st->a, nal = -al;
   double v[2] = {0.0, 0.0};
@@ -1326,19 +1359,17 @@ static int cg_body_fused(const Run& r, double* x) {
                              : (f ? k_cgf_spmv<true, false> : k_cgf_spmv<false, false>);
     int grid = spmv_grid(A);
     if (!A->stream_rows) grid = std::min(grid, resident_grid((const void*)ks, kSpmvRows));
-    ks<<<grid, kSpmvRows, 0, r.s>>>(k->st, n, A->rowptr, A->colind, A->val, P, W, k->slot,
-                                     A->l2_evict_first);
+    GP_CUDA(launch_pdl(ks, grid, kSpmvRows, r.s, k->st, n, (const int*)A->rowptr,
+                       (const int*)A->colind, (const double*)A->val, (const double*)P, W,
+                       k->slot, A->l2_evict_first));
   }
   const bool jac = r.pc->opt.type == PC_JACOBI;
   const bool f = arith_mode() == kFma;
   const int g = red_grid(n);
   if (jac) {
-    if (f)
-      k_cgf_update<true, true><<<g, kRedBlock, 0, r.s>>>(k->st, k->hist, n, x, R, P, W, Z,
-                                                         r.pc->diag, k->slot);
-    else
-      k_cgf_update<false, true><<<g, kRedBlock, 0, r.s>>>(k->st, k->hist, n, x, R, P, W, Z,
-                                                          r.pc->diag, k->slot);
+    GP_CUDA(launch_pdl(f ? k_cgf_update<true, true> : k_cgf_update<false, true>, g, kRedBlock,
+                       r.s, k->st, k->hist, n, x, R, (const double*)P, (const double*)W, Z,
+                       (const double*)r.pc->diag, k->slot));
   } else {
     if (f)
       k_cgf_update<true, false><<<g, kRedBlock, 0, r.s>>>(k->st, k->hist, n, x, R, P, W, Z,
@@ -1723,7 +1754,13 @@ static int capture(const Run& r, const double* b, double* x) {
       // several gated copies of the body per conditional trip amortise the
       // conditional node's re-launch; copies after convergence are no-ops
       for (int u = 0; u < body_unroll() && st == GP_OK; u++) st = run_body(rb, b, x);
-      if (st == GP_OK) k_loop_ctrl<<<1, 1, 0, k->stream2>>>(h, k->st);
+      if (st == GP_OK) {
+        cudaError_t el = launch_pdl(k_loop_ctrl, 1, 1, k->stream2, h, k->st);
+        if (el != cudaSuccess) {
+          set_error(std::string("loop control launch: ") + cudaGetErrorString(el));
+          st = GP_ERR_CUDA;
+        }
+      }
       cudaGraph_t bout = nullptr;
       cudaError_t eb = cudaStreamEndCapture(k->stream2, &bout);
       if (st == GP_OK && eb != cudaSuccess) {
