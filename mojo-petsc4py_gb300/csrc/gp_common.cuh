@@ -15,6 +15,9 @@
 //     kernel records an error code in device memory and moves on.
 #pragma once
 
+#include <cstdlib>
+#include <string>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -107,6 +110,33 @@ constexpr unsigned long long kPending = 0x7FF4DEAD0BADF00DULL;
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launch with programmatic dependent launch allowed (the kernel calls
+// pdl_wait() before touching its predecessor's output).  GPETSC_PDL=0 turns
+// the attribute off: ordinary stream order, same kernels.
+inline bool pdl_enabled() {
+  static bool v = [] {
+    const char* e = std::getenv("GPETSC_PDL");
+    return !(e && std::string(e) == "0");
+  }();
+  return v;
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t s,
+                              Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
 __device__ __forceinline__ double ld_relaxed(const double* p) {

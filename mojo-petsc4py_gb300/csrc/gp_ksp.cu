@@ -70,33 +70,6 @@ __device__ int conv_default(KspState* st, int n, double rnorm) {
       K<false><<<(G), (B), 0, (S)>>>(__VA_ARGS__);            \
   } while (0)
 
-// Launch with programmatic dependent launch allowed (the kernel calls
-// pdl_wait() before touching its predecessor's output).  GPETSC_PDL=0 turns
-// the attribute off: ordinary stream order, same kernels.
-static bool pdl_enabled() {
-  static bool v = [] {
-    const char* e = std::getenv("GPETSC_PDL");
-    return !(e && std::string(e) == "0");
-  }();
-  return v;
-}
-
-template <typename... KArgs, typename... Args>
-static cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t s,
-                              Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
-}
-
 // ------------------------------------------------------------ vector kernels
 static int vgrid(int n) { return std::max(1, std::min((n + 255) / 256, num_sms() * 8)); }
 

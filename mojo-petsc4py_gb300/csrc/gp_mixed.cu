@@ -999,6 +999,8 @@ __global__ void k_mx_beta(MixDev* st, int m) {
 
 // out = in / beta (which = 0) or in / sqrt(hn2) (which = 1), while active
 __global__ void k_mx_scale(int n, const float* in, float* out, const MixDev* st, int which) {
+  pdl_wait();
+  pdl_trigger();
   if (!st->active) return;
   const float s = which == 0 ? st->inv_beta : st->inv_hn;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -1013,6 +1015,8 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_tri(
     const float* __restrict__ val, const float* __restrict__ dinv, const float* __restrict__ rhs,
     const int* __restrict__ rhs_perm, const float* __restrict__ in, const int* __restrict__ in_perm,
     const float* __restrict__ in_scale, float* __restrict__ out, const int* __restrict__ out_perm) {
+  pdl_wait();
+  pdl_trigger();
   if (gated_off(gate, 1)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -1044,6 +1048,8 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_tri_ell(
     const int* __restrict__ rhs_perm, const float* __restrict__ in,
     const int* __restrict__ in_perm, const float* __restrict__ in_scale, float* __restrict__ out,
     const int* __restrict__ out_perm) {
+  pdl_wait();
+  pdl_trigger();
   if (gated_off(gate, 1)) return;
   const int stride = gridDim.x * blockDim.x;
   const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1092,6 +1098,8 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_spmv32(const int* gate, int n,
                                                          const float* __restrict__ val,
                                                          const float* __restrict__ x,
                                                          float* __restrict__ y) {
+  pdl_wait();
+  pdl_trigger();
   if (gated_off(gate, 1)) return;
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= n) return;
@@ -1111,6 +1119,8 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_maxpy_norm(const int* gate, in
                                                              float* __restrict__ w,
                                                              double* __restrict__ partials,
                                                              unsigned* ticket, double* out) {
+  pdl_wait();
+  pdl_trigger();
   if (gated_off(gate, 1)) return;
   __shared__ float hs[kMixMaxM + 1];
   __shared__ float sh[kMixBlock / 32];
@@ -1177,6 +1187,8 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_maxpy_norm(const int* gate, in
 // shared memory -- the chain is the FP64 arithmetic, not a memory round trip
 // per rotation.
 __global__ void k_mx_givens(MixDev* st, const double* __restrict__ h, int j, int m) {
+  pdl_wait();
+  pdl_trigger();
   if (!st->active) return;
   __shared__ double col[kMixMaxM + 1], cs[kMixMaxM], sn[kMixMaxM];
   for (int i = threadIdx.x; i <= j; i += blockDim.x) {
@@ -1269,6 +1281,8 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_mdot(const int* gate, int n,
                                                        const float* __restrict__ w,
                                                        double* __restrict__ partials,
                                                        unsigned* ticket, double* out) {
+  pdl_wait();
+  pdl_trigger();
   if (gated_off(gate, 1)) return;
   __shared__ float sh[kMixBlock / 32][kMixMaxM + 1];
   __shared__ bool last;
@@ -1349,8 +1363,8 @@ static void tri_pass(int W, const int* eci, const float* eval, const int* rp, co
   const int gr = (n + kMixBlock * kTriRows - 1) / (kMixBlock * kTriRows);
 #define GP_TRI_ELL(WW)                                                                     \
   case WW:                                                                                 \
-    k_mx_tri_ell<WW><<<gr, kMixBlock, 0, s>>>(gate, n, eci, eval, dinv, rhs, rhs_perm, in,  \
-                                             in_perm, in_scale, out, out_perm);            \
+    (void)launch_pdl(k_mx_tri_ell<WW>, gr, kMixBlock, s, gate, n, eci, eval, dinv, rhs,   \
+                     rhs_perm, in, in_perm, in_scale, out, out_perm);                      \
     return;
   switch (W) {
     GP_TRI_ELL(1)
@@ -1365,8 +1379,8 @@ static void tri_pass(int W, const int* eci, const float* eval, const int* rp, co
       break;
   }
 #undef GP_TRI_ELL
-  k_mx_tri<<<(n + kMixBlock - 1) / kMixBlock, kMixBlock, 0, s>>>(
-      gate, n, rp, ci, val, dinv, rhs, rhs_perm, in, in_perm, in_scale, out, out_perm);
+  (void)launch_pdl(k_mx_tri, (n + kMixBlock - 1) / kMixBlock, kMixBlock, s, gate, n, rp, ci, val,
+                   dinv, rhs, rhs_perm, in, in_perm, in_scale, out, out_perm);
 }
 
 // Record one refinement pass into the current capture on stream s.
@@ -1445,13 +1459,17 @@ static int record_pass(Mixed* M, const Csr* A, const Pc* pc, const double* b, do
       GP_TRY(pc_apply(const_cast<Pc*>(pc), DRef::of(M->y), DRef::of(M->r), s, act, 1));
       k_mx_cast32<<<g, kMixBlock, 0, s>>>(act, n, M->r, zj);
     }
-    k_mx_spmv32<<<gr, kMixBlock, 0, s>>>(act, n, A->rowptr, A->colind, A->val32, zj, M->w);
-    k_mx_mdot<<<mdot_grid(n), kMixBlock, 0, s>>>(act, n, M->V, j + 1, M->w, M->partials, M->ticket,
-                                       M->h_dev);
-    k_mx_maxpy_norm<<<g, kMixBlock, 0, s>>>(act, n, M->V, j + 1, M->h_dev, M->w, M->partials,
-                                            M->ticket, &st->hn2);
-    k_mx_givens<<<1, 32, 0, s>>>(st, M->h_dev, j, m);
-    if (j + 1 < m) k_mx_scale<<<g, kMixBlock, 0, s>>>(n, M->w, M->V + (size_t)(j + 1) * n, st, 1);
+    // the step's kernels start while their predecessor drains (each waits
+    // in pdl_wait() before reading it)
+    GP_CUDA(launch_pdl(k_mx_spmv32, gr, kMixBlock, s, act, n, A->rowptr, A->colind, A->val32,
+                       zj, M->w));
+    GP_CUDA(launch_pdl(k_mx_mdot, mdot_grid(n), kMixBlock, s, act, n, M->V, j + 1, M->w,
+                       M->partials, M->ticket, M->h_dev));
+    GP_CUDA(launch_pdl(k_mx_maxpy_norm, g, kMixBlock, s, act, n, M->V, j + 1, M->h_dev, M->w,
+                       M->partials, M->ticket, &st->hn2));
+    GP_CUDA(launch_pdl(k_mx_givens, 1, 32, s, st, M->h_dev, j, m));
+    if (j + 1 < m)
+      GP_CUDA(launch_pdl(k_mx_scale, g, kMixBlock, s, n, M->w, M->V + (size_t)(j + 1) * n, st, 1));
   }
   k_mx_backsub<<<1, 32, 0, s>>>(st, m);
   k_mx_correct<<<g, kMixBlock, 0, s>>>(n, M->Z, st, x);
