@@ -1048,24 +1048,52 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_tri_ell(
     const int* __restrict__ rhs_perm, const float* __restrict__ in,
     const int* __restrict__ in_perm, const float* __restrict__ in_scale, float* __restrict__ out,
     const int* __restrict__ out_perm) {
-  pdl_wait();
-  pdl_trigger();
-  if (gated_off(gate, 1)) return;
   const int stride = gridDim.x * blockDim.x;
   const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
   int c[kTriRows][W];
   float a[kTriRows][W], acc[kTriRows];
+  // The triangle is constant during a solve, so its loads go out before the
+  // wait on the previous kernel and overlap its drain.  The gate read before
+  // the wait only decides whether to load early (steps gated off after
+  // convergence skip the loads); it is read again after the wait, and a step
+  // found on then after all takes its rows one at a time.
+  const bool early = !gated_off(gate, 1);
+  if (early) {
+#pragma unroll
+    for (int q = 0; q < kTriRows; q++) {
+      const int i = i0 + q * stride;
+      if (i < n) {
+#pragma unroll
+        for (int e = 0; e < W; e++) {
+          c[q][e] = ci[(size_t)e * n + i];
+          a[q][e] = val[(size_t)e * n + i];
+        }
+      }
+    }
+  }
+  pdl_wait();
+  pdl_trigger();
+  if (gated_off(gate, 1)) return;
+  if (!early) {
+    for (int q = 0; q < kTriRows; q++) {
+      const int i = i0 + q * stride;
+      if (i >= n) break;
+      float r = rhs[rhs_perm ? rhs_perm[i] : i];
+      for (int e = 0; e < W; e++) {
+        const int cc = ci[(size_t)e * n + i];
+        float xin = in[in_perm ? in_perm[cc] : cc];
+        if (in_scale) xin *= in_scale[cc];
+        r = __fmaf_rn(-val[(size_t)e * n + i], xin, r);
+      }
+      const float o = dinv ? r * dinv[i] : r;
+      out[out_perm ? out_perm[i] : i] = o;
+    }
+    return;
+  }
 #pragma unroll
   for (int q = 0; q < kTriRows; q++) {
     const int i = i0 + q * stride;
-    if (i < n) {
-#pragma unroll
-      for (int e = 0; e < W; e++) {
-        c[q][e] = ci[(size_t)e * n + i];
-        a[q][e] = val[(size_t)e * n + i];
-      }
-      acc[q] = rhs[rhs_perm ? rhs_perm[i] : i];
-    }
+    if (i < n) acc[q] = rhs[rhs_perm ? rhs_perm[i] : i];
   }
 #pragma unroll
   for (int q = 0; q < kTriRows; q++) {
