@@ -13,13 +13,16 @@
 // reference's slot order with rounded multiplies and adds, so the result is
 // bit-identical to the sequential loop.
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <functional>
+#include <limits>
 #include <map>
 #include <queue>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "gp_pc.h"
@@ -659,9 +662,11 @@ struct TileModel {
 // first of `resident` CTAs to become free; a level of a chunk ends one level
 // time after the later of the previous level and the arrival of its rows'
 // values from earlier chunks.
+// The simulation stops as soon as the schedule passes `limit` (the caller
+// only needs to know that this chunk size loses) and returns the time so far.
 static double tile_estimate(int n, const std::vector<int>& dptr, const std::vector<int>& dcol,
                             bool forward, const TilePlan& tp, int resident,
-                            std::vector<double>& trow) {
+                            std::vector<double>& trow, double limit) {
   const TileModel m;
   const int nch = (int)tp.cstart.size() - 1;
   trow.assign(n, 0.0);
@@ -688,6 +693,7 @@ static double tile_estimate(int n, const std::vector<int>& dptr, const std::vect
     }
     freeq.push(t);
     end = std::max(end, t);
+    if (end > limit) break;
   }
   return end;
 }
@@ -727,25 +733,52 @@ static bool tile_choose(int mode, int n, int W, const std::vector<int>& dptr,
   }
   const TileModel m;
   const double ell_us = m.ell_level * std::max(nlevels, 1);
-  std::vector<double> trow;
+  // a chunk size is only taken below 0.8 of the level-ordered estimate, so a
+  // simulation past that bound can stop (a forced size is simulated in full)
+  const double limit = tu.tile_rows ? std::numeric_limits<double>::infinity() : 0.8 * ell_us;
+  const int sms = num_sms();
+  cands.erase(std::remove_if(cands.begin(), cands.end(), [&](int C) { return C < 8 || C > n * 2; }),
+              cands.end());
+  // candidates are independent: simulate them on host threads, then pick the
+  // shortest in candidate order (the same choice as one after another)
+  const int nc = (int)cands.size();
+  std::vector<TilePlan> plans(nc);
+  std::vector<char> ok(nc, 0);
+  auto eval = [&](int c) {
+    TilePlan& tp = plans[c];
+    tile_order(n, dptr, dcol, forward, std::min(cands[c], n), tp);
+    tp.smem = tile_smem_bytes(mode, tp.C, tp.max_levels, tp.max_ext, W);
+    if (tp.smem > (size_t)tu.tile_smem) return;
+    const int bps = tile_blocks_per_sm(tp.smem);
+    if (bps < 1) return;
+    std::vector<double> trow;
+    tp.est_us = tile_estimate(n, dptr, dcol, forward, tp, bps * sms, trow, limit);
+    ok[c] = 1;
+  };
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int nthreads = std::min({nc, hw, 8, n >= (1 << 16) ? nc : 1});
+  if (nthreads <= 1) {
+    for (int c = 0; c < nc; c++) eval(c);
+  } else {
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; t++)
+      pool.emplace_back([&]() {
+        for (int c; (c = next.fetch_add(1)) < nc;) eval(c);
+      });
+    for (auto& th : pool) th.join();
+  }
   bool found = false;
   *considered = 0;
-  for (int C : cands) {
-    if (C < 8 || C > n * 2) continue;
-    TilePlan tp;
-    tile_order(n, dptr, dcol, forward, std::min(C, n), tp);
-    tp.smem = tile_smem_bytes(mode, tp.C, tp.max_levels, tp.max_ext, W);
-    if (tp.smem > (size_t)tu.tile_smem) continue;
-    const int bps = tile_blocks_per_sm(tp.smem);
-    if (bps < 1) continue;
-    tp.est_us = tile_estimate(n, dptr, dcol, forward, tp, bps * num_sms(), trow);
+  for (int c = 0; c < nc; c++) {
+    if (!ok[c]) continue;
     (*considered)++;
-    if (!found || tp.est_us < best.est_us) {
-      best = std::move(tp);
+    if (!found || plans[c].est_us < best.est_us) {
+      best = std::move(plans[c]);
       found = true;
     }
   }
-  return found && (tu.tile_rows || best.est_us < 0.8 * ell_us);
+  return found && (tu.tile_rows || best.est_us < limit);
 }
 
 // The per-chunk blobs of a tiled sweep (layout read by k_tile_sweep).
