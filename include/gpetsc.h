@@ -81,7 +81,11 @@ int gp_mat_create_i32(gp_mat *out, int64_t nrows, int64_t ncols, int64_t nnz,
 int gp_mat_destroy(gp_mat A);
 /* New values for the same pattern (host or device pointer). */
 int gp_mat_set_values(gp_mat A, const double *values, int on_device, void *stream);
-/* Device pointer of the values array (valid until gp_mat_destroy). */
+/* Device pointer of the values array (valid until gp_mat_destroy).  After
+ * writing values through it, call gp_mat_set_values(A, that pointer, 1, s):
+ * no copy is made, and the copies derived from the values (the FP32 copy of
+ * the mixed form, A^T's values for gp_mat_mult_transpose) are refreshed on
+ * their next use. */
 int gp_mat_values_ptr(gp_mat A, double **d_values);
 int gp_mat_info(gp_mat A, int64_t *nrows, int64_t *ncols, int64_t *nnz);
 /* y = A x.        Replaces MatMult_SeqAIJ (src/ported.mojo:380-391). */
