@@ -3,14 +3,16 @@
 //
 //   MatMult_SeqAIJ           src/ported.mojo:380-391  -> k_spmv
 //   MatMultAdd_SeqAIJ        src/ported.mojo:394-405  -> k_spmv (init = v_i)
-//   MatMultTranspose_SeqAIJ  src/ported.mojo:408-431  -> k_spmv_t over A^T
+//   MatMultTranspose_SeqAIJ  src/ported.mojo:408-431  -> k_spmv over A^T (spmv_t)
 //   MatGetDiagonal_SeqAIJ    src/ported.mojo:434-447  -> k_diag
 //
 // The transpose is stored as a pattern (row pointers, the original row of each
 // entry, and the slot in A it came from), built once on the host from the
 // pattern with a stable counting sort.  Column c of A is then summed in
 // ascending original-row order, which is the order the reference's scatter
-// loop adds into y[c]: the gather is bit-identical to the scatter.
+// loop adds into y[c]: the gather is bit-identical to the scatter.  The values
+// of A^T are gathered through the source slots into a copy once per change of
+// A's values, so the multiply streams them like any CSR matrix.
 #include <algorithm>
 #include <cstdlib>
 #include <vector>
