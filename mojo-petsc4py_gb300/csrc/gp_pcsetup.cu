@@ -11,11 +11,11 @@
 // The level-of-fill rule is the reference's: a fill entry (i, j) reached
 // through pivot p gets level lev(i, p) + lev(p, j) + 1, is kept when that is
 // at most `levels`, and an entry reached several ways keeps its smallest level.
-// Sets of columns are kept in ordered maps rather than the reference's linked
-// lists; the resulting patterns are the same sets in the same (ascending)
-// order.
+// Rows are built in flat arrays over a dense level array (ILU: a sorted
+// linked list, as the reference's; IC: a sorted list of touched columns);
+// the resulting patterns are the same sets in the same (ascending) order.
 #include <algorithm>
-#include <map>
+#include <string>
 #include <vector>
 
 #include "gp_pc.h"
@@ -93,76 +93,188 @@ int color_order(const std::vector<int>& rowptr, const std::vector<int>& colind, 
   return GP_OK;
 }
 
+// Rows of a symbolic factor in flat form: row i is cols[rs[i] .. rs[i+1])
+// ascending, with their levels in lv; nL[i] counts the strictly lower ones.
+struct SymRows {
+  std::vector<int> rs, cols, lv, nL;
+};
+
+// The permuted row i of A: ascending distinct columns ic[colind] of row r[i].
+static void permuted_row(const Csr* A, const std::vector<int>& r, const std::vector<int>& ic,
+                         int i, std::vector<int>& out) {
+  out.clear();
+  const int ri = r[i];
+  for (int j = A->h_rowptr[ri]; j < A->h_rowptr[ri + 1]; j++) out.push_back(ic[A->h_colind[j]]);
+  std::sort(out.begin(), out.end());
+  out.erase(std::unique(out.begin(), out.end()), out.end());
+}
+
+// ILU(levels) rows.  Row i starts from A's permuted row at level 0; its
+// pivots p < i are visited in ascending order, fill included (a fill column
+// reached through p is always > p), and each adds U(p, :) past the diagonal
+// at level lev(i, p) + lev(p, j) + 1.  The row is a sorted linked list over
+// a dense level array, so no per-row allocation is made.
+static int ilu_rows_flat(const Csr* A, int levels, const std::vector<int>& r,
+                         const std::vector<int>& ic, SymRows& R) {
+  const int n = A->n;
+  R.rs.assign(n + 1, 0);
+  R.nL.assign(n, 0);
+  R.cols.clear();
+  R.lv.clear();
+  R.cols.reserve(A->nnz);
+  R.lv.reserve(A->nnz);
+  std::vector<int> lev(n, -1), nxt(levels > 0 ? n : 0), row;
+  for (int i = 0; i < n; i++) {
+    permuted_row(A, r, ic, i, row);
+    if (!std::binary_search(row.begin(), row.end(), i)) {
+      set_error("ILU: row " + std::to_string(r[i]) + " has no diagonal entry");
+      return GP_ERR_ARG;
+    }
+    if (levels == 0) {
+      R.nL[i] = (int)(std::lower_bound(row.begin(), row.end(), i) - row.begin());
+      R.cols.insert(R.cols.end(), row.begin(), row.end());
+      R.lv.insert(R.lv.end(), row.size(), 0);
+      R.rs[i + 1] = (int)R.cols.size();
+      continue;
+    }
+    // list end marker: n (above every column)
+    const int head = row[0];
+    for (size_t q = 0; q < row.size(); q++) {
+      lev[row[q]] = 0;
+      nxt[row[q]] = q + 1 < row.size() ? row[q + 1] : n;
+    }
+    for (int p = head; p < i; p = nxt[p]) {
+      const int lip = lev[p];
+      int cur = p;  // U(p, :) is ascending, so the insertion point only moves on
+      for (int q = R.rs[p] + R.nL[p] + 1; q < R.rs[p + 1]; q++) {
+        const int j = R.cols[q];
+        const int l = R.lv[q] + lip + 1;
+        if (l > levels) continue;
+        if (lev[j] < 0) {
+          while (nxt[cur] < j) cur = nxt[cur];
+          nxt[j] = nxt[cur];
+          nxt[cur] = j;
+          lev[j] = l;
+        } else if (lev[j] > l) {
+          lev[j] = l;
+        }
+      }
+    }
+    int cnt = 0;
+    for (int c = head; c != n; c = nxt[c]) {
+      R.cols.push_back(c);
+      R.lv.push_back(lev[c]);
+      if (c < i) cnt++;
+      lev[c] = -1;
+    }
+    R.nL[i] = cnt;
+    R.rs[i + 1] = (int)R.cols.size();
+  }
+  return GP_OK;
+}
+
+// IC(levels) rows: the strictly upper part of row k, from A's permuted row at
+// level 0 and the fill through every earlier row p holding column k, each
+// adding its columns past k at level lev(p, k) + lev(p, j) + 1 (the smallest
+// level is kept; the set and the levels do not depend on the order in which
+// the rows p are visited).
+static int icc_rows_flat(const Csr* A, int levels, const std::vector<int>& r,
+                         const std::vector<int>& ic, SymRows& R) {
+  const int n = A->n;
+  R.rs.assign(n + 1, 0);
+  R.nL.assign(n, 0);
+  R.cols.clear();
+  R.lv.clear();
+  R.cols.reserve(A->nnz);
+  R.lv.reserve(A->nnz);
+  std::vector<int> lev(n, -1), row, touched;
+  // rows p holding column k: per-column lists of (p, lev(p, k)) entries
+  std::vector<int> chead(levels > 0 ? n : 0, -1), enext, erow, elev;
+  for (int k = 0; k < n; k++) {
+    permuted_row(A, r, ic, k, row);
+    touched.clear();
+    for (int c : row)
+      if (c > k) {
+        lev[c] = 0;
+        touched.push_back(c);
+      }
+    if (levels > 0) {
+      for (int e = chead[k]; e >= 0; e = enext[e]) {
+        const int p = erow[e], lpk = elev[e];
+        for (int q = R.rs[p]; q < R.rs[p + 1]; q++) {
+          const int j = R.cols[q];
+          if (j <= k) continue;
+          const int l = R.lv[q] + lpk + 1;
+          if (l > levels) continue;
+          if (lev[j] < 0) {
+            lev[j] = l;
+            touched.push_back(j);
+          } else if (lev[j] > l) {
+            lev[j] = l;
+          }
+        }
+      }
+      std::sort(touched.begin(), touched.end());
+    }
+    for (int c : touched) {
+      R.cols.push_back(c);
+      R.lv.push_back(lev[c]);
+      if (levels > 0) {
+        enext.push_back(chead[c]);
+        erow.push_back(k);
+        elev.push_back(lev[c]);
+        chead[c] = (int)erow.size() - 1;
+      }
+      lev[c] = -1;
+    }
+    R.rs[k + 1] = (int)R.cols.size();
+  }
+  return GP_OK;
+}
+
+static void rows_to_pairs(const SymRows& R, int n,
+                          std::vector<std::vector<std::pair<int, int>>>& rows) {
+  rows.assign(n, {});
+  for (int i = 0; i < n; i++)
+    for (int q = R.rs[i]; q < R.rs[i + 1]; q++) rows[i].emplace_back(R.cols[q], R.lv[q]);
+}
+
 // Rows of the ILU(levels) pattern: ascending (column, level) pairs of each
 // permuted row, and the count of strictly lower entries in nL.
 int ilu_symbolic_rows(const Csr* A, int levels, const std::vector<int>& r,
                       const std::vector<int>& ic,
                       std::vector<std::vector<std::pair<int, int>>>& rows, std::vector<int>& nL) {
-  const int n = A->n;
-  const auto& rp = A->h_rowptr;
-  const auto& ci = A->h_colind;
-  rows.assign(n, {});
-  nL.assign(n, 0);
-  for (int i = 0; i < n; i++) {
-    std::map<int, int> row;
-    const int ri = r[i];
-    for (int j = rp[ri]; j < rp[ri + 1]; j++) row.emplace(ic[ci[j]], 0);
-    if (!row.count(i)) {
-      set_error("ILU: row " + std::to_string(ri) + " has no diagonal entry");
-      return GP_ERR_ARG;
-    }
-    if (levels > 0) {
-      for (auto it = row.begin(); it != row.end() && it->first < i; ++it) {
-        const int p = it->first, lip = it->second;
-        const auto& prow = rows[p];
-        for (int q = nL[p] + 1; q < (int)prow.size(); q++) {  // U(p, :) past the diagonal
-          const int j = prow[q].first;
-          const int lev = prow[q].second + lip + 1;
-          if (lev > levels) continue;
-          auto f = row.find(j);
-          if (f == row.end())
-            row.emplace(j, lev);
-          else if (f->second > lev)
-            f->second = lev;
-        }
-      }
-    }
-    rows[i].assign(row.begin(), row.end());
-    int cnt = 0;
-    while (cnt < (int)rows[i].size() && rows[i][cnt].first < i) cnt++;
-    nL[i] = cnt;
-  }
+  SymRows R;
+  GP_TRY(ilu_rows_flat(A, levels, r, ic, R));
+  rows_to_pairs(R, A->n, rows);
+  nL = R.nL;
   return GP_OK;
 }
 
 int ilu_symbolic(const Csr* A, int levels, const std::vector<int>& r, const std::vector<int>& ic,
                  FactorPattern& out) {
   const int n = A->n;
-  std::vector<std::vector<std::pair<int, int>>> rows;
-  std::vector<int> nL;
-  GP_TRY(ilu_symbolic_rows(A, levels, r, ic, rows, nL));
+  SymRows R;
+  GP_TRY(ilu_rows_flat(A, levels, r, ic, R));
   // reference layout
-  out.bi.assign(n + 1, 0);
-  int64_t total = 0;
-  for (int i = 0; i < n; i++) {
-    out.bi[i + 1] = out.bi[i] + nL[i];
-    total += rows[i].size();
-  }
+  const int64_t total = R.rs[n];
   if (total > INT32_MAX - 1) {
     set_error("ILU factor too large for 32-bit indices");
     return GP_ERR_ARG;
   }
+  out.bi.assign(n + 1, 0);
+  for (int i = 0; i < n; i++) out.bi[i + 1] = out.bi[i] + R.nL[i];
   out.nnz = (int)total;
   out.bj.assign(std::max<int64_t>(total, 1), 0);
   out.bdiag.assign(n + 1, 0);
   for (int i = 0; i < n; i++)
-    for (int q = 0; q < nL[i]; q++) out.bj[out.bi[i] + q] = rows[i][q].first;
+    for (int q = 0; q < R.nL[i]; q++) out.bj[out.bi[i] + q] = R.cols[R.rs[i] + q];
   const int nLtot = out.bi[n];
   out.bdiag[n] = nLtot - 1;
   int k = nLtot;
   for (int i = n - 1; i >= 0; i--) {
-    const int nz = (int)rows[i].size() - nL[i] - 1;
-    for (int q = 0; q < nz; q++) out.bj[k++] = rows[i][nL[i] + 1 + q].first;
+    const int nz = R.rs[i + 1] - R.rs[i] - R.nL[i] - 1;
+    for (int q = 0; q < nz; q++) out.bj[k++] = R.cols[R.rs[i] + R.nL[i] + 1 + q];
     out.bj[k++] = i;
     out.bdiag[i] = out.bdiag[i + 1] + nz + 1;
   }
@@ -176,58 +288,30 @@ int ilu_symbolic(const Csr* A, int levels, const std::vector<int>& r, const std:
 int icc_symbolic_rows(const Csr* A, int levels, const std::vector<int>& r,
                       const std::vector<int>& ic,
                       std::vector<std::vector<std::pair<int, int>>>& rows) {
-  const int n = A->n;
-  const auto& rp = A->h_rowptr;
-  const auto& ci = A->h_colind;
-  rows.assign(n, {});
-  std::vector<std::vector<std::pair<int, int>>> colsrc(n);  // column k <- (prow, level)
-  for (int k = 0; k < n; k++) {
-    std::map<int, int> row;
-    const int rk = r[k];
-    for (int j = rp[rk]; j < rp[rk + 1]; j++) {
-      const int c = ic[ci[j]];
-      if (c > k) row.emplace(c, 0);
-    }
-    if (levels > 0) {
-      for (const auto& src : colsrc[k]) {
-        const int p = src.first, lpk = src.second;
-        for (const auto& e : rows[p]) {
-          if (e.first <= k) continue;
-          const int lev = e.second + lpk + 1;
-          if (lev > levels) continue;
-          auto f = row.find(e.first);
-          if (f == row.end())
-            row.emplace(e.first, lev);
-          else if (f->second > lev)
-            f->second = lev;
-        }
-      }
-    }
-    rows[k].assign(row.begin(), row.end());
-    for (const auto& e : rows[k]) colsrc[e.first].emplace_back(k, e.second);
-  }
+  SymRows R;
+  GP_TRY(icc_rows_flat(A, levels, r, ic, R));
+  rows_to_pairs(R, A->n, rows);
   return GP_OK;
 }
 
 int icc_symbolic(const Csr* A, int levels, const std::vector<int>& r, const std::vector<int>& ic,
                  FactorPattern& out) {
   const int n = A->n;
-  std::vector<std::vector<std::pair<int, int>>> rows;
-  GP_TRY(icc_symbolic_rows(A, levels, r, ic, rows));
-  out.bi.assign(n + 1, 0);
-  int64_t total = 0;
-  for (int k = 0; k < n; k++) total += rows[k].size() + 1;
+  SymRows R;
+  GP_TRY(icc_rows_flat(A, levels, r, ic, R));
+  const int64_t total = (int64_t)R.rs[n] + n;
   if (total > INT32_MAX - 1) {
     set_error("IC factor too large for 32-bit indices");
     return GP_ERR_ARG;
   }
+  out.bi.assign(n + 1, 0);
   out.nnz = (int)total;
   out.bj.assign(std::max<int64_t>(total, 1), 0);
   out.bdiag.assign(n + 1, 0);
   int pos = 0;
   for (int k = 0; k < n; k++) {
     out.bi[k] = pos;
-    for (const auto& e : rows[k]) out.bj[pos++] = e.first;
+    for (int q = R.rs[k]; q < R.rs[k + 1]; q++) out.bj[pos++] = R.cols[q];
     out.bdiag[k] = pos;
     out.bj[pos++] = k;
   }
