@@ -46,3 +46,20 @@ def lap2d(k):
 
 def oracle_solve(kt, ip, ix, v, b, pt="none", **kw):
     return O.solve(kt, ip, ix, v, b, pc_type=pt, **kw)
+
+
+def dense_ic0_apply(B, x):
+    """IC(0) of B on B's lower pattern, L L^T, applied to x (dense, small)."""
+    m = B.shape[0]
+    L = np.tril(B).copy()
+    pat = np.tril(B) != 0
+    for k in range(m):
+        L[k, k] = np.sqrt(L[k, k])
+        for i in range(k + 1, m):
+            if pat[i, k]:
+                L[i, k] /= L[k, k]
+        for j in range(k + 1, m):
+            for i in range(j, m):
+                if pat[i, j] and pat[i, k] and pat[j, k]:
+                    L[i, j] -= L[i, k] * L[j, k]
+    return np.linalg.solve(L @ L.T, x)

@@ -188,9 +188,10 @@ def test_sweep_forms_edge_cases(name, pt, form, tiles, rows):
     np.testing.assert_array_equal(_apply(pc, x), O.OraclePC(pt, ip, ix, v).apply(x))
 
 
-@pytest.mark.xfail(reason="open: the reference's IC in a non-natural ordering mixes original "
-                          "and permuted indices (its result is not an IC factorization of the "
-                          "permuted matrix); the device path does not reproduce it yet",
+@pytest.mark.xfail(reason="the reference's IC in a non-natural ordering re-applies row i to "
+                          "row r[i] through its diagonal slot label (not an incomplete "
+                          "factorization of the permuted matrix); the product computes the "
+                          "incomplete Cholesky factor of P A P^T instead",
                    strict=False)
 @pytest.mark.parametrize("tiles,rows", [(False, 0), (True, 0), (True, 100)])
 @pytest.mark.parametrize("name", ["poisson2d_24", "poisson3d_10"])
@@ -204,3 +205,24 @@ def test_icc_in_rcm_order_matches_the_oracle(name, tiles, rows):
     x = np.random.default_rng(12).normal(size=n)
     want = O.OraclePC("icc", ip, ix, v, ordering="rcm").apply(x)
     np.testing.assert_array_equal(_apply(pc, x), want)
+
+
+@pytest.mark.parametrize("tiles,rows", [(False, 0), (True, 100)])
+def test_icc_in_rcm_order_is_the_incomplete_cholesky_of_the_permuted_matrix(tiles, rows):
+    """The device IC(0) in RCM order is the incomplete Cholesky factor of the
+    permuted matrix P A P^T (the reference's own result there is not; see the
+    expected failure above), to rounding."""
+    from helpers import dense_ic0_apply
+
+    ip, ix, v = gallery.laplacian_2d(10)
+    n = len(ip) - 1
+    A = np.zeros((n, n))
+    for i in range(n):
+        A[i, ix[ip[i]:ip[i + 1]]] = v[ip[i]:ip[i + 1]]
+    _lib.set_sweep_form(tiles, rows)
+    pc = _pc("icc", _mat(ip, ix, v), {"setFactorOrdering": "rcm"})
+    r = O.OraclePC("icc", ip, ix, v, ordering="rcm")._perms()[0]
+    x = np.random.default_rng(12).normal(size=n)
+    want = np.empty(n)
+    want[r] = dense_ic0_apply(A[np.ix_(r, r)], x[r])
+    np.testing.assert_allclose(_apply(pc, x), want, rtol=1e-12, atol=1e-12)

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from helpers import dense_to_csr
+from helpers import dense_ic0_apply, dense_to_csr
 from mojopetsc4py import _lib, gallery
 
 
@@ -152,29 +152,12 @@ def test_icc_fill_is_symmetric_to_ilu_fill(G):
             np.testing.assert_array_equal(ilu_upper, icc_upper, err_msg=f"{levels} row {i}")
 
 
-def _dense_ic0_apply(B, x):
-    """IC(0) of B on B's lower pattern, L L^T, applied to x (dense, small)."""
-    m = B.shape[0]
-    L = np.tril(B).copy()
-    pat = np.tril(B) != 0
-    for k in range(m):
-        L[k, k] = np.sqrt(L[k, k])
-        for i in range(k + 1, m):
-            if pat[i, k]:
-                L[i, k] /= L[k, k]
-        for j in range(k + 1, m):
-            for i in range(j, m):
-                if pat[i, j] and pat[i, k] and pat[j, k]:
-                    L[i, j] -= L[i, k] * L[j, k]
-    return np.linalg.solve(L @ L.T, x)
-
-
 def test_oracle_icc_natural_is_the_incomplete_cholesky():
     """Pins the oracle's IC(0) (the reference's MatICCFactor path) in natural
     order to a dense incomplete Cholesky of the same pattern.  In RCM order
     the reference's result is not an incomplete factorization of the permuted
-    matrix (it mixes original and permuted indices); that case is recorded as
-    an open divergence, not pinned here."""
+    matrix (its numeric phase re-applies row i to row r[i] through the
+    diagonal slot's label); that divergence is documented, not pinned."""
     ip, ix, v = gallery.laplacian_2d(8)
     n = len(ip) - 1
     A = np.zeros((n, n))
@@ -182,4 +165,4 @@ def test_oracle_icc_natural_is_the_incomplete_cholesky():
         A[i, ix[ip[i]:ip[i + 1]]] = v[ip[i]:ip[i + 1]]
     x = np.random.default_rng(12).normal(size=n)
     got = O.OraclePC("icc", ip, ix, v).apply(x)
-    np.testing.assert_allclose(got, _dense_ic0_apply(A, x), rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(got, dense_ic0_apply(A, x), rtol=1e-12, atol=1e-13)
