@@ -50,17 +50,26 @@ int gp_version(void);
 /* Message of the last failed call on this host thread. */
 const char *gp_last_error(void);
 /* Floating-point form of every kernel launched after the call (the process
- * default comes from the environment: GPETSC_ARITHMETIC=exact selects exact,
- * anything else FMA).
- *   GP_ARITH_EXACT  each product and sum rounded separately, in the
- *                   reference's order: results bit-identical to its
- *                   sequential loops (src/ported.mojo) on the same inputs.
- *   GP_ARITH_FMA    products folded into fused multiply-adds, same order:
- *                   half the FP64 instructions; results differ from the
- *                   exact form by rounding only.
+ * default comes from the environment: GPETSC_ARITHMETIC=exact or =ordered
+ * selects that form, anything else FMA).
+ *   GP_ARITH_EXACT    each product and sum rounded separately, in the
+ *                     reference's order: SpMV, the Vec maps, the PC applies
+ *                     and the factors are bit-identical to its sequential
+ *                     loops (src/ported.mojo) on the same inputs; reductions
+ *                     use a fixed parallel tree (equal to rounding).
+ *   GP_ARITH_FMA      products folded into fused multiply-adds, same order:
+ *                     half the FP64 instructions; results differ from the
+ *                     exact form by rounding only.
+ *   GP_ARITH_ORDERED  GP_ARITH_EXACT with every reduction (dot, norms,
+ *                     dotNorm2, asum, sum, GMRES's multi-dot) summed in the
+ *                     reference's blocked order (src/simdvec.mojo:332-473,
+ *                     src/ksp.mojo:956-1062): whole solves bit-identical to
+ *                     the reference's; each reduction is a sequential chain
+ *                     of n/16 adds (milliseconds at n = 2^21), a checking
+ *                     form, not a fast one.
  * No counterpart in the reference (its loops are compiled one way).  Solver
  * graphs captured in one form are re-captured when the form changes. */
-enum { GP_ARITH_EXACT = 0, GP_ARITH_FMA = 1 };
+enum { GP_ARITH_EXACT = 0, GP_ARITH_FMA = 1, GP_ARITH_ORDERED = 2 };
 int gp_set_arithmetic(int mode);
 int gp_get_arithmetic(void);
 /* Number of visible CUDA devices (0 when none). */

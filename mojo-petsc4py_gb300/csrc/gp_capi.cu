@@ -34,8 +34,10 @@ int gp_version(void) { return 100; }
 const char* gp_last_error(void) { return gp::last_error(); }
 
 int gp_set_arithmetic(int mode) {
-  if (mode != GP_ARITH_EXACT && mode != GP_ARITH_FMA) {
-    gp::set_error("gp_set_arithmetic: mode must be GP_ARITH_EXACT (0) or GP_ARITH_FMA (1)");
+  if (mode != GP_ARITH_EXACT && mode != GP_ARITH_FMA && mode != GP_ARITH_ORDERED) {
+    gp::set_error(
+        "gp_set_arithmetic: mode must be GP_ARITH_EXACT (0), GP_ARITH_FMA (1) or "
+        "GP_ARITH_ORDERED (2)");
     return GP_ERR_ARG;
   }
   gp::set_arith_mode(mode);

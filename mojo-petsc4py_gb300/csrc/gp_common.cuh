@@ -80,9 +80,12 @@ int num_sms();  // cached SM count of the current device
 // and the maps are bit-identical to them.  kFma: `a*x + y` is one fused
 // multiply-add; GB300 issues FP64 at 1/64 of FP32, and the unfused form makes
 // SpMV FP64-issue-bound below the HBM roofline, while the fused form halves
-// the FP64 instructions.  Default kFma; GPETSC_ARITHMETIC=exact selects the
-// other at load, gp_set_arithmetic() at run time.
-enum Arith : int { kExact = 0, kFma = 1 };
+// the FP64 instructions.  kOrdered: kExact, and every reduction of the
+// Krylov drivers and the Vec API summed in the reference's own blocked order
+// (gp_ordred.cuh) instead of a parallel tree -- slow, and bit-identical to
+// the reference's sequential solves.  Default kFma; GPETSC_ARITHMETIC=exact
+// or =ordered selects another at load, gp_set_arithmetic() at run time.
+enum Arith : int { kExact = 0, kFma = 1, kOrdered = 2 };
 int arith_mode();
 void set_arith_mode(int mode);
 int red_grid(int64_t n);  // deterministic reduction grid for length n

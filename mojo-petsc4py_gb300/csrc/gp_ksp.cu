@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "gp_ksp.h"
+#include "gp_ordred.cuh"
 #include "gp_spmv.cuh"
 
 namespace gp {
@@ -1170,7 +1171,10 @@ struct Run {
   }
   template <int OP>
   int red(const int* g, DRef x, DRef y, double* raw, double* sq, double* raw2 = nullptr) const {
-    if (arith_mode() == kFma)
+    if (arith_mode() == kOrdered) {
+      constexpr int OOP = OP == D_DOT ? ORD_DOT : OP == D_NRM ? ORD_NRM : ORD_DOTNRM;
+      k_ord_red<OOP><<<kOrdChains, 32, 0, s>>>(g, 1, n, x, y, k->slot, raw, sq, raw2);
+    } else if (arith_mode() == kFma)
       k_dred<OP, true><<<red_grid(n), kRedBlock, 0, s>>>(g, 1, n, x, y, k->slot, raw, sq, raw2);
     else
       k_dred<OP, false><<<red_grid(n), kRedBlock, 0, s>>>(g, 1, n, x, y, k->slot, raw, sq, raw2);
@@ -1296,7 +1300,8 @@ static int resident_grid(const void* kernel, int block) {
 
 static bool cg_fused_ok(const Run& r) {
   const KspOptions& o = r.k->opt;
-  return o.normtype == N_PRECOND && o.chknorm <= 1 &&
+  // the fused kernels sum their dots inside the vector passes (tree order)
+  return arith_mode() != kOrdered && o.normtype == N_PRECOND && o.chknorm <= 1 &&
          (int64_t)spmv_grid(r.A) <= (int64_t)kMaxBasis * kMaxRedGrid;
 }
 
@@ -1442,8 +1447,14 @@ static int cgs_pass(const Run& r, int gate_idx) {
   Ksp* k = r.k;
   const int* g = r.G(gate_idx);
   DRef v1 = DRef::at(&k->st->vv_it1);
-  FL(k_mdot, red_grid(r.n), kRedBlock, r.s, g, 1, r.n, v1, k->vv, &k->st->kcount, k->slot,
-                                              k->lhh);
+  if (arith_mode() == kOrdered) {
+    const int kmax = std::min(k->opt.restart + 1, kMaxBasis);
+    k_ord_mdot<<<kOrdChains * kmax, 32, 0, r.s>>>(g, 1, r.n, v1, k->vv, &k->st->kcount,
+                                                   k->slot, k->lhh);
+  } else {
+    FL(k_mdot, red_grid(r.n), kRedBlock, r.s, g, 1, r.n, v1, k->vv, &k->st->kcount, k->slot,
+                                                k->lhh);
+  }
   k_gm_cgs1<<<1, 1, 0, r.s>>>(k->st, k->hs, k->lhh, gate_idx);
   FL(k_maxpy_dyn, r.grid(), 256, r.s, g, 1, r.n, v1, k->vv, k->lhh, &k->st->kcount, 0);
   GP_CHECK_LAUNCH();

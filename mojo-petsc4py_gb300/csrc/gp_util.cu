@@ -18,12 +18,13 @@ static int g_arith = -1;
 int arith_mode() {
   if (g_arith < 0) {
     const char* e = std::getenv("GPETSC_ARITHMETIC");
-    g_arith = (e && std::string(e) == "exact") ? kExact : kFma;
+    const std::string v = e ? e : "";
+    g_arith = v == "exact" ? kExact : v == "ordered" ? kOrdered : kFma;
   }
   return g_arith;
 }
 
-void set_arith_mode(int mode) { g_arith = mode ? kFma : kExact; }
+void set_arith_mode(int mode) { g_arith = mode == kOrdered ? kOrdered : mode ? kFma : kExact; }
 
 int num_sms() {
   static int cached[64] = {0};

@@ -9,6 +9,7 @@
 #include <algorithm>
 
 #include "gp_internal.h"
+#include "gp_ordred.cuh"
 
 namespace gp {
 
@@ -385,6 +386,10 @@ __global__ void __launch_bounds__(kRedBlock) k_maxabs(int64_t n, const double* _
   }
 }
 
+// the ordered (reference-order) kernel for each reduction op
+constexpr int ORD_OF_RED_DOT = ORD_DOT, ORD_OF_RED_NORM2SQ = ORD_NRM, ORD_OF_RED_ASUM = ORD_ASUM,
+              ORD_OF_RED_SUM = ORD_SUM, ORD_OF_RED_DOTNORM2 = ORD_DOTNRM;
+
 int vec_reduce(cudaStream_t s, int op, int64_t n, const double* x, const double* y,
                double* out_host) {
   Scratch* sc;
@@ -396,8 +401,13 @@ int vec_reduce(cudaStream_t s, int op, int64_t n, const double* x, const double*
   }
   int g = red_grid(n);
   const bool f = arith_mode() == kFma;
+  const bool ordered = arith_mode() == kOrdered;
 #define RED_LAUNCH(OPC)                                                              \
-  if (f)                                                                             \
+  if (ordered)                                                                       \
+    k_ord_red<ORD_OF_##OPC><<<kOrdChains, 32, 0, s>>>(nullptr, 1, n, DRef::of(x),    \
+                                                    DRef::of(y), sc->slot, sc->d_out, \
+                                                    nullptr, sc->d_out + 1);          \
+  else if (f)                                                                        \
     k_reduce<OPC, true><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out);        \
   else                                                                               \
     k_reduce<OPC, false><<<g, kRedBlock, 0, s>>>(n, x, y, sc->slot, sc->d_out);

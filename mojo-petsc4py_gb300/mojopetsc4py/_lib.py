@@ -162,13 +162,15 @@ def device_count() -> int:
     return c.value
 
 
-ARITHMETIC = {"exact": 0, "fma": 1}
+ARITHMETIC = {"exact": 0, "fma": 1, "ordered": 2}
 
 
 def set_arithmetic(mode: str) -> None:
     """Select the kernels' floating-point form: "exact" (every product and
-    sum rounded separately, bit-identical to the reference's loops) or "fma"
-    (fused multiply-adds, the default)."""
+    sum rounded separately, bit-identical to the reference's loops; parallel
+    reductions), "ordered" ("exact" with every reduction summed in the
+    reference's blocked order, so whole solves are bit-identical to the
+    reference's; slow) or "fma" (fused multiply-adds, the default)."""
     if mode not in ARITHMETIC:
         raise ValueError(f"arithmetic must be one of {sorted(ARITHMETIC)}, got {mode!r}")
     check(lib().gp_set_arithmetic(ARITHMETIC[mode]))

@@ -39,9 +39,9 @@ def test_arithmetic_switch_round_trip():
     import mojopetsc4py
 
     assert mojopetsc4py.get_arithmetic() == "fma"
-    mojopetsc4py.set_arithmetic("exact")
-    assert mojopetsc4py.get_arithmetic() == "exact"
-    mojopetsc4py.set_arithmetic("fma")
+    for mode in ("exact", "ordered", "fma"):
+        mojopetsc4py.set_arithmetic(mode)
+        assert mojopetsc4py.get_arithmetic() == mode
     with pytest.raises(ValueError):
         mojopetsc4py.set_arithmetic("fast")
 

@@ -143,6 +143,19 @@ def test_vec_maps_bit_exact_and_reductions(n):
         cpu(want)
         np.testing.assert_array_equal(V.getArray(), want, err_msg=name)
     X, Y = vec(x), vec(y)
+    # the ordered arithmetic sums in the reference's blocked order: equal to
+    # the oracle's reductions to the last bit
+    out, out2 = np.zeros(2), np.zeros(1)
+    L.mp_vec_dot(a(x), a(y), a(out), n)
+    assert X.dot(Y) == out[0]
+    L.mp_vec_norm(a(x), 1, a(out), n)
+    assert X.norm() == out[0]
+    L.mp_vec_norm(a(x), 0, a(out), n)
+    assert X.norm(PETSc.NormType.NORM_1) == out[0]
+    L.mp_vec_sum(a(x), a(out), n)
+    assert X.sum() == out[0]
+    L.mp_vec_dot_norm2(a(x), a(y), a(out), a(out2), n)
+    assert X.dotNorm2(Y) == (out[0], out2[0])
     assert X.dot(Y) == pytest.approx(float(x @ y), rel=1e-13, abs=1e-13)
     assert X.norm() == pytest.approx(float(np.linalg.norm(x)), rel=1e-13)
     assert X.norm(PETSc.NormType.NORM_1) == pytest.approx(float(np.abs(x).sum()), rel=1e-13)

@@ -1,11 +1,14 @@
 """Device-resident Krylov solves against the CPU oracle on identical inputs.
 
-Parity bar: the same converged reason, the same iteration count for cg,
-gmres and fgmres, and the iterate within 1e-10 relative.  BiCGStab's
-iteration count is decided by which of two nearly equal residual estimates
-crosses rtol first, so it moves with the reduction order; it is held to the
-reference's own bound for that case (|difference| <= 20 iterations,
-iterate within 1e-8: tests/test_ksp_parity.py:264-283 of the reference)."""
+These suites run in the ordered arithmetic (tests/conftest.py): every
+product and sum is rounded separately in the reference's order and every
+reduction follows the reference's blocked summation, so a solve must be
+bit-identical to the oracle's -- the same converged reason, the same
+iteration count for every method including BiCGStab, the same iterate and
+the same residual history to the last bit.  In any other arithmetic (tests
+marked `exact`) the bar is the spec one: same reason, same iteration
+count for cg/gmres/fgmres, iterate within 1e-10; BiCGStab within 2
+iterations."""
 import json
 import os
 
@@ -13,7 +16,7 @@ import numpy as np
 import pytest
 
 from helpers import dense_to_csr, nonsym_banded, oracle_solve, spd_dense, tridiag_dense
-from mojopetsc4py import PETSc, gallery
+from mojopetsc4py import PETSc, _lib, gallery
 
 pytestmark = pytest.mark.gpu
 
@@ -51,9 +54,14 @@ def solve_gpu(kt, pt, ip, ix, v, b, x0=None, pc_opts=None, ksp_opts=None, tol=No
 
 def check(g, r, kt):
     assert g["reason"] == r["reason"]
+    if _lib.get_arithmetic() == "ordered":
+        assert g["its"] == r["its"]
+        np.testing.assert_array_equal(g["x"], r["x"])
+        np.testing.assert_array_equal(g["history"][: g["its"] + 1], r["history"])
+        return
     rel = np.linalg.norm(g["x"] - r["x"]) / max(np.linalg.norm(r["x"]), 1e-300)
     if kt == "bcgs":
-        assert abs(g["its"] - r["its"]) <= GOLD["bcgs_tolerance"]
+        assert abs(g["its"] - r["its"]) <= 2
         assert rel < 1e-8
     else:
         assert g["its"] == r["its"]
@@ -77,6 +85,21 @@ def test_laplacian_matrix_of_methods(kt, pt):
     check(solve_gpu(kt, pt, ip, ix, v, b, tol=tol), oracle_solve(kt, ip, ix, v, b, pt, **tol), kt)
 
 
+@pytest.mark.exact
+@pytest.mark.parametrize("kt", ["cg", "gmres", "fgmres"])
+@pytest.mark.parametrize("pt", PTS)
+def test_laplacian_matrix_of_methods_tree_reductions(kt, pt):
+    """The exact arithmetic with the parallel tree reductions (and the fused
+    CG): the spec bar instead of bit-identity.  (BiCGStab's count moves
+    by several iterations with any change of rounding -- 80 in the oracle,
+    83 here -- so it is checked bit for bit in the ordered arithmetic and to
+    2 iterations in the fused one on the benchmark's 128^3 case.)"""
+    ip, ix, v = gallery.laplacian_2d(32)
+    b = np.random.default_rng(5).normal(size=1024)
+    tol = dict(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=2000)
+    check(solve_gpu(kt, pt, ip, ix, v, b, tol=tol), oracle_solve(kt, ip, ix, v, b, pt, **tol), kt)
+
+
 @pytest.mark.parametrize("kt", ["gmres", "fgmres", "bcgs"])
 @pytest.mark.parametrize("pt", ["none", "jacobi", "sor", "ilu"])
 def test_nonsymmetric_convection_diffusion(kt, pt):
@@ -86,20 +109,29 @@ def test_nonsymmetric_convection_diffusion(kt, pt):
     check(solve_gpu(kt, pt, ip, ix, v, b, tol=tol), oracle_solve(kt, ip, ix, v, b, pt, **tol), kt)
 
 
+@pytest.mark.parametrize("k", [32, 64, 128])
 @pytest.mark.parametrize("key", list(GOLD["iterations"]))
-def test_published_iteration_counts_on_gpu(key):
+def test_published_iteration_counts_on_gpu(key, k):
+    """The reference's published counts (README.md:302-321), GMRES/FGMRES at
+    128^2 included (2000 iterations, CONVERGED_ITS).  BiCGStab's published
+    counts are not reproducible to the iteration by any one arithmetic (the
+    oracle gives 80/163/317 against 85/162/316, within the reference's own
+    bound of 20); on the GPU it is held to the oracle's count exactly."""
     kt, pt = key.split("+")
-    for k, want in GOLD["iterations"][key].items():
-        k = int(k)
-        if k > 64 and kt in ("gmres", "fgmres"):
-            continue
-        ip, ix, v = gallery.laplacian_2d(k)
-        b = np.random.default_rng(5).normal(size=k * k)
-        g = solve_gpu(kt, pt, ip, ix, v, b)
-        if kt == "bcgs":
-            assert abs(g["its"] - want) <= GOLD["bcgs_tolerance"]
-        else:
-            assert g["its"] == want, (key, k)
+    want = GOLD["iterations"][key].get(str(k))
+    if want is None:
+        pytest.skip("not published")
+    ip, ix, v = gallery.laplacian_2d(k)
+    b = np.random.default_rng(5).normal(size=k * k)
+    tol = dict(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=2000)
+    g = solve_gpu(kt, pt, ip, ix, v, b, tol=tol)
+    r = oracle_solve(kt, ip, ix, v, b, pt, **tol)
+    check(g, r, kt)
+    if kt == "bcgs":
+        assert abs(g["its"] - want) <= GOLD["bcgs_tolerance"]
+    else:
+        assert g["its"] == want, (key, k)
+        assert g["reason"] == (4 if want == 2000 else 2)
 
 
 def test_readme_example_on_gpu():
