@@ -9,19 +9,22 @@ is larger than the 129 MB L2, so consecutive solves stream it from HBM.
   value   device-resident solve time (b, x and the operator already in HBM)
   e2e     the same solve through the public API with host arrays: the step
           uploads b from host memory, solves, and reads x back
-  roofline  the SpMV kernel, timed alone with CUDA events (L2 flushed before
-          each launch), algorithmic bytes 12 nnz + 4 (n+1) + 16 n per launch
+  roofline  the SpMV kernel, timed with CUDA events over 20 back-to-back
+          launches after a 512 MB read (the 217 MB matrix is larger than L2,
+          so every launch streams it from HBM), algorithmic bytes
+          12 nnz + 4 (n+1) + 16 n per launch
   cpu_baseline  the CPU oracle (a single-threaded restatement of the
-          reference's algorithm) on the same system, a bounded sample of
-          iterations scaled by the iteration count
+          reference's algorithm) on the same system: one whole solve, timed
 
 `--impl reference` times the reference's CPU path (the oracle restatement;
 the Mojo reference cannot be built here) on the same workload and prints the
-same JSON line with "impl": "reference".
+same JSON line with "impl": "reference": every step is one whole solve.
 
-Multi-GPU (torchrun): every rank solves its own replica of the system (the
-path is sequential; there is no data-path collective), barrier and max over
-ranks around the timed region.
+Multi-GPU (`--gpus N`; started under torchrun, or relaunched under it when
+WORLD_SIZE is unset): every rank solves its own replica of the plain system
+(the path is sequential; there is no data-path collective), with a barrier
+and the max over ranks around the timed region; the batched form splits its
+systems over the ranks and gathers only the results.
 """
 
 from __future__ import annotations
@@ -44,6 +47,33 @@ K3 = 128
 RTOL = 1e-10
 MAX_IT = 10000
 METRIC = "solve ms to rtol 1e-10 (3-D 7-pt Poisson 128^3, CG+Jacobi, FP64)"
+
+
+def config(world):
+    """The workload, identical in both arms' JSON lines."""
+    return {"workload": "poisson3d-7pt-128^3 cg+jacobi rtol 1e-10", "n": K3 ** 3,
+            "nnz": 7 * K3 ** 3 - 6 * K3 ** 2, "method": "cg+jacobi", "rtol": RTOL,
+            "atol": 1e-50, "max_it": MAX_IT, "rhs": "uniform[-1, 1], numpy default_rng(5)",
+            "x0": "zero", "l2": "inputs larger than L2 (matrix 217 MB)",
+            "parallelism": f"replicas x{world}"}
+
+
+def cpu_info():
+    """Host CPU model and logical core count."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        import platform
+
+        model = platform.processor() or platform.machine()
+    return {"cpu_model": model, "os_cpu_count": os.cpu_count()}
 
 
 def problem():
@@ -130,21 +160,42 @@ class Clocks:
 
 
 def dist_setup():
+    """(world, rank, local rank, process group or None) from the torchrun
+    environment.  NCCL carries the default group on GPUs; a gloo group
+    carries host objects (the batched form's results)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     pg = None
     if world > 1:
+        import torch
         import torch.distributed as tdist
 
-        tdist.init_process_group("gloo")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:
+            tdist.init_process_group("gloo")
         pg = tdist
     return world, rank, local, pg
 
 
+_GLOO = None
+
+
+def host_group(pg):
+    """A gloo group over all ranks for host-side objects."""
+    global _GLOO
+    if pg is None:
+        return None
+    if _GLOO is None:
+        _GLOO = pg.new_group(backend="gloo") if pg.get_backend() != "gloo" else pg.group.WORLD
+    return _GLOO
+
+
 def barrier(pg):
     if pg is not None:
-        pg.barrier()
+        pg.barrier(group=host_group(pg))
 
 
 def max_over_ranks(pg, value):
@@ -153,57 +204,64 @@ def max_over_ranks(pg, value):
     import torch
 
     t = torch.tensor([value], dtype=torch.float64)
-    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX, group=host_group(pg))
     return float(t.item())
 
 
+def gather_to_root(pg, obj):
+    """List of every rank's `obj` on rank 0 (None elsewhere); [obj] alone."""
+    if pg is None:
+        return [obj]
+    out = [None] * pg.get_world_size() if pg.get_rank() == 0 else None
+    pg.gather_object(obj, out, dst=0, group=host_group(pg))
+    return out
+
+
 # ------------------------------------------------------------------ CPU leg
-def cpu_solve_sample(ip, ix, v, b, sample_its, full_its=None):
-    """The oracle's CG + Jacobi: a bounded run of `sample_its` iterations,
-    scaled to a full solve of `full_its` iterations."""
+def oracle_cg_jacobi(ip, ix, v, b, max_it=MAX_IT):
+    """One timed CG + Jacobi solve of the oracle: (seconds, result).  The
+    Jacobi set-up is outside the timing, as the reference's bench.py keeps
+    set-up out of its solve timings."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
     O.lib()
+    ip, ix, v, b = O.i64(ip), O.i64(ix), O.f64(v), O.f64(b)
     pc = O.OraclePC("jacobi", ip, ix, v)
     t0 = time.perf_counter()
-    r = O.solve("cg", ip, ix, v, b, pc=pc, rtol=RTOL, atol=1e-50, divtol=1e30,
-                max_it=sample_its)
-    dt = time.perf_counter() - t0
-    per_it = dt / max(r["its"], 1)
-    return per_it, r
+    r = O.solve("cg", ip, ix, v, b, pc=pc, rtol=RTOL, atol=1e-50, divtol=1e30, max_it=max_it)
+    return time.perf_counter() - t0, r
 
 
 def run_reference(args, world, rank, pg):
+    """The reference's CPU path (the oracle restatement, single-threaded as
+    the reference library is): every timed step is one whole CG + Jacobi
+    solve of the benchmark system; each warm-up step a 40-iteration solve,
+    which pages in the matrix and vectors."""
     if rank != 0:
         return
     ip, ix, v, b = problem()
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-
-    O.lib()
-    # iteration count of the full solve, from one full oracle run in warm-up
-    full = O.solve("cg", ip, ix, v, b, pc=O.OraclePC("jacobi", ip, ix, v), rtol=RTOL,
-                   atol=1e-50, divtol=1e30, max_it=MAX_IT)
-    its = full["its"]
-    sample = 40
-    for _ in range(max(args.warmup - 1, 0)):
-        cpu_solve_sample(ip, ix, v, b, sample)
-    per = []
+    for _ in range(args.warmup):
+        oracle_cg_jacobi(ip, ix, v, b, max_it=40)
+    per, its, reason = [], None, None
     for _ in range(args.steps):
-        p, _ = cpu_solve_sample(ip, ix, v, b, sample)
-        per.append(p)
-    ms = float(np.mean(per)) * its * 1e3
+        dt, r = oracle_cg_jacobi(ip, ix, v, b)
+        per.append(dt * 1e3)
+        its, reason = r["its"], r["reason"]
+    ms = float(np.mean(per))
     line = {
         "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "poisson3d-7pt-128^3 cg+jacobi rtol 1e-10", "n": len(b),
-                   "nnz": int(ip[-1]), "iterations": its},
+        "config": config(world),
+        "result": {"iterations": its, "reason": reason,
+                   "median_ms": round(float(np.median(per)), 3),
+                   "best_of_3_ms": round(float(min(per[:3])), 3)},
         "cpu_baseline": {"value": round(ms, 3), "unit": "ms", "cores": 1, "kind": "port",
-                         "sample": f"{sample} CG+Jacobi iterations per step, scaled to the "
-                                   f"{its}-iteration solve (measured once in warm-up)"},
+                         "sample": f"whole {its}-iteration CG+Jacobi solves, mean of "
+                                   f"{args.steps} (warm-up: {args.warmup} solves of 40 "
+                                   "iterations)", **cpu_info()},
         "e2e": {"value": round(ms, 3), "unit": "ms", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -375,27 +433,35 @@ def run_ours(args, world, rank, local, pg):
             except Exception as e:  # reported, never hidden
                 forms[name] = {"error": f"{type(e).__name__}: {e}"}
 
-    # ---- CPU baseline (rank 0 at N = 1 only)
+    # ---- the batched form split over the ranks (N > 1; every rank takes part)
+    if world > 1 and not args.quick and not args.no_forms:
+        try:
+            sharded = form_batched_sharded(torch, rank, world, pg)
+        except Exception as e:  # reported, never hidden
+            sharded = {"error": f"{type(e).__name__}: {e}"}
+        forms = {"batched_sharded": sharded}
+
+    # ---- CPU baseline (rank 0 at N = 1 only): one whole solve of the oracle
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        sample = 30
-        per_it, _ = cpu_solve_sample(ip, ix, v, b, sample)
-        cpu = {"value": round(per_it * its * 1e3, 3), "unit": "ms", "cores": 1, "kind": "port",
-               "sample": f"{sample} CG+Jacobi iterations of the oracle on this host, scaled to "
-                         f"the {its}-iteration solve"}
+        dt, rc = oracle_cg_jacobi(ip, ix, v, b)
+        cpu = {"value": round(dt * 1e3, 3), "unit": "ms", "cores": 1, "kind": "port",
+               "sample": f"one whole {rc['its']}-iteration CG+Jacobi solve of the same system "
+                         "on this host", **cpu_info()}
 
     if rank != 0:
         return
+    # whole-job figure: every rank solves one replica per step, so the job
+    # completes `world` solves in the max-over-ranks step time
     line = {
-        "metric": METRIC, "value": round(ms, 3), "unit": "ms", "n_gpus": world,
+        "metric": METRIC, "value": round(ms / world, 3), "unit": "ms", "n_gpus": world,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 3),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": "poisson3d-7pt-128^3 cg+jacobi rtol 1e-10", "n": n, "nnz": nnz,
-                   "iterations": its, "reason": reason, "true_rel_residual": resid,
-                   "l2": "inputs larger than L2 (matrix 217 MB)",
-                   "parallelism": f"replicas x{world}"},
-        "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": 8 * n,
+        "config": config(world),
+        "result": {"iterations": its, "reason": reason, "true_rel_residual": resid,
+                   "arithmetic": "fma"},
+        "e2e": {"value": round(e2e_ms / world, 3), "unit": "ms", "h2d_bytes_per_step": 8 * n,
                 "d2h_bytes_per_step": 8 * n + 1024},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
@@ -489,6 +555,53 @@ def form_batched(torch, PETSc):
     out["speedup_fp64_vs_plain"] = round(est / out["fp64"]["ms"], 1)
     out["speedup_fp32_refined_vs_plain"] = round(est / out["fp32_inner_fp64_refined"]["ms"], 1)
     return out
+
+
+def form_batched_sharded(torch, rank, world, pg):
+    """The batched form's 512 systems x 16 right-hand sides split over the
+    ranks by nnz * nrhs (batch.shard_systems): each rank solves its shard on
+    its own GPU with no collective; x, its and reason are gathered on rank 0
+    over gloo afterwards.  Timed: the shard solves, max over ranks."""
+    from mojopetsc4py import gallery
+    from mojopetsc4py.batch import sharded_solve
+
+    systems = gallery.rgg_batch(BATCH_SYSTEMS, seed=11)
+    n = sum(len(ip) - 1 for ip, _, _ in systems)
+    B = np.random.default_rng(12).normal(size=(n, 16))
+    t0 = time.perf_counter()
+    solver, X, info = sharded_solve(systems, B, rank, world, lambda o: gather_to_root(pg, o),
+                                    nrhs=16, pc="jacobi", precision="fp32", rtol=1e-8)
+    setup_s = time.perf_counter() - t0
+    ms = 0.0
+    if solver is not None:
+        Bd = torch.as_tensor(solver_rhs(solver, systems, B, rank, world), device="cuda")
+        Xd = torch.empty_like(Bd)
+        barrier(pg)
+        ms = _sync_ms(torch, lambda: solver.solve(Bd, pc="jacobi", precision="fp32",
+                                                   rtol=1e-8, out=Xd), 2)
+    else:
+        barrier(pg)
+    ms = max_over_ranks(pg, ms)
+    if rank != 0:
+        return None
+    return {"config": "512 RGG Laplacians x 16 RHS, CG + Jacobi, FP32 inner / FP64 refined, "
+                      "rtol 1e-8, systems split over ranks by nnz * nrhs",
+            "ranks": world, "max_rank_solve_ms": round(ms, 2),
+            "setup_and_first_solve_s": round(setup_s, 1),
+            "converged_pairs": int((info["reason"] > 0).sum()),
+            "pairs": int(info["reason"].size),
+            "max_true_rel_residual": float(info["relres"].max()),
+            "max_its": int(info["its"].max())}
+
+
+def solver_rhs(solver, systems, B, rank, world):
+    """This rank's right-hand-side rows, in its shard's system order."""
+    from mojopetsc4py.batch import shard_systems
+
+    costs = [int(ip[-1]) * 16 for ip, _, _ in systems]
+    mine = shard_systems(costs, world)[rank]
+    offs = np.concatenate([[0], np.cumsum([len(ip) - 1 for ip, _, _ in systems])])
+    return np.concatenate([B[offs[s]:offs[s + 1]] for s in mine])
 
 
 def form_mixed(torch, PETSc):
@@ -786,6 +899,20 @@ def _csr_matvec(ip, ix, v, x):
     return np.bincount(rows, weights=v * x[ix], minlength=len(ip) - 1)
 
 
+def relaunch(nproc):
+    """Run this script's command line under torch.distributed.run with one
+    rank per GPU (rendezvous on 127.0.0.1); returns its exit status."""
+    import socket
+
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+           f"--nproc-per-node={nproc}", "--master-addr", "127.0.0.1", "--master-port",
+           str(port), os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -812,7 +939,12 @@ def main():
     if args.max_it is not None:
         global MAX_IT
         MAX_IT = args.max_it
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: relaunch this command under torchrun
+        sys.exit(relaunch(args.gpus))
     world, rank, local, pg = dist_setup()
+    if world != args.gpus:
+        raise SystemExit(f"--gpus {args.gpus} but {world} rank(s) were started")
     if args.form:
         import torch
 

@@ -272,6 +272,14 @@ int gp_ksp_set_options(gp_ksp ksp, const gp_ksp_options *o);
 int gp_ksp_solve(gp_ksp ksp, gp_mat A, gp_pc pc, const double *b, double *x,
                  gp_ksp_result *result, double *hist, int64_t hist_len, void *stream);
 
+/* How later solves launch their kernels: 0 one captured CUDA graph per solve
+ * (the loop is a conditional node), 1 the same kernels launched one by one
+ * from a host loop that polls convergence every few iterations (each kernel
+ * then appears on its own in a profiler's launch list), -1 (the default) the
+ * process-wide choice of the environment (GPETSC_KSP_GRAPH=0 selects the
+ * host loop).  Results are identical.  No counterpart in the reference. */
+int gp_ksp_set_launch_form(gp_ksp ksp, int form);
+
 /* Kernel-launch accounting of the last solve: loop trips, kernels outside the
  * loop (prologue, epilogue) and kernels per trip.  Kernels launched =
  * top_kernels + trips * body_kernels. */

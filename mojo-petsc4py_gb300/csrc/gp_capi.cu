@@ -409,6 +409,13 @@ int gp_ksp_solve(gp_ksp ksp, gp_mat A, gp_pc pc, const double* b, double* x,
   })());
 }
 
+int gp_ksp_set_launch_form(gp_ksp ksp, int form) {
+  if (!ksp) return bad("gp_ksp_set_launch_form: null solver");
+  if (form < -1 || form > 1) return bad("gp_ksp_set_launch_form: form must be -1, 0 or 1");
+  ksp->k->launch_form = form;
+  return GP_OK;
+}
+
 int gp_ksp_stats(gp_ksp ksp, int64_t* trips, int64_t* top_kernels, int64_t* body_kernels) {
   if (!ksp) return bad("gp_ksp_stats: null argument");
   if (trips) *trips = ksp->k->last_trips;

@@ -1842,7 +1842,7 @@ int ksp_solve(Ksp* k, Csr* A, Pc* pc, const double* b, double* x, KspResult* res
   const int key[12] = {o.type,      o.normtype,    o.pc_side,          o.restart,
                        o.cgstype,   n,             pc->opt.type,       pc->opt.sor_flag,
                        o.guess_zero, pc->generation, arith_mode(),    o.orthog};
-  if (eager_mode()) {
+  if (k->launch_form == 1 || (k->launch_form < 0 && eager_mode())) {
     GP_TRY(run_eager(r, b, x));
   } else {
   const bool same = !moved && k->exec && k->cap_A == A && k->cap_pc == pc &&

@@ -90,6 +90,7 @@ struct Ksp {
   int64_t top_kernels = 0;         // kernels outside the loop body
   int64_t body_kernels = 0;        // kernels per loop trip
   int64_t last_trips = 0;
+  int launch_form = -1;  // -1 the environment's (GPETSC_KSP_GRAPH), 0 graph, 1 host loop
 };
 
 struct KspResult {

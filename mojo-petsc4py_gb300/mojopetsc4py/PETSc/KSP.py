@@ -138,6 +138,7 @@ class KSP:
         self._sol = None
         self._setupcalled = False
         self._gp = None
+        self._launch_form = -1
 
     def __del__(self):
         h = getattr(self, "_gp", None)
@@ -344,6 +345,7 @@ class KSP:
             h = ctypes.c_void_p()
             check(lib().gp_ksp_create(ctypes.byref(h)))
             self._gp = h.value
+        check(lib().gp_ksp_set_launch_form(self._gp, self._launch_form))
         opts = self._options(rhs)
         check(lib().gp_ksp_set_options(self._gp, ctypes.byref(opts)))
         hist = np.zeros(max(self._histlen, 0), dtype=np.float64)
@@ -358,6 +360,16 @@ class KSP:
         self._reason = int(res.reason)
         self._rnorm = float(res.rnorm)
         self._history = hist
+
+    def setLaunchForm(self, form: str = "graph"):
+        """Extension (no counterpart in the reference): "graph" runs each
+        solve as one captured CUDA graph; "host" launches the same kernels
+        one by one from a host loop, so a profiler lists each of them;
+        "default" follows GPETSC_KSP_GRAPH.  Results are identical."""
+        forms = {"default": -1, "graph": 0, "host": 1}
+        if form not in forms:
+            raise ValueError(f"launch form must be one of {sorted(forms)}")
+        self._launch_form = forms[form]
 
     def getLaunchStats(self):
         """(loop trips, kernels outside the loop, kernels per trip) of the last

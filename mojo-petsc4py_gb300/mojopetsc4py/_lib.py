@@ -116,6 +116,7 @@ GP_SIGNATURES = {
     "gp_ksp_set_options": ([P, ctypes.POINTER(KspOptions)], ctypes.c_int),
     "gp_ksp_solve": ([P, P, P, P, P, ctypes.POINTER(KspResult), P, I64, P], ctypes.c_int),
     "gp_ksp_stats": ([P, P, P, P], ctypes.c_int),
+    "gp_ksp_set_launch_form": ([P, ctypes.c_int], ctypes.c_int),
 }
 
 _lib = None

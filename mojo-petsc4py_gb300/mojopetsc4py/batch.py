@@ -140,3 +140,75 @@ class BatchedCG:
         info = {"its": its.reshape(shape), "reason": reason.reshape(shape),
                 "relres": relres.reshape(shape), "passes": passes.value}
         return (X.cpu().numpy() if host else X), info
+
+
+def assemble_shards(shards, parts, sizes, nrhs: int):
+    """Reassemble the ranks' results of a sharded batch in system order.
+
+    shards  one list of system indices per rank (ascending, as shard_systems
+            returns them)
+    parts   one dict per rank: "X" -- its systems' solutions stacked row-wise,
+            shape (sum of their sizes, nrhs); "its", "reason", "relres" --
+            shape (len(shard), nrhs)
+    sizes   rows of every system of the whole batch
+    Returns (X of shape (sum sizes, nrhs), info with its / reason / relres of
+    shape (nsys, nrhs)).  Raises ValueError unless every system appears in
+    exactly one shard with a part of matching shape."""
+    nsys = len(sizes)
+    offs = np.zeros(nsys + 1, dtype=np.int64)
+    offs[1:] = np.cumsum(sizes)
+    if len(shards) != len(parts):
+        raise ValueError("one part per shard expected")
+    seen = np.zeros(nsys, dtype=np.int64)
+    X = np.empty((int(offs[-1]), nrhs), dtype=np.float64)
+    its = np.zeros((nsys, nrhs), dtype=np.int64)
+    reason = np.zeros((nsys, nrhs), dtype=np.int32)
+    relres = np.zeros((nsys, nrhs), dtype=np.float64)
+    for shard, part in zip(shards, parts):
+        rows = int(sum(sizes[s] for s in shard))
+        if np.shape(part["X"]) != (rows, nrhs) or np.shape(part["its"]) != (len(shard), nrhs):
+            raise ValueError("part shape does not match its shard")
+        r = 0
+        for k, s in enumerate(shard):
+            m = int(sizes[s])
+            X[offs[s]:offs[s] + m] = part["X"][r:r + m]
+            its[s], reason[s], relres[s] = part["its"][k], part["reason"][k], part["relres"][k]
+            seen[s] += 1
+            r += m
+    if not np.all(seen == 1):
+        raise ValueError("every system must belong to exactly one shard")
+    return X, {"its": its, "reason": reason, "relres": relres}
+
+
+def sharded_solve(systems, B, rank: int, world: int, gather, nrhs: int = 16,
+                  autotune: bool = True, **solve_kw):
+    """Solve this rank's shard of a batch and gather the results on rank 0.
+
+    Every rank passes the whole batch (`systems`, and `B` as an
+    (sum n_s, nrhs) host array); shard_systems decides the split the same
+    way on every rank, so no message is needed before the solve.  `gather`
+    is a host-side collective: gather(obj) returns the list of all ranks'
+    objects on rank 0 and None elsewhere (a gloo gather_object, or
+    `lambda o: [o]` for one rank).  Returns (solver, X, info) on rank 0 --
+    X and info for the whole batch in system order -- and (solver, None,
+    None) elsewhere; the solver is this rank's, for timing repeat solves."""
+    sizes = [len(ip) - 1 for ip, _, _ in systems]
+    costs = [int(ip[-1]) * nrhs for ip, _, _ in systems]
+    shards = shard_systems(costs, world)
+    mine = shards[rank]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    if mine:
+        solver = BatchedCG([systems[s] for s in mine], nrhs=nrhs, autotune=autotune)
+        Bm = np.concatenate([B[offs[s]:offs[s + 1]] for s in mine])
+        Xm, info = solver.solve(Bm, **solve_kw)
+    else:  # more ranks than systems
+        solver, Xm = None, np.zeros((0, nrhs))
+        info = {"its": np.zeros((0, nrhs), dtype=np.int64),
+                "reason": np.zeros((0, nrhs), dtype=np.int32),
+                "relres": np.zeros((0, nrhs))}
+    parts = gather({"X": Xm, "its": info["its"], "reason": info["reason"],
+                    "relres": info["relres"]})
+    if parts is None:
+        return solver, None, None
+    X, full = assemble_shards(shards, parts, sizes, nrhs)
+    return solver, X, full

@@ -37,6 +37,10 @@ def test_static_scratch_reduction_matches_the_allocating_entry(op, n):
     x = torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
     y = torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
     want = reduce_host(op, x, y)
+    # the same sums in numpy (FP64, pairwise): an independent value
+    xh, yh = x.cpu().numpy(), y.cpu().numpy()
+    ref = {0: [xh @ yh], 1: [xh @ xh], 2: [np.abs(xh).sum()], 3: [xh.sum()],
+           4: [xh @ yh, xh @ xh], 5: [np.abs(xh).max()]}[op]
     out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda")
     for _ in range(2):
         out.fill_(float("nan"))
@@ -44,6 +48,11 @@ def test_static_scratch_reduction_matches_the_allocating_entry(op, n):
         got = out.cpu().numpy()[: len(want)]
         # same kernel and grid: equal to the last bit; the bound is the test's
         np.testing.assert_allclose(got, want, rtol=1e-13, atol=0)
+        # sums of n terms of either sign: rounding relative to sum |terms|
+        scale = {0: np.abs(xh * yh).sum(), 3: np.abs(xh).sum()}.get(op, abs(ref[0]))
+        np.testing.assert_allclose(got[0], ref[0], rtol=0, atol=1e-13 * scale + 1e-300)
+        if op == 4:
+            np.testing.assert_allclose(got[1], ref[1], rtol=1e-13)
 
 
 def test_empty_vector_gives_zero():
