@@ -96,7 +96,8 @@ __device__ __forceinline__ void ew(int n, double* y, F f, const double* a,
       });
 }
 
-constexpr int kBodyUnroll = 1;  // default loop-body copies per graph trip
+constexpr int kBodyUnroll = 1;    // default loop-body copies per graph trip
+constexpr int kBodyUnrollCg = 8;  // the same for the fused CG body
 constexpr int kEagerPoll = 8;   // host-driven loop: trips between state polls
 
 __global__ void k_copy_d(const int* gate, int want, int n, DRef xr, DRef yr) {
@@ -504,23 +505,46 @@ __device__ void cg_tail(KspState* st, double* hist, double dp, double zr, bool f
   st->g[G_ON] = 1;
 }
 
+// Launched with programmatic dependent launch: p is not written by the
+// predecessor (the update), so the first batch of p is loaded before the wait
+// and its latency overlaps the predecessor's reduction tail.
 template <bool FMA>
 __global__ void k_cgf_p(KspState* st, int n, double* __restrict__ p,
                         const double* __restrict__ z) {
   pdl_trigger();
+  constexpr int U = kVecBatch;
+  const unsigned stride = gridDim.x * blockDim.x, un = (unsigned)n;
+  const unsigned i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  double zv[U], pv[U];
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const unsigned i = i0 + u * stride;
+    if (i < un) pv[u] = p[i];
+  }
+  pdl_wait();
   if (st->active != 1) return;
   const double bc = st->bcoef;
-  constexpr int U = kVecBatch;
-  double zv[U], pv[U];
-  if (bc == 0.0) {
-    grid_batched<U>(n, [&](int u, unsigned i) { zv[u] = z[i]; },
-                    [&](int u, unsigned i) { p[i] = zv[u]; });
-  } else if (bc == 1.0) {
-    grid_batched<U>(n, [&](int u, unsigned i) { zv[u] = z[i]; pv[u] = p[i]; },
-                    [&](int u, unsigned i) { p[i] = madd<FMA>(bc, zv[u], pv[u]); });
-  } else {
-    grid_batched<U>(n, [&](int u, unsigned i) { zv[u] = z[i]; pv[u] = p[i]; },
-                    [&](int u, unsigned i) { p[i] = madd<FMA>(bc, pv[u], zv[u]); });
+  for (unsigned j0 = i0; j0 < un; j0 += U * stride) {
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const unsigned i = j0 + u * stride;
+      if (i < un) {
+        if (j0 != i0) pv[u] = p[i];
+        zv[u] = z[i];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const unsigned i = j0 + u * stride;
+      if (i >= un) continue;
+      // VecAYPX's branches (src/ported.mojo:285-294): a copy at i = 0
+      if (bc == 0.0)
+        p[i] = zv[u];
+      else if (bc == 1.0)
+        p[i] = madd<FMA>(bc, zv[u], pv[u]);
+      else
+        p[i] = madd<FMA>(bc, pv[u], zv[u]);
+    }
   }
 }
 
@@ -532,23 +556,33 @@ __global__ void __launch_bounds__(kSpmvRows) k_cgf_spmv(KspState* st, int n,
                                                         const double* __restrict__ p,
                                                         double* __restrict__ w, RedSlot slot,
                                                         int evict_first) {
-  pdl_wait();
-  pdl_trigger();
-  if (st->active != 1) return;
   double v[1] = {0.0};
   if constexpr (!STREAM) {
     const uint64_t pol = spmv_policy(evict_first);
+    // the matrix is constant: the first tile's row bounds and first slots
+    // are loaded before the wait for p, overlapping the predecessor's tail
+    const int row0 = blockIdx.x * kSpmvRows + threadIdx.x;
+    SpmvPre pre;
+    if (row0 < n) spmv_row_preload(row0, rowptr, colind, val, pol, pre);
+    pdl_wait();
+    pdl_trigger();
+    if (st->active != 1) return;
     // a resident grid walks the row tiles, so each CTA pays the reduction
     // tail once rather than once per 256 rows
     for (int r0 = blockIdx.x * kSpmvRows; r0 < n; r0 += gridDim.x * kSpmvRows) {
       const int row = r0 + threadIdx.x;
       if (row < n) {
-        const double s = spmv_row<FMA>(row, rowptr, colind, val, p, 0.0, pol);
+        const double s = row == row0
+                             ? spmv_row_from<FMA>(pre, colind, val, p, 0.0, pol)
+                             : spmv_row<FMA>(row, rowptr, colind, val, p, 0.0, pol);
         w[row] = s;
         v[0] = madd<FMA>(p[row], s, v[0]);
       }
     }
   } else {
+    pdl_wait();
+    pdl_trigger();
+    if (st->active != 1) return;
     const int r0 = blockIdx.x * kSpmvRows;
     const int row = r0 + threadIdx.x;
     double s;
@@ -578,44 +612,84 @@ __global__ void __launch_bounds__(kSpmvRows) k_cgf_spmv(KspState* st, int n,
   }
 }
 
+// Loop control folded into the last kernel of a body: `loop` 0 none, 1 the
+// trip bookkeeping of the host-driven loop, 2 bookkeeping and the graph's
+// loop condition.  Called by one thread per launch.
+__device__ __forceinline__ void body_loop_ctrl(int loop, cudaGraphConditionalHandle h,
+                                               KspState* st) {
+  if (!loop) return;
+  const bool run = loop_trip(st);
+  if (loop == 2) cudaGraphSetConditional(h, run ? 1u : 0u);
+}
+
 // x += a p; r -= a w; (JACOBI) z = D r with ||z||^2 and z.r; else the PC
-// follows and k_cgf_red reduces.
+// follows and k_cgf_red reduces.  With `loop` set (Jacobi only) the kernel
+// also ends the loop trip: the thread that finishes the reduction, or block 0
+// when the body is switched off.
 template <bool FMA, bool JACOBI>
 __global__ void __launch_bounds__(kRedBlock, 4) k_cgf_update(
     KspState* st, double* hist, int n, double* __restrict__ x, double* __restrict__ r,
     const double* __restrict__ p, const double* w, double* z, const double* __restrict__ d,
-    RedSlot slot) {
+    RedSlot slot, int loop, cudaGraphConditionalHandle h) {
+  // x, r, p and d are not written by the predecessor (the SpMV writes only
+  // w): the first batch of them is loaded before the wait
+  constexpr int U = kVecBatch;
+  const unsigned stride = gridDim.x * blockDim.x, un = (unsigned)n;
+  const unsigned i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  double pv[U], xv[U], wv[U], rv[U], dv[U];
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const unsigned i = i0 + u * stride;
+    if (i < un) {
+      pv[u] = p[i];
+      xv[u] = x[i];
+      rv[u] = r[i];
+      if constexpr (JACOBI) dv[u] = d[i];
+    }
+  }
   pdl_wait();
   pdl_trigger();
-  if (st->active != 1) return;
+  if (st->active != 1) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) body_loop_ctrl(loop, h, st);
+    return;
+  }
   const double al = st->a, nal = -al;
   double v[2] = {0.0, 0.0};
-  constexpr int U = kVecBatch;
-  double pv[U], xv[U], wv[U], rv[U], dv[U];
-  grid_batched<U>(
-      n,
-      [&](int u, unsigned i) {
-        pv[u] = p[i];
-        xv[u] = x[i];
-        wv[u] = w[i];
-        rv[u] = r[i];
-        if constexpr (JACOBI) dv[u] = d[i];
-      },
-      [&](int u, unsigned i) {
-        x[i] = madd<FMA>(al, pv[u], xv[u]);
-        const double ri = madd<FMA>(nal, wv[u], rv[u]);
-        r[i] = ri;
-        if constexpr (JACOBI) {
-          const double zi = mul(ri, dv[u]);
-          z[i] = zi;
-          v[0] = madd<FMA>(zi, zi, v[0]);
-          v[1] = madd<FMA>(zi, ri, v[1]);
+  for (unsigned j0 = i0; j0 < un; j0 += U * stride) {
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const unsigned i = j0 + u * stride;
+      if (i < un) {
+        if (j0 != i0) {
+          pv[u] = p[i];
+          xv[u] = x[i];
+          rv[u] = r[i];
+          if constexpr (JACOBI) dv[u] = d[i];
         }
-      });
+        wv[u] = w[i];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const unsigned i = j0 + u * stride;
+      if (i >= un) continue;
+      x[i] = madd<FMA>(al, pv[u], xv[u]);
+      const double ri = madd<FMA>(nal, wv[u], rv[u]);
+      r[i] = ri;
+      if constexpr (JACOBI) {
+        const double zi = mul(ri, dv[u]);
+        z[i] = zi;
+        v[0] = madd<FMA>(zi, zi, v[0]);
+        v[1] = madd<FMA>(zi, ri, v[1]);
+      }
+    }
+  }
   if constexpr (JACOBI) {
     double tot[2];
-    if (grid_finish<2>(v, slot, tot) && threadIdx.x == 0)
+    if (grid_finish<2>(v, slot, tot) && threadIdx.x == 0) {
       cg_tail(st, hist, __dsqrt_rn(tot[0]), tot[1], false);
+      body_loop_ctrl(loop, h, st);
+    }
   }
 }
 
@@ -1155,6 +1229,10 @@ struct Run {
   Pc* pc;
   int n;
   cudaStream_t s;
+  // loop control taken over by the body's last kernel (see body_ends_trip):
+  // 0 none, 1 host-driven trip bookkeeping, 2 also the graph condition
+  int loop = 0;
+  cudaGraphConditionalHandle cond = 0;
   const int* G(int idx) const { return &k->st->g[idx]; }
   double* S(double KspState::*f) const { return &(k->st->*f); }
   int grid() const { return vgrid(n); }
@@ -1330,7 +1408,8 @@ static int cg_body_fused(const Run& r, double* x) {
   double* P = k->work + 2 * n;
   double* W = Z;  // the reference's W = Z aliasing
   const Csr* A = r.A;
-  FL(k_cgf_p, r.grid(), 256, r.s, k->st, n, P, Z);
+  GP_CUDA(launch_pdl(arith_mode() == kFma ? k_cgf_p<true> : k_cgf_p<false>, r.grid(), 256, r.s,
+                     k->st, n, P, (const double*)Z));
   {
     const bool f = arith_mode() == kFma;
     auto ks = A->stream_rows ? (f ? k_cgf_spmv<true, true> : k_cgf_spmv<false, true>)
@@ -1347,14 +1426,14 @@ static int cg_body_fused(const Run& r, double* x) {
   if (jac) {
     GP_CUDA(launch_pdl(f ? k_cgf_update<true, true> : k_cgf_update<false, true>, g, kRedBlock,
                        r.s, k->st, k->hist, n, x, R, (const double*)P, (const double*)W, Z,
-                       (const double*)r.pc->diag, k->slot));
+                       (const double*)r.pc->diag, k->slot, r.loop, r.cond));
   } else {
     if (f)
       k_cgf_update<true, false><<<g, kRedBlock, 0, r.s>>>(k->st, k->hist, n, x, R, P, W, Z,
-                                                          nullptr, k->slot);
+                                                          nullptr, k->slot, 0, 0);
     else
       k_cgf_update<false, false><<<g, kRedBlock, 0, r.s>>>(k->st, k->hist, n, x, R, P, W, Z,
-                                                           nullptr, k->slot);
+                                                           nullptr, k->slot, 0, 0);
     GP_TRY(r.pcapply(r.G(G_ON), DRef::of(R), DRef::of(Z)));
     FL(k_cgf_red, g, kRedBlock, r.s, k->st, k->hist, n, Z, R, k->slot, 0);
   }
@@ -1647,6 +1726,12 @@ static int run_prologue(const Run& r, const double* b, double* x) {
   return GP_OK;
 }
 
+// Whether the body's last kernel ends the loop trip itself (the fused CG with
+// Jacobi: its update kernel), so no separate loop-control kernel follows.
+static bool body_ends_trip(const Run& r) {
+  return r.k->opt.type == KSP_CG && cg_fused_ok(r) && r.pc->opt.type == PC_JACOBI;
+}
+
 static int run_body(const Run& r, const double* b, double* x) {
   switch (r.k->opt.type) {
     case KSP_CG: return cg_fused_ok(r) ? cg_body_fused(r, x) : cg_body(r, x);
@@ -1657,14 +1742,16 @@ static int run_body(const Run& r, const double* b, double* x) {
   return GP_OK;
 }
 
-// Loop-body copies per conditional trip (GPETSC_KSP_UNROLL, 1..16).
-static int body_unroll() {
-  static int u = [] {
+// Loop-body copies per conditional trip (GPETSC_KSP_UNROLL, 1..16; by default
+// kBodyUnrollCg for the three-kernel fused CG body, whose trips are short
+// enough that the conditional node's re-launch shows, else kBodyUnroll).
+static int body_unroll(const Run& r) {
+  static int env = [] {
     const char* e = std::getenv("GPETSC_KSP_UNROLL");
-    const int v = e ? std::atoi(e) : kBodyUnroll;
-    return std::max(1, std::min(16, v));
+    return e ? std::max(1, std::min(16, std::atoi(e))) : 0;
   }();
-  return u;
+  if (env) return env;
+  return body_ends_trip(r) ? kBodyUnrollCg : kBodyUnroll;
 }
 
 // GPETSC_KSP_GRAPH=0: drive the loop from the host (same kernels, launched on
@@ -1680,9 +1767,12 @@ static bool eager_mode() {
 static int run_eager(const Run& r, const double* b, double* x) {
   Ksp* k = r.k;
   GP_TRY(run_prologue(r, b, x));
+  const bool own = body_ends_trip(r);
+  Run rl = r;
+  rl.loop = own ? 1 : 0;
   for (int64_t trip = 1;; trip++) {
-    GP_TRY(run_body(r, b, x));
-    k_loop_trip<<<1, 1, 0, r.s>>>(k->st);
+    GP_TRY(run_body(rl, b, x));
+    if (!own) k_loop_trip<<<1, 1, 0, r.s>>>(k->st);
     GP_CHECK_LAUNCH();
     if (trip % kEagerPoll == 0) {
       int active = 0;
@@ -1735,10 +1825,17 @@ static int capture(const Run& r, const double* b, double* x) {
     } else {
       Run rb = r;
       rb.s = k->stream2;
+      const bool own = body_ends_trip(r);
       // several gated copies of the body per conditional trip amortise the
       // conditional node's re-launch; copies after convergence are no-ops
-      for (int u = 0; u < body_unroll() && st == GP_OK; u++) st = run_body(rb, b, x);
-      if (st == GP_OK) {
+      const int unroll = body_unroll(r);
+      for (int u = 0; u < unroll && st == GP_OK; u++) {
+        const bool last = u + 1 == unroll;
+        rb.loop = own && last ? 2 : 0;
+        rb.cond = h;
+        st = run_body(rb, b, x);
+      }
+      if (st == GP_OK && !own) {
         cudaError_t el = launch_pdl(k_loop_ctrl, 1, 1, k->stream2, h, k->st);
         if (el != cudaSuccess) {
           set_error(std::string("loop control launch: ") + cudaGetErrorString(el));

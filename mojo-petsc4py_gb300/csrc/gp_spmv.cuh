@@ -90,6 +90,57 @@ __device__ __forceinline__ double spmv_row(int row, const int* __restrict__ rowp
   return acc;
 }
 
+// A row's bounds and first batch of slots, loaded ahead of the x gather
+// (spmv_row_preload), and the row's sum from there (spmv_row_from): the same
+// loads and the same fold as spmv_row.
+struct SpmvPre {
+  int j, e;
+  int cc[4];
+  double vv[4];
+};
+
+template <typename VT>
+__device__ __forceinline__ void spmv_row_preload(int row, const int* __restrict__ rowptr,
+                                                 const int* __restrict__ colind,
+                                                 const VT* __restrict__ val, uint64_t pol,
+                                                 SpmvPre& pre) {
+  pre.j = rowptr[row];
+  pre.e = rowptr[row + 1];
+#pragma unroll
+  for (int u = 0; u < 4; u++)
+    if (pre.j + u < pre.e) {
+      pre.cc[u] = ld_stream(colind + pre.j + u, pol);
+      pre.vv[u] = (double)ld_stream(val + pre.j + u, pol);
+    }
+}
+
+template <bool FMA, typename VT, typename XT>
+__device__ __forceinline__ double spmv_row_from(const SpmvPre& pre,
+                                                const int* __restrict__ colind,
+                                                const VT* __restrict__ val,
+                                                const XT* __restrict__ x, double init,
+                                                uint64_t pol) {
+  double acc = init;
+  const int b = pre.j, e = pre.e;
+#pragma unroll
+  for (int u = 0; u < 4; u++)
+    if (b + u < e) acc = madd<FMA>(pre.vv[u], (double)x[pre.cc[u]], acc);
+  for (int j0 = b + 4; j0 < e; j0 += 4) {
+    int cc[4];
+    double vv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (j0 + u < e) {
+        cc[u] = ld_stream(colind + j0 + u, pol);
+        vv[u] = (double)ld_stream(val + j0 + u, pol);
+      }
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (j0 + u < e) acc = madd<FMA>(vv[u], (double)x[cc[u]], acc);
+  }
+  return acc;
+}
+
 template <typename VT, typename XT, typename AT>
 struct SpmvSmem {
   AT prod[kSpmvChunk];
