@@ -925,12 +925,16 @@ def relaunch(nproc):
 
 
 def main():
+    global MAX_IT, K3
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="headline solve only")
+    ap.add_argument("--grid", type=int, default=K3,
+                    help="grid size k of the k^3 system (128 is the benchmark; other sizes for "
+                         "profiling runs)")
     ap.add_argument("--method", choices=list(METHODS), default="cg+jacobi",
                     help="method of the timed solve (cg+jacobi is the benchmark; the others "
                          "for profiling, with --quick)")
@@ -951,8 +955,8 @@ def main():
                     help="cap the iterations (profiling runs only; not a bench value)")
     args = ap.parse_args()
     if args.max_it is not None:
-        global MAX_IT
         MAX_IT = args.max_it
+    K3 = args.grid
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         # one process per GPU: relaunch this command under torchrun
         sys.exit(relaunch(args.gpus))

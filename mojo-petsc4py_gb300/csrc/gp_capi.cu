@@ -266,6 +266,25 @@ int gp_set_sweep_form(int32_t tiles, int32_t tile_rows) {
   return GP_OK;
 }
 
+int gp_set_sweep_bricks(int32_t mode, int32_t lines_j, int32_t lines_k, int32_t max_ctas) {
+  if (mode < 0 || mode > 2 || lines_j < 0 || lines_k < 0 || (int64_t)lines_j * lines_k > 256 ||
+      max_ctas < 0)
+    return bad("gp_set_sweep_bricks: mode must be 0, 1 or 2, lines_j * lines_k <= 256 and "
+               "max_ctas >= 0");
+  gp::set_sweep_bricks(mode, lines_j, lines_k, max_ctas);
+  return GP_OK;
+}
+
+int gp_pc_sweep_bricks(gp_pc pc, int32_t which, int32_t* brick, int32_t* dims) {
+  if (!pc || !brick || !dims || (which != 0 && which != 1))
+    return bad("gp_pc_sweep_bricks: null argument or which not 0/1");
+  const gp::EllSweep& e = which == 0 ? pc->pc->ef : pc->pc->eb;
+  *brick = e.brick ? 1 : 0;
+  const int32_t v[5] = {e.gx, e.gy, e.gz, e.BJ, e.BK};
+  for (int k = 0; k < 5; k++) dims[k] = e.brick ? v[k] : 0;
+  return GP_OK;
+}
+
 int gp_pc_sweep_form(gp_pc pc, int32_t which, int32_t* tiled, int32_t* rows_per_chunk,
                      int32_t* chunks) {
   if (!pc || !tiled || !rows_per_chunk || !chunks || (which != 0 && which != 1))

@@ -155,7 +155,10 @@ __global__ void k_ell_refresh_g(const int* gate, int want, int n, const int* __r
   if (gated_off(gate, want)) return;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
     const int c = cnt[p];
-    for (int e = 0; e < c; e++) coef[(size_t)e * n + p] = src[cslot[(size_t)e * n + p]];
+    for (int e = 0; e < c; e++) {
+      const int cs = cslot[(size_t)e * n + p];
+      coef[(size_t)e * n + p] = cs >= 0 ? src[cs] : 0.0;  // < 0: no term (brick form)
+    }
   }
 }
 

@@ -64,8 +64,32 @@ struct EllSweep {
   int* cstart = nullptr;          // [nchunks + 1] first position of each chunk
   double est_us = 0.0;            // simulated duration of one tiled sweep
   int rows_per_chunk = 0;         // chunk size of the tiled layout
+  // Brick form (gp_brick.cu, k_brick_sweep): the sweep's dependencies are the
+  // unit steps of a grid gx x gy x gz; CTAs take bricks of BJ x BK grid lines
+  // and each thread walks one line.  Per-row arrays in natural row order
+  // (cslot / coef as [direction][n], in_idx, out_idx, dslot / dval); values
+  // are indexed by row.
+  bool brick = false;
+  int gx = 0, gy = 0, gz = 0, BJ = 0, BK = 0, nbricks = 0, bgrid = 0;
+  int bord = 0;            // fold order of a row's terms: 0 k, j, i; 1 i, j, k
+  bool in_ident = false;
+  int* border = nullptr;   // [2 * nbricks]: (J, K) of each brick in hand-out order
 };
 void ell_free(EllSweep& e);
+// Brick layout of a sweep when its dependencies have the grid structure and
+// (unless forced) the model puts it below `other_us`; *built says whether.
+int brick_build(EllSweep& e, int mode, int n, bool forward, const std::vector<int>& dptr,
+                const std::vector<int>& dcol, const std::vector<int>& dsl,
+                const std::vector<int>& in_row, const std::vector<int>& out_row,
+                const std::vector<int>& dslot_row, double other_us, bool* built);
+int brick_sweep(int mode, const EllSweep& e, const int* gate, int want, DRef in, DRef out,
+                double* val, const double* fval, double* aux, const double* auxin,
+                const double* idiag, double omega, int use_t, int write_out, unsigned* tickets,
+                DevErr* err, cudaStream_t s);
+// Brick form of later set-ups: mode 0 never, 1 where modelled faster, 2
+// wherever the structure allows; bj, bk > 0 force the lines of a brick;
+// max_ctas > 0 caps the persistent grid.
+void set_sweep_bricks(int mode, int bj, int bk, int max_ctas);
 // Lay out one sweep.  forward: dependencies precede each row (ascending
 // processing); otherwise they follow it.  `order` is the level order, used
 // when the sweep is not tiled.

@@ -552,7 +552,10 @@ __global__ void k_ell_refresh(int n, int W, const int* __restrict__ cnt,
                               double* __restrict__ dval) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
     const int c = cnt[p];
-    for (int e = 0; e < c; e++) coef[(size_t)e * n + p] = src[cslot[(size_t)e * n + p]];
+    for (int e = 0; e < c; e++) {
+      const int cs = cslot[(size_t)e * n + p];
+      coef[(size_t)e * n + p] = cs >= 0 ? src[cs] : 0.0;  // < 0: no term (brick form)
+    }
     if (dslot) dval[p] = src[dslot[p]];
   }
 }
@@ -566,8 +569,8 @@ static int up(T** d, const std::vector<T>& h) {
 }
 
 void ell_free(EllSweep& e) {
-  void* ptrs[] = {e.cnt,  e.dep,    e.cslot, e.coef,     e.in_idx, e.out_idx,
-                  e.dslot, e.dval,  e.rowof, e.blob,     e.blob_off, e.cstart};
+  void* ptrs[] = {e.cnt,  e.dep,   e.cslot, e.coef,     e.in_idx, e.out_idx, e.dslot,
+                  e.dval, e.rowof, e.blob,  e.blob_off, e.cstart, e.border};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   e = EllSweep();
@@ -902,6 +905,23 @@ static int ell_build_impl(EllSweep& e, int mode, int n, bool forward,
     nlev = sweep_levels(n, dptr, dcol, forward);
     tiled = tile_choose(mode, n, W, dptr, dcol, forward, nlev, tu, tp, &considered);
   }
+  if (allow_tiles && n > 0) {
+    // the brick form, where the sweep is a grid in natural order and the
+    // model puts it below the better of the other two forms
+    if (!nlev) nlev = sweep_levels(n, dptr, dcol, forward);
+    double other = TileModel().ell_level * nlev;
+    if (tiled) other = std::min(other, tp.est_us);
+    bool built = false;
+    GP_TRY(brick_build(e, mode, n, forward, dptr, dcol, dsl, in_row, out_row, dslot_row, other,
+                       &built));
+    if (built) {
+      if (pos_of_row) {
+        pos_of_row->resize(n);
+        for (int i = 0; i < n; i++) (*pos_of_row)[i] = i;
+      }
+      return GP_OK;
+    }
+  }
   const std::vector<int>& order = tiled ? tp.order : order_in;
   std::vector<int> pos(n);
   for (int p = 0; p < n; p++) pos[order[p]] = p;
@@ -1104,6 +1124,9 @@ int ell_sweep(int mode, const EllSweep& e, const int* gate, int want, DRef in, D
               const double* idiag, double omega, int use_t, int write_out, unsigned* tickets,
               DevErr* err, const double* coefsrc, cudaStream_t s) {
   if (e.n == 0) return GP_OK;
+  if (e.brick)
+    return brick_sweep(mode, e, gate, want, in, out, val, fval, aux, auxin, idiag, omega, use_t,
+                       write_out, tickets, err, s);
   EllArgs a;
   a.n = e.n;
   a.cnt = e.cnt;

@@ -106,6 +106,8 @@ GP_SIGNATURES = {
     "gp_wait_probe": ([ctypes.c_int32, ctypes.c_int32, P], ctypes.c_int),
     "gp_set_sweep_form": ([ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
     "gp_pc_sweep_form": ([P, ctypes.c_int32, P, P, P], ctypes.c_int),
+    "gp_set_sweep_bricks": ([ctypes.c_int32] * 4, ctypes.c_int),
+    "gp_pc_sweep_bricks": ([P, ctypes.c_int32, P, P], ctypes.c_int),
     "gp_pc_apply": ([P, P, P, P], ctypes.c_int),
     "gp_pc_apply_symmetric": ([P, P, P, P], ctypes.c_int),
     "gp_pc_factor_info": ([P, P, P], ctypes.c_int),
@@ -187,6 +189,27 @@ def set_sweep_form(tiles: bool = True, tile_rows: int = 0) -> None:
     takes the chunked form where its simulated schedule is faster, or with
     `tile_rows` > 0 forces chunks of that many rows.  Both are bit-identical."""
     check(lib().gp_set_sweep_form(1 if tiles else 0, int(tile_rows)))
+
+
+def set_sweep_bricks(mode: int = 0, lines_j: int = 0, lines_k: int = 0,
+                     max_ctas: int = 0) -> None:
+    """Brick form of the triangular sweeps of later PC set-ups (grid-structured
+    sweeps only): mode 0 never (the default), 1 where modelled faster, 2
+    whenever the structure allows; `lines_j` x `lines_k` forces the grid lines
+    of a brick; `max_ctas` caps the persistent grid.  Bit-identical to the
+    other forms."""
+    check(lib().gp_set_sweep_bricks(int(mode), int(lines_j), int(lines_k), int(max_ctas)))
+
+
+def sweep_bricks(pc_handle) -> dict:
+    """Brick form and dims of a set-up PC's forward and backward sweeps."""
+    out = {}
+    for which, name in ((0, "forward"), (1, "backward")):
+        b = ctypes.c_int32()
+        d = (ctypes.c_int32 * 5)()
+        check(lib().gp_pc_sweep_bricks(pc_handle, which, ctypes.byref(b), d))
+        out[name] = {"brick": bool(b.value), "grid": tuple(d[:3]), "lines": tuple(d[3:])}
+    return out
 
 
 def sweep_form(pc_handle) -> dict:

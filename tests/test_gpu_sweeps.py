@@ -1,9 +1,12 @@
-"""The two forms of the ILU / IC / SOR triangular sweeps against the oracle.
+"""The three forms of the ILU / IC / SOR triangular sweeps against the oracle.
 
 The level-ordered form hands out rows in dependency-level order, 32 to a
 warp; the chunked form gives runs of consecutive rows to one CTA, whose
 compute warp walks the chunk level by level with in-chunk values in shared
-memory while its fetch warps poll the values of earlier chunks.  Both must
+memory while its fetch warps poll the values of earlier chunks; the brick
+form (grid-structured sweeps in natural order) gives a brick of grid lines to
+one CTA, one line a thread, with the neighbouring lines' values in shared
+memory and only the brick faces passed through L2.  All must
 reproduce the reference's sequential sweeps bit for bit in the exact
 arithmetic, whatever the chunk size: chunk sizes that cut grid lines (so a
 dependency chain runs across chunks), tiny chunks, and one chunk holding a
@@ -49,6 +52,7 @@ PCS = [
 def _restore_form():
     yield
     _lib.set_sweep_form(True, 0)
+    _lib.set_sweep_bricks(0, 0, 0, 0)
 
 
 def _mat(ip, ix, v):
@@ -100,6 +104,43 @@ def test_sweep_forms_bit_exact(name, pt, gopts, oopts, form, tiles, rows):
     np.testing.assert_array_equal(_apply(pc, x2), O.OraclePC(pt, ip, ix, v, **oopts).apply(x2))
 
 
+# (name, lines_j, lines_k, CTA cap); 0 x 0 lets the set-up choose
+BRICKS = [
+    ("bricks-chosen", 0, 0, 0),
+    ("bricks-4x4", 4, 4, 0),
+    ("bricks-1x8", 1, 8, 0),    # one line along j: every j value crosses a brick
+    ("bricks-8x1", 8, 1, 0),
+    ("bricks-3x5", 3, 5, 0),    # cuts 24- and 10-line grids unevenly
+    ("bricks-16x16", 16, 16, 0),
+    ("bricks-2x2-3ctas", 2, 2, 3),  # three CTAs walk every brick in turn
+]
+
+
+@pytest.mark.parametrize("form,bj,bk,ctas", BRICKS, ids=[f[0] for f in BRICKS])
+@pytest.mark.parametrize("pt,gopts,oopts", PCS)
+@pytest.mark.parametrize("name", sorted(MATRICES))
+def test_brick_form_bit_exact(name, pt, gopts, oopts, form, bj, bk, ctas):
+    """The brick form wherever the sweep's dependencies are the unit steps of
+    the grid (ILU(0), IC(0), SOR in natural order); fill-in (ILU(1)) and a
+    reordering (RCM) break that structure and keep the other forms."""
+    if pt == "icc" and name == "convdiff_9":
+        pytest.skip("IC is for symmetric operators")
+    ip, ix, v = MATRICES[name]()
+    n = len(ip) - 1
+    _lib.set_sweep_bricks(2, bj, bk, ctas)
+    pc = _pc(pt, _mat(ip, ix, v), gopts)
+    got = _lib.sweep_bricks(pc._handle())
+    structured = not ({"setFactorLevels", "setFactorOrdering"} & set(gopts))
+    assert got["forward"]["brick"] == structured and got["backward"]["brick"] == structured, got
+    if structured and bj:
+        assert got["forward"]["lines"] == (bj, bk)
+    x = np.random.default_rng(5).normal(size=n)
+    want = O.OraclePC(pt, ip, ix, v, **oopts).apply(x)
+    np.testing.assert_array_equal(_apply(pc, x), want)
+    x2 = np.random.default_rng(6).normal(size=n)
+    np.testing.assert_array_equal(_apply(pc, x2), O.OraclePC(pt, ip, ix, v, **oopts).apply(x2))
+
+
 @pytest.mark.fma
 @pytest.mark.parametrize("pt", ["ilu", "icc", "sor"])
 def test_fused_forms_agree(pt):
@@ -107,24 +148,27 @@ def test_fused_forms_agree(pt):
     n = len(ip) - 1
     x = np.random.default_rng(8).normal(size=n)
     out = []
-    for tiles, rows in ((False, 0), (True, 160), (True, 333)):
+    for tiles, rows, bricks in ((False, 0, 0), (True, 160, 0), (True, 333, 0), (False, 0, 2)):
         _lib.set_sweep_form(tiles, rows)
+        _lib.set_sweep_bricks(bricks)
         out.append(_apply(_pc(pt, _mat(ip, ix, v), {}), x))
     np.testing.assert_array_equal(out[0], out[1])
     np.testing.assert_array_equal(out[0], out[2])
+    np.testing.assert_array_equal(out[0], out[3])
     # and the fused sweeps stay within rounding of the reference's
     want = O.OraclePC(pt, ip, ix, v).apply(x)
     np.testing.assert_allclose(out[0], want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
 
 
-@pytest.mark.parametrize("tiles,rows", [(False, 0), (True, 64)])
-def test_solves_match_the_oracle_in_both_forms(tiles, rows):
+@pytest.mark.parametrize("tiles,rows,bricks", [(False, 0, 0), (True, 64, 0), (False, 0, 2)])
+def test_solves_match_the_oracle_in_every_form(tiles, rows, bricks):
     """A whole captured CG+ICC and GMRES+ILU solve on each form: same
     iteration count and reason as the oracle, iterate to 1e-10."""
     ip, ix, v = gallery.laplacian_2d(32)
     n = len(ip) - 1
     b = np.random.default_rng(5).normal(size=n)
     _lib.set_sweep_form(tiles, rows)
+    _lib.set_sweep_bricks(bricks)
     for kt, pt in (("cg", "icc"), ("gmres", "ilu")):
         A = _mat(ip, ix, v)
         pc = PETSc.PC().create()
@@ -183,6 +227,19 @@ def test_sweep_forms_edge_cases(name, pt, form, tiles, rows):
     ip, ix, v = EDGE[name]()
     n = len(ip) - 1
     _lib.set_sweep_form(tiles, rows)
+    pc = _pc(pt, _mat(ip, ix, v), {})
+    x = np.random.default_rng(11).normal(size=n)
+    np.testing.assert_array_equal(_apply(pc, x), O.OraclePC(pt, ip, ix, v).apply(x))
+
+
+@pytest.mark.parametrize("pt", ["ilu", "icc", "sor"])
+@pytest.mark.parametrize("name", sorted(EDGE))
+def test_brick_form_edge_cases(name, pt):
+    """The same systems with the brick form allowed wherever the structure is
+    found (a two-row line takes it; the others keep the other forms)."""
+    ip, ix, v = EDGE[name]()
+    n = len(ip) - 1
+    _lib.set_sweep_bricks(2, 2, 2, 0)
     pc = _pc(pt, _mat(ip, ix, v), {})
     x = np.random.default_rng(11).normal(size=n)
     np.testing.assert_array_equal(_apply(pc, x), O.OraclePC(pt, ip, ix, v).apply(x))
