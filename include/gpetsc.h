@@ -242,6 +242,14 @@ int gp_pc_sweep_bricks(gp_pc pc, int32_t which, int32_t *brick, int32_t *dims);
  * solver graphs captured with this PC stay valid. */
 int gp_pc_update_values(gp_pc pc, void *stream);
 int gp_pc_apply(gp_pc pc, const double *x, double *y, void *stream);
+/* y = M^-T x, the true transpose of the preconditioner: for ILU the
+ * triangular solves with U^T and then L^T of the same factor (sweeps laid out
+ * on the first call, so make that call outside any stream capture); none,
+ * Jacobi and IC are symmetric and apply M^-1; SOR returns GP_ERR_UNSUPPORTED.
+ * No counterpart in the reference, whose applyTranspose is the plain apply
+ * (python/mojopetsc4py/PETSc/PC.py:635-642); it is what PCApplyTranspose of
+ * upstream PETSc computes. */
+int gp_pc_apply_transpose(gp_pc pc, const double *x, double *y, void *stream);
 /* Jacobi's symmetric half (src/ksp.mojo:201-208); other types apply M^-1. */
 int gp_pc_apply_symmetric(gp_pc pc, const double *x, double *y, void *stream);
 /* Factor sizes and host copies in the reference's layout (ILU: bi, bj, ba,
@@ -289,6 +297,13 @@ int gp_ksp_set_options(gp_ksp ksp, const gp_ksp_options *o);
 int gp_ksp_solve(gp_ksp ksp, gp_mat A, gp_pc pc, const double *b, double *x,
                  gp_ksp_result *result, double *hist, int64_t hist_len, void *stream);
 
+/* transpose = 1: later solves solve A^T x = b with the same operator and
+ * preconditioner -- every multiply by A becomes one by A^T (the cached
+ * transposed pattern) and every preconditioner apply the true transposed one
+ * (gp_pc_apply_transpose), as upstream PETSc's KSPSolveTranspose does; the
+ * fused CG kernels are not used then.  0 (the default) solves A x = b.  No
+ * counterpart in the reference. */
+int gp_ksp_set_transpose(gp_ksp ksp, int transpose);
 /* How later solves launch their kernels: 0 one captured CUDA graph per solve
  * (the loop is a conditional node), 1 the same kernels launched one by one
  * from a host loop that polls convergence every few iterations (each kernel

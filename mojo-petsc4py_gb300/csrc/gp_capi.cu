@@ -311,6 +311,18 @@ int gp_pc_apply(gp_pc pc, const double* x, double* y, void* stream) {
   })());
 }
 
+int gp_pc_apply_transpose(gp_pc pc, const double* x, double* y, void* stream) {
+  if (!pc || !x || !y) return bad("gp_pc_apply_transpose: null argument");
+  if (x == y) return bad("gp_pc_apply_transpose: y may not alias x");
+  GUARD(([&]() {
+    int st = gp::pc_transpose_prepare(pc->pc, S(stream));
+    if (st) return st;
+    st = gp::pc_apply_transpose(pc->pc, gp::DRef::of(x), gp::DRef::of(y), S(stream));
+    if (st) return st;
+    return gp::pc_check(pc->pc, S(stream));
+  })());
+}
+
 int gp_pc_apply_symmetric(gp_pc pc, const double* x, double* y, void* stream) {
   if (!pc || !x || !y) return bad("gp_pc_apply_symmetric: null argument");
   if (x == y) return bad("gp_pc_apply_symmetric: y may not alias x");
@@ -426,6 +438,13 @@ int gp_ksp_solve(gp_ksp ksp, gp_mat A, gp_pc pc, const double* b, double* x,
     result->rnorm = r.rnorm;
     return st;
   })());
+}
+
+int gp_ksp_set_transpose(gp_ksp ksp, int transpose) {
+  if (!ksp) return bad("gp_ksp_set_transpose: null solver");
+  if (transpose != 0 && transpose != 1) return bad("gp_ksp_set_transpose: 0 or 1");
+  ksp->k->transpose = transpose;
+  return GP_OK;
 }
 
 int gp_ksp_set_launch_form(gp_ksp ksp, int form) {

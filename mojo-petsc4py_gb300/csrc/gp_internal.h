@@ -99,6 +99,10 @@ int csr_make_val32(Csr* A, cudaStream_t s);
 int spmv(cudaStream_t s, const Csr* A, DRef x, DRef y, const int* gate = nullptr, int want = 0);
 int spmv_add(cudaStream_t s, const Csr* A, const double* x, const double* v, double* y);
 int spmv_t(cudaStream_t s, Csr* A, const double* x, double* y);
+// A^T's pattern and values brought up to date (host work and a gather; call
+// before capturing a loop that multiplies by A^T), then the multiply alone.
+int spmv_t_prepare(cudaStream_t s, Csr* A);
+int spmv_t(cudaStream_t s, const Csr* A, DRef x, DRef y, const int* gate, int want);
 int mat_diagonal(cudaStream_t s, const Csr* A, double* d);
 int spmv_grid(const Csr* A);
 

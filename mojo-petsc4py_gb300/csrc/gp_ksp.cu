@@ -1259,9 +1259,17 @@ struct Run {
     GP_CHECK_LAUNCH();
     return GP_OK;
   }
-  int matmult(const int* g, DRef x, DRef y) const { return spmv(s, A, x, y, g, 1); }
-  int pcapply(const int* g, DRef x, DRef y) const { return pc_apply(pc, x, y, s, g, 1); }
-  int pcsym(const int* g, DRef x, DRef y) const { return pc_apply_symmetric(pc, x, y, s, g, 1); }
+  // KSPSolveTranspose: A^T and M^-T in place of A and M^-1
+  int matmult(const int* g, DRef x, DRef y) const {
+    return k->transpose ? spmv_t(s, A, x, y, g, 1) : spmv(s, A, x, y, g, 1);
+  }
+  int pcapply(const int* g, DRef x, DRef y) const {
+    return k->transpose ? pc_apply_transpose(pc, x, y, s, g, 1) : pc_apply(pc, x, y, s, g, 1);
+  }
+  int pcsym(const int* g, DRef x, DRef y) const {
+    if (k->transpose && pc->opt.type != PC_JACOBI) return pc_apply_transpose(pc, x, y, s, g, 1);
+    return pc_apply_symmetric(pc, x, y, s, g, 1);
+  }
   // KSP_PCApplyBAorAB, src/ksp.mojo:246-265
   int apply_ba(const int* g, int side, DRef x, DRef y, DRef w) const {
     if (side == 1) {
@@ -1379,7 +1387,9 @@ static int resident_grid(const void* kernel, int block) {
 static bool cg_fused_ok(const Run& r) {
   const KspOptions& o = r.k->opt;
   // the fused kernels sum their dots inside the vector passes (tree order)
-  return arith_mode() != kOrdered && o.normtype == N_PRECOND && o.chknorm <= 1 &&
+  // and multiply by A itself
+  return arith_mode() != kOrdered && !r.k->transpose && o.normtype == N_PRECOND &&
+         o.chknorm <= 1 &&
          (int64_t)spmv_grid(r.A) <= (int64_t)kMaxBasis * kMaxRedGrid;
 }
 
@@ -1934,23 +1944,29 @@ int ksp_solve(Ksp* k, Csr* A, Pc* pc, const double* b, double* x, KspResult* res
   // a zero initial guess means x = 0 on entry (KSP.solve zeroes x first,
   // python/mojopetsc4py/PETSc/KSP.py:367-449): done here for every caller
   if (o.guess_zero && n) GP_CUDA(cudaMemsetAsync(x, 0, (size_t)n * sizeof(double), s));
+  if (k->transpose) {
+    // host work and value gathers of the transposed solve, outside capture
+    GP_TRY(spmv_t_prepare(s, A));
+    GP_TRY(pc_transpose_prepare(pc, s));
+  }
   Run r{k, A, pc, n, s};
   // the solve graph depends on the buffers and on every option that shapes it
-  const int key[12] = {o.type,      o.normtype,    o.pc_side,          o.restart,
+  const int key[13] = {o.type,      o.normtype,    o.pc_side,          o.restart,
                        o.cgstype,   n,             pc->opt.type,       pc->opt.sor_flag,
-                       o.guess_zero, pc->generation, arith_mode(),    o.orthog};
+                       o.guess_zero, pc->generation, arith_mode(),    o.orthog,
+                       k->transpose};
   if (k->launch_form == 1 || (k->launch_form < 0 && eager_mode())) {
     GP_TRY(run_eager(r, b, x));
   } else {
   const bool same = !moved && k->exec && k->cap_A == A && k->cap_pc == pc &&
-                    std::equal(key, key + 12, k->cap_key) && k->cap_b == b && k->cap_x == x;
+                    std::equal(key, key + 13, k->cap_key) && k->cap_b == b && k->cap_x == x;
   if (!same) {
     GP_TRY(capture(r, b, x));
     k->cap_A = A;
     k->cap_pc = pc;
     k->cap_b = b;
     k->cap_x = x;
-    std::copy(key, key + 12, k->cap_key);
+    std::copy(key, key + 13, k->cap_key);
   }
   GP_CUDA(cudaGraphLaunch(k->exec, s));
   }

@@ -85,12 +85,13 @@ struct Ksp {
   const void* cap_pc = nullptr;
   const void* cap_b = nullptr;
   const void* cap_x = nullptr;
-  int cap_key[12] = {0};
+  int cap_key[13] = {0};
   cudaStream_t stream2 = nullptr;  // body capture stream
   int64_t top_kernels = 0;         // kernels outside the loop body
   int64_t body_kernels = 0;        // kernels per loop trip
   int64_t last_trips = 0;
   int launch_form = -1;  // -1 the environment's (GPETSC_KSP_GRAPH), 0 graph, 1 host loop
+  int transpose = 0;     // solve A^T x = b (A^T multiply, transposed preconditioner)
 };
 
 struct KspResult {

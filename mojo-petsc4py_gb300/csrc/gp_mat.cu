@@ -359,7 +359,7 @@ int spmv_add(cudaStream_t s, const Csr* A, const double* x, const double* v, dou
 // (gathered once per value change through the source slots).  Each row of
 // A^T folds its entries in ascending row order of A, the order in which
 // MatMultTranspose_SeqAIJ (src/ported.mojo:408-431) accumulates y_c.
-int spmv_t(cudaStream_t s, Csr* A, const double* x, double* y) {
+int spmv_t_prepare(cudaStream_t s, Csr* A) {
   GP_TRY(csr_build_transpose(A, s));
   if (A->ncols == 0) return GP_OK;
   if (!A->t_val) {
@@ -372,14 +372,24 @@ int spmv_t(cudaStream_t s, Csr* A, const double* x, double* y) {
     GP_CHECK_LAUNCH();
   }
   A->t_val_stale = false;
+  return GP_OK;
+}
+
+int spmv_t(cudaStream_t s, const Csr* A, DRef x, DRef y, const int* gate, int want) {
+  if (A->ncols == 0) return GP_OK;
   const bool f = arith_mode() == kFma;
   auto k = A->t_stream_rows ? (f ? k_spmv<true, true> : k_spmv<false, true>)
                             : (f ? k_spmv<true, false> : k_spmv<false, false>);
   k<<<(A->ncols + kSpmvRows - 1) / kSpmvRows, kSpmvRows, 0, s>>>(
-      A->ncols, A->t_rowptr, A->t_colind, A->t_val, DRef::of(x), nullptr, DRef::of(y), nullptr, 0,
+      A->ncols, A->t_rowptr, A->t_colind, A->t_val, x, nullptr, y, gate, want,
       A->l2_evict_first);
   GP_CHECK_LAUNCH();
   return GP_OK;
+}
+
+int spmv_t(cudaStream_t s, Csr* A, const double* x, double* y) {
+  GP_TRY(spmv_t_prepare(s, A));
+  return spmv_t(s, A, DRef::of(x), DRef::of(y), nullptr, 0);
 }
 
 int mat_diagonal(cudaStream_t s, const Csr* A, double* d) {

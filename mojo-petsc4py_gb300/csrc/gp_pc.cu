@@ -431,6 +431,8 @@ static void free_all(Pc* pc) {
     if (p) cudaFree(p);
   ell_free(pc->ef);
   ell_free(pc->eb);
+  ell_free(pc->etf);
+  ell_free(pc->etb);
   PcOptions keep = pc->opt;
   *pc = Pc();
   pc->opt = keep;
@@ -814,6 +816,10 @@ int pc_factor_numeric(Pc* pc, cudaStream_t s) {
   GP_CHECK_LAUNCH();
   GP_TRY(ell_refresh(pc->ef, pc->ba, s));
   GP_TRY(ell_refresh(pc->eb, pc->ba, s));
+  if (pc->trans_ready) {
+    GP_TRY(ell_refresh(pc->etf, pc->ba, s));
+    GP_TRY(ell_refresh(pc->etb, pc->ba, s));
+  }
   return pc_check(pc, s);
 }
 
@@ -975,6 +981,107 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
       break;
     default: set_error("unsupported PC type"); return GP_ERR_UNSUPPORTED;
   }
+  GP_CHECK_LAUNCH();
+  return GP_OK;
+}
+
+// The transposed ILU apply.  The forward apply is y = S_c U^-1 L^-1 G_r x
+// (G_r gathers x[r[i]], S_c scatters y[c[i]]), so
+//   M^-T x = G_r^T L^-T U^-T S_c^T x:
+// gather t_i = x[c[i]]; solve U^T z = t (a forward sweep: row i of U^T holds
+// U(k, i) for the rows k < i whose U part has column i, and U's diagonal is
+// stored inverted); solve L^T w = z (a backward sweep over L(k, i), k > i,
+// unit diagonal); scatter y[r[i]] = w_i.  Both sweeps are laid out once, in
+// the level-ordered form, and gather their coefficients from the factor.
+// There is no counterpart in the reference, whose applyTranspose is apply
+// (python/mojopetsc4py/PETSc/PC.py:635-642).
+int pc_transpose_prepare(Pc* pc, cudaStream_t s) {
+  if (!pc->ready) {
+    set_error("PC used before set-up");
+    return GP_ERR_NOT_SETUP;
+  }
+  if (pc->opt.type == PC_SOR) {
+    set_error("transposed apply: SOR on a nonsymmetric operator is not supported");
+    return GP_ERR_UNSUPPORTED;
+  }
+  if (pc->opt.type != PC_ILU || pc->trans_ready || pc->n == 0) return GP_OK;
+  const int n = pc->n;
+  const FactorPattern& P = pc->pat;
+  // U^T: per column i, the rows k < i holding it in their U part, ascending k
+  std::vector<int> up(n + 1, 0), uc, us, dsl(n);
+  {
+    std::vector<std::vector<std::pair<int, int>>> cols(n);
+    for (int k = 0; k < n; k++)
+      for (int j = P.bdiag[k + 1] + 1; j < P.bdiag[k]; j++) cols[P.bj[j]].emplace_back(k, j);
+    for (int i = 0; i < n; i++) {
+      std::sort(cols[i].begin(), cols[i].end());
+      for (auto& e : cols[i]) {
+        uc.push_back(e.first);
+        us.push_back(e.second);
+      }
+      up[i + 1] = (int)uc.size();
+      dsl[i] = P.bdiag[i];
+    }
+  }
+  // L^T: per column i, the rows k > i holding it in their L part, ascending k
+  std::vector<int> lp(n + 1, 0), lc, ls;
+  {
+    std::vector<std::vector<std::pair<int, int>>> cols(n);
+    for (int k = 0; k < n; k++)
+      for (int j = P.bi[k]; j < P.bi[k + 1]; j++) cols[P.bj[j]].emplace_back(k, j);
+    for (int i = 0; i < n; i++) {
+      std::sort(cols[i].begin(), cols[i].end());
+      for (auto& e : cols[i]) {
+        lc.push_back(e.first);
+        ls.push_back(e.second);
+      }
+      lp[i + 1] = (int)lc.size();
+    }
+  }
+  std::vector<int> perm_c(n), of, ob, fpos, none;
+  GP_CUDA(cudaMemcpy(perm_c.data(), pc->perm_c, n * sizeof(int), cudaMemcpyDeviceToHost));
+  int nlev = 0;
+  level_order(n, up, uc, true, of, &nlev);
+  level_order(n, lp, lc, false, ob, &nlev);
+  GP_TRY(ell_build_levels(pc->etf, ELL_ILU_B, n, true, of, up, uc, us, perm_c, none, dsl, &fpos));
+  GP_TRY(ell_build_levels(pc->etb, ELL_ILU_F, n, false, ob, lp, lc, ls, fpos, P.r, none, nullptr));
+  if (!pc->etf.ok || !pc->etb.ok) {
+    ell_free(pc->etf);
+    ell_free(pc->etb);
+    set_error("transposed apply: a row of U^T or L^T has more than 16 entries");
+    return GP_ERR_UNSUPPORTED;
+  }
+  GP_TRY(ell_refresh(pc->etf, pc->ba, s));
+  GP_TRY(ell_refresh(pc->etb, pc->ba, s));
+  pc->trans_ready = true;
+  return GP_OK;
+}
+
+int pc_apply_transpose(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) {
+  if (!pc->ready) {
+    set_error("PC used before set-up");
+    return GP_ERR_NOT_SETUP;
+  }
+  if (pc->opt.type != PC_ILU) {
+    if (pc->opt.type == PC_SOR) {
+      set_error("transposed apply: SOR on a nonsymmetric operator is not supported");
+      return GP_ERR_UNSUPPORTED;
+    }
+    return pc_apply(pc, x, y, s, gate, want);  // symmetric: none, Jacobi, IC
+  }
+  const int n = pc->n;
+  if (n == 0) return GP_OK;
+  if (!pc->trans_ready) {
+    set_error("transposed apply used before pc_transpose_prepare");
+    return GP_ERR_NOT_SETUP;
+  }
+  k_fill_pending<<<grid_for(n), 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
+  // U^T z = x[c]: input gathered from x by the sweep's in_idx, no output
+  GP_TRY(ell_sweep(ELL_ILU_B, pc->etf, gate, want, x, y, pc->yf, nullptr, nullptr, nullptr,
+                   nullptr, 0.0, 0, 0, pc->tickets, pc->err, pc->ba, s));
+  // L^T w = z: input from the first sweep's values, output scattered to y[r]
+  GP_TRY(ell_sweep(ELL_ILU_F, pc->etb, gate, want, x, y, pc->yb, pc->yf, nullptr, nullptr,
+                   nullptr, 0.0, 0, 1, pc->tickets + 2, pc->err, pc->ba, s));
   GP_CHECK_LAUNCH();
   return GP_OK;
 }

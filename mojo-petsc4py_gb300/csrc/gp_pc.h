@@ -100,6 +100,12 @@ int ell_build(EllSweep& e, int mode, int n, bool forward, const std::vector<int>
               const std::vector<int>& out_row, const std::vector<int>& dslot_row,
               std::vector<int>* pos_of_row);
 int ell_refresh(EllSweep& e, const double* src, cudaStream_t s);
+// ell_build in the level-ordered form only (no chunked or brick layout).
+int ell_build_levels(EllSweep& e, int mode, int n, bool forward, const std::vector<int>& order,
+                     const std::vector<int>& dptr, const std::vector<int>& dcol,
+                     const std::vector<int>& dsl, const std::vector<int>& in_row,
+                     const std::vector<int>& out_row, const std::vector<int>& dslot_row,
+                     std::vector<int>* pos_of_row);
 int sweep_wait_probe(int budget, int set, cudaStream_t s);
 // Sweep form of later set-ups (gp_set_sweep_form).
 void set_sweep_form(int tiles, int tile_rows);
@@ -164,6 +170,10 @@ struct Pc {
 
   SweepPlan fwd, bwd, num;
   EllSweep ef, eb;           // ELL forms of the forward and backward sweeps
+  // ILU transposed apply (built on first use): sweeps over U^T (forward) and
+  // L^T (backward) of the same factor
+  EllSweep etf, etb;
+  bool trans_ready = false;
   // sweep work: value-as-flag arrays and SOR checkpoint
   double* yf = nullptr;
   double* yb = nullptr;
@@ -178,6 +188,13 @@ int pc_destroy(Pc* pc);
 int pc_setup(Pc* pc, Csr* A, cudaStream_t s);
 // y = M^-1 x (x, y distinct device vectors).  Gate for captured loops.
 int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate = nullptr, int want = 0);
+// y = M^-T x: the true transpose of the preconditioner (ILU: sweeps over U^T
+// then L^T of the factor; none, Jacobi and IC are symmetric, so their apply;
+// SOR: GP_ERR_UNSUPPORTED).  pc_transpose_prepare builds what it needs on the
+// host (outside any stream capture).
+int pc_transpose_prepare(Pc* pc, cudaStream_t s);
+int pc_apply_transpose(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate = nullptr,
+                       int want = 0);
 // Jacobi symmetric half; other types fall back to pc_apply.
 int pc_apply_symmetric(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate = nullptr,
                        int want = 0);

@@ -15,6 +15,7 @@
 // linked list, as the reference's; IC: a sorted list of touched columns);
 // the resulting patterns are the same sets in the same (ascending) order.
 #include <algorithm>
+#include <climits>
 #include <string>
 #include <vector>
 
@@ -109,6 +110,14 @@ static void permuted_row(const Csr* A, const std::vector<int>& r, const std::vec
   out.erase(std::unique(out.begin(), out.end()), out.end());
 }
 
+// Row offsets are int32 (the factor's device indices): the slot count is
+// checked in 64 bits before each narrowing, against `limit`.
+static bool slots_fit(size_t count, int64_t limit, const char* who) {
+  if ((int64_t)count <= limit) return true;
+  set_error(std::string(who) + " factor too large for 32-bit indices");
+  return false;
+}
+
 // ILU(levels) rows.  Row i starts from A's permuted row at level 0; its
 // pivots p < i are visited in ascending order, fill included (a fill column
 // reached through p is always > p), and each adds U(p, :) past the diagonal
@@ -134,6 +143,7 @@ static int ilu_rows_flat(const Csr* A, int levels, const std::vector<int>& r,
       R.nL[i] = (int)(std::lower_bound(row.begin(), row.end(), i) - row.begin());
       R.cols.insert(R.cols.end(), row.begin(), row.end());
       R.lv.insert(R.lv.end(), row.size(), 0);
+      if (!slots_fit(R.cols.size(), INT32_MAX - 1, "ILU")) return GP_ERR_ARG;
       R.rs[i + 1] = (int)R.cols.size();
       continue;
     }
@@ -168,6 +178,7 @@ static int ilu_rows_flat(const Csr* A, int levels, const std::vector<int>& r,
       lev[c] = -1;
     }
     R.nL[i] = cnt;
+    if (!slots_fit(R.cols.size(), INT32_MAX - 1, "ILU")) return GP_ERR_ARG;
     R.rs[i + 1] = (int)R.cols.size();
   }
   return GP_OK;
@@ -220,6 +231,7 @@ static int icc_rows_flat(const Csr* A, int levels, const std::vector<int>& r,
       R.cols.push_back(c);
       R.lv.push_back(lev[c]);
       if (levels > 0) {
+        if (!slots_fit(erow.size() + 1, INT32_MAX - 1, "IC")) return GP_ERR_ARG;
         enext.push_back(chead[c]);
         erow.push_back(k);
         elev.push_back(lev[c]);
@@ -227,6 +239,8 @@ static int icc_rows_flat(const Csr* A, int levels, const std::vector<int>& r,
       }
       lev[c] = -1;
     }
+    // the diagonal slots (one a row) come on top of the strict rows
+    if (!slots_fit(R.cols.size(), (int64_t)INT32_MAX - 1 - n, "IC")) return GP_ERR_ARG;
     R.rs[k + 1] = (int)R.cols.size();
   }
   return GP_OK;

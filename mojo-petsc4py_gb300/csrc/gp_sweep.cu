@@ -17,9 +17,11 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <exception>
 #include <functional>
 #include <limits>
 #include <map>
+#include <mutex>
 #include <queue>
 #include <string>
 #include <thread>
@@ -145,11 +147,14 @@ __global__ void __launch_bounds__(kEllBlock) k_ell_sweep(const int* gate, int wa
           cf[e] = a.coef[(size_t)e * n + p];
         }
       }
-      if constexpr (MODE == ELL_ILU_F || MODE == ELL_ICC_F) {
+      if constexpr (MODE == ELL_ILU_F) {
+        // from an earlier sweep's values when given (the transposed apply)
+        sum = (a.fval ? a.fval : in)[a.in_idx[p]];
+      } else if constexpr (MODE == ELL_ICC_F) {
         sum = in[a.in_idx[p]];
-        if (MODE == ELL_ICC_F) dv = a.dval[p];
+        dv = a.dval[p];
       } else if constexpr (MODE == ELL_ILU_B) {
-        sum = a.fval[a.in_idx[p]];
+        sum = (a.fval ? a.fval : in)[a.in_idx[p]];
         dv = a.dval[p];
       } else if constexpr (MODE == ELL_ICC_B) {
         sum = a.auxin[a.in_idx[p]];
@@ -185,10 +190,11 @@ __global__ void __launch_bounds__(kEllBlock) k_ell_sweep(const int* gate, int wa
         }
         if (ecur >= c) {
           if constexpr (MODE == ELL_ILU_F) {
+            if (a.out_idx) out[a.out_idx[p]] = sum;
             st_relaxed(&a.val[p], sum);
           } else if constexpr (MODE == ELL_ILU_B) {
             const double y = mul(sum, dv);
-            out[a.out_idx[p]] = y;
+            if (a.out_idx) out[a.out_idx[p]] = y;
             st_relaxed(&a.val[p], y);
           } else if constexpr (MODE == ELL_ICC_F) {
             a.aux[p] = mul(sum, dv);
@@ -385,7 +391,11 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_sweep(const int* gate,
     const bool staged = mbar_wait(bar, parity, kEllSpin);
     if (!staged) {
       if (lane == 0 && atomicCAS(&a.err->code, 0, GP_ERR_TIMEOUT) == 0) a.err->where = 40 + MODE;
-      mbar_wait(bar, parity, kEllSpin);  // let the copies in flight land before leaving
+      // let the copies in flight land before leaving; a bulk copy that has
+      // not landed after this second bounded wait is not recovered from: the
+      // CTA leaves with the timeout recorded and the host reports the sweep
+      // as failed (GP_ERR_TIMEOUT)
+      mbar_wait(bar, parity, kEllSpin);
     }
     parity ^= 1u;
     if (__syncthreads_or(!staged)) break;
@@ -763,13 +773,25 @@ static bool tile_choose(int mode, int n, int W, const std::vector<int>& dptr,
   if (nthreads <= 1) {
     for (int c = 0; c < nc; c++) eval(c);
   } else {
+    // an exception (bad_alloc) inside a worker would end the process; it is
+    // caught there and rethrown on this thread, where the C ABI's guard turns
+    // it into an error status
     std::atomic<int> next{0};
+    std::exception_ptr failure;
+    std::mutex failure_mu;
     std::vector<std::thread> pool;
     for (int t = 0; t < nthreads; t++)
       pool.emplace_back([&]() {
-        for (int c; (c = next.fetch_add(1)) < nc;) eval(c);
+        try {
+          for (int c; (c = next.fetch_add(1)) < nc;) eval(c);
+        } catch (...) {
+          std::lock_guard<std::mutex> lock(failure_mu);
+          if (!failure) failure = std::current_exception();
+          next.store(nc);
+        }
       });
     for (auto& th : pool) th.join();
+    if (failure) std::rethrow_exception(failure);
   }
   bool found = false;
   *considered = 0;
@@ -989,6 +1011,15 @@ int ell_build(EllSweep& e, int mode, int n, bool forward, const std::vector<int>
               std::vector<int>* pos_of_row) {
   return ell_build_impl(e, mode, n, forward, order, dptr, dcol, dsl, in_row, out_row,
                         dslot_row, pos_of_row, true);
+}
+
+int ell_build_levels(EllSweep& e, int mode, int n, bool forward, const std::vector<int>& order,
+                     const std::vector<int>& dptr, const std::vector<int>& dcol,
+                     const std::vector<int>& dsl, const std::vector<int>& in_row,
+                     const std::vector<int>& out_row, const std::vector<int>& dslot_row,
+                     std::vector<int>* pos_of_row) {
+  return ell_build_impl(e, mode, n, forward, order, dptr, dcol, dsl, in_row, out_row,
+                        dslot_row, pos_of_row, false);
 }
 
 // Run the wait once on a pending flag (set = 0) or a ready one (set = 1) and

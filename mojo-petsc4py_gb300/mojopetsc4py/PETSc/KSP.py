@@ -287,7 +287,7 @@ class KSP:
         if self._normtype == NormType_.NORM_DEFAULT:
             self._normtype = NormType_.NORM_PRECONDITIONED
 
-    def _rhs_norm(self, b: Vec) -> float:
+    def _rhs_norm(self, b: Vec, transpose: bool = False) -> float:
         """KSPConvergedDefault's right-hand-side norm for a nonzero guess
         (the reference computes it in Python, KSP.py:496-507; here the
         preconditioner apply and the norm run on the GPU)."""
@@ -296,7 +296,10 @@ class KSP:
         if self._normtype == NormType_.UNPRECONDITIONED or self._pc_side == 1:
             return float(b.norm())
         z = b.duplicate()
-        self._pc.apply(b, z)
+        if transpose:
+            self._pc._apply_transpose_exact(b, z)
+        else:
+            self._pc.apply(b, z)
         if self._normtype == NormType_.PRECONDITIONED:
             return float(z.norm())
         return math.sqrt(abs(z.dot(b)))
@@ -324,6 +327,17 @@ class KSP:
     def solve(self, b: Vec, x: Vec) -> None:
         """Solve A x = b on the GPU; with the default zero initial guess the
         contents of x on entry are ignored."""
+        self._solve(b, x, False)
+
+    def solveTranspose(self, b: Vec, x: Vec) -> None:
+        """Solve A^T x = b with the same operator and preconditioner: every
+        multiply by A becomes one by A^T and every preconditioner apply the
+        true transposed one (for ILU, the triangular solves with U^T and L^T
+        of the same factor).  petsc4py's KSP.solveTranspose; the reference
+        has no transposed solve."""
+        self._solve(b, x, True)
+
+    def _solve(self, b: Vec, x: Vec, transpose: bool) -> None:
         if self._amat is None:
             raise RuntimeError("KSP.setOperators() has not been called")
         A = self._amat
@@ -340,12 +354,13 @@ class KSP:
         self._pc.setUp()
         self._rhs, self._sol = b, x
         self._resolve_normtype()
-        rhs = 0.0 if self._guess_zero else self._rhs_norm(b)
+        rhs = 0.0 if self._guess_zero else self._rhs_norm(b, transpose)
         if self._gp is None:
             h = ctypes.c_void_p()
             check(lib().gp_ksp_create(ctypes.byref(h)))
             self._gp = h.value
         check(lib().gp_ksp_set_launch_form(self._gp, self._launch_form))
+        check(lib().gp_ksp_set_transpose(self._gp, 1 if transpose else 0))
         opts = self._options(rhs)
         check(lib().gp_ksp_set_options(self._gp, ctypes.byref(opts)))
         hist = np.zeros(max(self._histlen, 0), dtype=np.float64)

@@ -120,6 +120,7 @@ class PC:
         self._rowl1_scale = 1.0
         self._gp = None
         self._gp_key = None
+        self._exact_transpose = False
 
     def __del__(self):
         h = getattr(self, "_gp", None)
@@ -327,9 +328,26 @@ class PC:
 
     def applyTranspose(self, x: Vec, y: Vec) -> None:
         """The reference's applyTranspose is `apply` for every type
-        (python/mojopetsc4py/PETSc/PC.py:635-642); kept so for parity.  The
-        adjoint solver uses the true transpose (`applyTransposeExact`)."""
-        self.apply(x, y)
+        (python/mojopetsc4py/PETSc/PC.py:635-642), and so is this one by
+        default.  After `setUseExactTranspose(True)` it applies the true
+        transpose M^-T (for ILU the solves with U^T and L^T of the factor),
+        as upstream PETSc's PCApplyTranspose does."""
+        if self._exact_transpose:
+            self._apply_transpose_exact(x, y)
+        else:
+            self.apply(x, y)
+
+    def setUseExactTranspose(self, flag: bool = True) -> None:
+        """Extension (no counterpart in the reference): make applyTranspose
+        the true transposed apply instead of the reference's plain apply."""
+        self._exact_transpose = bool(flag)
+
+    def _apply_transpose_exact(self, x: Vec, y: Vec) -> None:
+        self.setUp()
+        self._check_pair(x, y)
+        if self._pmat._nrows:
+            check(lib().gp_pc_apply_transpose(self._gp, x._dptr(), y._optr(),
+                                              dev.stream_ptr()))
 
     def applySymmetricLeft(self, x: Vec, y: Vec) -> None:
         self.setUp()

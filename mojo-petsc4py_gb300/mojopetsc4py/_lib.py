@@ -110,6 +110,7 @@ GP_SIGNATURES = {
     "gp_pc_sweep_bricks": ([P, ctypes.c_int32, P, P], ctypes.c_int),
     "gp_pc_apply": ([P, P, P, P], ctypes.c_int),
     "gp_pc_apply_symmetric": ([P, P, P, P], ctypes.c_int),
+    "gp_pc_apply_transpose": ([P, P, P, P], ctypes.c_int),
     "gp_pc_factor_info": ([P, P, P], ctypes.c_int),
     "gp_pc_factor_get": ([P, P, P, P, P, P], ctypes.c_int),
     "gp_ksp_options_default": ([ctypes.POINTER(KspOptions)], None),
@@ -119,6 +120,7 @@ GP_SIGNATURES = {
     "gp_ksp_solve": ([P, P, P, P, P, ctypes.POINTER(KspResult), P, I64, P], ctypes.c_int),
     "gp_ksp_stats": ([P, P, P, P], ctypes.c_int),
     "gp_ksp_set_launch_form": ([P, ctypes.c_int], ctypes.c_int),
+    "gp_ksp_set_transpose": ([P, ctypes.c_int], ctypes.c_int),
 }
 
 _lib = None

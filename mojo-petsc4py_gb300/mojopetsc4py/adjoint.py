@@ -11,18 +11,21 @@ The hand-written backward pass runs the adjoint solve
 
     A^T lambda = dL/dx
 
-with the transposed matrix built on the device (`gp_mat_transpose`, the
-reference's `Mat.transpose`, python/mojopetsc4py/PETSc/Mat.py:555-563) and
-returns
+and returns
 
     dL/db      = lambda
     dL/dA_ij   = -lambda_i x_j     on the stored nonzeros (gp_mat_outer_on_pattern)
 
-The adjoint solve uses the same Krylov method with the preconditioner built
-on A^T.  For ILU(0) on a structurally symmetric pattern, the incomplete
-factorisation of A^T is the transpose of that of A in exact arithmetic (the
-ILU(0) conditions -- M = LU with L, U on the pattern and M = A there -- are
-invariant under transposition), so this is the transposed preconditioner.
+In FP64 the adjoint solve is the transposed solve of the forward system
+(KSPSolveTranspose, `gp_ksp_set_transpose`): the same Krylov method, every
+multiply by A replaced by one by A^T (the matrix's cached transposed
+pattern, the reference's MatMultTranspose, src/ported.mojo:408-431) and every
+preconditioner apply by the true transposed apply of the forward
+preconditioner (for ILU the solves with U^T and L^T of the same factor) --
+no second matrix and no second factorisation.  SOR, which has no transposed
+apply here, solves with the transposed matrix built on the device
+(`gp_mat_transpose`, the reference's `Mat.transpose`,
+python/mojopetsc4py/PETSc/Mat.py:555-563) and its own SOR.
 
 With `precision="mixed"` both solves are the library's mixed-precision form
 (`gp_mixed_solve`): FP32 FGMRES(restart) preconditioned with the ILU(0) factor
@@ -66,6 +69,16 @@ class _Solver:
         self.its = 0
         self.reason = 0
         self.rnorm = 0.0
+        self.ksp_t = None  # the transposed solve's KSP (its own captured graph)
+
+    def _options(self):
+        o = KspOptions()
+        lib().gp_ksp_options_default(ctypes.byref(o))
+        o.type = _KSP[self.ksp_type]
+        o.rtol, o.atol = self.rtol, self.atol
+        o.max_it = self.max_it
+        o.restart = self.restart
+        return o
 
     def setup(self, fresh_pattern: bool):
         st = dev.stream_ptr()
@@ -86,15 +99,18 @@ class _Solver:
             h = ctypes.c_void_p()
             check(lib().gp_ksp_create(ctypes.byref(h)))
             self.ksp = h.value
-            o = KspOptions()
-            lib().gp_ksp_options_default(ctypes.byref(o))
-            o.type = _KSP[self.ksp_type]
-            o.rtol, o.atol = self.rtol, self.atol
-            o.max_it = self.max_it
-            o.restart = self.restart
-            check(lib().gp_ksp_set_options(self.ksp, ctypes.byref(o)))
+            check(lib().gp_ksp_set_options(self.ksp, ctypes.byref(self._options())))
 
-    def solve(self, b, x):
+    def solve(self, b, x, transpose: bool = False):
+        """A x = b, or A^T x = b with `transpose` (same matrix, same
+        preconditioner: gp_ksp_set_transpose)."""
+        if transpose and self.ksp_t is None:
+            h = ctypes.c_void_p()
+            check(lib().gp_ksp_create(ctypes.byref(h)))
+            self.ksp_t = h.value
+            check(lib().gp_ksp_set_options(self.ksp_t, ctypes.byref(self._options())))
+            check(lib().gp_ksp_set_transpose(self.ksp_t, 1))
+        ksp = self.ksp_t if transpose else self.ksp
         # the solve graph is keyed on the vector addresses: solve between two
         # fixed buffers so one captured graph serves every call
         if getattr(self, "_bbuf", None) is None or self._bbuf.numel() != b.numel():
@@ -103,7 +119,7 @@ class _Solver:
         else:
             self._bbuf.copy_(b)
         res = KspResult()
-        check(lib().gp_ksp_solve(self.ksp, self.mat, self.pc, dev.ptr(self._bbuf),
+        check(lib().gp_ksp_solve(ksp, self.mat, self.pc, dev.ptr(self._bbuf),
                                  dev.ptr(self._xbuf), ctypes.byref(res), None, 0,
                                  dev.stream_ptr()))
         x.copy_(self._xbuf)
@@ -115,9 +131,21 @@ class _Solver:
     def close(self):
         if self.ksp is not None:
             lib().gp_ksp_destroy(self.ksp)
+        if self.ksp_t is not None:
+            lib().gp_ksp_destroy(self.ksp_t)
         if self.pc is not None:
             lib().gp_pc_destroy(self.pc)
-        self.ksp = self.pc = None
+        self.ksp = self.ksp_t = self.pc = None
+
+
+class _TransposeView:
+    """Iteration statistics of a solver's last transposed solve."""
+
+    def __init__(self, solver):
+        self.its, self.reason, self.rnorm = solver.its, solver.reason, solver.rnorm
+
+    def close(self):
+        pass
 
 
 class _MixedSolver:
@@ -275,6 +303,17 @@ class SparseSystem:
     def solve_transpose(self, g):
         """lambda with A^T lambda = g for the current values."""
         g = self._check(g, self.n, "g")
+        if self.precision == "fp64" and self.forward_solver.pc_type != "sor":
+            # the forward system's transposed solve: same matrix, same factor
+            s = self.forward_solver
+            if self._fwd_version != self._version:
+                s.setup(fresh_pattern=self._fwd_version < 0)
+                self._fwd_version = self._version
+            lam = self._torch.empty_like(g)
+            if self.n:
+                s.solve(g, lam, transpose=True)
+            self.adjoint_solver = _TransposeView(s)
+            return lam
         st = dev.stream_ptr()
         fresh = False
         if self._matT is None:
