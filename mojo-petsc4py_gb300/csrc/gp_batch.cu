@@ -7,7 +7,7 @@
 // sparse pass serves all R columns and the column loads of a row are one
 // contiguous 8R-byte run.  Every (system, column) pair runs its own CG
 // recurrence -- the PETSc CG of KSPSolve_CG (src/ksp.mojo:271-389), default
-// preconditioned norm, Jacobi or no preconditioner -- with its own scalars,
+// preconditioned norm, Jacobi, IC(0) or no preconditioner -- with its own scalars,
 // stopping test and iteration count.  A pair that stops is frozen; a system
 // whose R pairs all stopped drops out of every later pass.
 //
@@ -358,6 +358,55 @@ __global__ void k_bupdate(BatchDev b, const T* __restrict__ dinv, T* __restrict_
   }
 }
 
+// x += a p; r -= a w, active pairs only (the preconditioner and the pair
+// dots follow: IC(0))
+template <int R>
+__global__ void k_bupdate_xr(BatchDev b, double* __restrict__ x, double* __restrict__ r,
+                             const double* __restrict__ p, const double* __restrict__ w) {
+  TILE_LOOP(tile) {
+    const int s = b.tile_sys[tile];
+    if (!b.sys_active[s]) continue;
+    const int q = s * R + threadIdx.x % R;  // blockDim is a multiple of R
+    if (!b.active[q]) continue;
+    const double al = b.a[q];
+    const int r0 = b.tile_row0[tile], ne = b.tile_nrows[tile] * R;
+    const size_t o0 = (size_t)r0 * R;
+    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+      x[o0 + e] = fmadd<double>(al, p[o0 + e], x[o0 + e]);
+      r[o0 + e] = fmadd<double>(-al, w[o0 + e], r[o0 + e]);
+    }
+  }
+}
+
+// pair ||z||^2 and z.r after a separate preconditioner apply; the system's
+// last tile runs the pairs' tails
+template <int R, bool FIRST>
+__global__ void k_bdots(BatchDev b, const double* __restrict__ r, const double* __restrict__ z) {
+  extern __shared__ unsigned char smem_raw[];
+  double* sh = reinterpret_cast<double*>(smem_raw);
+  const int t = threadIdx.x, slots = blockDim.x / R;
+  TILE_LOOP(tile) {
+    const int s = b.tile_sys[tile];
+    if (!b.sys_active[s]) continue;
+    const int r0 = b.tile_row0[tile], nr = b.tile_nrows[tile];
+    double acc[2][1] = {{0.0}, {0.0}};
+    const bool on = b.active[s * R + t % R] != 0;
+    for (int rr = t / R; rr < nr && on; rr += slots) {
+      const size_t o = (size_t)(r0 + rr) * R + t % R;
+      const double zi = z[o];
+      acc[0][0] = fmadd<double>(zi, zi, acc[0][0]);
+      acc[1][0] = fmadd<double>(zi, r[o], acc[1][0]);
+    }
+    tile_partials<double, R, 1, 2>(b, tile, acc, sh);
+    if (system_last(b, s)) {
+      const double* tot = system_sums(b, s, R, 2);
+      if (t < R) pair_after_update(b, s, s * R + t, tot[2 * t], tot[2 * t + 1], FIRST);
+      __syncthreads();
+      if (t == 0) b.sys_ticket[s] = 0u;
+    }
+  }
+}
+
 __global__ void k_bctrl(cudaGraphConditionalHandle h, int* active_systems, int* trips,
                         int cap) {
   *trips += 1;
@@ -565,6 +614,11 @@ struct Batch {
   double *r = nullptr, *p = nullptr, *z = nullptr;
   float *x32 = nullptr, *r32 = nullptr, *p32 = nullptr, *z32 = nullptr;
   double *bnorm = nullptr, *rn = nullptr;
+  // IC(0) of the block-diagonal matrix (set up on its first use) and its
+  // sweeps' scratch (n * R each)
+  Csr* icc_A = nullptr;
+  Pc* icc = nullptr;
+  double *icc_vf = nullptr, *icc_vb = nullptr, *icc_ys = nullptr;
   Tuning tune, tune32;          // FP64 and FP32 sparse-pass choices
   const Tuning* cur = &tune;    // the one the current solve launches with
   bool tuned = false;
@@ -688,6 +742,43 @@ static void launch_p(const Batch& B, const BatchDev& d, T* p, const T* z, cudaSt
   k<<<g, B.cur->block, 0, s>>>(d, p, z);
 }
 
+template <int R>
+static void launch_update_xr(const Batch& B, const BatchDev& d, double* x, double* r,
+                             const double* p, const double* w, cudaStream_t s) {
+  auto k = k_bupdate_xr<R>;
+  const int g = std::max(1, std::min(B.ntiles, resident((const void*)k, B.cur->block, 0)));
+  k<<<g, B.cur->block, 0, s>>>(d, x, r, p, w);
+}
+
+template <int R, bool FIRST>
+static void launch_dots(const Batch& B, const BatchDev& d, const double* r, const double* z,
+                        cudaStream_t s) {
+  auto k = k_bdots<R, FIRST>;
+  Launch l = shape_of<double, R, 1, 2>(B, (const void*)k);
+  k<<<l.grid, l.block, l.smem, s>>>(d, r, z);
+}
+
+// IC(0) of the block-diagonal batch matrix in its (renumbered) rows: the
+// library's PC set-up on the whole matrix -- no entry couples two systems,
+// so this is each system's IC(0) -- built once, on the first IC solve.
+static int batch_icc_setup(Batch& B, cudaStream_t s) {
+  if (B.icc) return GP_OK;
+  std::vector<double> hv((size_t)std::max<int64_t>(B.nnz, 1));
+  if (B.nnz)
+    GP_CUDA(cudaMemcpy(hv.data(), B.val, (size_t)B.nnz * sizeof(double),
+                       cudaMemcpyDeviceToHost));
+  GP_TRY(csr_create_i32(&B.icc_A, B.n, B.n, B.nnz, B.h_rowptr.data(), B.h_colind.data(),
+                        hv.data(), s));
+  GP_TRY(pc_create(&B.icc));
+  B.icc->opt.type = PC_ICC;
+  GP_TRY(pc_setup(B.icc, B.icc_A, s));
+  const size_t nv = std::max<size_t>((size_t)B.n * B.R, 1);
+  GP_CUDA(cudaMalloc(&B.icc_vf, nv * sizeof(double)));
+  GP_CUDA(cudaMalloc(&B.icc_vb, nv * sizeof(double)));
+  GP_CUDA(cudaMalloc(&B.icc_ys, nv * sizeof(double)));
+  return GP_OK;
+}
+
 template <int R, int VR>
 static void launch_resid(const Batch& B, const BatchDev& d, const double* b, const double* x,
                          int freeze, cudaStream_t s) {
@@ -766,9 +857,11 @@ void batch_destroy(Batch* B) {
   void* ptrs[] = {B->rowptr, B->colind, B->diagpos, B->val, B->val32, B->dinv, B->dinv32,
                   B->sys_ticket, B->sys_active, B->sys_pairs_left, B->counters, B->pair_d,
                   B->pair_i, B->r, B->p, B->z, B->x32, B->r32, B->p32, B->z32, B->bnorm,
-                  B->rn, B->perm, B->bp, B->xp};
+                  B->rn, B->perm, B->bp, B->xp, B->icc_vf, B->icc_vb, B->icc_ys};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (B->icc) pc_destroy(B->icc);
+  if (B->icc_A) csr_destroy(B->icc_A);
   if (B->cap_stream) cudaStreamDestroy(B->cap_stream);
   delete B;
 }
@@ -1190,7 +1283,34 @@ static int solve_shape(Batch& B, const BatchOptions& o, const double* b, double*
     Launch l = shape_of<double, R, 1, 1>(B, (const void*)k);
     k<<<l.grid, l.block, l.smem, st>>>(d64, b, B.bnorm);
   };
-  if (o.precision == 0) {
+  if (o.precision == 0 && o.pc == 6) {
+    // IC(0): the update leaves z alone; z = M^-1 r, then the pair dots
+    auto icc = [&](cudaStream_t st) {
+      return pc_apply_icc_cols(B.icc, R, B.r, B.z, B.icc_vf, B.icc_vb, B.icc_ys, st);
+    };
+    int pst = GP_OK;
+    GP_TRY(run_loop(
+          B, 0, s2, b, x, key, o.max_it + 8,
+          [&](cudaStream_t st) {
+            cudaMemsetAsync(B.counters, 0, 2 * sizeof(int), st);
+            cudaMemsetAsync(x, 0, nv * sizeof(double), st);
+            cudaMemcpyAsync(B.r, b, nv * sizeof(double), cudaMemcpyDeviceToDevice, st);
+            norms(st);
+            launch_state(B, d64, nullptr, st);
+            if (pst == GP_OK) pst = icc(st);
+            launch_dots<R, true>(B, d64, B.r, B.z, st);
+          },
+          [&](cudaStream_t st) {
+            launch_p<double, R>(B, d64, B.p, B.z, st);
+            launch_spmm<double, R, VR>(B, d64, B.val, B.p, B.z, st);  // W shares Z's storage
+            launch_update_xr<R>(B, d64, x, B.r, B.p, B.z, st);
+            if (pst == GP_OK) pst = icc(st);
+            launch_dots<R, false>(B, d64, B.r, B.z, st);
+          },
+          [&](cudaStream_t st) { launch_resid<R, VR>(B, d64, b, x, 0, st); }));
+    GP_TRY(pst);
+    GP_TRY(pc_check(B.icc, s));
+  } else if (o.precision == 0) {
     GP_TRY(run_loop(
           B, 0, s2, b, x, key, o.max_it + 8,
           [&](cudaStream_t st) {
@@ -1281,10 +1401,15 @@ static int solve_shape(Batch& B, const BatchOptions& o, const double* b, double*
 
 int batch_solve(Batch* B, const BatchOptions& o, const double* b, double* x, cudaStream_t s,
                 BatchResult& res) {
-  if (o.pc != 0 && o.pc != 2) {
-    set_error("batched CG: preconditioner must be none (0) or jacobi (2)");
+  if (o.pc != 0 && o.pc != 2 && o.pc != 6) {
+    set_error("batched CG: preconditioner must be none (0), jacobi (2) or icc (6)");
     return GP_ERR_UNSUPPORTED;
   }
+  if (o.pc == 6 && o.precision != 0) {
+    set_error("batched CG: icc(0) runs in the FP64 form (precision 0)");
+    return GP_ERR_UNSUPPORTED;
+  }
+  if (o.pc == 6) GP_TRY(batch_icc_setup(*B, s));
   if (o.max_it < 1 || o.max_outer < 1 || !(o.rtol >= 0.0)) {
     set_error("batched CG: bad tolerances");
     return GP_ERR_ARG;

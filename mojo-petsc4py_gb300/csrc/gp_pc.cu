@@ -80,6 +80,7 @@ __device__ __forceinline__ void sweep_rows(int n, const int* __restrict__ order,
 }
 
 static int sweep_grid() { return num_sms() * 4; }
+static int grid_for(int n) { return std::max(1, std::min((n + 255) / 256, num_sms() * 8)); }
 
 // ------------------------------------------------------------------ Jacobi
 __global__ void k_jacobi_fill(int n, int jtype, int sym, int use_abs, int fix_diag, double scale,
@@ -290,6 +291,91 @@ __global__ void __launch_bounds__(kSweepBlock) k_icc_bwd(
     x[perm_c[i]] = z;
     st_relaxed(&yb[i], z);
   });
+}
+
+// ------------------------------------------------------------------ IC solve, R columns
+// The same two sweeps on R right-hand sides stored row-major (element (row,
+// c) at row * R + c): each row is handed to R lanes of a warp, one column a
+// lane, each waiting on its own column's values.  Every column is folded with
+// exactly the operations of k_icc_fwd / k_icc_bwd.
+template <class RowFn>
+__device__ __forceinline__ void sweep_rows_cols(int R, int n, const int* __restrict__ order,
+                                                unsigned* tickets, RowFn&& fn) {
+  const int lane = threadIdx.x & 31, per = 32 / R;
+  for (;;) {
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(&tickets[0], (unsigned)per);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= (unsigned)n) break;
+    const unsigned k = base + lane / R;
+    if (lane < per * R && k < (unsigned)n) fn(order[k], lane % R);
+    __syncwarp();
+  }
+  if (lane == 0) {
+    const unsigned total = gridDim.x * (blockDim.x / 32);
+    if (atomic_add_acq_rel(&tickets[1], 1u) == total - 1) {
+      tickets[0] = 0u;
+      tickets[1] = 0u;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSweepBlock) k_icc_fwd_cols(
+    int R, int n, const int* __restrict__ order, unsigned* tickets, const int* __restrict__ tptr,
+    const int* __restrict__ trow, const int* __restrict__ tslot, const double* __restrict__ ua,
+    const int* __restrict__ bdiag, const int* __restrict__ perm_c, const double* __restrict__ b,
+    double* yf, double* __restrict__ ys, DevErr* err) {
+  sweep_rows_cols(R, n, order, tickets, [&](int k, int c) {
+    double w = b[(size_t)perm_c[k] * R + c];
+    const int eend = tptr[k + 1];
+    for (int e = tptr[k]; e < eend; e++)
+      w = add(w, mul(ua[tslot[e]], wait_value(&yf[(size_t)trow[e] * R + c], err, 15)));
+    ys[(size_t)k * R + c] = mul(w, ua[bdiag[k]]);
+    st_relaxed(&yf[(size_t)k * R + c], w);
+  });
+}
+
+__global__ void __launch_bounds__(kSweepBlock) k_icc_bwd_cols(
+    int R, int n, const int* __restrict__ order, unsigned* tickets, const int* __restrict__ bi,
+    const int* __restrict__ bj, const double* __restrict__ ua, const int* __restrict__ bdiag,
+    const int* __restrict__ perm_c, const double* __restrict__ ys, double* yb,
+    double* __restrict__ x, DevErr* err) {
+  sweep_rows_cols(R, n, order, tickets, [&](int i, int c) {
+    double z = ys[(size_t)i * R + c];
+    const int jend = bdiag[i];
+    for (int j = bi[i]; j < jend; j++)
+      z = add(z, mul(ua[j], wait_value(&yb[(size_t)bj[j] * R + c], err, 16)));
+    x[(size_t)perm_c[i] * R + c] = z;
+    st_relaxed(&yb[(size_t)i * R + c], z);
+  });
+}
+
+int pc_apply_icc_cols(Pc* pc, int R, const double* x, double* y, double* vf, double* vb,
+                      double* ys, cudaStream_t s) {
+  if (!pc->ready || pc->opt.type != PC_ICC) {
+    set_error("pc_apply_icc_cols: an IC preconditioner that has been set up is needed");
+    return GP_ERR_NOT_SETUP;
+  }
+  if (R < 1 || R > 32 || (32 % R)) {
+    set_error("pc_apply_icc_cols: R must divide 32");
+    return GP_ERR_ARG;
+  }
+  const int n = pc->n;
+  if (n == 0) return GP_OK;
+  if ((int64_t)n * R > INT32_MAX) {
+    set_error("pc_apply_icc_cols: n * R must fit in 32 bits");
+    return GP_ERR_ARG;
+  }
+  k_fill_pending<<<grid_for(n * R), 256, 0, s>>>(nullptr, 0, n * R, vf, vb);
+  const int sg = sweep_grid();
+  k_icc_fwd_cols<<<sg, kSweepBlock, 0, s>>>(R, n, pc->fwd.order, pc->tickets, pc->tptr,
+                                            pc->trow, pc->tslot, pc->ba, pc->bdiag, pc->perm_c,
+                                            x, vf, ys, pc->err);
+  k_icc_bwd_cols<<<sg, kSweepBlock, 0, s>>>(R, n, pc->bwd.order, pc->tickets + 2, pc->bi,
+                                            pc->bj, pc->ba, pc->bdiag, pc->perm_c, ys, vb, y,
+                                            pc->err);
+  GP_CHECK_LAUNCH();
+  return GP_OK;
 }
 
 // ------------------------------------------------------------------ ILU numeric
@@ -895,7 +981,6 @@ int pc_setup(Pc* pc, Csr* A, cudaStream_t s) {
   return GP_OK;
 }
 
-static int grid_for(int n) { return std::max(1, std::min((n + 255) / 256, num_sms() * 8)); }
 
 int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) {
   if (!pc->ready) {

@@ -195,6 +195,11 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate = nullptr, 
 int pc_transpose_prepare(Pc* pc, cudaStream_t s);
 int pc_apply_transpose(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate = nullptr,
                        int want = 0);
+// IC(0)/IC(k) apply to R columns stored row-major (x, y: n * R; vf, vb, ys:
+// n * R scratch), R dividing 32; no gate (not for captured solver loops of
+// the single-vector drivers; the batched CG captures it).
+int pc_apply_icc_cols(Pc* pc, int R, const double* x, double* y, double* vf, double* vb,
+                      double* ys, cudaStream_t s);
 // Jacobi symmetric half; other types fall back to pc_apply.
 int pc_apply_symmetric(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate = nullptr,
                        int want = 0);

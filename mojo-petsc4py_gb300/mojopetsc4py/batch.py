@@ -24,7 +24,7 @@ import numpy as np
 from . import _device as dev
 from ._lib import check, lib
 
-_PC = {"none": 0, "jacobi": 2}
+_PC = {"none": 0, "jacobi": 2, "icc": 6}
 _PREC = {"fp64": 0, "fp32": 1}
 
 
