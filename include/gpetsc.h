@@ -76,6 +76,32 @@ int gp_get_arithmetic(void);
 int gp_device_count(int *count);
 int gp_set_device(int device);
 
+/* ------------------------------------------------------------ memory
+ * Device and page-locked host memory and copies, so a host program needs no
+ * CUDA binding besides this library (the Python package keeps every Vec and
+ * Mat device copy in these blocks).  No counterpart in the reference, whose
+ * vectors live in host numpy arrays (python/mojopetsc4py/PETSc/Vec.py:81-116).
+ *
+ * gp_device_alloc  `bytes` of device memory on the current device, from a
+ *                  stream-ordered pool the library keeps for the process:
+ *                  ordered on `stream` (NULL: the default stream); blocks
+ *                  freed with gp_device_free are reused without a device
+ *                  synchronisation.  bytes == 0 gives NULL.
+ * gp_device_free   returns a block, ordered after the work queued on
+ *                  `stream` (free on the stream that last used it).
+ * gp_host_alloc    page-locked host memory (full-rate copies), recycled by
+ *                  size within the process; gp_host_free returns it.
+ * gp_copy          one cudaMemcpyAsync of `bytes` on `stream`, direction
+ *                  from the pointers (unified addressing); with sync != 0 it
+ *                  then waits for the stream.
+ * gp_stream_synchronize  waits for the work queued on `stream`. */
+int gp_device_alloc(void **ptr, int64_t bytes, void *stream);
+int gp_device_free(void *ptr, void *stream);
+int gp_host_alloc(void **ptr, int64_t bytes);
+int gp_host_free(void *ptr);
+int gp_copy(void *dst, const void *src, int64_t bytes, int sync, void *stream);
+int gp_stream_synchronize(void *stream);
+
 /* ------------------------------------------------------------ Mat */
 typedef struct gp_mat_s *gp_mat;
 

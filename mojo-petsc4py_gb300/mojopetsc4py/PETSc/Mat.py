@@ -133,11 +133,11 @@ class Mat:
                 vals = np.ascontiguousarray(self._data[:nnz], dtype=np.float64)
                 check(lib().gp_mat_set_values(self._gp, vals.ctypes.data if nnz else None, 0,
                                               dev.stream_ptr()))
-                dev.torch().cuda.current_stream().synchronize()
+                dev.synchronize()
                 self._gp_vver = self._vver
             return self._gp
         self._drop_device()
-        dev.torch()  # a CUDA device is required
+        dev.require_device()
         n, nnz = self._nrows, self._nnz_used
         irow = np.ascontiguousarray(self._irow[: n + 1], dtype=np.int64)
         icol = np.ascontiguousarray(self._icol[:nnz], dtype=np.int64)
@@ -151,7 +151,7 @@ class Mat:
         return self._gp
 
     def _values_tensor(self):
-        """Device values as a torch tensor view (shares memory)."""
+        """Device address of the values array (shares memory)."""
         p = ctypes.c_void_p()
         check(lib().gp_mat_values_ptr(self._device(), ctypes.byref(p)))
         return p.value

@@ -87,14 +87,13 @@ class Vec:
         """Device pointer with the device copy current (for reading)."""
         n = self._size()
         if self._d is None:
-            self._d = dev.empty(n)
+            self._d = dev.DeviceArray(n)
             if self._loc == _DEVICE:
                 self._loc = _HOST
         if self._loc == _HOST:
-            if n:
-                self._d.copy_(dev.torch().from_numpy(self._h), non_blocking=False)
+            dev.upload(self._d.ptr, self._h)
             self._loc = _BOTH
-        return dev.ptr(self._d)
+        return self._d.ptr
 
     def _wptr(self) -> int:
         """Device pointer for a kernel that writes: the device side becomes the
@@ -108,21 +107,14 @@ class Vec:
         reading it: no upload needed."""
         n = self._size()
         if self._d is None:
-            self._d = dev.empty(n)
+            self._d = dev.DeviceArray(n)
         self._loc = _DEVICE
-        return dev.ptr(self._d)
+        return self._d.ptr
 
     def _sync_host(self):
         if self._loc == _DEVICE:
-            if len(self._h):
-                dev.torch().cuda.current_stream().synchronize()
-                dev.torch().from_numpy(self._h).copy_(self._d)
+            dev.download(self._h, self._d.ptr)
             self._loc = _BOTH
-
-    def _tensor(self):
-        """The device copy as a torch tensor (current)."""
-        self._dptr()
-        return self._d
 
     # ---------------------------------------------------------- creation
     def create(self, comm=None) -> "Vec":

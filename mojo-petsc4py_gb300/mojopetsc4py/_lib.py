@@ -68,6 +68,12 @@ GP_SIGNATURES = {
     "gp_get_arithmetic": ([], ctypes.c_int),
     "gp_device_count": ([ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     "gp_set_device": ([ctypes.c_int], ctypes.c_int),
+    "gp_device_alloc": ([PP, I64, P], ctypes.c_int),
+    "gp_device_free": ([P, P], ctypes.c_int),
+    "gp_host_alloc": ([PP, I64], ctypes.c_int),
+    "gp_host_free": ([P], ctypes.c_int),
+    "gp_copy": ([P, P, I64, ctypes.c_int, P], ctypes.c_int),
+    "gp_stream_synchronize": ([P], ctypes.c_int),
     "gp_mixed_options_default": ([P], None),
     "gp_mixed_create": ([PP], ctypes.c_int),
     "gp_mixed_destroy": ([P], ctypes.c_int),

@@ -5,8 +5,10 @@ sides each, solved together on the GPU (include/gpetsc.h, gp_batch_*).
     X, info = solver.solve(B, pc="jacobi", precision="fp64", rtol=1e-8)
 
 `B` stacks the systems' right-hand sides row-wise: an (sum n_s, nrhs) FP64
-array (numpy on the host or a CUDA tensor); `X` has the same shape and
-placement.  Each (system, column) pair follows the CG recurrence of
+array, either on the host (anything numpy reads) or on the device (anything
+with __cuda_array_interface__: a CUDA torch tensor, a CuPy array, the
+library's own DeviceArray).  `X` has the same shape: a numpy array for a host
+`B`, a tensor of the same kind for a torch `B`, else a DeviceArray.  Each (system, column) pair follows the CG recurrence of
 KSPSolve_CG (src/ksp.mojo:271-389) with its own stopping test.
 precision="fp32" solves each pair with an FP32 inner CG inside FP64
 iterative refinement until the true FP64 residual meets rtol.
@@ -18,6 +20,7 @@ no collective beyond gathering the results.
 from __future__ import annotations
 
 import ctypes
+import sys
 
 import numpy as np
 
@@ -71,7 +74,7 @@ class BatchedCG:
     def __init__(self, systems, nrhs: int = 16, autotune: bool = True):
         if nrhs not in (1, 2, 4, 8, 16):
             raise ValueError("nrhs must be 1, 2, 4, 8 or 16")
-        torch = dev.torch()
+        dev.require_device()
         self.nrhs = nrhs
         self.sys_rows, indptr, indices, data = stack_systems(systems)
         self.nsys = len(systems)
@@ -82,7 +85,6 @@ class BatchedCG:
                                     data.ctypes.data if len(data) else None, nrhs,
                                     dev.stream_ptr()))
         self._h = h.value
-        self._torch = torch
         if autotune:
             check(lib().gp_batch_autotune(self._h, dev.stream_ptr()))
 
@@ -113,16 +115,34 @@ class BatchedCG:
     def solve(self, B, pc: str = "jacobi", precision: str = "fp64", rtol: float = 1e-8,
               atol: float = 1e-50, divtol: float = 1e4, max_it: int = 10000,
               max_outer: int = 20, inner_rtol: float = 1e-4, out=None):
-        torch = self._torch
         if pc not in _PC or precision not in _PREC:
             raise NotImplementedError(f"batched CG supports pc {sorted(_PC)} and precision "
                                       f"{sorted(_PREC)}")
-        host = not isinstance(B, torch.Tensor)
-        Bt = torch.as_tensor(np.ascontiguousarray(B, dtype=np.float64)) if host else B
-        if tuple(Bt.shape) != (self.n, self.nrhs) or Bt.dtype != torch.float64:
-            raise ValueError(f"B must be float64 of shape ({self.n}, {self.nrhs})")
-        Bd = Bt.to("cuda").contiguous()
-        X = out if out is not None else torch.empty_like(Bd)
+        shape = (self.n, self.nrhs)
+        bad = ValueError(f"B must be float64 of shape ({self.n}, {self.nrhs})")
+        view = dev.device_view(B)
+        host = view is None
+        if host:
+            Bh = np.ascontiguousarray(B, dtype=np.float64)
+            if Bh.shape != shape:
+                raise bad
+            Bd = dev.from_host(Bh)
+            bp = Bd.ptr
+        else:
+            bp, bshape, bdtype = view
+            if bshape != shape or bdtype != np.float64:
+                raise bad
+        if out is not None:
+            X = out
+            oview = dev.device_view(out)
+            if oview is None or oview[1] != shape or oview[2] != np.float64:
+                raise ValueError("out must be a float64 device array of B's shape")
+            xp = oview[0]
+        else:
+            X = dev.DeviceArray(shape)
+            xp = X.ptr
+            if not host and type(B).__module__.split(".")[0] == "torch":
+                X = sys.modules["torch"].as_tensor(X, device=B.device)
         o = BatchOptions()
         lib().gp_batch_options_default(ctypes.byref(o))
         o.pc_type, o.precision = _PC[pc], _PREC[precision]
@@ -133,13 +153,15 @@ class BatchedCG:
         reason = np.zeros(npairs, dtype=np.int32)
         relres = np.zeros(npairs, dtype=np.float64)
         passes = ctypes.c_int32()
-        check(lib().gp_batch_solve_cg(self._h, ctypes.byref(o), dev.ptr(Bd), dev.ptr(X),
+        check(lib().gp_batch_solve_cg(self._h, ctypes.byref(o), bp, xp,
                                       its.ctypes.data, reason.ctypes.data, relres.ctypes.data,
                                       ctypes.byref(passes), dev.stream_ptr()))
-        shape = (self.nsys, self.nrhs)
-        info = {"its": its.reshape(shape), "reason": reason.reshape(shape),
-                "relres": relres.reshape(shape), "passes": passes.value}
-        return (X.cpu().numpy() if host else X), info
+        pshape = (self.nsys, self.nrhs)
+        info = {"its": its.reshape(pshape), "reason": reason.reshape(pshape),
+                "relres": relres.reshape(pshape), "passes": passes.value}
+        if host and out is None:
+            return X.to_host(), info
+        return X, info
 
 
 def assemble_shards(shards, parts, sizes, nrhs: int):
