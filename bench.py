@@ -480,7 +480,9 @@ def run_ours(args, world, rank, local, pg):
                      "algorithmic_bytes": algo, "launch_us": round(t_spmv * 1e6, 2),
                      "peak_kind": f"{peak_kind} hbm_gbs"},
         "cpu_baseline": cpu,
-        "gpu_launches": int(args.steps * (top + trips * body)),
+        # counted from the captured graph; None when the loop is host-driven
+        # (GPETSC_KSP_GRAPH=0, profiling runs)
+        "gpu_launches": int(args.steps * (top + trips * body)) if top >= 0 else None,
         "clocks": clocks,
         "methods": methods,
         "forms": forms,

@@ -271,11 +271,34 @@ __global__ void __launch_bounds__(kRedBlock) k_mdot(const int* gate, int want, i
       for (int q = 0; q < 8; q++)
         if (q < jn) v[q] = madd<FMA>(a, basis[(size_t)(j0 + q) * n + i], v[q]);
     }
+    // warp sums of the 8 values by halving exchanges: at offset 16 a lane
+    // keeps the half of the values its lane bit selects and adds its
+    // partner's copy of that half (4 adds), then 2 at offset 8, 1 at offset
+    // 4, and a plain pair of steps at 2 and 1 -- 9 FP64 adds a lane instead
+    // of 8 shuffle trees of 5; lane 4 q' ends with value q' = the bits
+    // (lane >> 2) read high to low.
+    {
+      const bool h4 = lane & 16, h3 = lane & 8, h2 = lane & 4;
+      double u4[4], u2[2];
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
+      for (int q = 0; q < 4; q++) {
+        const double keep = h4 ? v[q + 4] : v[q], send = h4 ? v[q] : v[q + 4];
+        u4[q] = add(keep, __shfl_xor_sync(0xffffffffu, send, 16));
+      }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v[q] = add(v[q], __shfl_down_sync(0xffffffffu, v[q], o));
-      if (lane == 0 && q < jn) sh[wid][j0 + q] = v[q];
+      for (int q = 0; q < 2; q++) {
+        const double keep = h3 ? u4[q + 2] : u4[q], send = h3 ? u4[q] : u4[q + 2];
+        u2[q] = add(keep, __shfl_xor_sync(0xffffffffu, send, 8));
+      }
+      double t;
+      {
+        const double keep = h2 ? u2[1] : u2[0], send = h2 ? u2[0] : u2[1];
+        t = add(keep, __shfl_xor_sync(0xffffffffu, send, 4));
+      }
+      t = add(t, __shfl_xor_sync(0xffffffffu, t, 2));
+      t = add(t, __shfl_xor_sync(0xffffffffu, t, 1));
+      const int q = (h4 ? 4 : 0) + (h3 ? 2 : 0) + (h2 ? 1 : 0);
+      if ((lane & 3) == 0 && q < jn) sh[wid][j0 + q] = t;
     }
   }
   __syncthreads();
@@ -524,6 +547,9 @@ __global__ void k_cgf_p(KspState* st, int n, double* __restrict__ p,
   pdl_wait();
   if (st->active != 1) return;
   const double bc = st->bcoef;
+  // VecAYPX's branches (src/ported.mojo:285-294): a copy at i = 0.  Decided
+  // once per thread: an FP64 compare per element costs FP64 issue slots.
+  const int br = bc == 0.0 ? 0 : bc == 1.0 ? 1 : 2;
   for (unsigned j0 = i0; j0 < un; j0 += U * stride) {
 #pragma unroll
     for (int u = 0; u < U; u++) {
@@ -537,10 +563,9 @@ __global__ void k_cgf_p(KspState* st, int n, double* __restrict__ p,
     for (int u = 0; u < U; u++) {
       const unsigned i = j0 + u * stride;
       if (i >= un) continue;
-      // VecAYPX's branches (src/ported.mojo:285-294): a copy at i = 0
-      if (bc == 0.0)
+      if (br == 0)
         p[i] = zv[u];
-      else if (bc == 1.0)
+      else if (br == 1)
         p[i] = madd<FMA>(bc, zv[u], pv[u]);
       else
         p[i] = madd<FMA>(bc, pv[u], zv[u]);
