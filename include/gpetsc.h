@@ -241,9 +241,10 @@ int gp_wait_probe(int32_t spins, int32_t set, void *stream);
  * sequential host loops). */
 int gp_set_sweep_form(int32_t tiles, int32_t tile_rows);
 /* Which form a set-up PC's sweeps got: for the forward (which = 0) and the
- * backward (which = 1) sweep, tiled (0/1), rows per chunk and chunks (0 when
- * not tiled), and the number of dependency levels.  No counterpart in the
- * reference. */
+ * backward (which = 1) sweep, and the two sweeps of the transposed apply
+ * (2: U^T, 3: L^T; reported once a transposed apply has prepared them),
+ * tiled (0/1), rows per chunk and chunks (0 when not tiled).  No counterpart
+ * in the reference. */
 int gp_pc_sweep_form(gp_pc pc, int32_t which, int32_t *tiled, int32_t *rows_per_chunk,
                      int32_t *chunks);
 /* Brick form of the sweeps of later set-ups, for sweeps whose dependencies are

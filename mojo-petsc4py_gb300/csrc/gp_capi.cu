@@ -287,9 +287,10 @@ int gp_pc_sweep_bricks(gp_pc pc, int32_t which, int32_t* brick, int32_t* dims) {
 
 int gp_pc_sweep_form(gp_pc pc, int32_t which, int32_t* tiled, int32_t* rows_per_chunk,
                      int32_t* chunks) {
-  if (!pc || !tiled || !rows_per_chunk || !chunks || (which != 0 && which != 1))
-    return bad("gp_pc_sweep_form: null argument or which not 0/1");
-  const gp::EllSweep& e = which == 0 ? pc->pc->ef : pc->pc->eb;
+  if (!pc || !tiled || !rows_per_chunk || !chunks || which < 0 || which > 3)
+    return bad("gp_pc_sweep_form: null argument or which not 0..3");
+  const gp::Pc* p = pc->pc;
+  const gp::EllSweep& e = which == 0 ? p->ef : which == 1 ? p->eb : which == 2 ? p->etf : p->etb;
   *tiled = e.tiled ? 1 : 0;
   *rows_per_chunk = e.tiled ? e.rows_per_chunk : 0;
   *chunks = e.tiled ? e.nchunks : 0;

@@ -1128,8 +1128,8 @@ int pc_transpose_prepare(Pc* pc, cudaStream_t s) {
   int nlev = 0;
   level_order(n, up, uc, true, of, &nlev);
   level_order(n, lp, lc, false, ob, &nlev);
-  GP_TRY(ell_build_levels(pc->etf, ELL_ILU_B, n, true, of, up, uc, us, perm_c, none, dsl, &fpos));
-  GP_TRY(ell_build_levels(pc->etb, ELL_ILU_F, n, false, ob, lp, lc, ls, fpos, P.r, none, nullptr));
+  GP_TRY(ell_build_chunked(pc->etf, ELL_ILU_B, n, true, of, up, uc, us, perm_c, none, dsl, &fpos));
+  GP_TRY(ell_build_chunked(pc->etb, ELL_ILU_F, n, false, ob, lp, lc, ls, fpos, P.r, none, nullptr));
   if (!pc->etf.ok || !pc->etb.ok) {
     ell_free(pc->etf);
     ell_free(pc->etb);

@@ -100,6 +100,13 @@ int ell_build(EllSweep& e, int mode, int n, bool forward, const std::vector<int>
               const std::vector<int>& out_row, const std::vector<int>& dslot_row,
               std::vector<int>* pos_of_row);
 int ell_refresh(EllSweep& e, const double* src, cudaStream_t s);
+// ell_build choosing between the level-ordered and the chunked form only (no
+// brick layout: its kernel reads the reference's inputs of each mode only).
+int ell_build_chunked(EllSweep& e, int mode, int n, bool forward, const std::vector<int>& order,
+                      const std::vector<int>& dptr, const std::vector<int>& dcol,
+                      const std::vector<int>& dsl, const std::vector<int>& in_row,
+                      const std::vector<int>& out_row, const std::vector<int>& dslot_row,
+                      std::vector<int>* pos_of_row);
 // ell_build in the level-ordered form only (no chunked or brick layout).
 int ell_build_levels(EllSweep& e, int mode, int n, bool forward, const std::vector<int>& order,
                      const std::vector<int>& dptr, const std::vector<int>& dcol,

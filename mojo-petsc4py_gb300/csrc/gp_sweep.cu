@@ -419,12 +419,13 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_sweep(const int* gate,
         }
       }
       if constexpr (MODE == ELL_ILU_F) {
-        s_sum[r] = in[iidx[r]];
+        // from an earlier sweep's values when given (the transposed apply)
+        s_sum[r] = (a.fval ? a.fval : in)[iidx[r]];
       } else if constexpr (MODE == ELL_ICC_F) {
         s_sum[r] = in[iidx[r]];
         s_dv[r] = t.coefsrc[gidx[r]];
       } else if constexpr (MODE == ELL_ILU_B) {
-        s_sum[r] = a.fval[iidx[r]];
+        s_sum[r] = (a.fval ? a.fval : in)[iidx[r]];
         s_dv[r] = t.coefsrc[gidx[r]];
       } else if constexpr (MODE == ELL_ICC_B) {
         s_sum[r] = a.auxin[iidx[r]];
@@ -512,9 +513,10 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_sweep(const int* gate,
           double res;
           if constexpr (MODE == ELL_ILU_F) {
             res = sum;
+            if (a.write_out) out[oidx[r]] = res;
           } else if constexpr (MODE == ELL_ILU_B) {
             res = mul(sum, s_dv[r]);
-            out[oidx[r]] = res;
+            if (a.write_out) out[oidx[r]] = res;
           } else if constexpr (MODE == ELL_ICC_F) {
             a.aux[p] = mul(sum, s_dv[r]);
             res = sum;
@@ -912,7 +914,8 @@ static int ell_build_impl(EllSweep& e, int mode, int n, bool forward,
                           const std::vector<int>& dptr, const std::vector<int>& dcol,
                           const std::vector<int>& dsl, const std::vector<int>& in_row,
                           const std::vector<int>& out_row, const std::vector<int>& dslot_row,
-                          std::vector<int>* pos_of_row, bool allow_tiles) {
+                          std::vector<int>* pos_of_row, bool allow_tiles,
+                          bool allow_bricks = true) {
   ell_free(e);
   int W = 0;
   for (int i = 0; i < n; i++) W = std::max(W, dptr[i + 1] - dptr[i]);
@@ -927,7 +930,7 @@ static int ell_build_impl(EllSweep& e, int mode, int n, bool forward,
     nlev = sweep_levels(n, dptr, dcol, forward);
     tiled = tile_choose(mode, n, W, dptr, dcol, forward, nlev, tu, tp, &considered);
   }
-  if (allow_tiles && n > 0) {
+  if (allow_tiles && allow_bricks && n > 0) {
     // the brick form, where the sweep is a grid in natural order and the
     // model puts it below the better of the other two forms
     if (!nlev) nlev = sweep_levels(n, dptr, dcol, forward);
@@ -1011,6 +1014,15 @@ int ell_build(EllSweep& e, int mode, int n, bool forward, const std::vector<int>
               std::vector<int>* pos_of_row) {
   return ell_build_impl(e, mode, n, forward, order, dptr, dcol, dsl, in_row, out_row,
                         dslot_row, pos_of_row, true);
+}
+
+int ell_build_chunked(EllSweep& e, int mode, int n, bool forward, const std::vector<int>& order,
+                      const std::vector<int>& dptr, const std::vector<int>& dcol,
+                      const std::vector<int>& dsl, const std::vector<int>& in_row,
+                      const std::vector<int>& out_row, const std::vector<int>& dslot_row,
+                      std::vector<int>* pos_of_row) {
+  return ell_build_impl(e, mode, n, forward, order, dptr, dcol, dsl, in_row, out_row,
+                        dslot_row, pos_of_row, true, false);
 }
 
 int ell_build_levels(EllSweep& e, int mode, int n, bool forward, const std::vector<int>& order,

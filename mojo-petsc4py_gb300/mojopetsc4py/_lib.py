@@ -220,11 +220,13 @@ def sweep_bricks(pc_handle) -> dict:
     return out
 
 
-def sweep_form(pc_handle) -> dict:
+def sweep_form(pc_handle, transposed: bool = False) -> dict:
     """The sweep layout a set-up PC got: per sweep, tiled or not, rows per
-    chunk and chunk count."""
+    chunk and chunk count (with `transposed`, the two sweeps of the transposed
+    ILU apply, U^T then L^T)."""
     out = {}
-    for which, name in ((0, "forward"), (1, "backward")):
+    names = ((2, "first"), (3, "second")) if transposed else ((0, "forward"), (1, "backward"))
+    for which, name in names:
         t, r, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
         check(lib().gp_pc_sweep_form(pc_handle, which, ctypes.byref(t), ctypes.byref(r),
                                      ctypes.byref(c)))

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from helpers import dense_to_csr, nonsym_banded
-from mojopetsc4py import PETSc, gallery
+from mojopetsc4py import PETSc, _lib, gallery
 from mojopetsc4py._lib import GPError
 
 pytestmark = pytest.mark.gpu
@@ -134,3 +134,43 @@ def test_solve_transpose_solves_the_transposed_system(kt, pt):
     x = PETSc.Vec().createSeq(n)
     ksp.solve(PETSc.Vec().createWithArray(b), x)
     assert np.linalg.norm(b - dense @ x.getArray()) <= 1e-9 * np.linalg.norm(b)
+
+
+FORMS = [("level-order", False, 0), ("chosen", True, 0), ("chunks-64", True, 64),
+         ("chunks-333", True, 333)]
+
+
+@pytest.fixture
+def _restore_form():
+    yield
+    _lib.set_sweep_form(True, 0)
+
+
+@pytest.mark.usefixtures("_restore_form")
+@pytest.mark.parametrize("opts", ILU_OPTS, ids=["ilu0", "ilu1", "ilu0-rcm"])
+def test_transposed_apply_is_the_same_in_every_sweep_form(opts):
+    """The transposed sweeps (U^T, then L^T) take the chunked form where the
+    set-up's schedule model prefers it, like the plain ones; every form gives
+    the same bits."""
+    kappa = np.exp(gallery.gaussian_random_field(24, np.random.default_rng(3), corr=6.0))
+    ip, ix, v = gallery.advection_diffusion_2d(kappa, peclet=2.0)
+    n = len(ip) - 1
+    x = np.random.default_rng(8).normal(size=n)
+    got = {}
+    for name, tiles, rows in FORMS:
+        _lib.set_sweep_form(tiles, rows)
+        pc = _pc("ilu", _mat(ip, ix, v), **opts)
+        got[name] = _apply(pc.applyTranspose, x)
+        form = _lib.sweep_form(pc._handle(), transposed=True)
+        if rows:
+            assert form["first"]["tiled"] and form["second"]["tiled"], form
+        if not tiles:
+            assert not form["first"]["tiled"] and not form["second"]["tiled"], form
+    for name in got:
+        np.testing.assert_array_equal(got[name], got["level-order"], err_msg=name)
+    # and it is still the transpose of the plain apply
+    z = np.random.default_rng(9).normal(size=n)
+    pc = _pc("ilu", _mat(ip, ix, v), **opts)
+    lhs = got["chosen"] @ z
+    rhs = x @ _apply(pc.apply, z)
+    assert abs(lhs - rhs) <= 1e-12 * (abs(lhs) + abs(rhs))
