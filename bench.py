@@ -427,6 +427,26 @@ def run_ours(args, world, rank, local, pg):
             methods[name] = {"ms": round(m2, 3), "its": k2.getIterationNumber(),
                              "reason": k2.getConvergedReason(),
                              "pc_setup_ms": round(setup_ms, 2)}
+        # the headline solve in the two other arithmetics: exact (rounded
+        # products and sums, parallel tree reductions) and ordered (the
+        # reference's blocked reduction order: a checking form whose iterate
+        # is compared with the oracle's bit for bit below)
+        from mojopetsc4py import _lib as gplib
+
+        other = {}
+        for mode, reps in (("exact", 3), ("ordered", 1)):
+            gplib.set_arithmetic(mode)
+            try:
+                k3 = build_solver(PETSc, A, "cg", "jacobi")
+                x3 = PETSc.Vec().createSeq(n)
+                k3.solve(bv, x3)  # capture
+                m3 = time_solves(torch, k3, bv, x3, reps)
+                other[mode] = {"ms": round(m3, 3), "its": k3.getIterationNumber(),
+                               "reason": k3.getConvergedReason(),
+                               "x": x3.getArray().copy()}
+            finally:
+                gplib.set_arithmetic("fma")
+        methods["cg+jacobi"]["other_arithmetics"] = other
 
     # ---- the three further forms on their own workloads (N = 1)
     forms = None
@@ -454,6 +474,16 @@ def run_ours(args, world, rank, local, pg):
         cpu = {"value": round(dt * 1e3, 3), "unit": "ms", "cores": 1, "kind": "port",
                "sample": f"one whole {rc['its']}-iteration CG+Jacobi solve of the same system "
                          "on this host", **cpu_info()}
+        # parity of the timed solves against the oracle's, same inputs
+        rx = np.asarray(rc["x"])
+        methods["cg+jacobi"]["vs_oracle"] = {
+            "oracle_its": int(rc["its"]), "oracle_reason": int(rc["reason"]),
+            "fma_rel_diff": float(np.linalg.norm(xh - rx) / np.linalg.norm(rx))}
+        for mode, r in methods["cg+jacobi"].get("other_arithmetics", {}).items():
+            r["rel_diff_vs_oracle"] = float(np.linalg.norm(r["x"] - rx) / np.linalg.norm(rx))
+            r["bit_identical_to_oracle"] = bool(np.array_equal(r["x"], rx))
+    for r in methods["cg+jacobi"].get("other_arithmetics", {}).values():
+        r.pop("x", None)
 
     if rank != 0:
         return
