@@ -73,6 +73,10 @@ constexpr int kRedBlock = 256;     // block for reductions
 constexpr int kMaxRedGrid = 2048;  // partials buffer size per reduction slot
 
 int num_sms();  // cached SM count of the current device
+// A process-wide unique, increasing id (never 0): cached graphs key on the ids
+// of the objects they were captured from, never on host addresses, which the
+// allocator hands out again after a free.
+unsigned long long next_uid();
 
 // Arithmetic of the bandwidth-bound kernels (SpMV, Vec maps, reductions,
 // solver updates).  kExact: every `a*x + y` is a rounded multiply then a

@@ -79,6 +79,8 @@ struct Csr {
   std::vector<int> h_rowptr, h_colind;
   bool owns = true;
   int device = -1;
+  unsigned long long uid = 0;   // next_uid() at creation
+  unsigned long long vver = 0;  // bumped whenever the values change
 };
 
 int csr_create(Csr** out, int64_t nrows, int64_t ncols, int64_t nnz, const int64_t* h_rowptr,

@@ -1974,21 +1974,27 @@ int ksp_solve(Ksp* k, Csr* A, Pc* pc, const double* b, double* x, KspResult* res
     GP_TRY(spmv_t_prepare(s, A));
     GP_TRY(pc_transpose_prepare(pc, s));
   }
+  GP_TRY(pc_values_sync(pc, s));
   Run r{k, A, pc, n, s};
-  // the solve graph depends on the buffers and on every option that shapes it
-  const int key[13] = {o.type,      o.normtype,    o.pc_side,          o.restart,
-                       o.cgstype,   n,             pc->opt.type,       pc->opt.sor_flag,
-                       o.guess_zero, pc->generation, arith_mode(),    o.orthog,
+  // the solve graph depends on the buffers and on every option that shapes
+  // it; the operator and the PC set-up by their unique ids (an address can
+  // come back from the allocator for a new object)
+  const int key[13] = {o.type,      o.normtype,    o.pc_side,    o.restart,
+                       o.cgstype,   n,             pc->opt.type, pc->opt.sor_flag,
+                       o.guess_zero, 0,            arith_mode(), o.orthog,
                        k->transpose};
   if (k->launch_form == 1 || (k->launch_form < 0 && eager_mode())) {
     GP_TRY(run_eager(r, b, x));
   } else {
   const bool same = !moved && k->exec && k->cap_A == A && k->cap_pc == pc &&
+                    k->cap_A_uid == A->uid && k->cap_pc_gen == pc->generation &&
                     std::equal(key, key + 13, k->cap_key) && k->cap_b == b && k->cap_x == x;
   if (!same) {
     GP_TRY(capture(r, b, x));
     k->cap_A = A;
     k->cap_pc = pc;
+    k->cap_A_uid = A->uid;
+    k->cap_pc_gen = pc->generation;
     k->cap_b = b;
     k->cap_x = x;
     std::copy(key, key + 13, k->cap_key);

@@ -83,6 +83,8 @@ struct Ksp {
   // what the graph was captured for
   const void* cap_A = nullptr;
   const void* cap_pc = nullptr;
+  unsigned long long cap_A_uid = 0;  // Csr::uid of the captured operator
+  unsigned long long cap_pc_gen = 0;  // Pc::generation of the captured PC
   const void* cap_b = nullptr;
   const void* cap_x = nullptr;
   int cap_key[13] = {0};

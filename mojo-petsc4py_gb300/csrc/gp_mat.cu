@@ -126,6 +126,7 @@ int csr_create(Csr** out, int64_t nrows, int64_t ncols, int64_t nnz, const int64
     return st;
   }
   GP_CUDA(cudaGetDevice(&A->device));
+  A->uid = next_uid();
   *out = A;
   return GP_OK;
 }
@@ -147,6 +148,7 @@ int csr_create_i32(Csr** out, int64_t nrows, int64_t ncols, int64_t nnz,
     return st;
   }
   GP_CUDA(cudaGetDevice(&A->device));
+  A->uid = next_uid();
   *out = A;
   return GP_OK;
 }
@@ -160,6 +162,7 @@ int csr_set_values(Csr* A, const double* val, int on_device, cudaStream_t s) {
                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
   A->val32_stale = true;  // converted again, in place, by the next csr_make_val32
   A->t_val_stale = true;  // gathered again by the next transpose multiply
+  A->vver += 1;
   return GP_OK;
 }
 
@@ -247,6 +250,7 @@ int csr_transpose_values(Csr* A, Csr* T, cudaStream_t s) {
   }
   T->val32_stale = true;
   T->t_val_stale = true;
+  T->vver += 1;
   return GP_OK;
 }
 

@@ -420,11 +420,13 @@ struct Mixed {
   int n = 0, m = 0, device = -1;
   BlockTri bl, bu;       // block layouts of L and U (tri_block != 0)
   int bt_rows = 0;       // their block length (0: not built)
-  int bt_generation = -1, bt_epoch = -1;
+  unsigned long long bt_generation = 0;
+  int bt_epoch = -1;
   bool ident_r = false, ident_c = false;  // factor row / solution permutations are identities
   const Csr* A = nullptr;
   const Pc* pc = nullptr;
-  int pc_generation = -1, pc_epoch = -1;
+  unsigned long long pc_generation = 0;
+  int pc_epoch = -1;
   // FP32 factor triangles (CSR) and permutations
   int *lrp = nullptr, *lci = nullptr, *lslot = nullptr;
   int *urp = nullptr, *uci = nullptr, *uslot = nullptr, *dslot = nullptr;
@@ -451,6 +453,7 @@ struct Mixed {
   cudaGraphExec_t exec = nullptr;
   const void* cap_key[6] = {};
   int cap_ikey[5] = {};
+  unsigned long long cap_A_uid = 0, cap_pc_gen = 0;
 };
 
 static void mixed_free(Mixed* M) {
@@ -1537,9 +1540,12 @@ int mixed_solve_graph(Mixed* M, Csr* A, Pc* pc, const double* b, double* x,
   GP_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
   const void* key[6] = {A, pc, b, x, pc->ba, A->val32};
   const int bt = (o.tri_sweeps > 0 && o.tri_block != 0) ? M->bt_rows : 0;
-  const int ikey[5] = {n, m, o.tri_sweeps, pc->generation, bt};
+  const int ikey[5] = {n, m, o.tri_sweeps, 0, bt};
+  // the operator and the PC set-up by their unique ids as well as their
+  // addresses (an address can come back from the allocator)
   const bool same = M->exec && std::equal(key, key + 6, M->cap_key) &&
-                    std::equal(ikey, ikey + 5, M->cap_ikey);
+                    std::equal(ikey, ikey + 5, M->cap_ikey) && M->cap_A_uid == A->uid &&
+                    M->cap_pc_gen == pc->generation;
   if (!same) {
     if (M->exec) cudaGraphExecDestroy(M->exec);
     if (M->graph) cudaGraphDestroy(M->graph);
@@ -1561,6 +1567,8 @@ int mixed_solve_graph(Mixed* M, Csr* A, Pc* pc, const double* b, double* x,
     GP_CUDA(cudaGraphInstantiate(&M->exec, gph, 0));
     std::copy(key, key + 6, M->cap_key);
     std::copy(ikey, ikey + 5, M->cap_ikey);
+    M->cap_A_uid = A->uid;
+    M->cap_pc_gen = pc->generation;
   }
   res = MixedResult();
   for (int pass = 0; pass <= o.max_outer; pass++) {

@@ -138,10 +138,28 @@ __global__ void k_copy_g(const int* gate, int want, int n, DRef xr, DRef yr) {
 }
 
 // ------------------------------------------------------------------ SOR
+__global__ void k_clear_word(const int* gate, int want, int* w) {
+  if (gated_off(gate, want)) return;
+  *w = 0;
+}
+
+static bool stream_capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &st) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return st != cudaStreamCaptureStatusNone;
+}
+
+// With `stale` given, runs only while *stale is nonzero (A's values changed
+// since the last run): the result depends on the values alone.
 __global__ void k_sor_diag(int n, double omega, double fshift, const int* __restrict__ diagpos,
                            const double* __restrict__ val, double* __restrict__ idiag,
-                           double* __restrict__ mdiag, const int* gate = nullptr, int want = 0) {
+                           double* __restrict__ mdiag, const int* gate = nullptr, int want = 0,
+                           const int* stale = nullptr) {
   if (gated_off(gate, want)) return;
+  if (stale && *stale == 0) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double a = val[diagpos[i]];
@@ -149,11 +167,13 @@ __global__ void k_sor_diag(int n, double omega, double fshift, const int* __rest
   idiag[i] = (omega == 1.0 && fshift <= 0.0) ? div_(1.0, a) : div_(omega, add(fshift, a));
 }
 
-// SOR's ELL coefficients follow A's current values (gathered each apply)
+// SOR's ELL coefficients follow A's current values (gathered by an apply
+// while *stale is nonzero)
 __global__ void k_ell_refresh_g(const int* gate, int want, int n, const int* __restrict__ cnt,
                                 const int* __restrict__ cslot, const double* __restrict__ src,
-                                double* __restrict__ coef) {
+                                double* __restrict__ coef, const int* stale) {
   if (gated_off(gate, want)) return;
+  if (*stale == 0) return;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
     const int c = cnt[p];
     for (int e = 0; e < c; e++) {
@@ -512,7 +532,7 @@ static void free_all(Pc* pc) {
                   pc->perm_r, pc->perm_c, pc->perm_ic, pc->ba, pc->ba_orig, pc->done, pc->cptr, pc->crow,
                   pc->cslot, pc->tptr, pc->trow, pc->tslot, pc->amap, pc->fwd.order,
                   pc->bwd.order, pc->num.order, pc->yf, pc->yb, pc->ys, pc->t, pc->tickets,
-                  pc->err, pc->upd_ptr, pc->upd_dst, pc->upd_src};
+                  pc->err, pc->upd_ptr, pc->upd_dst, pc->upd_src, pc->sor_stale};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   ell_free(pc->ef);
@@ -608,6 +628,9 @@ static int setup_sor(Pc* pc, cudaStream_t s) {
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
   GP_TRY(ell_build(pc->ef, ELL_SOR_F, n, true, of, lp, lc, ls, none, none, none, &fpos));
   GP_TRY(ell_build(pc->eb, ELL_SOR_B, n, false, ob, up, uc, us, fpos, none, none, nullptr));
+  GP_CUDA(cudaMalloc(&pc->sor_stale, sizeof(int)));
+  GP_CUDA(cudaMemsetAsync(pc->sor_stale, 1, sizeof(int), s));  // nonzero: recompute
+  pc->sor_vver = A->vver;
   if (n) {
     k_sor_diag<<<(n + 255) / 256, 256, 0, s>>>(n, pc->opt.omega, pc->opt.fshift, A->diagpos,
                                                 A->val, pc->idiag, pc->mdiag);
@@ -931,13 +954,27 @@ int pc_update_values(Pc* pc, cudaStream_t s) {
       return GP_OK;
     case PC_ILU:
     case PC_ICC: return pc_factor_numeric(pc, s);
-    default: return GP_OK;  // none; SOR reads A's values on every apply
+    case PC_SOR:
+      // recomputed from the values by the next apply
+      GP_CUDA(cudaMemsetAsync(pc->sor_stale, 1, sizeof(int), s));
+      pc->sor_vver = A->vver;
+      return GP_OK;
+    default: return GP_OK;  // none
   }
+}
+
+int pc_values_sync(Pc* pc, cudaStream_t s) {
+  if (pc->opt.type != PC_SOR || !pc->ready || !pc->A || !pc->sor_stale) return GP_OK;
+  if (pc->A->vver != pc->sor_vver) {
+    GP_CUDA(cudaMemsetAsync(pc->sor_stale, 1, sizeof(int), s));
+    pc->sor_vver = pc->A->vver;
+  }
+  return GP_OK;
 }
 
 int pc_setup(Pc* pc, Csr* A, cudaStream_t s) {
   free_all(pc);
-  pc->generation += 1;
+  pc->generation = next_uid();
   pc->A = A;
   pc->n = A->n;
   GP_CUDA(cudaGetDevice(&pc->device));
@@ -1003,18 +1040,25 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
       const Csr* A = pc->A;
       const int flag = pc->opt.sor_flag;
       const bool fw = flag & kSorForward, bw = flag & kSorBackward;
-      // MatInvertDiagonalForSOR_SeqAIJ runs on every apply, from the current
-      // values, as in the reference
+      // The reference runs MatInvertDiagonalForSOR_SeqAIJ on every apply, from
+      // the current values (src/ported.mojo:610-633).  The inverted diagonal
+      // and the sweeps' coefficients are functions of the values alone, so
+      // they are recomputed only while the device word sor_stale is set: by
+      // set-up, and before a launch when A's values changed since
+      // (pc_values_sync; a captured solve calls it before every launch).
+      if (!stream_capturing(s)) GP_TRY(pc_values_sync(pc, s));
       k_sor_diag<<<(n + 255) / 256, 256, 0, s>>>(n, pc->opt.omega, pc->opt.fshift, A->diagpos,
-                                                  A->val, pc->idiag, pc->mdiag, gate, want);
+                                                  A->val, pc->idiag, pc->mdiag, gate, want,
+                                                  pc->sor_stale);
       k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
       if (pc->ef.ok && pc->eb.ok) {
         if (!pc->ef.tiled)
           k_ell_refresh_g<<<g, 256, 0, s>>>(gate, want, pc->ef.n, pc->ef.cnt, pc->ef.cslot,
-                                            A->val, pc->ef.coef);
+                                            A->val, pc->ef.coef, pc->sor_stale);
         if (!pc->eb.tiled)
           k_ell_refresh_g<<<g, 256, 0, s>>>(gate, want, pc->eb.n, pc->eb.cnt, pc->eb.cslot,
-                                            A->val, pc->eb.coef);
+                                            A->val, pc->eb.coef, pc->sor_stale);
+        k_clear_word<<<1, 1, 0, s>>>(gate, want, pc->sor_stale);
         if (fw)
           GP_TRY(ell_sweep(ELL_SOR_F, pc->ef, gate, want, x, y, pc->yf, nullptr, pc->t, nullptr,
                            pc->idiag, pc->opt.omega, 0, bw ? 0 : 1, tk0, pc->err, A->val, s));
@@ -1023,6 +1067,7 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
                            pc->idiag, pc->opt.omega, fw ? 1 : 0, 1, tk1, pc->err, A->val, s));
         break;
       }
+      k_clear_word<<<1, 1, 0, s>>>(gate, want, pc->sor_stale);
       if (fw)
         k_sor_fwd<<<sg, kSweepBlock, 0, s>>>(gate, want, n, pc->fwd.order, tk0, A->rowptr,
                                              A->colind, A->val, A->diagpos, pc->idiag, x, pc->t,
@@ -1188,6 +1233,7 @@ int pc_apply_symmetric(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, 
 int pc_import_factor(Pc* pc, int type, const FactorPattern& pat, const std::vector<int>& perm_c,
                      const double* ba_host, Csr* A, cudaStream_t s) {
   free_all(pc);
+  pc->generation = next_uid();
   pc->opt.type = type;
   pc->n = (int)pat.bi.size() - 1;
   pc->A = A;
@@ -1221,6 +1267,7 @@ int pc_import_factor(Pc* pc, int type, const FactorPattern& pat, const std::vect
 // Jacobi with its diagonals given (the reference's pci block carries them).
 int pc_import_jacobi(Pc* pc, int n, const double* diag, const double* diagsqrt, cudaStream_t s) {
   free_all(pc);
+  pc->generation = next_uid();
   pc->opt.type = PC_JACOBI;
   pc->n = n;
   GP_CUDA(cudaGetDevice(&pc->device));

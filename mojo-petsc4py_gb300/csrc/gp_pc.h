@@ -140,7 +140,9 @@ struct Pc {
   int device = -1;
   bool ready = false;
   int epoch = 0;
-  int generation = 0;   // bumped by every set-up (device arrays reallocated)
+  // a fresh next_uid() at every set-up (device arrays reallocated): cached
+  // solve graphs compare it, never the PC's address
+  unsigned long long generation = 0;
 
   // Jacobi
   double* diag = nullptr;
@@ -149,6 +151,11 @@ struct Pc {
   // SOR (uses A's arrays and diagpos)
   double* idiag = nullptr;
   double* mdiag = nullptr;
+  // SOR: nonzero while the inverted diagonal and the sweeps' coefficients
+  // must be recomputed from A's values (device word, read by the apply's
+  // kernels); sor_vver is the A->vver they were last marked for
+  int* sor_stale = nullptr;
+  unsigned long long sor_vver = 0;
 
   // factor (ILU / IC), reference layout on the device
   FactorPattern pat;
@@ -217,6 +224,10 @@ int pc_factor_numeric(Pc* pc, cudaStream_t s);
 // Same operator pattern, new values: redo only the numeric phase (factor
 // values, Jacobi diagonals) in the arrays of the last set-up.
 int pc_update_values(Pc* pc, cudaStream_t s);
+// Mark SOR's value-derived arrays for recomputation when the operator's values
+// changed since they were last marked (outside stream capture; a captured
+// solve graph calls it before every launch).
+int pc_values_sync(Pc* pc, cudaStream_t s);
 int pc_import_factor(Pc* pc, int type, const FactorPattern& pat, const std::vector<int>& perm_c,
                      const double* ba_host, Csr* A, cudaStream_t s);
 int pc_import_jacobi(Pc* pc, int n, const double* diag, const double* diagsqrt, cudaStream_t s);

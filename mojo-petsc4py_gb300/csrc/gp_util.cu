@@ -1,4 +1,5 @@
 // Library-wide utilities: error text, device properties, standalone scratch.
+#include <atomic>
 #include <cstdlib>
 #include <mutex>
 #include <string>
@@ -25,6 +26,11 @@ int arith_mode() {
 }
 
 void set_arith_mode(int mode) { g_arith = mode == kOrdered ? kOrdered : mode ? kFma : kExact; }
+
+unsigned long long next_uid() {
+  static std::atomic<unsigned long long> next{1};
+  return next.fetch_add(1, std::memory_order_relaxed);
+}
 
 int num_sms() {
   static int cached[64] = {0};
