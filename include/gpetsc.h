@@ -144,6 +144,34 @@ int gp_mat_outer_on_pattern(gp_mat A, const double *u, const double *v, double a
 
 /* d = diag(A).    Replaces MatGetDiagonal_SeqAIJ (src/ported.mojo:434-447). */
 int gp_mat_get_diagonal(gp_mat A, double *d, void *stream);
+/* The matrix's CSR copied to host arrays (int64 indptr[nrows+1], int64
+ * indices[nnz], values[nnz]; nnz from gp_mat_info). */
+int gp_mat_get_csr(gp_mat A, int64_t *indptr, int64_t *indices, double *values, void *stream);
+
+/* ------------------------------------------------------------ assembly
+ * Matrix assembly on the device; the reference assembles in Python
+ * (python/mojopetsc4py/PETSc/Mat.py:383-413, 682-746).
+ *
+ * gp_coo_assemble  CSR (host arrays: int64 indptr[nrows+1]; indices and
+ *                  out_values of capacity >= nentries) from entries given in
+ *                  call order.  For each (row, col) the entries fold from
+ *                  0.0: add[e] != 0 adds (value + v, rounded), add[e] == 0
+ *                  sets -- MatSetValues with ADD_VALUES / INSERT_VALUES in
+ *                  that order (Mat.py:434-439).  Columns ascend in each row;
+ *                  *nnz receives the number of distinct entries.  GP_ERR_ARG
+ *                  when an index is out of range.
+ * gp_dense_to_csr  CSR of the entries v != 0.0 of a row-major dense host
+ *                  array, row by row in column order (from_dense,
+ *                  Mat.py:719-746); GP_ERR_ARG with *nnz set when more than
+ *                  `capacity` entries are nonzero.
+ * The sorts are stable radix sorts on the device. */
+int gp_coo_assemble(int64_t nrows, int64_t ncols, int64_t nentries, const int64_t *rows,
+                    const int64_t *cols, const double *values, const uint8_t *add,
+                    int64_t *indptr, int64_t *indices, double *out_values, int64_t *nnz,
+                    void *stream);
+int gp_dense_to_csr(int64_t nrows, int64_t ncols, const double *dense, int64_t capacity,
+                    int64_t *indptr, int64_t *indices, double *values, int64_t *nnz,
+                    void *stream);
 
 /* ------------------------------------------------------------ Vec */
 /* Elementwise operations (src/ported.mojo:75-341, src/simdvec.mojo:40-319).

@@ -181,30 +181,7 @@ int csr_destroy(Csr* A) {
   return GP_OK;
 }
 
-int csr_build_transpose(Csr* A, cudaStream_t s) {
-  if (A->t_rowptr) return GP_OK;
-  const int n = A->n, m = A->ncols;
-  std::vector<int> trp(m + 1, 0), tcol(std::max<int64_t>(A->nnz, 1)), tsrc(std::max<int64_t>(A->nnz, 1));
-  for (int64_t j = 0; j < A->nnz; j++) trp[A->h_colind[j] + 1]++;
-  for (int c = 0; c < m; c++) trp[c + 1] += trp[c];
-  std::vector<int> fill(trp.begin(), trp.end() - 1);
-  for (int i = 0; i < n; i++)
-    for (int j = A->h_rowptr[i]; j < A->h_rowptr[i + 1]; j++) {
-      int c = A->h_colind[j];
-      int k = fill[c]++;
-      tcol[k] = i;
-      tsrc[k] = j;
-    }
-  GP_TRY(dev_upload(&A->t_rowptr, trp.data(), (size_t)m + 1, s));
-  GP_TRY(dev_upload(&A->t_colind, tcol.data(), (size_t)A->nnz, s));
-  GP_TRY(dev_upload(&A->t_src, tsrc.data(), (size_t)A->nnz, s));
-  int64_t maxlen = 0;
-  for (int c = 0; c < m; c++) maxlen = std::max<int64_t>(maxlen, trp[c + 1] - trp[c]);
-  const double avg = m ? (double)A->nnz / m : 0.0;
-  A->t_stream_rows = maxlen > kSpmvMaxRowLen || (double)maxlen > 8.0 * avg + 8.0;
-  GP_CUDA(cudaStreamSynchronize(s));
-  return GP_OK;
-}
+// csr_build_transpose (the pattern of A^T) is in gp_assemble.cu.
 
 // At.val[k] = A.val[t_src[k]]: the values of A^T in its row order.
 __global__ void k_gather_values(int64_t nnz, const int* __restrict__ src,

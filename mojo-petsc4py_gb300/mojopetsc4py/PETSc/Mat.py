@@ -1,12 +1,16 @@
 """Sequential AIJ (CSR) matrices, mirroring the reference's `Mat`
 (python/mojopetsc4py/PETSc/Mat.py).
 
-Assembly stays on the host exactly as in the reference: int64 row starts,
-column indices ascending within a row, float64 values, and a pending-entry
-dict for `setValue(s)` that is sorted into CSR on demand.  The multiply,
-the transposed multiply and the diagonal run on the GPU against a device
-mirror (int32 indices) that is created on first use and refreshed when the
-pattern or the values change.
+The host arrays are the reference's: int64 row starts, column indices
+ascending within a row, float64 values.  Entries set after an assembly are
+kept pending and folded into CSR on demand with the reference's semantics
+(Mat.py:383-413, 434-439: per (row, col), INSERT sets and ADD adds, in call
+order, from 0.0).  Blocks of entries (`setValues` with many indices) are
+logged as arrays and large logs are folded on the GPU (gp_coo_assemble: a
+stable radix sort and one fold per entry); `from_dense` and `transpose` also
+run on the GPU for large matrices.  The multiply, the transposed multiply
+and the diagonal run on the GPU against a device mirror (int32 indices) that
+is created on first use and refreshed when the pattern or the values change.
 """
 
 from __future__ import annotations
@@ -18,6 +22,104 @@ import numpy as np
 from .. import _device as dev
 from .._lib import check, lib
 from .Vec import Vec
+
+
+# logs of at least this many entries are folded on the GPU (smaller ones on
+# the host, where a device round trip would cost more than the fold)
+DEVICE_ASSEMBLY_MIN = 1 << 15
+# setValues blocks of at least this many entries are logged as arrays (smaller
+# ones go entry by entry, as in the reference)
+BLOCK_LOG_MIN = 64
+
+
+class _Pending:
+    """Entries set since the last assembly.
+
+    base    the CSR arrays at the first entry that had no slot (their values
+            start the fold of their (row, col)), or None
+    chunks  logged blocks in call order: (rows, cols, values, add) arrays
+    single  (row, col) -> value folded as the reference's dict does; a key
+            is here only while no logged block holds it (a single entry set
+            after a block was logged folds everything first)
+    """
+
+    __slots__ = ("base", "chunks", "single")
+
+    def __init__(self, base=None):
+        self.base = base
+        self.chunks = []
+        self.single = {}
+
+    def base_value(self, row, col):
+        if self.base is None:
+            return 0.0
+        irow, icol, data = self.base
+        lo, hi = int(irow[row]), int(irow[row + 1])
+        pos = lo + int(np.searchsorted(icol[lo:hi], col))
+        if pos < hi and int(icol[pos]) == col:
+            return float(data[pos])
+        return 0.0
+
+    def flush_single(self):
+        if self.single:
+            keys = np.array(list(self.single.keys()), dtype=np.int64).reshape(-1, 2)
+            vals = np.fromiter(self.single.values(), dtype=np.float64, count=len(self.single))
+            self.chunks.append((keys[:, 0].copy(), keys[:, 1].copy(), vals,
+                                np.zeros(len(vals), dtype=np.uint8)))
+            self.single = {}
+
+    def log(self, nrows):
+        """All entries in fold order: the base CSR (inserts), the blocks, then
+        the single entries (inserts of their folded values)."""
+        self.flush_single()
+        parts = []
+        if self.base is not None:
+            irow, icol, data = self.base
+            rows = np.repeat(np.arange(nrows, dtype=np.int64), np.diff(irow))
+            parts.append((rows, icol, data, np.zeros(len(data), dtype=np.uint8)))
+        parts.extend(self.chunks)
+        if not parts:
+            e = np.zeros(0, dtype=np.int64)
+            return e, e, np.zeros(0), np.zeros(0, dtype=np.uint8)
+        return tuple(np.concatenate([p[k] for p in parts]) for k in range(4))
+
+
+def _fold_host(nrows, ncols, rows, cols, vals, add):
+    """CSR of an entry log on the host (same fold as gp_coo_assemble)."""
+    key = rows * ncols + cols
+    order = np.argsort(key, kind="stable")
+    ks, vs, ad = key[order], vals[order], add[order]
+    head = np.flatnonzero(np.r_[True, ks[1:] != ks[:-1]]) if len(ks) else np.zeros(0, np.int64)
+    count = np.diff(np.r_[head, len(ks)])
+    out = np.where(ad[head] != 0, 0.0 + vs[head], vs[head])
+    for s in np.flatnonzero(count > 1):
+        acc = 0.0
+        for q in range(int(head[s]), int(head[s]) + int(count[s])):
+            acc = acc + float(vs[q]) if ad[q] else float(vs[q])
+        out[s] = acc
+    ukey = ks[head]
+    r, c = ukey // max(ncols, 1), ukey % max(ncols, 1)
+    indptr = np.zeros(nrows + 1, dtype=np.int64)
+    if nrows:
+        indptr[1:] = np.cumsum(np.bincount(r, minlength=nrows))
+    return indptr, c.astype(np.int64), out.astype(np.float64)
+
+
+def _fold(nrows, ncols, rows, cols, vals, add):
+    n = len(rows)
+    if n >= DEVICE_ASSEMBLY_MIN and dev.has_device():
+        indptr = np.zeros(nrows + 1, dtype=np.int64)
+        indices = np.zeros(max(n, 1), dtype=np.int64)
+        out = np.zeros(max(n, 1), dtype=np.float64)
+        nnz = ctypes.c_int64()
+        rows, cols = np.ascontiguousarray(rows, np.int64), np.ascontiguousarray(cols, np.int64)
+        vals, add = np.ascontiguousarray(vals, np.float64), np.ascontiguousarray(add, np.uint8)
+        check(lib().gp_coo_assemble(nrows, ncols, n, rows.ctypes.data, cols.ctypes.data,
+                                    vals.ctypes.data, add.ctypes.data, indptr.ctypes.data,
+                                    indices.ctypes.data, out.ctypes.data, ctypes.byref(nnz),
+                                    dev.stream_ptr()))
+        return indptr, indices[: nnz.value].copy(), out[: nnz.value].copy()
+    return _fold_host(nrows, ncols, rows, cols, vals, add)
 
 
 class MatType:
@@ -174,7 +276,7 @@ class Mat:
         self._data = np.zeros(max(m * per_row, 1), dtype=np.float64)
         self._nnz_used = 0
         self._assembled = True
-        self._pending = {}
+        self._pending = _Pending()
         self._touch_pattern()
         return self
 
@@ -351,25 +453,15 @@ class Mat:
         return self
 
     def _materialize(self):
-        """Sort and coalesce the pending entries into CSR."""
+        """Fold the pending entries into CSR (Mat.py:383-413 of the
+        reference: sorted by (row, col), each entry's ops in call order)."""
         if self._pending is None:
             return
-        rows = self._pending
-        n = self._nrows
-        counts = np.zeros(n, dtype=np.int64)
-        for r, cols in rows.items():
-            counts[r] = len(cols)
-        irow = np.zeros(n + 1, dtype=np.int64)
-        irow[1:] = np.cumsum(counts)
+        rows, cols, vals, add = self._pending.log(self._nrows)
+        irow, icol, data = _fold(self._nrows, self._ncols, rows, cols, vals, add)
         total = int(irow[-1])
-        icol = np.zeros(max(total, 1), dtype=np.int64)
-        data = np.zeros(max(total, 1), dtype=np.float64)
-        for r, cols in rows.items():
-            k = int(irow[r])
-            for c in sorted(cols):
-                icol[k] = c
-                data[k] = cols[c]
-                k += 1
+        if total == 0:
+            icol, data = np.zeros(1, dtype=np.int64), np.zeros(1, dtype=np.float64)
         self._irow, self._icol, self._data = irow, icol, data
         self._nnz_used = total
         self._pending = None
@@ -385,8 +477,14 @@ class Mat:
         return pos
 
     def _entry(self, row: int, col: int) -> float:
-        if self._pending is not None:
-            return float(self._pending.get(row, {}).get(col, 0.0))
+        p = self._pending
+        if p is not None:
+            v = p.single.get((row, col))
+            if v is not None:
+                return float(v)
+            if not p.chunks:
+                return p.base_value(row, col)
+            self._materialize()
         j = self._locate(row, col)
         return 0.0 if j < 0 else float(self._data[j])
 
@@ -401,16 +499,13 @@ class Mat:
         return out
 
     def _spill(self):
-        """Move the CSR entries into the pending dict so a later setValue keeps
-        them."""
+        """Keep the CSR entries as the base of the pending entries, so later
+        entries fold onto them."""
         if self._pending is not None:
             return
-        pend = {}
-        for i in range(self._nrows):
-            lo, hi = int(self._irow[i]), int(self._irow[i + 1])
-            if hi > lo:
-                pend[i] = {int(self._icol[j]): float(self._data[j]) for j in range(lo, hi)}
-        self._pending = pend
+        nnz = self._nnz_used
+        self._pending = _Pending((self._irow[: self._nrows + 1].copy(),
+                                  self._icol[:nnz].copy(), self._data[:nnz].copy()))
 
     def _setValue(self, row, col, value, addv):
         if row < 0 or row >= self._nrows or col < 0 or col >= self._ncols:
@@ -422,8 +517,14 @@ class Mat:
                 self._touch_values()
                 return
         self._spill()
-        cols = self._pending.setdefault(row, {})
-        cols[col] = cols.get(col, 0.0) + value if addv else value
+        p = self._pending
+        cur = p.single.get((row, col))
+        if cur is None:
+            if p.chunks:  # the entry may sit in a logged block: fold first
+                self._materialize()
+                return self._setValue(row, col, value, addv)
+            cur = p.base_value(row, col)
+        p.single[(row, col)] = cur + value if addv else value
 
     def setValue(self, row, col, value, addv=None) -> None:
         self._setValue(int(row), int(col), float(value), addv is not None)
@@ -437,9 +538,47 @@ class Mat:
                 f" at least {need} values are needed"
             )
         add = addv is not None
-        for i, r in enumerate(rows):
-            for j, c in enumerate(cols):
-                self._setValue(int(r), int(c), float(vals[i * len(cols) + j]), add)
+        if need < BLOCK_LOG_MIN:
+            for i, r in enumerate(rows):
+                for j, c in enumerate(cols):
+                    self._setValue(int(r), int(c), float(vals[i * len(cols) + j]), add)
+            return
+        r = np.asarray(rows, dtype=np.int64).ravel()
+        c = np.asarray(cols, dtype=np.int64).ravel()
+        R, C = np.repeat(r, len(c)), np.tile(c, len(r))
+        bad = (R < 0) | (R >= self._nrows) | (C < 0) | (C >= self._ncols)
+        if bad.any():
+            k = int(np.argmax(bad))
+            raise ValueError(f"entry ({int(R[k])}, {int(C[k])}) is out of range")
+        self._log_block(R, C, np.array(vals[:need], dtype=np.float64), add)
+
+    def _log_block(self, R, C, V, add):
+        """A block of entries in call order (rows R, columns C, values V)."""
+        if self._pending is None:
+            # every entry has a slot and no slot repeats: values in place
+            pos = self._locate_many(R, C)
+            if (pos >= 0).all() and len(np.unique(pos)) == len(pos):
+                if add:
+                    self._data[pos] = self._data[pos] + V
+                else:
+                    self._data[pos] = V
+                self._touch_values()
+                return
+        self._spill()
+        p = self._pending
+        p.flush_single()
+        p.chunks.append((R, C, V, np.full(len(R), 1 if add else 0, dtype=np.uint8)))
+
+    def _locate_many(self, R, C):
+        """Slots of the entries (R, C) in the CSR arrays (-1 where absent)."""
+        nnz = self._nnz_used
+        key = self._icol[:nnz] + np.repeat(np.arange(self._nrows, dtype=np.int64),
+                                           np.diff(self._irow[: self._nrows + 1])) * self._ncols
+        want = R * self._ncols + C
+        pos = np.searchsorted(key, want)
+        ok = pos < nnz
+        ok[ok] = key[pos[ok]] == want[ok]
+        return np.where(ok, pos, -1)
 
     def setValueBlocked(self, rows, cols, value, addv=None) -> None:
         add = addv is not None
@@ -598,10 +737,26 @@ class Mat:
 
 
 def _transpose(m: Mat) -> Mat:
-    """A^T in CSR (a stable counting sort by column; duplicate entries kept in
-    row order)."""
+    """A^T in CSR (a stable sort by column, so each row of A^T lists its
+    entries in ascending original row; Mat.py:682-716 of the reference).
+    Large matrices are transposed on the GPU (gp_mat_transpose: the pattern
+    by a stable radix sort, the values gathered through it)."""
     rows, cols, vals = m.getValuesCSR()
     nnz = len(cols)
+    if nnz >= DEVICE_ASSEMBLY_MIN and dev.has_device():
+        t = ctypes.c_void_p()
+        check(lib().gp_mat_transpose(m._device(), ctypes.byref(t), dev.stream_ptr()))
+        try:
+            indptr = np.zeros(m._ncols + 1, dtype=np.int64)
+            indices = np.zeros(nnz, dtype=np.int64)
+            values = np.zeros(nnz, dtype=np.float64)
+            check(lib().gp_mat_get_csr(t.value, indptr.ctypes.data, indices.ctypes.data,
+                                       values.ctypes.data, dev.stream_ptr()))
+        finally:
+            lib().gp_mat_destroy(t.value)
+        out = Mat().createSeqAIJ((m._ncols, m._nrows), nnz=1)
+        out.setValuesCSR(indptr, indices, values)
+        return out
     row_of = np.repeat(np.arange(m._nrows, dtype=np.int64), np.diff(rows))
     order = np.argsort(cols, kind="stable")
     counts = np.bincount(cols, minlength=m._ncols) if nnz else np.zeros(m._ncols, np.int64)
@@ -620,6 +775,17 @@ def from_dense(array, mat=None) -> Mat:
     n, m = arr.shape
     out = mat if mat is not None else Mat()
     out.createSeqAIJ((n, m))
+    if arr.size >= DEVICE_ASSEMBLY_MIN and dev.has_device():
+        cap = int(np.count_nonzero(arr))
+        indptr = np.zeros(n + 1, dtype=np.int64)
+        indices = np.zeros(max(cap, 1), dtype=np.int64)
+        values = np.zeros(max(cap, 1), dtype=np.float64)
+        nnz = ctypes.c_int64()
+        check(lib().gp_dense_to_csr(n, m, arr.ctypes.data, cap, indptr.ctypes.data,
+                                    indices.ctypes.data, values.ctypes.data, ctypes.byref(nnz),
+                                    dev.stream_ptr()))
+        out.setValuesCSR(indptr, indices[: nnz.value], values[: nnz.value])
+        return out
     rr, cc = np.nonzero(arr)
     indptr = np.zeros(n + 1, dtype=np.int64)
     indptr[1:] = np.cumsum(np.bincount(rr, minlength=n)) if n else []

@@ -74,6 +74,9 @@ GP_SIGNATURES = {
     "gp_host_free": ([P], ctypes.c_int),
     "gp_copy": ([P, P, I64, ctypes.c_int, P], ctypes.c_int),
     "gp_stream_synchronize": ([P], ctypes.c_int),
+    "gp_coo_assemble": ([I64, I64, I64, P, P, P, P, P, P, P, P, P], ctypes.c_int),
+    "gp_dense_to_csr": ([I64, I64, P, I64, P, P, P, P, P], ctypes.c_int),
+    "gp_mat_get_csr": ([P, P, P, P, P], ctypes.c_int),
     "gp_mixed_options_default": ([P], None),
     "gp_mixed_create": ([PP], ctypes.c_int),
     "gp_mixed_destroy": ([P], ctypes.c_int),
