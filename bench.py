@@ -223,19 +223,30 @@ def gather_to_root(pg, obj):
 
 
 # ------------------------------------------------------------------ CPU leg
-def oracle_cg_jacobi(ip, ix, v, b, max_it=MAX_IT):
+# the oracle's timing build (FMA contraction, -O3; -march=native is not used
+# because the host code must build the same on x86_64 and aarch64)
+ORACLE_TIMING_BUILD = "gcc -O3 -ffp-contract=fast -fno-fast-math, 1 thread"
+
+
+def oracle_cg_jacobi(ip, ix, v, b, max_it=MAX_IT, build="timing"):
     """One timed CG + Jacobi solve of the oracle: (seconds, result).  The
     Jacobi set-up is outside the timing, as the reference's bench.py keeps
-    set-up out of its solve timings."""
+    set-up out of its solve timings.  `build` "timing" (the CPU baseline) or
+    "parity" (the checker, whose iterate the GPU results are compared with)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
-    O.lib()
-    ip, ix, v, b = O.i64(ip), O.i64(ix), O.f64(v), O.f64(b)
-    pc = O.OraclePC("jacobi", ip, ix, v)
-    t0 = time.perf_counter()
-    r = O.solve("cg", ip, ix, v, b, pc=pc, rtol=RTOL, atol=1e-50, divtol=1e30, max_it=max_it)
-    return time.perf_counter() - t0, r
+    O.set_build(build)
+    try:
+        O.lib()
+        ip, ix, v, b = O.i64(ip), O.i64(ix), O.f64(v), O.f64(b)
+        pc = O.OraclePC("jacobi", ip, ix, v)
+        t0 = time.perf_counter()
+        r = O.solve("cg", ip, ix, v, b, pc=pc, rtol=RTOL, atol=1e-50, divtol=1e30,
+                    max_it=max_it)
+        return time.perf_counter() - t0, r
+    finally:
+        O.set_build("parity")
 
 
 def run_reference(args, world, rank, pg):
@@ -266,7 +277,8 @@ def run_reference(args, world, rank, pg):
         "cpu_baseline": {"value": round(ms, 3), "unit": "ms", "cores": 1, "kind": "port",
                          "sample": f"whole {its}-iteration CG+Jacobi solves, mean of "
                                    f"{args.steps} (warm-up: {args.warmup} solves of 40 "
-                                   "iterations)", **cpu_info()},
+                                   "iterations)", "build": ORACLE_TIMING_BUILD,
+                         **cpu_info()},
         "e2e": {"value": round(ms, 3), "unit": "ms", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -470,11 +482,13 @@ def run_ours(args, world, rank, local, pg):
     # ---- CPU baseline (rank 0 at N = 1 only): one whole solve of the oracle
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        dt, rc = oracle_cg_jacobi(ip, ix, v, b)
+        dt, rt = oracle_cg_jacobi(ip, ix, v, b)
         cpu = {"value": round(dt * 1e3, 3), "unit": "ms", "cores": 1, "kind": "port",
-               "sample": f"one whole {rc['its']}-iteration CG+Jacobi solve of the same system "
-                         "on this host", **cpu_info()}
-        # parity of the timed solves against the oracle's, same inputs
+               "sample": f"one whole {rt['its']}-iteration CG+Jacobi solve of the same system "
+                         "on this host", "build": ORACLE_TIMING_BUILD, **cpu_info()}
+        # parity of the timed solves against the oracle's parity build, same
+        # inputs (untimed)
+        _, rc = oracle_cg_jacobi(ip, ix, v, b, build="parity")
         rx = np.asarray(rc["x"])
         methods["cg+jacobi"]["vs_oracle"] = {
             "oracle_its": int(rc["its"]), "oracle_reason": int(rc["reason"]),

@@ -24,6 +24,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
+# the timing build of the CPU baseline (FMA contraction; see the Makefile)
+LIB_TIMING = os.path.join(HERE, "_build", "liboracle_timing.so")
 
 I = ctypes.c_int64
 F = ctypes.c_double
@@ -93,7 +95,6 @@ SIGNATURES = {
     "mp_ksp_solve_fgmres": ([I] + [P] * 14, None),
 }
 
-_lib = None
 
 
 def build() -> str:
@@ -102,17 +103,32 @@ def build() -> str:
     return LIB
 
 
+_libs = {}
+_which = "parity"
+
+
+def set_build(which: str) -> None:
+    """Select the library every later call uses: "parity" (the default, every
+    check) or "timing" (the CPU baseline's timed solves)."""
+    global _which
+    if which not in ("parity", "timing"):
+        raise ValueError(which)
+    _which = which
+
+
 def lib() -> ctypes.CDLL:
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB):
+    L = _libs.get(_which)
+    if L is None:
+        path = LIB if _which == "parity" else LIB_TIMING
+        if not os.path.exists(path):
             build()
-        _lib = ctypes.CDLL(LIB)
+        L = ctypes.CDLL(path)
         for name, (argtypes, restype) in SIGNATURES.items():
-            fn = getattr(_lib, name)
+            fn = getattr(L, name)
             fn.argtypes = argtypes
             fn.restype = restype
-    return _lib
+        _libs[_which] = L
+    return L
 
 
 def a(arr) -> int:
