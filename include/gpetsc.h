@@ -277,16 +277,18 @@ int gp_pc_sweep_form(gp_pc pc, int32_t which, int32_t *tiled, int32_t *rows_per_
                      int32_t *chunks);
 /* Brick form of the sweeps of later set-ups, for sweeps whose dependencies are
  * the unit steps of a Cartesian grid in natural order (5-/7-point stencils and
- * operators with their pattern): CTAs take bricks of lines_j x lines_k grid
- * lines and each thread walks one line, so most values pass through
- * registers and shared memory instead of L2.
- *   mode 0  never (the default);  1 where its model beats the other forms;
+ * operators with their pattern): CTAs take bricks of lines_j grid lines of one
+ * plane and each thread walks one line, so most values pass through registers
+ * and shared memory instead of L2; the values of neighbouring bricks are
+ * fetched into a shared-memory ring by fetch warps.
+ *   mode 0  never;  1 where its model beats the other forms;
  *   2  wherever the grid structure is found.
- *   lines_j, lines_k > 0 force the brick's lines (product <= 256); 0 lets
- *   the set-up choose.  max_ctas > 0 caps the persistent grid (each CTA then
- *   walks several bricks); 0 sizes it to the device.
+ *   lines_j in 1..128 forces the brick's lines; 0 lets the set-up choose.
+ *   lines_k must be 0 or 1 (a brick lies in one plane).  max_ctas > 0 caps
+ *   the persistent grid (each CTA then walks several bricks); 0 sizes it to
+ *   the device.
  * Bit-identical to the other forms.  Defaults from GPETSC_SWEEP_BRICKS and
- * GPETSC_BRICK_DIMS=JxK.  No counterpart in the reference. */
+ * GPETSC_BRICK_LINES.  No counterpart in the reference. */
 int gp_set_sweep_bricks(int32_t mode, int32_t lines_j, int32_t lines_k, int32_t max_ctas);
 /* Whether a set-up PC's forward (which = 0) or backward (1) sweep got the
  * brick form, and dims[5] = grid nx, ny, nz and the brick's lines_j, lines_k

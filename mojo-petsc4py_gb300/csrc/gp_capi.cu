@@ -267,11 +267,11 @@ int gp_set_sweep_form(int32_t tiles, int32_t tile_rows) {
 }
 
 int gp_set_sweep_bricks(int32_t mode, int32_t lines_j, int32_t lines_k, int32_t max_ctas) {
-  if (mode < 0 || mode > 2 || lines_j < 0 || lines_k < 0 || (int64_t)lines_j * lines_k > 256 ||
+  if (mode < 0 || mode > 2 || lines_j < 0 || lines_j > 128 || lines_k < 0 || lines_k > 1 ||
       max_ctas < 0)
-    return bad("gp_set_sweep_bricks: mode must be 0, 1 or 2, lines_j * lines_k <= 256 and "
-               "max_ctas >= 0");
-  gp::set_sweep_bricks(mode, lines_j, lines_k, max_ctas);
+    return bad("gp_set_sweep_bricks: mode must be 0, 1 or 2, 0 <= lines_j <= 128, lines_k 0 "
+               "or 1 and max_ctas >= 0");
+  gp::set_sweep_bricks(mode, lines_j, max_ctas);
   return GP_OK;
 }
 

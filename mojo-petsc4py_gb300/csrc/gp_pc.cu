@@ -604,9 +604,6 @@ static int setup_sor(Pc* pc, cudaStream_t s) {
   GP_TRY(check_sorted_with_diag(A, "SOR"));
   GP_TRY(dalloc(&pc->idiag, n));
   GP_TRY(dalloc(&pc->mdiag, n));
-  GP_TRY(dalloc(&pc->t, n));
-  GP_TRY(dalloc(&pc->yf, n));
-  GP_TRY(dalloc(&pc->yb, n));
   std::vector<int> lp(n + 1, 0), lc, ls, up(n + 1, 0), uc, us;
   for (int i = 0; i < n; i++) {
     for (int j = A->h_rowptr[i]; j < A->h_rowptr[i + 1]; j++) {
@@ -628,6 +625,10 @@ static int setup_sor(Pc* pc, cudaStream_t s) {
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
   GP_TRY(ell_build(pc->ef, ELL_SOR_F, n, true, of, lp, lc, ls, none, none, none, &fpos));
   GP_TRY(ell_build(pc->eb, ELL_SOR_B, n, false, ob, up, uc, us, fpos, none, none, nullptr));
+  pc->vlen = std::max({n, pc->ef.n, pc->eb.n});
+  GP_TRY(dalloc(&pc->t, pc->vlen));
+  GP_TRY(dalloc(&pc->yf, pc->vlen));
+  GP_TRY(dalloc(&pc->yb, pc->vlen));
   GP_CUDA(cudaMalloc(&pc->sor_stale, sizeof(int)));
   GP_CUDA(cudaMemsetAsync(pc->sor_stale, 1, sizeof(int), s));  // nonzero: recompute
   pc->sor_vver = A->vver;
@@ -732,8 +733,9 @@ static int ilu_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
   GP_TRY(dalloc(&pc->ba, std::max(P.nnz, 1)));
   GP_CUDA(cudaMalloc(&pc->done, std::max(n, 1) * sizeof(int)));
   GP_CUDA(cudaMemsetAsync(pc->done, 0, std::max(n, 1) * sizeof(int), s));
-  GP_TRY(dalloc(&pc->yf, n));
-  GP_TRY(dalloc(&pc->yb, n));
+  pc->vlen = std::max({n, pc->ef.n, pc->eb.n});
+  GP_TRY(dalloc(&pc->yf, pc->vlen));
+  GP_TRY(dalloc(&pc->yb, pc->vlen));
   GP_CUDA(cudaStreamSynchronize(s));  // host vectors above go out of scope
   return GP_OK;
 }
@@ -866,9 +868,10 @@ static int icc_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
   GP_TRY(dalloc(&pc->ba_orig, std::max(P.nnz, 1)));
   GP_CUDA(cudaMalloc(&pc->done, std::max(n, 1) * sizeof(int)));
   GP_CUDA(cudaMemsetAsync(pc->done, 0, std::max(n, 1) * sizeof(int), s));
-  GP_TRY(dalloc(&pc->yf, n));
-  GP_TRY(dalloc(&pc->yb, n));
-  GP_TRY(dalloc(&pc->ys, n));
+  pc->vlen = std::max({n, pc->ef.n, pc->eb.n});
+  GP_TRY(dalloc(&pc->yf, pc->vlen));
+  GP_TRY(dalloc(&pc->yb, pc->vlen));
+  GP_TRY(dalloc(&pc->ys, pc->vlen));
   GP_CUDA(cudaStreamSynchronize(s));
   return GP_OK;
 }
@@ -1050,7 +1053,7 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
       k_sor_diag<<<(n + 255) / 256, 256, 0, s>>>(n, pc->opt.omega, pc->opt.fshift, A->diagpos,
                                                   A->val, pc->idiag, pc->mdiag, gate, want,
                                                   pc->sor_stale);
-      k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
+      k_fill_pending<<<grid_for(pc->vlen), 256, 0, s>>>(gate, want, pc->vlen, pc->yf, pc->yb);
       if (pc->ef.ok && pc->eb.ok) {
         if (!pc->ef.tiled)
           k_ell_refresh_g<<<g, 256, 0, s>>>(gate, want, pc->ef.n, pc->ef.cnt, pc->ef.cslot,
@@ -1080,7 +1083,7 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
       break;
     }
     case PC_ILU:
-      k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
+      k_fill_pending<<<grid_for(pc->vlen), 256, 0, s>>>(gate, want, pc->vlen, pc->yf, pc->yb);
       if (pc->ef.ok && pc->eb.ok) {
         GP_TRY(ell_sweep(ELL_ILU_F, pc->ef, gate, want, x, y, pc->yf, nullptr, nullptr, nullptr,
                          nullptr, 0.0, 0, 0, tk0, pc->err, pc->ba, s));
@@ -1094,7 +1097,7 @@ int pc_apply(Pc* pc, DRef x, DRef y, cudaStream_t s, const int* gate, int want) 
                                            pc->bdiag, pc->perm_c, pc->yf, pc->yb, y, pc->err);
       break;
     case PC_ICC:
-      k_fill_pending<<<g, 256, 0, s>>>(gate, want, n, pc->yf, pc->yb);
+      k_fill_pending<<<grid_for(pc->vlen), 256, 0, s>>>(gate, want, pc->vlen, pc->yf, pc->yb);
       if (pc->ef.ok && pc->eb.ok) {
         GP_TRY(ell_sweep(ELL_ICC_F, pc->ef, gate, want, x, y, pc->yf, nullptr, pc->ys, nullptr,
                          nullptr, 0.0, 0, 0, tk0, pc->err, pc->ba, s));

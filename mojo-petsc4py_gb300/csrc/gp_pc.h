@@ -65,31 +65,35 @@ struct EllSweep {
   double est_us = 0.0;            // simulated duration of one tiled sweep
   int rows_per_chunk = 0;         // chunk size of the tiled layout
   // Brick form (gp_brick.cu, k_brick_sweep): the sweep's dependencies are the
-  // unit steps of a grid gx x gy x gz; CTAs take bricks of BJ x BK grid lines
-  // and each thread walks one line.  Per-row arrays in natural row order
-  // (cslot / coef as [direction][n], in_idx, out_idx, dslot / dval); values
-  // are indexed by row.
+  // unit steps of a grid gx x gy x gz; CTAs take bricks of BJ grid lines of
+  // one plane (BK = 1) and each thread walks one line.  `n` counts positions,
+  // step-major within each brick with holes (nrows rows); the per-position
+  // arrays are cslot / coef as [direction][n], in_idx, out_idx (absent when
+  // the identity), dslot / dval, and values are indexed by position.
   bool brick = false;
-  int gx = 0, gy = 0, gz = 0, BJ = 0, BK = 0, nbricks = 0, bgrid = 0;
+  int gx = 0, gy = 0, gz = 0, BJ = 0, BK = 0, nbJ = 0, nbricks = 0, bgrid = 0, nrows = 0;
   int bord = 0;            // fold order of a row's terms: 0 k, j, i; 1 i, j, k
-  bool in_ident = false;
+  bool in_ident = false, out_ident = false;
   int* border = nullptr;   // [2 * nbricks]: (J, K) of each brick in hand-out order
+  int* bbase = nullptr;    // [nbJ * gz]: first position of brick (J, K) at J + nbJ K
 };
 void ell_free(EllSweep& e);
 // Brick layout of a sweep when its dependencies have the grid structure and
 // (unless forced) the model puts it below `other_us`; *built says whether.
+// pos_of_row: each row's position in the brick layout.
 int brick_build(EllSweep& e, int mode, int n, bool forward, const std::vector<int>& dptr,
                 const std::vector<int>& dcol, const std::vector<int>& dsl,
                 const std::vector<int>& in_row, const std::vector<int>& out_row,
-                const std::vector<int>& dslot_row, double other_us, bool* built);
+                const std::vector<int>& dslot_row, double other_us, bool* built,
+                std::vector<int>* pos_of_row);
 int brick_sweep(int mode, const EllSweep& e, const int* gate, int want, DRef in, DRef out,
                 double* val, const double* fval, double* aux, const double* auxin,
                 const double* idiag, double omega, int use_t, int write_out, unsigned* tickets,
                 DevErr* err, cudaStream_t s);
 // Brick form of later set-ups: mode 0 never, 1 where modelled faster, 2
-// wherever the structure allows; bj, bk > 0 force the lines of a brick;
+// wherever the structure allows; lines > 0 forces the lines of a brick;
 // max_ctas > 0 caps the persistent grid.
-void set_sweep_bricks(int mode, int bj, int bk, int max_ctas);
+void set_sweep_bricks(int mode, int lines, int max_ctas);
 // Lay out one sweep.  forward: dependencies precede each row (ascending
 // processing); otherwise they follow it.  `order` is the level order, used
 // when the sweep is not tiled.
@@ -137,6 +141,9 @@ struct Pc {
   PcOptions opt;
   Csr* A = nullptr;  // operator the PC was set up from (not owned)
   int n = 0;
+  // entries of the sweeps' value arrays yf, yb, ys, t: the rows, or more
+  // where a sweep's layout has holes (the brick form)
+  int vlen = 0;
   int device = -1;
   bool ready = false;
   int epoch = 0;

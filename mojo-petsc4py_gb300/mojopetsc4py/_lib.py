@@ -205,10 +205,10 @@ def set_sweep_form(tiles: bool = True, tile_rows: int = 0) -> None:
 def set_sweep_bricks(mode: int = 0, lines_j: int = 0, lines_k: int = 0,
                      max_ctas: int = 0) -> None:
     """Brick form of the triangular sweeps of later PC set-ups (grid-structured
-    sweeps only): mode 0 never (the default), 1 where modelled faster, 2
-    whenever the structure allows; `lines_j` x `lines_k` forces the grid lines
-    of a brick; `max_ctas` caps the persistent grid.  Bit-identical to the
-    other forms."""
+    sweeps only): mode 0 never, 1 where modelled faster, 2 whenever the
+    structure allows; `lines_j` (1-128) forces the grid lines of a brick, which
+    always lies in one plane (`lines_k` 0 or 1); `max_ctas` caps the persistent
+    grid.  Bit-identical to the other forms."""
     check(lib().gp_set_sweep_bricks(int(mode), int(lines_j), int(lines_k), int(max_ctas)))
 
 

@@ -68,3 +68,13 @@ def test_loads_without_a_device():
     lib = _lib.lib()
     assert lib.gp_version() >= 100
     assert _lib.device_count() >= 0
+
+
+def test_brick_settings_are_checked_on_the_host():
+    """The brick form's lines lie in one plane: lines_k above 1, or more than
+    128 lines, is an argument error (no device needed)."""
+    lib = _lib.lib()
+    assert lib.gp_set_sweep_bricks(0, 0, 2, 0) == 1
+    assert lib.gp_set_sweep_bricks(0, 129, 1, 0) == 1
+    assert lib.gp_set_sweep_bricks(0, 64, 1, 0) == 0
+    assert lib.gp_set_sweep_bricks(0, 0, 0, 0) == 0

@@ -4,9 +4,10 @@ The level-ordered form hands out rows in dependency-level order, 32 to a
 warp; the chunked form gives runs of consecutive rows to one CTA, whose
 compute warp walks the chunk level by level with in-chunk values in shared
 memory while its fetch warps poll the values of earlier chunks; the brick
-form (grid-structured sweeps in natural order) gives a brick of grid lines to
-one CTA, one line a thread, with the neighbouring lines' values in shared
-memory and only the brick faces passed through L2.  All must
+form (grid-structured sweeps in natural order) gives a brick of grid lines of
+one plane to one CTA, one line a thread, with the neighbouring line's values
+in shared memory and the faces of other bricks fetched from L2 into a
+shared-memory ring.  All must
 reproduce the reference's sequential sweeps bit for bit in the exact
 arithmetic, whatever the chunk size: chunk sizes that cut grid lines (so a
 dependency chain runs across chunks), tiny chunks, and one chunk holding a
@@ -21,9 +22,25 @@ from mojopetsc4py import PETSc, _lib, gallery
 
 pytestmark = pytest.mark.gpu
 
+def _laplacian_box(nx, ny, nz):
+    """7-point Laplacian on an nx x ny x nz grid, x fastest (ragged bricks)."""
+    n = nx * ny * nz
+    p = np.arange(n, dtype=np.int64)
+    ix, iy, iz = p % nx, (p // nx) % ny, p // (nx * ny)
+    c = np.stack([np.where(iz > 0, p - nx * ny, -1), np.where(iy > 0, p - nx, -1),
+                  np.where(ix > 0, p - 1, -1), p, np.where(ix < nx - 1, p + 1, -1),
+                  np.where(iy < ny - 1, p + nx, -1), np.where(iz < nz - 1, p + nx * ny, -1)], 1)
+    v = np.where(c == p[:, None], 6.0, -1.0)
+    keep = c >= 0
+    ip = np.zeros(n + 1, np.int32)
+    ip[1:] = np.cumsum(keep.sum(1))
+    return ip, c[keep].astype(np.int32), v[keep]
+
+
 MATRICES = {
     "poisson2d_24": lambda: gallery.laplacian_2d(24),
     "poisson3d_10": lambda: gallery.laplacian_3d(10),
+    "poisson3d_13x7x6": lambda: _laplacian_box(13, 7, 6),
     "convdiff_9": lambda: gallery.convection_diffusion_3d(9),
 }
 
@@ -104,22 +121,22 @@ def test_sweep_forms_bit_exact(name, pt, gopts, oopts, form, tiles, rows):
     np.testing.assert_array_equal(_apply(pc, x2), O.OraclePC(pt, ip, ix, v, **oopts).apply(x2))
 
 
-# (name, lines_j, lines_k, CTA cap); 0 x 0 lets the set-up choose
+# (name, lines of a brick, CTA cap); 0 lines lets the set-up choose
 BRICKS = [
-    ("bricks-chosen", 0, 0, 0),
-    ("bricks-4x4", 4, 4, 0),
-    ("bricks-1x8", 1, 8, 0),    # one line along j: every j value crosses a brick
-    ("bricks-8x1", 8, 1, 0),
-    ("bricks-3x5", 3, 5, 0),    # cuts 24- and 10-line grids unevenly
-    ("bricks-16x16", 16, 16, 0),
-    ("bricks-2x2-3ctas", 2, 2, 3),  # three CTAs walk every brick in turn
+    ("bricks-chosen", 0, 0),
+    ("bricks-4", 4, 0),
+    ("bricks-1", 1, 0),      # one line a brick: every j - 1 value crosses a brick
+    ("bricks-8", 8, 0),
+    ("bricks-3", 3, 0),      # cuts 24-, 10-, 9- and 7-line planes unevenly
+    ("bricks-planes", 128, 0),  # capped at the grid: one plane a brick
+    ("bricks-2-3ctas", 2, 3),   # three CTAs walk every brick in turn
 ]
 
 
-@pytest.mark.parametrize("form,bj,bk,ctas", BRICKS, ids=[f[0] for f in BRICKS])
+@pytest.mark.parametrize("form,bj,ctas", BRICKS, ids=[f[0] for f in BRICKS])
 @pytest.mark.parametrize("pt,gopts,oopts", PCS)
 @pytest.mark.parametrize("name", sorted(MATRICES))
-def test_brick_form_bit_exact(name, pt, gopts, oopts, form, bj, bk, ctas):
+def test_brick_form_bit_exact(name, pt, gopts, oopts, form, bj, ctas):
     """The brick form wherever the sweep's dependencies are the unit steps of
     the grid (ILU(0), IC(0), SOR in natural order); fill-in (ILU(1)) and a
     reordering (RCM) break that structure and keep the other forms."""
@@ -127,13 +144,14 @@ def test_brick_form_bit_exact(name, pt, gopts, oopts, form, bj, bk, ctas):
         pytest.skip("IC is for symmetric operators")
     ip, ix, v = MATRICES[name]()
     n = len(ip) - 1
-    _lib.set_sweep_bricks(2, bj, bk, ctas)
+    _lib.set_sweep_bricks(2, bj, 0, ctas)
     pc = _pc(pt, _mat(ip, ix, v), gopts)
     got = _lib.sweep_bricks(pc._handle())
     structured = not ({"setFactorLevels", "setFactorOrdering"} & set(gopts))
     assert got["forward"]["brick"] == structured and got["backward"]["brick"] == structured, got
     if structured and bj:
-        assert got["forward"]["lines"] == (bj, bk)
+        nx, ny, _ = got["forward"]["grid"]
+        assert got["forward"]["lines"] == (min(bj, nx, ny), 1)
     x = np.random.default_rng(5).normal(size=n)
     want = O.OraclePC(pt, ip, ix, v, **oopts).apply(x)
     np.testing.assert_array_equal(_apply(pc, x), want)
@@ -239,7 +257,7 @@ def test_brick_form_edge_cases(name, pt):
     found (a two-row line takes it; the others keep the other forms)."""
     ip, ix, v = EDGE[name]()
     n = len(ip) - 1
-    _lib.set_sweep_bricks(2, 2, 2, 0)
+    _lib.set_sweep_bricks(2, 2, 0, 0)
     pc = _pc(pt, _mat(ip, ix, v), {})
     x = np.random.default_rng(11).normal(size=n)
     np.testing.assert_array_equal(_apply(pc, x), O.OraclePC(pt, ip, ix, v).apply(x))
