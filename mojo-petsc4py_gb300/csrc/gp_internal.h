@@ -5,11 +5,58 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+#include <exception>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "gp_common.cuh"
 
 namespace gp {
+
+// Phase times of a preconditioner set-up: setup_mark(name) records the time
+// since the previous mark; setup_report() prints the phases to stderr and
+// starts over.  Both do nothing unless GPETSC_SETUP_TIMING is set.
+void setup_mark(const char* phase);
+void setup_report(const char* what);
+
+// Host-side parallel loop of the set-up phases: f(lo, hi) over contiguous
+// ranges covering [0, n), on up to 16 host threads (the caller's included),
+// one range for n below `grain`.  An exception thrown by a worker is rethrown
+// on the caller after every thread has joined, where the C ABI's guard turns
+// it into an error status.
+template <class F>
+void host_parallel_for(int64_t n, F f, int64_t grain = 1 << 15) {
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int nt = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)hw, 16, n / grain}));
+  if (nt <= 1) {
+    if (n > 0) f((int64_t)0, n);
+    return;
+  }
+  std::exception_ptr failure;
+  std::mutex mu;
+  auto run = [&](int k) {
+    try {
+      f(n * k / nt, n * (k + 1) / nt);
+    } catch (...) {
+      std::lock_guard<std::mutex> g(mu);
+      if (!failure) failure = std::current_exception();
+    }
+  };
+  std::vector<std::thread> pool;
+  int started = 1;
+  try {
+    pool.reserve(nt - 1);
+    for (int k = 1; k < nt; k++, started++) pool.emplace_back(run, k);
+  } catch (...) {
+    // a thread that could not start: its range and the later ones run here
+  }
+  for (int k = started; k < nt; k++) run(k);
+  run(0);
+  for (auto& th : pool) th.join();
+  if (failure) std::rethrow_exception(failure);
+}
 
 // Reduction scratch owned by the library for one stream user (standalone Vec
 // and Mat calls).  Solvers carry their own.

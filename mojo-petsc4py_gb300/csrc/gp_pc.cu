@@ -604,27 +604,55 @@ static int setup_sor(Pc* pc, cudaStream_t s) {
   GP_TRY(check_sorted_with_diag(A, "SOR"));
   GP_TRY(dalloc(&pc->idiag, n));
   GP_TRY(dalloc(&pc->mdiag, n));
+  // the strict triangles' columns and slots: counts per row, prefix sums,
+  // then each row fills its own range (host threads)
   std::vector<int> lp(n + 1, 0), lc, ls, up(n + 1, 0), uc, us;
-  for (int i = 0; i < n; i++) {
-    for (int j = A->h_rowptr[i]; j < A->h_rowptr[i + 1]; j++) {
-      int c = A->h_colind[j];
-      if (c < i) {
-        lc.push_back(c);
-        ls.push_back(j);
+  const int* rp = A->h_rowptr.data();
+  const int* ci = A->h_colind.data();
+  host_parallel_for(n, [&](int64_t i0, int64_t i1) {
+    for (int i = (int)i0; i < (int)i1; i++) {
+      int nl = 0, nu = 0;
+      for (int j = rp[i]; j < rp[i + 1]; j++) {
+        nl += ci[j] < i;
+        nu += ci[j] > i;
       }
-      if (c > i) {
-        uc.push_back(c);
-        us.push_back(j);
+      lp[i + 1] = nl;
+      up[i + 1] = nu;
+    }
+  });
+  for (int i = 0; i < n; i++) {
+    lp[i + 1] += lp[i];
+    up[i + 1] += up[i];
+  }
+  lc.resize(lp[n]);
+  ls.resize(lp[n]);
+  uc.resize(up[n]);
+  us.resize(up[n]);
+  host_parallel_for(n, [&](int64_t i0, int64_t i1) {
+    for (int i = (int)i0; i < (int)i1; i++) {
+      int ql = lp[i], qu = up[i];
+      for (int j = rp[i]; j < rp[i + 1]; j++) {
+        const int c = ci[j];
+        if (c < i) {
+          lc[ql] = c;
+          ls[ql++] = j;
+        }
+        if (c > i) {
+          uc[qu] = c;
+          us[qu++] = j;
+        }
       }
     }
-    lp[i + 1] = (int)lc.size();
-    up[i + 1] = (int)uc.size();
-  }
+  });
   std::vector<int> of, ob, fpos, none;
+  setup_mark("triangles");
   GP_TRY(plan(pc->fwd, n, lp, lc, true, s, &of));
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
+  setup_mark("levels");
   GP_TRY(ell_build(pc->ef, ELL_SOR_F, n, true, of, lp, lc, ls, none, none, none, &fpos));
+  setup_mark("fwd-layout");
   GP_TRY(ell_build(pc->eb, ELL_SOR_B, n, false, ob, up, uc, us, fpos, none, none, nullptr));
+  setup_mark("bwd-layout");
   pc->vlen = std::max({n, pc->ef.n, pc->eb.n});
   GP_TRY(dalloc(&pc->t, pc->vlen));
   GP_TRY(dalloc(&pc->yf, pc->vlen));
@@ -665,21 +693,30 @@ static int ilu_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
   std::vector<int> lp(n + 1), lc(P.bj.begin(), P.bj.begin() + P.bi[n]), ls(P.bi[n]);
   for (int i = 0; i <= n; i++) lp[i] = P.bi[i];
   for (int j = 0; j < P.bi[n]; j++) ls[j] = j;
+  // U rows (strict part, stored reversed between bdiag[i + 1] and bdiag[i])
   std::vector<int> up(n + 1, 0), uc, us, dsl(n);
-  uc.reserve(std::max(P.nnz - P.bi[n], 0));
-  for (int i = 0; i < n; i++) {
-    for (int j = P.bdiag[i + 1] + 1; j < P.bdiag[i]; j++) {
-      uc.push_back(P.bj[j]);
-      us.push_back(j);
+  for (int i = 0; i < n; i++) up[i + 1] = up[i] + (P.bdiag[i] - P.bdiag[i + 1] - 1);
+  uc.resize(up[n]);
+  us.resize(up[n]);
+  host_parallel_for(n, [&](int64_t i0, int64_t i1) {
+    for (int i = (int)i0; i < (int)i1; i++) {
+      int q = up[i];
+      for (int j = P.bdiag[i + 1] + 1; j < P.bdiag[i]; j++, q++) {
+        uc[q] = P.bj[j];
+        us[q] = j;
+      }
+      dsl[i] = P.bdiag[i];
     }
-    up[i + 1] = (int)uc.size();
-    dsl[i] = P.bdiag[i];
-  }
+  });
   std::vector<int> of, ob, fpos, none;
+  setup_mark("triangles");
   GP_TRY(plan(pc->fwd, n, lp, lc, true, s, &of));
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
+  setup_mark("levels");
   GP_TRY(ell_build(pc->ef, ELL_ILU_F, n, true, of, lp, lc, ls, P.r, none, none, &fpos));
+  setup_mark("fwd-layout");
   GP_TRY(ell_build(pc->eb, ELL_ILU_B, n, false, ob, up, uc, us, fpos, perm_c, dsl, nullptr));
+  setup_mark("bwd-layout");
   // the numeric phase's update lists (the searches of the elimination, once);
   // kept to the end of the function: the copies below are asynchronous
   std::vector<int> uptr(P.bi[n] + 1, 0), udst, usrc;
@@ -706,20 +743,49 @@ static int ilu_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
       }
       return -1;
     };
-    for (int i = 0; i < n; i++)
-      for (int k = P.bi[i]; k < P.bi[i + 1]; k++) {
-        const int row = P.bj[k];
-        const int pj = P.bdiag[row + 1] + 1;
-        const int nz = P.bdiag[row] - P.bdiag[row + 1] - 1;
-        for (int j = 0; j < nz; j++) {
-          const int d = find(P.bj[pj + j], i);
-          if (d >= 0) {
-            udst.push_back(d);
-            usrc.push_back(pj + j);
-          }
-        }
-        uptr[k + 1] = (int)udst.size();
+    // count the updates of each L slot, then fill them: both passes over
+    // rows on host threads (a row's L slots are its own), the same lists in
+    // the same order as one pass
+    auto each = [&](int i, int k, auto&& hit) {
+      const int row = P.bj[k];
+      const int pj = P.bdiag[row + 1] + 1;
+      const int nz = P.bdiag[row] - P.bdiag[row + 1] - 1;
+      for (int j = 0; j < nz; j++) {
+        const int d = find(P.bj[pj + j], i);
+        if (d >= 0) hit(d, pj + j);
       }
+    };
+    host_parallel_for(n, [&](int64_t i0, int64_t i1) {
+      for (int i = (int)i0; i < (int)i1; i++)
+        for (int k = P.bi[i]; k < P.bi[i + 1]; k++) {
+          int c = 0;
+          each(i, k, [&](int, int) { c++; });
+          uptr[k + 1] = c;
+        }
+    });
+    int64_t tot = 0;
+    for (int k = 0; k < P.bi[n]; k++) {
+      tot += uptr[k + 1];
+      if (tot > INT32_MAX - 1) {
+        set_error("ILU: the factor's update lists are too large for 32-bit indices");
+        return GP_ERR_ARG;
+      }
+      uptr[k + 1] = (int)tot;
+    }
+    udst.resize(tot);
+    usrc.resize(tot);
+    host_parallel_for(n, [&](int64_t i0, int64_t i1) {
+      for (int i = (int)i0; i < (int)i1; i++)
+        for (int k = P.bi[i]; k < P.bi[i + 1]; k++) {
+          int q = uptr[k];
+          each(i, k, [&](int d, int src) {
+            udst[q] = d;
+            usrc[q] = src;
+            q++;
+          });
+        }
+    });
+    setup_mark("update-lists");
     GP_TRY(upload(&pc->upd_ptr, uptr, s));
     GP_TRY(upload(&pc->upd_dst, udst, s));
     GP_TRY(upload(&pc->upd_src, usrc, s));
@@ -745,25 +811,28 @@ static int ilu_amap(Pc* pc, const Csr* A, cudaStream_t s) {
   const int n = A->n;
   const FactorPattern& P = pc->pat;
   std::vector<int> amap(std::max<int64_t>(A->nnz, 1), -1);
-  for (int i = 0; i < n; i++) {
-    const int ri = P.r[i];
-    for (int j = A->h_rowptr[ri]; j < A->h_rowptr[ri + 1]; j++) {
-      const int c = P.ic[A->h_colind[j]];
-      int lo, hi;
-      if (c < i) {
-        lo = P.bi[i];
-        hi = P.bi[i + 1];
-      } else if (c == i) {
-        amap[j] = P.bdiag[i];
-        continue;
-      } else {
-        lo = P.bdiag[i + 1] + 1;
-        hi = P.bdiag[i];
+  // rows are independent: each writes the slots of its own entries
+  host_parallel_for(n, [&](int64_t i0, int64_t i1) {
+    for (int i = (int)i0; i < (int)i1; i++) {
+      const int ri = P.r[i];
+      for (int j = A->h_rowptr[ri]; j < A->h_rowptr[ri + 1]; j++) {
+        const int c = P.ic[A->h_colind[j]];
+        int lo, hi;
+        if (c < i) {
+          lo = P.bi[i];
+          hi = P.bi[i + 1];
+        } else if (c == i) {
+          amap[j] = P.bdiag[i];
+          continue;
+        } else {
+          lo = P.bdiag[i + 1] + 1;
+          hi = P.bdiag[i];
+        }
+        auto it = std::lower_bound(P.bj.begin() + lo, P.bj.begin() + hi, c);
+        if (it != P.bj.begin() + hi && *it == c) amap[j] = (int)(it - P.bj.begin());
       }
-      auto it = std::lower_bound(P.bj.begin() + lo, P.bj.begin() + hi, c);
-      if (it != P.bj.begin() + hi && *it == c) amap[j] = (int)(it - P.bj.begin());
     }
-  }
+  });
   if (pc->amap) cudaFree(pc->amap);
   pc->amap = nullptr;
   GP_TRY(upload(&pc->amap, amap, s));
@@ -775,7 +844,9 @@ static int setup_ilu(Pc* pc, cudaStream_t s) {
   const Csr* A = pc->A;
   std::vector<int> r, ic;
   GP_TRY(perms(pc, r, ic));
+  setup_mark("ordering");
   GP_TRY(ilu_symbolic(A, pc->opt.levels, r, ic, pc->pat));
+  setup_mark("symbolic");
   // the factor lives in the permuted ordering; the solution is mapped back
   // with the row ordering itself (python/mojopetsc4py/PETSc/PC.py:434-437)
   GP_TRY(ilu_prepare(pc, r, s));
@@ -789,14 +860,18 @@ static int setup_ilu(Pc* pc, cudaStream_t s) {
 static int icc_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
   const int n = pc->n;
   FactorPattern& P = pc->pat;
+  // each row's contributors are visited while that row is processed, so
+  // they go straight into the flat lists in row order
   std::vector<int> c2r(n, n), il(n, 0), cptr(n + 1, 0), crow, cslot;
-  std::vector<std::vector<std::pair<int, int>>> visits(n);
+  crow.reserve(std::max(P.nnz - n, 0));
+  cslot.reserve(std::max(P.nnz - n, 0));
   for (int k = 0; k < n; k++) {  // src/ported.mojo:1040-1124 on the pattern alone
     int i = c2r[k];
     while (i < k) {
       const int nexti = c2r[i];
       const int ili = il[i];
-      visits[k].emplace_back(i, ili);
+      crow.push_back(i);
+      cslot.push_back(ili);
       const int jmin = ili + 1, jmax = P.bi[i + 1];
       if (jmin < jmax) {
         il[i] = jmin;
@@ -812,12 +887,6 @@ static int icc_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
       const int cj = P.bj[jmin];
       c2r[k] = c2r[cj];
       c2r[cj] = k;
-    }
-  }
-  for (int k = 0; k < n; k++) {
-    for (auto& v : visits[k]) {
-      crow.push_back(v.first);
-      cslot.push_back(v.second);
     }
     cptr[k + 1] = (int)crow.size();
   }
@@ -847,11 +916,15 @@ static int icc_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
     dsl[i] = P.bdiag[i];
   }
   std::vector<int> of, ob, fpos, none;
+  setup_mark("chains-transpose");
   GP_TRY(plan(pc->num, n, cptr, crow, true, s));
   GP_TRY(plan(pc->fwd, n, tptr, trow_deps, true, s, &of));
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
+  setup_mark("levels");
   GP_TRY(ell_build(pc->ef, ELL_ICC_F, n, true, of, tptr, trow_deps, tsl, perm_c, none, dsl, &fpos));
+  setup_mark("fwd-layout");
   GP_TRY(ell_build(pc->eb, ELL_ICC_B, n, false, ob, up, uc, us, fpos, perm_c, none, nullptr));
+  setup_mark("bwd-layout");
   GP_TRY(upload(&pc->bi, P.bi, s));
   GP_TRY(upload(&pc->bj, P.bj, s));
   GP_TRY(upload(&pc->bdiag, P.bdiag, s));
@@ -880,19 +953,21 @@ static int icc_amap(Pc* pc, const Csr* A, cudaStream_t s) {
   const int n = A->n;
   const FactorPattern& P = pc->pat;
   std::vector<int> amap(std::max<int64_t>(A->nnz, 1), -1);
-  for (int k = 0; k < n; k++) {
-    const int rk = P.r[k];
-    for (int j = A->h_rowptr[rk]; j < A->h_rowptr[rk + 1]; j++) {
-      const int c = P.ic[A->h_colind[j]];
-      if (c < k) continue;
-      if (c == k) {
-        amap[j] = P.bdiag[k];
-        continue;
+  host_parallel_for(n, [&](int64_t k0, int64_t k1) {
+    for (int k = (int)k0; k < (int)k1; k++) {
+      const int rk = P.r[k];
+      for (int j = A->h_rowptr[rk]; j < A->h_rowptr[rk + 1]; j++) {
+        const int c = P.ic[A->h_colind[j]];
+        if (c < k) continue;
+        if (c == k) {
+          amap[j] = P.bdiag[k];
+          continue;
+        }
+        auto it = std::lower_bound(P.bj.begin() + P.bi[k], P.bj.begin() + P.bdiag[k], c);
+        if (it != P.bj.begin() + P.bdiag[k] && *it == c) amap[j] = (int)(it - P.bj.begin());
       }
-      auto it = std::lower_bound(P.bj.begin() + P.bi[k], P.bj.begin() + P.bdiag[k], c);
-      if (it != P.bj.begin() + P.bdiag[k] && *it == c) amap[j] = (int)(it - P.bj.begin());
     }
-  }
+  });
   if (pc->amap) cudaFree(pc->amap);
   pc->amap = nullptr;
   GP_TRY(upload(&pc->amap, amap, s));
@@ -904,7 +979,9 @@ static int setup_icc(Pc* pc, cudaStream_t s) {
   const Csr* A = pc->A;
   std::vector<int> r, ic;
   GP_TRY(perms(pc, r, ic));
+  setup_mark("ordering");
   GP_TRY(icc_symbolic(A, pc->opt.levels, r, ic, pc->pat));
+  setup_mark("symbolic");
   GP_TRY(icc_prepare(pc, r, s));
   return icc_amap(pc, A, s);
 }
@@ -976,6 +1053,7 @@ int pc_values_sync(Pc* pc, cudaStream_t s) {
 }
 
 int pc_setup(Pc* pc, Csr* A, cudaStream_t s) {
+  setup_report("(before)");
   free_all(pc);
   pc->generation = next_uid();
   pc->A = A;
@@ -1006,14 +1084,25 @@ int pc_setup(Pc* pc, Csr* A, cudaStream_t s) {
         GP_CHECK_LAUNCH();
       }
       break;
-    case PC_SOR: GP_TRY(setup_sor(pc, s)); break;
+    case PC_SOR:
+      GP_TRY(setup_sor(pc, s));
+      GP_CUDA(cudaStreamSynchronize(s));
+      setup_mark("rest");
+      setup_report("sor");
+      break;
     case PC_ILU:
       GP_TRY(setup_ilu(pc, s));
+      setup_mark("amap");
       GP_TRY(pc_factor_numeric(pc, s));
+      setup_mark("numeric");
+      setup_report("ilu");
       break;
     case PC_ICC:
       GP_TRY(setup_icc(pc, s));
+      setup_mark("amap");
       GP_TRY(pc_factor_numeric(pc, s));
+      setup_mark("numeric");
+      setup_report("icc");
       break;
     default: set_error("unsupported PC type"); return GP_ERR_UNSUPPORTED;
   }

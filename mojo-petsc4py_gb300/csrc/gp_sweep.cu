@@ -777,7 +777,7 @@ static bool tile_choose(int mode, int n, int W, const std::vector<int>& dptr,
     ok[c] = 1;
   };
   const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-  const int nthreads = std::min({nc, hw, 8, n >= (1 << 16) ? nc : 1});
+  const int nthreads = std::min({nc, hw, 16, n >= (1 << 16) ? nc : 1});
   if (nthreads <= 1) {
     for (int c = 0; c < nc; c++) eval(c);
   } else {
@@ -935,6 +935,7 @@ static int ell_build_impl(EllSweep& e, int mode, int n, bool forward,
   if (tu.tiles && allow_tiles && n > 0) {
     nlev = sweep_levels(n, dptr, dcol, forward);
     tiled = tile_choose(mode, n, W, dptr, dcol, forward, nlev, tu, tp, &considered);
+    setup_mark("chunk-model");
   }
   if (allow_tiles && allow_bricks && n > 0) {
     // the brick form, where the sweep is a grid in natural order and the
@@ -945,6 +946,7 @@ static int ell_build_impl(EllSweep& e, int mode, int n, bool forward,
     bool built = false;
     GP_TRY(brick_build(e, mode, n, forward, dptr, dcol, dsl, in_row, out_row, dslot_row, other,
                        &built, pos_of_row));
+    setup_mark("brick-check");
     if (built) return GP_OK;
   }
   const std::vector<int>& order = tiled ? tp.order : order_in;
@@ -953,18 +955,22 @@ static int ell_build_impl(EllSweep& e, int mode, int n, bool forward,
   const int Wc = std::max(W, 1);
   std::vector<int> cnt(n), dep((size_t)Wc * n, 0), cs((size_t)Wc * n, 0), rowof(n);
   std::vector<int> in(n, 0), out(n, -1), ds(n, 0);
-  for (int p = 0; p < n; p++) {
-    const int i = order[p];
-    rowof[p] = i;
-    cnt[p] = dptr[i + 1] - dptr[i];
-    for (int q = 0; q < cnt[p]; q++) {
-      dep[(size_t)q * n + p] = pos[dcol[dptr[i] + q]];
-      cs[(size_t)q * n + p] = dsl[dptr[i] + q];
+  // positions are independent: host threads fill ranges of them
+  host_parallel_for(n, [&](int64_t p0, int64_t p1) {
+    for (int p = (int)p0; p < (int)p1; p++) {
+      const int i = order[p];
+      rowof[p] = i;
+      cnt[p] = dptr[i + 1] - dptr[i];
+      for (int q = 0; q < cnt[p]; q++) {
+        dep[(size_t)q * n + p] = pos[dcol[dptr[i] + q]];
+        cs[(size_t)q * n + p] = dsl[dptr[i] + q];
+      }
+      if (!in_row.empty()) in[p] = in_row[i];
+      if (!out_row.empty()) out[p] = out_row[i];
+      if (!dslot_row.empty()) ds[p] = dslot_row[i];
     }
-    if (!in_row.empty()) in[p] = in_row[i];
-    if (!out_row.empty()) out[p] = out_row[i];
-    if (!dslot_row.empty()) ds[p] = dslot_row[i];
-  }
+  });
+  setup_mark("layout");
   if (tiled) {
     int st = tile_upload(e, mode, tp, W, cnt, dep, cs, in, out, ds, !dslot_row.empty(), rowof);
     int bps = 0;

@@ -1,5 +1,7 @@
 // Library-wide utilities: error text, device properties, standalone scratch.
 #include <atomic>
+#include <chrono>
+#include <cstdio>
 #include <cstdlib>
 #include <mutex>
 #include <string>
@@ -83,6 +85,39 @@ int scratch_get(Scratch** out, int64_t need_grid) {
   }
   *out = &sc;
   return GP_OK;
+}
+
+namespace {
+struct SetupClock {
+  bool on = std::getenv("GPETSC_SETUP_TIMING") != nullptr;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now(), last = t0;
+  std::string log;
+};
+SetupClock& setup_clock() {
+  static thread_local SetupClock c;
+  return c;
+}
+}  // namespace
+
+void setup_mark(const char* phase) {
+  SetupClock& c = setup_clock();
+  if (!c.on) return;
+  const auto t = std::chrono::steady_clock::now();
+  char buf[96];
+  std::snprintf(buf, sizeof buf, " %s %.1f", phase,
+                std::chrono::duration<double, std::milli>(t - c.last).count());
+  c.log += buf;
+  c.last = t;
+}
+
+void setup_report(const char* what) {
+  SetupClock& c = setup_clock();
+  if (!c.on) return;
+  const auto t = std::chrono::steady_clock::now();
+  std::fprintf(stderr, "gpetsc setup %s (ms):%s; total %.1f\n", what, c.log.c_str(),
+               std::chrono::duration<double, std::milli>(t - c.t0).count());
+  c.log.clear();
+  c.t0 = c.last = t;
 }
 
 }  // namespace gp
