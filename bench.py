@@ -10,9 +10,10 @@ is larger than the 129 MB L2, so consecutive solves stream it from HBM.
   e2e     the same solve through the public API with host arrays: the step
           uploads b from host memory, solves, and reads x back
   roofline  the SpMV kernel, timed with CUDA events over 20 back-to-back
-          launches after a 512 MB read (the 217 MB matrix is larger than L2,
-          so every launch streams it from HBM), algorithmic bytes
-          12 nnz + 4 (n+1) + 16 n per launch
+          launches after a 512 MB read (the matrix, 188 MB with its 16-bit
+          column offsets, is larger than L2, so every launch streams it from
+          HBM), algorithmic bytes (8 + c) nnz + 4 (n+1) + 16 n per launch, c
+          the column bytes the kernel reads (2 or 4)
   cpu_baseline  the CPU oracle (a single-threaded restatement of the
           reference's algorithm) on the same system: one whole solve, timed
 
@@ -346,8 +347,21 @@ def spmv_roofline(torch, PETSc, A, n, nnz, launches=20):
     e1.record()
     torch.cuda.synchronize()
     t = e0.elapsed_time(e1) * 1e-3 / launches
-    algo = 12 * nnz + 4 * (n + 1) + 8 * n + 8 * n
-    return algo, t, ctypes
+    ib = spmv_index_bytes(h)
+    algo = (8 + ib) * nnz + 4 * (n + 1) + 8 * n + 8 * n
+    return algo, t, ib
+
+
+def spmv_index_bytes(h):
+    """Column bytes the SpMV reads per entry: 2 (row-relative 16-bit offsets)
+    or 4 (32-bit indices)."""
+    import ctypes
+
+    from mojopetsc4py._lib import check, lib
+
+    b = ctypes.c_int32()
+    check(lib().gp_mat_spmv_index_bytes(h, ctypes.byref(b)))
+    return b.value
 
 
 def run_spmv_only(args):
@@ -414,7 +428,7 @@ def run_ours(args, world, rank, local, pg):
     resid = float(np.linalg.norm(b - _csr_matvec(ip, ix, v, xh)) / np.linalg.norm(b))
 
     # ---- SpMV roofline (kernel alone, L2 flushed before each launch)
-    algo, t_spmv, _ = spmv_roofline(torch, PETSc, A, n, nnz)
+    algo, t_spmv, spmv_ib = spmv_roofline(torch, PETSc, A, n, nnz)
     peak, peak_kind = peaks()
     achieved = algo / t_spmv / 1e9
     traffic = profiled_traffic("spmv_fp64_poisson3d_128.md")
@@ -520,7 +534,10 @@ def run_ours(args, world, rank, local, pg):
                 "d2h_bytes_per_step": 8 * n + 1024},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": traffic, "kernel": "k_spmv (CSR fp64/int32)",
+                     "traffic": traffic,
+                     "kernel": "k_spmv (CSR fp64, int32 row pointers, "
+                               + ("16-bit row-relative column offsets)" if spmv_ib == 2
+                                  else "int32 columns)"),
                      "algorithmic_bytes": algo, "launch_us": round(t_spmv * 1e6, 2),
                      "peak_kind": f"{peak_kind} hbm_gbs"},
         "cpu_baseline": cpu,
@@ -946,11 +963,11 @@ def form_bandwidth(torch, PETSc):
         pc.setOperators(A)
         pc.setUp()
         h, xp, yp, hp = A._device(), xv._dptr(), yv._optr(), pc._handle()
-        mb = 12 * nnz + 4 * (n + 1) + 16 * n
+        mb = (8 + spmv_index_bytes(h)) * nnz + 4 * (n + 1) + 16 * n
         mats[f"{k}^3"] = {
             "n": n, "nnz": nnz,
             "spmv": entry(mb, nnz, lambda: check(L.gp_mat_mult(h, xp, yp, st))),
-            "spmv_transpose": entry(mb, nnz, lambda: check(
+            "spmv_transpose": entry(12 * nnz + 4 * (n + 1) + 16 * n, nnz, lambda: check(
                 L.gp_mat_mult_transpose(h, xp, yp, st))),
             "jacobi_apply": entry(24 * n, n, lambda: check(L.gp_pc_apply(hp, xp, yp, st)))}
         del A, xv, yv, pc
@@ -959,7 +976,8 @@ def form_bandwidth(torch, PETSc):
             "timing": f"cold: one launch between CUDA events after a 512 MB read, median of "
                       f"{reps}; stream: mean of {burst} back-to-back launches (launches moving "
                       "more than L2); algorithmic bytes = 8 per vector operand and element, "
-                      "SpMV 12 nnz + 4 (n+1) + 16 n, Jacobi 24 n",
+                      "SpMV (8 + column bytes) nnz + 4 (n+1) + 16 n (column bytes 2 with "
+                      "16-bit offsets, 4 with 32-bit indices; A^T keeps 4), Jacobi 24 n",
             "vec": vec, "sparse": mats}
 
 

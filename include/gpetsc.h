@@ -123,6 +123,12 @@ int gp_mat_set_values(gp_mat A, const double *values, int on_device, void *strea
  * their next use. */
 int gp_mat_values_ptr(gp_mat A, double **d_values);
 int gp_mat_info(gp_mat A, int64_t *nrows, int64_t *ncols, int64_t *nnz);
+/* Bytes of column data the SpMV reads per stored entry: 2 where the matrix
+ * takes the row-per-thread form and every |column - row| fits 16 bits (the
+ * kernels then read row-relative 16-bit offsets, made at creation), else 4
+ * (32-bit column indices).  Either way each row is summed in the same order
+ * with the same operations.  No counterpart in the reference. */
+int gp_mat_spmv_index_bytes(gp_mat A, int32_t *bytes);
 /* y = A x.        Replaces MatMult_SeqAIJ (src/ported.mojo:380-391). */
 int gp_mat_mult(gp_mat A, const double *x, double *y, void *stream);
 /* y = A x + v.    Replaces MatMultAdd_SeqAIJ (src/ported.mojo:394-405). */

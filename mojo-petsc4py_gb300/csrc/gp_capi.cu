@@ -113,6 +113,12 @@ int gp_mat_info(gp_mat A, int64_t* nrows, int64_t* ncols, int64_t* nnz) {
   return GP_OK;
 }
 
+int gp_mat_spmv_index_bytes(gp_mat A, int32_t* bytes) {
+  if (!A || !bytes) return bad("gp_mat_spmv_index_bytes: null argument");
+  *bytes = A->A->coff16 ? 2 : 4;
+  return GP_OK;
+}
+
 int gp_mat_mult(gp_mat A, const double* x, double* y, void* stream) {
   if (!A || !x || !y) return bad("gp_mat_mult: null argument");
   if (x == y) return bad("gp_mat_mult: y may not alias x");

@@ -115,6 +115,10 @@ struct Csr {
   int* diagpos = nullptr;    // device, n: slot of a_ii or -1
   bool stream_rows = false;  // SpMV form: false row per thread, true row stream
   int l2_evict_first = 1;    // row form: matrix loads marked L2 evict-first
+  // row form: each slot's column as an offset from its row (col - row), when
+  // every offset fits 16 bits; the row kernels then read 2 bytes an entry
+  // instead of 4 (null: they read colind)
+  short* coff16 = nullptr;
   // transpose (built on demand): rows of A^T in ascending original row order
   int* t_rowptr = nullptr;
   int* t_colind = nullptr;

@@ -573,10 +573,10 @@ __global__ void k_cgf_p(KspState* st, int n, double* __restrict__ p,
   }
 }
 
-template <bool FMA, bool STREAM>
+template <bool FMA, bool STREAM, typename CT = int>
 __global__ void __launch_bounds__(kSpmvRows) k_cgf_spmv(KspState* st, int n,
                                                         const int* __restrict__ rowptr,
-                                                        const int* __restrict__ colind,
+                                                        const CT* __restrict__ colind,
                                                         const double* __restrict__ val,
                                                         const double* __restrict__ p,
                                                         double* __restrict__ w, RedSlot slot,
@@ -1447,13 +1447,21 @@ static int cg_body_fused(const Run& r, double* x) {
                      k->st, n, P, (const double*)Z));
   {
     const bool f = arith_mode() == kFma;
-    auto ks = A->stream_rows ? (f ? k_cgf_spmv<true, true> : k_cgf_spmv<false, true>)
-                             : (f ? k_cgf_spmv<true, false> : k_cgf_spmv<false, false>);
-    int grid = spmv_grid(A);
-    if (!A->stream_rows) grid = std::min(grid, resident_grid((const void*)ks, kSpmvRows));
-    GP_CUDA(launch_pdl(ks, grid, kSpmvRows, r.s, k->st, n, (const int*)A->rowptr,
-                       (const int*)A->colind, (const double*)A->val, (const double*)P, W,
-                       k->slot, A->l2_evict_first));
+    if (A->coff16) {  // row form with 16-bit column offsets
+      auto ks = f ? k_cgf_spmv<true, false, short> : k_cgf_spmv<false, false, short>;
+      const int grid = std::min(spmv_grid(A), resident_grid((const void*)ks, kSpmvRows));
+      GP_CUDA(launch_pdl(ks, grid, kSpmvRows, r.s, k->st, n, (const int*)A->rowptr,
+                         (const short*)A->coff16, (const double*)A->val, (const double*)P, W,
+                         k->slot, A->l2_evict_first));
+    } else {
+      auto ks = A->stream_rows ? (f ? k_cgf_spmv<true, true> : k_cgf_spmv<false, true>)
+                               : (f ? k_cgf_spmv<true, false> : k_cgf_spmv<false, false>);
+      int grid = spmv_grid(A);
+      if (!A->stream_rows) grid = std::min(grid, resident_grid((const void*)ks, kSpmvRows));
+      GP_CUDA(launch_pdl(ks, grid, kSpmvRows, r.s, k->st, n, (const int*)A->rowptr,
+                         (const int*)A->colind, (const double*)A->val, (const double*)P, W,
+                         k->slot, A->l2_evict_first));
+    }
   }
   const bool jac = r.pc->opt.type == PC_JACOBI;
   const bool f = arith_mode() == kFma;

@@ -15,6 +15,7 @@
 // A's values, so the multiply streams them like any CSR matrix.
 #include <algorithm>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "gp_internal.h"
@@ -52,6 +53,14 @@ static int dev_upload(T** d, const T* h, size_t count, cudaStream_t s) {
   return GP_OK;
 }
 
+static bool spmv_coff16_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("GPETSC_SPMV_COFF16");
+    return !(e && std::string(e) == "0");
+  }();
+  return on;
+}
+
 static int csr_finish(Csr* A, const double* h_val, cudaStream_t s) {
   const int n = A->n;
   std::vector<int> diag(std::max(n, 1), -1);
@@ -69,8 +78,29 @@ static int csr_finish(Csr* A, const double* h_val, cudaStream_t s) {
   const double avg = n ? (double)A->nnz / n : 0.0;
   A->stream_rows = maxlen > kSpmvMaxRowLen || (double)maxlen > 8.0 * avg + 8.0;
   A->l2_evict_first = spmv_evict_first(n, A->nnz);
+  // 16-bit column offsets for the row form when every |col - row| fits
+  // (banded and stencil operators); GPETSC_SPMV_COFF16=0 keeps 32-bit columns
+  std::vector<short> coff;
+  if (!A->stream_rows && A->nnz > 0 && spmv_coff16_enabled()) {
+    bool fits = true;
+    for (int i = 0; i < n && fits; i++)
+      for (int j = A->h_rowptr[i]; j < A->h_rowptr[i + 1]; j++) {
+        const int d = A->h_colind[j] - i;
+        if (d < -32768 || d > 32767) {
+          fits = false;
+          break;
+        }
+      }
+    if (fits) {
+      coff.resize(A->nnz);
+      for (int i = 0; i < n; i++)
+        for (int j = A->h_rowptr[i]; j < A->h_rowptr[i + 1]; j++)
+          coff[j] = (short)(A->h_colind[j] - i);
+    }
+  }
   GP_TRY(dev_upload(&A->rowptr, A->h_rowptr.data(), (size_t)n + 1, s));
   GP_TRY(dev_upload(&A->colind, A->h_colind.data(), (size_t)A->nnz, s));
+  if (!coff.empty()) GP_TRY(dev_upload(&A->coff16, coff.data(), coff.size(), s));
   GP_TRY(dev_upload(&A->val, h_val, (size_t)A->nnz, s));
   GP_TRY(dev_upload(&A->diagpos, diag.data(), (size_t)n, s));
   // the host staging vectors must stay alive until the copies land
@@ -170,6 +200,7 @@ int csr_destroy(Csr* A) {
   if (!A) return GP_OK;
   cudaFree(A->rowptr);
   cudaFree(A->colind);
+  cudaFree(A->coff16);
   cudaFree(A->val);
   cudaFree(A->val32);
   cudaFree(A->diagpos);
@@ -275,9 +306,9 @@ int csr_make_val32(Csr* A, cudaStream_t s) {
 
 // y = A x, or y = v + A x when v is given (MatMultAdd starts each row's sum
 // from v_i).  Optional gate for use inside captured solver loops.
-template <bool FMA, bool STREAM>
+template <bool FMA, bool STREAM, typename CT = int>
 __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict__ rowptr,
-                                                    const int* __restrict__ colind,
+                                                    const CT* __restrict__ colind,
                                                     const double* __restrict__ val, DRef xr,
                                                     const double* __restrict__ v, DRef yr,
                                                     const int* gate, int want, int evict_first) {
@@ -292,6 +323,7 @@ __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict
       y[row] = spmv_row<FMA>(row, rowptr, colind, val, x, init, spmv_policy(evict_first));
     return;
   }
+  else {
   double s;
   if constexpr (FMA) {
     __shared__ SpmvSmemF<double, double, double> sm;
@@ -301,11 +333,18 @@ __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict
     s = spmv_block_rows<double, double, double>(sm, n, r0, rowptr, colind, val, x, init);
   }
   if (row < n) y[row] = s;
+  }
 }
 
 static void launch_spmv(cudaStream_t s, const Csr* A, DRef x, const double* v, DRef y,
                         const int* gate, int want) {
   const bool f = arith_mode() == kFma;
+  if (A->coff16) {  // row form with 16-bit column offsets
+    auto k = f ? k_spmv<true, false, short> : k_spmv<false, false, short>;
+    k<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->coff16, A->val, x, v, y, gate,
+                                         want, A->l2_evict_first);
+    return;
+  }
   auto k = A->stream_rows ? (f ? k_spmv<true, true> : k_spmv<false, true>)
                           : (f ? k_spmv<true, false> : k_spmv<false, false>);
   k<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, v, y, gate, want,

@@ -63,11 +63,27 @@ __device__ __forceinline__ int ld_stream(const int* a, uint64_t pol) {
   asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
   return v;
 }
+__device__ __forceinline__ short ld_stream(const short* a, uint64_t pol) {
+  unsigned short v;
+  asm volatile("ld.global.nc.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(a), "l"(pol));
+  return (short)v;
+}
 
-// Row `row`'s sum, starting from `init` (caller checks row < n).
-template <bool FMA, typename VT, typename XT>
+// A slot's column in the row form: a 32-bit column index, or a 16-bit offset
+// from the row (Csr::coff16).
+__device__ __forceinline__ int spmv_col(const int* c, int j, int row, uint64_t pol) {
+  (void)row;
+  return ld_stream(c + j, pol);
+}
+__device__ __forceinline__ int spmv_col(const short* c, int j, int row, uint64_t pol) {
+  return row + (int)ld_stream(c + j, pol);
+}
+
+// Row `row`'s sum, starting from `init` (caller checks row < n).  CT: int
+// (column indices) or short (offsets from the row).
+template <bool FMA, typename VT, typename XT, typename CT>
 __device__ __forceinline__ double spmv_row(int row, const int* __restrict__ rowptr,
-                                           const int* __restrict__ colind,
+                                           const CT* __restrict__ colind,
                                            const VT* __restrict__ val, const XT* __restrict__ x,
                                            double init, uint64_t pol) {
   const int b = rowptr[row], e = rowptr[row + 1];
@@ -80,7 +96,7 @@ __device__ __forceinline__ double spmv_row(int row, const int* __restrict__ rowp
 #pragma unroll
     for (int u = 0; u < 4; u++)
       if (j0 + u < e) {
-        cc[u] = ld_stream(colind + j0 + u, pol);
+        cc[u] = spmv_col(colind, j0 + u, row, pol);
         vv[u] = (double)ld_stream(val + j0 + u, pol);
       }
 #pragma unroll
@@ -94,34 +110,35 @@ __device__ __forceinline__ double spmv_row(int row, const int* __restrict__ rowp
 // (spmv_row_preload), and the row's sum from there (spmv_row_from): the same
 // loads and the same fold as spmv_row.
 struct SpmvPre {
-  int j, e;
+  int row, j, e;
   int cc[4];
   double vv[4];
 };
 
-template <typename VT>
+template <typename VT, typename CT>
 __device__ __forceinline__ void spmv_row_preload(int row, const int* __restrict__ rowptr,
-                                                 const int* __restrict__ colind,
+                                                 const CT* __restrict__ colind,
                                                  const VT* __restrict__ val, uint64_t pol,
                                                  SpmvPre& pre) {
+  pre.row = row;
   pre.j = rowptr[row];
   pre.e = rowptr[row + 1];
 #pragma unroll
   for (int u = 0; u < 4; u++)
     if (pre.j + u < pre.e) {
-      pre.cc[u] = ld_stream(colind + pre.j + u, pol);
+      pre.cc[u] = spmv_col(colind, pre.j + u, row, pol);
       pre.vv[u] = (double)ld_stream(val + pre.j + u, pol);
     }
 }
 
-template <bool FMA, typename VT, typename XT>
+template <bool FMA, typename VT, typename XT, typename CT>
 __device__ __forceinline__ double spmv_row_from(const SpmvPre& pre,
-                                                const int* __restrict__ colind,
+                                                const CT* __restrict__ colind,
                                                 const VT* __restrict__ val,
                                                 const XT* __restrict__ x, double init,
                                                 uint64_t pol) {
   double acc = init;
-  const int b = pre.j, e = pre.e;
+  const int b = pre.j, e = pre.e, row = pre.row;
 #pragma unroll
   for (int u = 0; u < 4; u++)
     if (b + u < e) acc = madd<FMA>(pre.vv[u], (double)x[pre.cc[u]], acc);
@@ -131,7 +148,7 @@ __device__ __forceinline__ double spmv_row_from(const SpmvPre& pre,
 #pragma unroll
     for (int u = 0; u < 4; u++)
       if (j0 + u < e) {
-        cc[u] = ld_stream(colind + j0 + u, pol);
+        cc[u] = spmv_col(colind, j0 + u, row, pol);
         vv[u] = (double)ld_stream(val + j0 + u, pol);
       }
 #pragma unroll

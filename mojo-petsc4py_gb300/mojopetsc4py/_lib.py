@@ -93,6 +93,7 @@ GP_SIGNATURES = {
     "gp_mat_set_values": ([P, P, ctypes.c_int, P], ctypes.c_int),
     "gp_mat_values_ptr": ([P, PP], ctypes.c_int),
     "gp_mat_info": ([P, P, P, P], ctypes.c_int),
+    "gp_mat_spmv_index_bytes": ([P, P], ctypes.c_int),
     "gp_mat_mult": ([P, P, P, P], ctypes.c_int),
     "gp_mat_mult_add": ([P, P, P, P, P], ctypes.c_int),
     "gp_mat_mult_transpose": ([P, P, P, P], ctypes.c_int),

@@ -66,6 +66,81 @@ def test_spmv_bit_exact(name):
     np.testing.assert_array_equal(d, want4)
 
 
+def _index_bytes(A):
+    import ctypes
+
+    from mojopetsc4py._lib import check, lib
+
+    b = ctypes.c_int32()
+    check(lib().gp_mat_spmv_index_bytes(A._device(), ctypes.byref(b)))
+    return b.value
+
+
+@pytest.mark.parametrize("far", [False, True])
+def test_spmv_column_offsets_of_16_bits_and_wide_bands(far):
+    """Row-form matrices whose every |column - row| fits 16 bits are read
+    through row-relative 16-bit offsets; one entry 40000 columns away keeps
+    32-bit columns.  Both give the oracle's products bit for bit, in the
+    standalone multiply and inside a fused CG solve."""
+    ip, ix, v = gallery.laplacian_3d(36)  # n = 46656: offsets up to 1296
+    n = len(ip) - 1
+    if far:
+        # add a symmetric pair (0, 40000) / (40000, 0) with a small value
+        rows = [list(ix[ip[i]:ip[i + 1]]) for i in range(n)]
+        vals = [list(v[ip[i]:ip[i + 1]]) for i in range(n)]
+        for r, c in ((0, 40000), (40000, 0)):
+            k = int(np.searchsorted(rows[r], c))
+            rows[r].insert(k, c)
+            vals[r].insert(k, -1e-3)
+        ip = np.zeros(n + 1, np.int32)
+        ip[1:] = np.cumsum([len(r) for r in rows])
+        ix = np.concatenate(rows).astype(np.int32)
+        v = np.concatenate(vals)
+    A = mat(ip, ix, v)
+    assert _index_bytes(A) == (4 if far else 2)
+    x = np.random.default_rng(4).normal(size=n)
+    y = A.mult(vec(x)).getArray()
+    want = np.zeros(n)
+    ip64, ix64 = O.i64(ip), O.i64(ix)  # kept alive across the call
+    O.lib().mp_mat_mult(a(x), a(want), a(ip64), a(ix64), a(v), n)
+    np.testing.assert_array_equal(y, want)
+    b = np.random.default_rng(5).uniform(-1, 1, n)
+    ksp = PETSc.KSP().create()
+    ksp.setType("cg")
+    ksp.getPC().setType("jacobi")
+    ksp.setOperators(A)
+    ksp.setTolerances(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=2000)
+    xv = PETSc.Vec().createSeq(n)
+    ksp.solve(vec(b), xv)
+    ref = O.solve("cg", ip, ix, v, b, pc_type="jacobi", rtol=1e-10, atol=1e-50, divtol=1e30,
+                  max_it=2000)
+    assert ksp.getIterationNumber() == ref["its"]
+    np.testing.assert_array_equal(xv.getArray(), ref["x"])
+
+
+@pytest.mark.fma
+def test_fused_cg_reads_16_bit_column_offsets():
+    """The fused CG's SpMV (the timed path) on a matrix with 16-bit column
+    offsets: the oracle's iteration count and reason, iterate within 1e-10."""
+    ip, ix, v = gallery.laplacian_3d(36)
+    n = len(ip) - 1
+    A = mat(ip, ix, v)
+    assert _index_bytes(A) == 2
+    b = np.random.default_rng(6).uniform(-1, 1, n)
+    ksp = PETSc.KSP().create()
+    ksp.setType("cg")
+    ksp.getPC().setType("jacobi")
+    ksp.setOperators(A)
+    ksp.setTolerances(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=2000)
+    xv = PETSc.Vec().createSeq(n)
+    ksp.solve(vec(b), xv)
+    ref = O.solve("cg", ip, ix, v, b, pc_type="jacobi", rtol=1e-10, atol=1e-50, divtol=1e30,
+                  max_it=2000)
+    assert (ksp.getIterationNumber(), ksp.getConvergedReason()) == (ref["its"], ref["reason"])
+    rel = np.linalg.norm(xv.getArray() - ref["x"]) / np.linalg.norm(ref["x"])
+    assert rel <= 1e-10, rel
+
+
 def test_spmv_rectangular_and_long_rows():
     rng = np.random.default_rng(3)
     d = rng.normal(size=(300, 5000)) * (rng.random((300, 5000)) < 0.6)
