@@ -971,6 +971,21 @@ def form_bandwidth(torch, PETSc):
                 L.gp_mat_mult_transpose(h, xp, yp, st))),
             "jacobi_apply": entry(24 * n, n, lambda: check(L.gp_pc_apply(hp, xp, yp, st)))}
         del A, xv, yv, pc
+    # skewed rows: a path graph with 8 hub rows of ~100k entries (row stream;
+    # in the FMA arithmetic the hubs are summed by segments of 2048 slots)
+    ip, ix, v = gallery.hub_laplacian(1 << 20, 8, 100_000)
+    n, nnz = len(ip) - 1, int(ip[-1])
+    A = PETSc.Mat().createSeqAIJ((n, n))
+    A.setValuesCSR(ip, ix, v)
+    A.assemble()
+    xv = PETSc.Vec().createWithArray(np.random.default_rng(3).normal(size=n))
+    yv = PETSc.Vec().createSeq(n)
+    h, xp, yp = A._device(), xv._dptr(), yv._optr()
+    mats["hubs_2^20"] = {
+        "n": n, "nnz": nnz, "longest_row": int(np.diff(ip).max()),
+        "spmv": entry(12 * nnz + 4 * (n + 1) + 16 * n, nnz,
+                      lambda: check(L.gp_mat_mult(h, xp, yp, st)))}
+    del A, xv, yv
     return {"peak_gbs": peak, "peak_kind": f"{kind} hbm_gbs",
             "fp64_ops_per_s": FP64_OPS_PER_S,
             "timing": f"cold: one launch between CUDA events after a 512 MB read, median of "

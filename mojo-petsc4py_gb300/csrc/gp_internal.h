@@ -119,6 +119,17 @@ struct Csr {
   // every offset fits 16 bits; the row kernels then read 2 bytes an entry
   // instead of 4 (null: they read colind)
   short* coff16 = nullptr;
+  // row-stream form, FMA arithmetic: rows longer than kSpmvLongRow slots are
+  // summed by segments of kSpmvLongSeg slots, one CTA a segment, instead of by
+  // one thread (long_rows ascending; each long row's segments are
+  // long_seg[i] .. long_seg[i + 1] - 1; seg_part holds the segment sums and
+  // long_ticket counts a row's finished segments)
+  int nlong = 0, nseg = 0;
+  int* long_rows = nullptr;
+  int* long_seg = nullptr;
+  int* seg_long = nullptr;       // [nseg] index into long_rows
+  double* seg_part = nullptr;    // [nseg]
+  unsigned* long_ticket = nullptr;  // [nlong]
   // transpose (built on demand): rows of A^T in ascending original row order
   int* t_rowptr = nullptr;
   int* t_colind = nullptr;

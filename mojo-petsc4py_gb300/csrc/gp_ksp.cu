@@ -1413,8 +1413,10 @@ static bool cg_fused_ok(const Run& r) {
   const KspOptions& o = r.k->opt;
   // the fused kernels sum their dots inside the vector passes (tree order)
   // and multiply by A itself
+  // (a matrix whose long rows are summed by segments multiplies through
+  // spmv(), which runs the segment kernel: the general loop)
   return arith_mode() != kOrdered && !r.k->transpose && o.normtype == N_PRECOND &&
-         o.chknorm <= 1 &&
+         o.chknorm <= 1 && r.A->nlong == 0 &&
          (int64_t)spmv_grid(r.A) <= (int64_t)kMaxBasis * kMaxRedGrid;
 }
 

@@ -14,6 +14,7 @@
 // of A^T are gathered through the source slots into a copy once per change of
 // A's values, so the multiply streams them like any CSR matrix.
 #include <algorithm>
+#include <climits>
 #include <cstdlib>
 #include <string>
 #include <vector>
@@ -51,6 +52,14 @@ static int dev_upload(T** d, const T* h, size_t count, cudaStream_t s) {
   GP_CUDA(cudaMalloc(d, std::max<size_t>(count, 1) * sizeof(T)));
   if (count) GP_CUDA(cudaMemcpyAsync(*d, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
   return GP_OK;
+}
+
+static bool spmv_split_long_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("GPETSC_SPMV_SPLIT_LONG");
+    return !(e && std::string(e) == "0");
+  }();
+  return on;
 }
 
 static bool spmv_coff16_enabled() {
@@ -98,9 +107,33 @@ static int csr_finish(Csr* A, const double* h_val, cudaStream_t s) {
           coff[j] = (short)(A->h_colind[j] - i);
     }
   }
+  // row stream: rows longer than kSpmvLongRow slots are summed by segments in
+  // the FMA arithmetic (GPETSC_SPMV_SPLIT_LONG=0 keeps one thread a row)
+  std::vector<int> lrows, lseg(1, 0), slong;
+  if (A->stream_rows && spmv_split_long_enabled()) {
+    for (int i = 0; i < n; i++) {
+      const int len = A->h_rowptr[i + 1] - A->h_rowptr[i];
+      if (len > kSpmvLongRow) {
+        const int nseg = (len + kSpmvLongSeg - 1) / kSpmvLongSeg;
+        for (int q = 0; q < nseg; q++) slong.push_back((int)lrows.size());
+        lrows.push_back(i);
+        lseg.push_back(lseg.back() + nseg);
+      }
+    }
+  }
   GP_TRY(dev_upload(&A->rowptr, A->h_rowptr.data(), (size_t)n + 1, s));
   GP_TRY(dev_upload(&A->colind, A->h_colind.data(), (size_t)A->nnz, s));
   if (!coff.empty()) GP_TRY(dev_upload(&A->coff16, coff.data(), coff.size(), s));
+  if (!lrows.empty()) {
+    A->nlong = (int)lrows.size();
+    A->nseg = lseg.back();
+    GP_TRY(dev_upload(&A->long_rows, lrows.data(), lrows.size(), s));
+    GP_TRY(dev_upload(&A->long_seg, lseg.data(), lseg.size(), s));
+    GP_TRY(dev_upload(&A->seg_long, slong.data(), slong.size(), s));
+    GP_CUDA(cudaMalloc(&A->seg_part, (size_t)A->nseg * sizeof(double)));
+    GP_CUDA(cudaMalloc(&A->long_ticket, (size_t)A->nlong * sizeof(unsigned)));
+    GP_CUDA(cudaMemsetAsync(A->long_ticket, 0, (size_t)A->nlong * sizeof(unsigned), s));
+  }
   GP_TRY(dev_upload(&A->val, h_val, (size_t)A->nnz, s));
   GP_TRY(dev_upload(&A->diagpos, diag.data(), (size_t)n, s));
   // the host staging vectors must stay alive until the copies land
@@ -201,6 +234,11 @@ int csr_destroy(Csr* A) {
   cudaFree(A->rowptr);
   cudaFree(A->colind);
   cudaFree(A->coff16);
+  cudaFree(A->long_rows);
+  cudaFree(A->long_seg);
+  cudaFree(A->seg_long);
+  cudaFree(A->seg_part);
+  cudaFree(A->long_ticket);
   cudaFree(A->val);
   cudaFree(A->val32);
   cudaFree(A->diagpos);
@@ -311,7 +349,8 @@ __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict
                                                     const CT* __restrict__ colind,
                                                     const double* __restrict__ val, DRef xr,
                                                     const double* __restrict__ v, DRef yr,
-                                                    const int* gate, int want, int evict_first) {
+                                                    const int* gate, int want, int evict_first,
+                                                    int long_min = INT_MAX) {
   if (gated_off(gate, want)) return;
   const double* __restrict__ x = xr.get();
   double* __restrict__ y = yr.get();
@@ -325,15 +364,61 @@ __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict
   }
   else {
   double s;
+  bool skipped = false;
   if constexpr (FMA) {
     __shared__ SpmvSmemF<double, double, double> sm;
-    s = spmv_block_rows_fma<double, double, double>(sm, n, r0, rowptr, colind, val, x, init);
+    s = spmv_block_rows_fma<double, double, double>(sm, n, r0, rowptr, colind, val, x, init,
+                                                    long_min, &skipped);
   } else {
     __shared__ SpmvSmem<double, double, double> sm;
     s = spmv_block_rows<double, double, double>(sm, n, r0, rowptr, colind, val, x, init);
   }
-  if (row < n) y[row] = s;
+  if (row < n && !skipped) y[row] = s;
   }
+}
+
+// The long rows of the FMA row stream, by segments: CTA s sums segment s of
+// its row (kSpmvLongSeg slots: thread-strided FMAs, then a fixed tree), and
+// the CTA that finishes a row's last segment adds the row's segment sums in
+// segment order to its start value (v_i for MatMultAdd, else 0) and stores it.
+// The sum's order is fixed, so results repeat run to run; it differs from one
+// FMA chain by rounding only.
+__global__ void __launch_bounds__(kSpmvRows) k_spmv_long(
+    const int* __restrict__ rowptr, const int* __restrict__ colind, const double* __restrict__ val,
+    DRef xr, const double* __restrict__ v, DRef yr, const int* __restrict__ long_rows,
+    const int* __restrict__ long_seg, const int* __restrict__ seg_long, double* seg_part,
+    unsigned* ticket, const int* gate, int want) {
+  if (gated_off(gate, want)) return;
+  const double* __restrict__ x = xr.get();
+  double* __restrict__ y = yr.get();
+  __shared__ double red[kSpmvRows / 32];
+  __shared__ bool last;
+  const int s = blockIdx.x, li = seg_long[s];
+  const int row = long_rows[li];
+  const int b = rowptr[row] + (s - long_seg[li]) * kSpmvLongSeg;
+  const int e = min(b + kSpmvLongSeg, rowptr[row + 1]);
+  double acc = 0.0;
+  for (int j = b + threadIdx.x; j < e; j += kSpmvRows) acc = __fma_rn(val[j], x[colind[j]], acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc = __dadd_rn(acc, __shfl_down_sync(0xffffffffu, acc, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = red[0];
+    for (int w = 1; w < kSpmvRows / 32; w++) t = __dadd_rn(t, red[w]);
+    seg_part[s] = t;
+    __threadfence();
+    const unsigned nseg = (unsigned)(long_seg[li + 1] - long_seg[li]);
+    last = atomicAdd(&ticket[li], 1u) == nseg - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  double sum = v ? v[row] : 0.0;
+  for (int q = long_seg[li]; q < long_seg[li + 1]; q++)
+    sum = __dadd_rn(sum, *(volatile double*)&seg_part[q]);
+  y[row] = sum;
+  ticket[li] = 0u;
 }
 
 static void launch_spmv(cudaStream_t s, const Csr* A, DRef x, const double* v, DRef y,
@@ -342,13 +427,18 @@ static void launch_spmv(cudaStream_t s, const Csr* A, DRef x, const double* v, D
   if (A->coff16) {  // row form with 16-bit column offsets
     auto k = f ? k_spmv<true, false, short> : k_spmv<false, false, short>;
     k<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->coff16, A->val, x, v, y, gate,
-                                         want, A->l2_evict_first);
+                                         want, A->l2_evict_first, INT_MAX);
     return;
   }
   auto k = A->stream_rows ? (f ? k_spmv<true, true> : k_spmv<false, true>)
                           : (f ? k_spmv<true, false> : k_spmv<false, false>);
+  const bool split = f && A->nlong > 0;
   k<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, v, y, gate, want,
-                                       A->l2_evict_first);
+                                       A->l2_evict_first, split ? kSpmvLongRow : INT_MAX);
+  if (split)
+    k_spmv_long<<<A->nseg, kSpmvRows, 0, s>>>(A->rowptr, A->colind, A->val, x, v, y, A->long_rows,
+                                             A->long_seg, A->seg_long, A->seg_part,
+                                             A->long_ticket, gate, want);
 }
 
 __global__ void k_diag(int n, const int* __restrict__ diagpos, const double* __restrict__ val,
@@ -402,7 +492,7 @@ int spmv_t(cudaStream_t s, const Csr* A, DRef x, DRef y, const int* gate, int wa
                             : (f ? k_spmv<true, false> : k_spmv<false, false>);
   k<<<(A->ncols + kSpmvRows - 1) / kSpmvRows, kSpmvRows, 0, s>>>(
       A->ncols, A->t_rowptr, A->t_colind, A->t_val, x, nullptr, y, gate, want,
-      A->l2_evict_first);
+      A->l2_evict_first, INT_MAX);
   GP_CHECK_LAUNCH();
   return GP_OK;
 }

@@ -24,6 +24,8 @@
 // is fully coalesced apart from the x gather.
 #pragma once
 
+#include <climits>
+
 #include "gp_common.cuh"
 
 namespace gp {
@@ -31,6 +33,8 @@ namespace gp {
 constexpr int kSpmvRows = 256;    // rows per CTA == threads per CTA
 constexpr int kSpmvChunk = 2048;  // products staged per pass
 constexpr int kSpmvMaxRowLen = 64;  // longest row the row-per-thread form takes
+constexpr int kSpmvLongRow = 2048;  // FMA row stream: longer rows go by segments
+constexpr int kSpmvLongSeg = 2048;  // slots of one segment (one CTA)
 
 // L2 evict-first loads for data read once per product.
 __device__ __forceinline__ uint64_t l2_evict_first() {
@@ -221,14 +225,23 @@ struct SpmvSmemF {
   AT v[kSpmvChunkF];
   AT xv[kSpmvChunkF];
   int rp[kSpmvRows + 1];
+  int nlong;                  // rows of this CTA longer than `long_min`
+  int lb[kSpmvRows], le[kSpmvRows];  // their slot ranges, in row order
+  int wcount[kSpmvRows / 32];
 };
 
+// Rows longer than `long_min` slots are left to the segmented kernel
+// (k_spmv_long): their slots are not staged and their thread does not fold;
+// *skipped tells the caller not to store the row.  long_min = INT_MAX keeps
+// every row here.
 template <typename VT, typename XT, typename AT>
 __device__ __forceinline__ AT spmv_block_rows_fma(SpmvSmemF<VT, XT, AT>& sm, int n, int r0,
                                                   const int* __restrict__ rowptr,
                                                   const int* __restrict__ colind,
                                                   const VT* __restrict__ val,
-                                                  const XT* __restrict__ x, AT init) {
+                                                  const XT* __restrict__ x, AT init,
+                                                  int long_min = INT_MAX,
+                                                  bool* skipped = nullptr) {
   const int tid = threadIdx.x;
   const int nr = min(kSpmvRows, n - r0);
   for (int t = tid; t <= nr; t += blockDim.x) sm.rp[t] = rowptr[r0 + t];
@@ -240,24 +253,50 @@ __device__ __forceinline__ AT spmv_block_rows_fma(SpmvSmemF<VT, XT, AT>& sm, int
     my_b = sm.rp[tid];
     my_e = sm.rp[tid + 1];
   }
+  const bool mine_long = tid < nr && my_e - my_b > long_min;
+  if (skipped) *skipped = mine_long;
+  // the long rows' slot ranges, in row order (a ballot per warp, then the
+  // warps' counts added up)
+  int nlong = 0;
+  if (long_min != INT_MAX) {
+    const unsigned bal = __ballot_sync(0xffffffffu, mine_long);
+    if ((tid & 31) == 0) sm.wcount[tid >> 5] = __popc(bal);
+    __syncthreads();
+    int before = __popc(bal & ((1u << (tid & 31)) - 1u));
+    for (int w = 0; w < (tid >> 5); w++) before += sm.wcount[w];
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) nlong += sm.wcount[w];
+    if (mine_long) {
+      sm.lb[before] = my_b;
+      sm.le[before] = my_e;
+    }
+    __syncthreads();
+  }
   AT sum = init;
-  for (int c0 = base; c0 < end; c0 += kSpmvChunkF) {
-    const int cn = min(kSpmvChunkF, end - c0);
+  // stage and fold the slot range between long rows, interval by interval
+  int seg_lo = base;
+  for (int li = 0; li <= nlong; li++) {
+    const int seg_hi = li < nlong ? sm.lb[li] : end;
+    for (int c0 = seg_lo; c0 < seg_hi; c0 += kSpmvChunkF) {
+      const int cn = min(kSpmvChunkF, seg_hi - c0);
 #pragma unroll 6
-    for (int k = tid; k < cn; k += kSpmvRows) {
-      const int slot = c0 + k;
-      sm.v[k] = (AT)val[slot];
-      sm.xv[k] = (AT)x[colind[slot]];
+      for (int k = tid; k < cn; k += kSpmvRows) {
+        const int slot = c0 + k;
+        sm.v[k] = (AT)val[slot];
+        sm.xv[k] = (AT)x[colind[slot]];
+      }
+      __syncthreads();
+      if (!mine_long) {
+        const int lo = max(my_b, c0), hi = min(my_e, c0 + cn);
+        for (int j = lo; j < hi; j++) {
+          if constexpr (sizeof(AT) == 8)
+            sum = __fma_rn(sm.v[j - c0], sm.xv[j - c0], sum);
+          else
+            sum = __fmaf_rn(sm.v[j - c0], sm.xv[j - c0], sum);
+        }
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    const int lo = max(my_b, c0), hi = min(my_e, c0 + cn);
-    for (int j = lo; j < hi; j++) {
-      if constexpr (sizeof(AT) == 8)
-        sum = __fma_rn(sm.v[j - c0], sm.xv[j - c0], sum);
-      else
-        sum = __fmaf_rn(sm.v[j - c0], sm.xv[j - c0], sum);
-    }
-    __syncthreads();
+    if (li < nlong) seg_lo = sm.le[li];
   }
   return sum;
 }

@@ -119,6 +119,40 @@ def rgg_laplacian(n: int, rng: np.random.Generator, mean_degree: float = 8.0,
     return indptr, j.astype(np.int32), v.astype(np.float64)
 
 
+def hub_laplacian(n: int, hubs: int, spokes: int, seed: int = 9, shift: float = 1e-2):
+    """A graph Laplacian with a few very long rows: the path 0-1-...-(n-1)
+    with unit weights plus `hubs` rows each joined to `spokes` distinct random
+    rows (weights U[0.5, 2]); L = D - W + shift*I (SPD).  Row lengths are 2-3
+    except the hubs' (~spokes), the skew a one-thread-a-row SpMV handles worst."""
+    rng = np.random.default_rng(seed)
+    pi = np.arange(n - 1)
+    ei, ej, ew = [pi], [pi + 1], [np.ones(n - 1)]
+    for h in range(hubs):
+        js = rng.choice(np.arange(h + 2, n), size=spokes, replace=False)
+        ei.append(np.full(spokes, h))
+        ej.append(js)
+        ew.append(rng.uniform(0.5, 2.0, size=spokes))
+    ei, ej, ew = np.concatenate(ei), np.concatenate(ej), np.concatenate(ew)
+    # an edge drawn twice (two hubs' spokes meeting) keeps the sum of its weights
+    key = np.minimum(ei, ej).astype(np.int64) * n + np.maximum(ei, ej)
+    key, inv = np.unique(key, return_inverse=True)
+    w = np.zeros(len(key))
+    np.add.at(w, inv, ew)
+    a, b = key // n, key % n
+    deg = np.zeros(n)
+    np.add.at(deg, a, w)
+    np.add.at(deg, b, w)
+    i = np.concatenate([a, b, np.arange(n)])
+    j = np.concatenate([b, a, np.arange(n)])
+    v = np.concatenate([-w, -w, deg + shift])
+    order = np.lexsort((j, i))
+    i, j, v = i[order], j[order], v[order]
+    indptr = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(indptr, i + 1, 1)
+    indptr = np.cumsum(indptr).astype(np.int32)
+    return indptr, j.astype(np.int32), v.astype(np.float64)
+
+
 def rgg_batch(count: int = 512, seed: int = 11, nmin: int = 1024, nmax: int = 65536):
     """`count` RGG Laplacians with sizes log-uniform in [nmin, nmax]."""
     rng = np.random.default_rng(seed)

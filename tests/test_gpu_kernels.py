@@ -141,6 +141,56 @@ def test_fused_cg_reads_16_bit_column_offsets():
     assert rel <= 1e-10, rel
 
 
+@pytest.mark.fma
+def test_long_rows_are_summed_by_segments_in_the_fused_arithmetic():
+    """Rows longer than 2048 slots in the row-stream form are summed by
+    segments (one CTA a segment, a fixed tree, the segments in order): within
+    rounding of the reference's products, the same bits run to run, and a CG
+    solve with the oracle's iteration count and an iterate within 1e-10."""
+    ip, ix, v = gallery.hub_laplacian(20000, 4, 5000)
+    n = len(ip) - 1
+    assert np.diff(ip).max() > 2048
+    ip64, ix64 = O.i64(ip), O.i64(ix)
+    A = mat(ip, ix, v)
+    x = np.random.default_rng(4).normal(size=n)
+    y = A.mult(vec(x)).getArray()
+    want = np.zeros(n)
+    O.lib().mp_mat_mult(a(x), a(want), a(ip64), a(ix64), a(v), n)
+    scale = np.zeros(n)
+    np.add.at(scale, np.repeat(np.arange(n), np.diff(ip)), np.abs(v * x[ix]))
+    assert np.all(np.abs(y - want) <= 1e-14 * scale + 1e-300)
+    np.testing.assert_array_equal(A.mult(vec(x)).getArray(), y)
+    w = np.random.default_rng(5).normal(size=n)
+    y2 = A.multAdd(vec(x), vec(w)).getArray()
+    assert np.all(np.abs(y2 - (want + w)) <= 1e-14 * (scale + np.abs(w)) + 1e-300)
+    b = np.random.default_rng(6).uniform(-1, 1, n)
+    ksp = PETSc.KSP().create()
+    ksp.setType("cg")
+    ksp.getPC().setType("jacobi")
+    ksp.setOperators(A)
+    ksp.setTolerances(rtol=1e-10, atol=1e-50, divtol=1e30, max_it=5000)
+    xv = PETSc.Vec().createSeq(n)
+    ksp.solve(vec(b), xv)
+    ref = O.solve("cg", ip, ix, v, b, pc_type="jacobi", rtol=1e-10, atol=1e-50, divtol=1e30,
+                  max_it=5000)
+    assert (ksp.getIterationNumber(), ksp.getConvergedReason()) == (ref["its"], ref["reason"])
+    rel = np.linalg.norm(xv.getArray() - ref["x"]) / np.linalg.norm(ref["x"])
+    assert rel <= 1e-10, rel
+
+
+def test_long_rows_keep_the_reference_fold_in_the_ordered_arithmetic():
+    """The same matrix in the ordered arithmetic: every row, the long ones
+    included, is folded slot by slot as the reference does (bit-identical)."""
+    ip, ix, v = gallery.hub_laplacian(20000, 4, 5000)
+    n = len(ip) - 1
+    ip64, ix64 = O.i64(ip), O.i64(ix)
+    A = mat(ip, ix, v)
+    x = np.random.default_rng(4).normal(size=n)
+    want = np.zeros(n)
+    O.lib().mp_mat_mult(a(x), a(want), a(ip64), a(ix64), a(v), n)
+    np.testing.assert_array_equal(A.mult(vec(x)).getArray(), want)
+
+
 def test_spmv_rectangular_and_long_rows():
     rng = np.random.default_rng(3)
     d = rng.normal(size=(300, 5000)) * (rng.random((300, 5000)) < 0.6)
