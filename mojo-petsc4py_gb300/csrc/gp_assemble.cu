@@ -359,6 +359,7 @@ int csr_build_transpose(Csr* A, cudaStream_t s) {
   for (int c = 0; c < m; c++) maxlen = std::max<int64_t>(maxlen, trp[c + 1] - trp[c]);
   const double avg = m ? (double)nnz / m : 0.0;
   A->t_stream_rows = maxlen > kSpmvMaxRowLen || (double)maxlen > 8.0 * avg + 8.0;
+  if (A->t_stream_rows) GP_TRY(long_rows_build(A->t_lr, m, trp.data(), s));
   return GP_OK;
 }
 

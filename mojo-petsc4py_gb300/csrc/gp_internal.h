@@ -103,6 +103,23 @@ struct DevReduceArgs {
 };
 
 // ------------------------------------------------------------- CSR matrix
+// Row-stream form, FMA arithmetic: rows longer than kSpmvLongRow slots are
+// summed by segments of kSpmvLongSeg slots, one CTA a segment, instead of by
+// one thread (rows ascending; row i's segments are seg[i] .. seg[i + 1] - 1;
+// part holds the segment sums and ticket counts a row's finished segments).
+struct SpmvLongRows {
+  int nlong = 0, nseg = 0;
+  int* rows = nullptr;
+  int* seg = nullptr;
+  int* seg_long = nullptr;    // [nseg] index into rows
+  double* part = nullptr;     // [nseg]
+  unsigned* ticket = nullptr;  // [nlong]
+};
+// Lists the long rows of a row pointer (host copy) on the device; nothing
+// when none or GPETSC_SPMV_SPLIT_LONG=0.
+int long_rows_build(SpmvLongRows& L, int n, const int* h_rowptr, cudaStream_t s);
+void long_rows_free(SpmvLongRows& L);
+
 struct Csr {
   int n = 0;        // rows
   int ncols = 0;
@@ -119,17 +136,8 @@ struct Csr {
   // every offset fits 16 bits; the row kernels then read 2 bytes an entry
   // instead of 4 (null: they read colind)
   short* coff16 = nullptr;
-  // row-stream form, FMA arithmetic: rows longer than kSpmvLongRow slots are
-  // summed by segments of kSpmvLongSeg slots, one CTA a segment, instead of by
-  // one thread (long_rows ascending; each long row's segments are
-  // long_seg[i] .. long_seg[i + 1] - 1; seg_part holds the segment sums and
-  // long_ticket counts a row's finished segments)
-  int nlong = 0, nseg = 0;
-  int* long_rows = nullptr;
-  int* long_seg = nullptr;
-  int* seg_long = nullptr;       // [nseg] index into long_rows
-  double* seg_part = nullptr;    // [nseg]
-  unsigned* long_ticket = nullptr;  // [nlong]
+  SpmvLongRows lr;             // row stream: long rows of A
+  SpmvLongRows t_lr;           // and of A^T (built with its pattern)
   // transpose (built on demand): rows of A^T in ascending original row order
   int* t_rowptr = nullptr;
   int* t_colind = nullptr;

@@ -1416,7 +1416,7 @@ static bool cg_fused_ok(const Run& r) {
   // (a matrix whose long rows are summed by segments multiplies through
   // spmv(), which runs the segment kernel: the general loop)
   return arith_mode() != kOrdered && !r.k->transpose && o.normtype == N_PRECOND &&
-         o.chknorm <= 1 && r.A->nlong == 0 &&
+         o.chknorm <= 1 && r.A->lr.nlong == 0 &&
          (int64_t)spmv_grid(r.A) <= (int64_t)kMaxBasis * kMaxRedGrid;
 }
 

@@ -62,6 +62,41 @@ static bool spmv_split_long_enabled() {
   return on;
 }
 
+int long_rows_build(SpmvLongRows& L, int n, const int* h_rowptr, cudaStream_t s) {
+  long_rows_free(L);
+  if (!spmv_split_long_enabled()) return GP_OK;
+  std::vector<int> rows, seg(1, 0), seg_long;
+  for (int i = 0; i < n; i++) {
+    const int len = h_rowptr[i + 1] - h_rowptr[i];
+    if (len > kSpmvLongRow) {
+      const int ns = (len + kSpmvLongSeg - 1) / kSpmvLongSeg;
+      for (int q = 0; q < ns; q++) seg_long.push_back((int)rows.size());
+      rows.push_back(i);
+      seg.push_back(seg.back() + ns);
+    }
+  }
+  if (rows.empty()) return GP_OK;
+  L.nlong = (int)rows.size();
+  L.nseg = seg.back();
+  GP_TRY(dev_upload(&L.rows, rows.data(), rows.size(), s));
+  GP_TRY(dev_upload(&L.seg, seg.data(), seg.size(), s));
+  GP_TRY(dev_upload(&L.seg_long, seg_long.data(), seg_long.size(), s));
+  GP_CUDA(cudaMalloc(&L.part, (size_t)L.nseg * sizeof(double)));
+  GP_CUDA(cudaMalloc(&L.ticket, (size_t)L.nlong * sizeof(unsigned)));
+  GP_CUDA(cudaMemsetAsync(L.ticket, 0, (size_t)L.nlong * sizeof(unsigned), s));
+  GP_CUDA(cudaStreamSynchronize(s));  // the host lists go out of scope
+  return GP_OK;
+}
+
+void long_rows_free(SpmvLongRows& L) {
+  cudaFree(L.rows);
+  cudaFree(L.seg);
+  cudaFree(L.seg_long);
+  cudaFree(L.part);
+  cudaFree(L.ticket);
+  L = SpmvLongRows();
+}
+
 static bool spmv_coff16_enabled() {
   static const bool on = [] {
     const char* e = std::getenv("GPETSC_SPMV_COFF16");
@@ -107,33 +142,12 @@ static int csr_finish(Csr* A, const double* h_val, cudaStream_t s) {
           coff[j] = (short)(A->h_colind[j] - i);
     }
   }
-  // row stream: rows longer than kSpmvLongRow slots are summed by segments in
-  // the FMA arithmetic (GPETSC_SPMV_SPLIT_LONG=0 keeps one thread a row)
-  std::vector<int> lrows, lseg(1, 0), slong;
-  if (A->stream_rows && spmv_split_long_enabled()) {
-    for (int i = 0; i < n; i++) {
-      const int len = A->h_rowptr[i + 1] - A->h_rowptr[i];
-      if (len > kSpmvLongRow) {
-        const int nseg = (len + kSpmvLongSeg - 1) / kSpmvLongSeg;
-        for (int q = 0; q < nseg; q++) slong.push_back((int)lrows.size());
-        lrows.push_back(i);
-        lseg.push_back(lseg.back() + nseg);
-      }
-    }
-  }
   GP_TRY(dev_upload(&A->rowptr, A->h_rowptr.data(), (size_t)n + 1, s));
   GP_TRY(dev_upload(&A->colind, A->h_colind.data(), (size_t)A->nnz, s));
   if (!coff.empty()) GP_TRY(dev_upload(&A->coff16, coff.data(), coff.size(), s));
-  if (!lrows.empty()) {
-    A->nlong = (int)lrows.size();
-    A->nseg = lseg.back();
-    GP_TRY(dev_upload(&A->long_rows, lrows.data(), lrows.size(), s));
-    GP_TRY(dev_upload(&A->long_seg, lseg.data(), lseg.size(), s));
-    GP_TRY(dev_upload(&A->seg_long, slong.data(), slong.size(), s));
-    GP_CUDA(cudaMalloc(&A->seg_part, (size_t)A->nseg * sizeof(double)));
-    GP_CUDA(cudaMalloc(&A->long_ticket, (size_t)A->nlong * sizeof(unsigned)));
-    GP_CUDA(cudaMemsetAsync(A->long_ticket, 0, (size_t)A->nlong * sizeof(unsigned), s));
-  }
+  // row stream: rows longer than kSpmvLongRow slots are summed by segments in
+  // the FMA arithmetic
+  if (A->stream_rows) GP_TRY(long_rows_build(A->lr, n, A->h_rowptr.data(), s));
   GP_TRY(dev_upload(&A->val, h_val, (size_t)A->nnz, s));
   GP_TRY(dev_upload(&A->diagpos, diag.data(), (size_t)n, s));
   // the host staging vectors must stay alive until the copies land
@@ -234,11 +248,8 @@ int csr_destroy(Csr* A) {
   cudaFree(A->rowptr);
   cudaFree(A->colind);
   cudaFree(A->coff16);
-  cudaFree(A->long_rows);
-  cudaFree(A->long_seg);
-  cudaFree(A->seg_long);
-  cudaFree(A->seg_part);
-  cudaFree(A->long_ticket);
+  long_rows_free(A->lr);
+  long_rows_free(A->t_lr);
   cudaFree(A->val);
   cudaFree(A->val32);
   cudaFree(A->diagpos);
@@ -385,10 +396,13 @@ __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict
 // FMA chain by rounding only.
 __global__ void __launch_bounds__(kSpmvRows) k_spmv_long(
     const int* __restrict__ rowptr, const int* __restrict__ colind, const double* __restrict__ val,
-    DRef xr, const double* __restrict__ v, DRef yr, const int* __restrict__ long_rows,
-    const int* __restrict__ long_seg, const int* __restrict__ seg_long, double* seg_part,
-    unsigned* ticket, const int* gate, int want) {
+    DRef xr, const double* __restrict__ v, DRef yr, SpmvLongRows L, const int* gate, int want) {
   if (gated_off(gate, want)) return;
+  const int* __restrict__ long_rows = L.rows;
+  const int* __restrict__ long_seg = L.seg;
+  const int* __restrict__ seg_long = L.seg_long;
+  double* seg_part = L.part;
+  unsigned* ticket = L.ticket;
   const double* __restrict__ x = xr.get();
   double* __restrict__ y = yr.get();
   __shared__ double red[kSpmvRows / 32];
@@ -432,13 +446,12 @@ static void launch_spmv(cudaStream_t s, const Csr* A, DRef x, const double* v, D
   }
   auto k = A->stream_rows ? (f ? k_spmv<true, true> : k_spmv<false, true>)
                           : (f ? k_spmv<true, false> : k_spmv<false, false>);
-  const bool split = f && A->nlong > 0;
+  const bool split = f && A->lr.nlong > 0;
   k<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, v, y, gate, want,
                                        A->l2_evict_first, split ? kSpmvLongRow : INT_MAX);
   if (split)
-    k_spmv_long<<<A->nseg, kSpmvRows, 0, s>>>(A->rowptr, A->colind, A->val, x, v, y, A->long_rows,
-                                             A->long_seg, A->seg_long, A->seg_part,
-                                             A->long_ticket, gate, want);
+    k_spmv_long<<<A->lr.nseg, kSpmvRows, 0, s>>>(A->rowptr, A->colind, A->val, x, v, y, A->lr,
+                                                gate, want);
 }
 
 __global__ void k_diag(int n, const int* __restrict__ diagpos, const double* __restrict__ val,
@@ -490,9 +503,13 @@ int spmv_t(cudaStream_t s, const Csr* A, DRef x, DRef y, const int* gate, int wa
   const bool f = arith_mode() == kFma;
   auto k = A->t_stream_rows ? (f ? k_spmv<true, true> : k_spmv<false, true>)
                             : (f ? k_spmv<true, false> : k_spmv<false, false>);
+  const bool split = f && A->t_lr.nlong > 0;
   k<<<(A->ncols + kSpmvRows - 1) / kSpmvRows, kSpmvRows, 0, s>>>(
       A->ncols, A->t_rowptr, A->t_colind, A->t_val, x, nullptr, y, gate, want,
-      A->l2_evict_first, INT_MAX);
+      A->l2_evict_first, split ? kSpmvLongRow : INT_MAX);
+  if (split)
+    k_spmv_long<<<A->t_lr.nseg, kSpmvRows, 0, s>>>(A->t_rowptr, A->t_colind, A->t_val, x,
+                                                  nullptr, y, A->t_lr, gate, want);
   GP_CHECK_LAUNCH();
   return GP_OK;
 }

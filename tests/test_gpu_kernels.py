@@ -160,6 +160,9 @@ def test_long_rows_are_summed_by_segments_in_the_fused_arithmetic():
     np.add.at(scale, np.repeat(np.arange(n), np.diff(ip)), np.abs(v * x[ix]))
     assert np.all(np.abs(y - want) <= 1e-14 * scale + 1e-300)
     np.testing.assert_array_equal(A.mult(vec(x)).getArray(), y)
+    # A^T's long rows (A's dense columns) are split the same way: for this
+    # symmetric matrix they hold A's rows in the same order, the same bits
+    np.testing.assert_array_equal(A.multTranspose(vec(x)).getArray(), y)
     w = np.random.default_rng(5).normal(size=n)
     y2 = A.multAdd(vec(x), vec(w)).getArray()
     assert np.all(np.abs(y2 - (want + w)) <= 1e-14 * (scale + np.abs(w)) + 1e-300)
