@@ -91,6 +91,7 @@ struct SweepTuning {
   // best of a scan (1-4 CTAs a SM x 0-300 ns back-off) of the level-ordered
   // IC(0)/ILU(0)/SOR sweeps on 128^3 with the per-lane polling kernel
   int ctas_per_sm = 1, sleep_after = 8, sleep_ns = 0;
+  int block = kEllBlock;  // GPETSC_SWEEP_BLOCK: threads of a level-ordered sweep CTA (32-256)
   int tiles = 1;                // GPETSC_SWEEP_TILES=0: always the level-ordered ELL form
   int tile_smem = kTileSmemMax;  // GPETSC_TILE_SMEM: shared memory cap of one chunk
   int tile_rows = 0;            // GPETSC_TILE_ROWS: force this chunk size (0: chosen)
@@ -105,6 +106,7 @@ static SweepTuning& sweep_tuning_mut() {
     v.ctas_per_sm = std::max(1, std::min(8, env("GPETSC_SWEEP_CTAS_PER_SM", v.ctas_per_sm)));
     v.sleep_after = std::max(0, env("GPETSC_SWEEP_SLEEP_AFTER", v.sleep_after));
     v.sleep_ns = std::max(0, std::min(1000, env("GPETSC_SWEEP_SLEEP_NS", v.sleep_ns)));
+    v.block = std::max(1, std::min(kEllBlock / 32, env("GPETSC_SWEEP_BLOCK", v.block) / 32)) * 32;
     v.tiles = env("GPETSC_SWEEP_TILES", v.tiles) != 0;
     v.tile_smem = std::max(16 * 1024, std::min(kTileSmemMax, env("GPETSC_TILE_SMEM", v.tile_smem)));
     v.tile_rows = std::max(0, std::min(8192, env("GPETSC_TILE_ROWS", v.tile_rows)));
@@ -1151,12 +1153,13 @@ template <int MODE, bool FMA>
 static void launch_mode_a(const EllSweep& e, const int* gate, int want, EllArgs a, DRef in,
                           DRef out, cudaStream_t s) {
   const int g = num_sms() * sweep_tuning().ctas_per_sm;
+  const int b = sweep_tuning().block;
   if (e.W <= 4)
-    k_ell_sweep<MODE, 4, FMA><<<g, kEllBlock, 0, s>>>(gate, want, a, in, out);
+    k_ell_sweep<MODE, 4, FMA><<<g, b, 0, s>>>(gate, want, a, in, out);
   else if (e.W <= 8)
-    k_ell_sweep<MODE, 8, FMA><<<g, kEllBlock, 0, s>>>(gate, want, a, in, out);
+    k_ell_sweep<MODE, 8, FMA><<<g, b, 0, s>>>(gate, want, a, in, out);
   else
-    k_ell_sweep<MODE, kEllMaxW, FMA><<<g, kEllBlock, 0, s>>>(gate, want, a, in, out);
+    k_ell_sweep<MODE, kEllMaxW, FMA><<<g, b, 0, s>>>(gate, want, a, in, out);
 }
 
 template <int MODE>
