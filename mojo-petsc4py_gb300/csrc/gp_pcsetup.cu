@@ -15,6 +15,7 @@
 // linked list, as the reference's; IC: a sorted list of touched columns);
 // the resulting patterns are the same sets in the same (ascending) order.
 #include <algorithm>
+#include <mutex>
 #include <climits>
 #include <string>
 #include <vector>
@@ -110,6 +111,65 @@ static void permuted_row(const Csr* A, const std::vector<int>& r, const std::vec
   out.erase(std::unique(out.begin(), out.end()), out.end());
 }
 
+// Level 0: every row is the operator's permuted row, so rows are independent:
+// counted on host threads, prefix-summed, then filled on host threads (the
+// same rows and levels as the general loop).  `keep(i, c)` selects the
+// columns a row keeps; nL (when given) counts each row's columns below i.
+template <class Keep>
+static int rows_level0(const Csr* A, const std::vector<int>& r, const std::vector<int>& ic,
+                       Keep keep, SymRows& R, bool need_diag, const char* who) {
+  const int n = A->n;
+  R.rs.assign(n + 1, 0);
+  R.nL.assign(n, 0);
+  std::vector<int> missing(1, -1);
+  std::mutex mu;
+  host_parallel_for(n, [&](int64_t i0, int64_t i1) {
+    std::vector<int> row;
+    for (int i = (int)i0; i < (int)i1; i++) {
+      permuted_row(A, r, ic, i, row);
+      if (need_diag && !std::binary_search(row.begin(), row.end(), i)) {
+        // the first such row in the factor's order, as a row-by-row pass finds
+        std::lock_guard<std::mutex> g(mu);
+        if (missing[0] < 0 || i < missing[0]) missing[0] = i;
+      }
+      int cnt = 0, low = 0;
+      for (int c : row)
+        if (keep(i, c)) {
+          cnt++;
+          low += c < i;
+        }
+      R.rs[i + 1] = cnt;
+      R.nL[i] = low;
+    }
+  });
+  if (missing[0] >= 0) {
+    set_error(std::string(who) + ": row " + std::to_string(r[missing[0]]) +
+              " has no diagonal entry");
+    return GP_ERR_ARG;
+  }
+  int64_t tot = 0;
+  for (int i = 0; i < n; i++) {
+    tot += R.rs[i + 1];
+    if (tot > INT32_MAX - 1 - (int64_t)n) {
+      set_error(std::string(who) + " factor too large for 32-bit indices");
+      return GP_ERR_ARG;
+    }
+    R.rs[i + 1] = (int)tot;
+  }
+  R.cols.assign(tot, 0);
+  R.lv.assign(tot, 0);
+  host_parallel_for(n, [&](int64_t i0, int64_t i1) {
+    std::vector<int> row;
+    for (int i = (int)i0; i < (int)i1; i++) {
+      permuted_row(A, r, ic, i, row);
+      int q = R.rs[i];
+      for (int c : row)
+        if (keep(i, c)) R.cols[q++] = c;
+    }
+  });
+  return GP_OK;
+}
+
 // Row offsets are int32 (the factor's device indices): the slot count is
 // checked in 64 bits before each narrowing, against `limit`.
 static bool slots_fit(size_t count, int64_t limit, const char* who) {
@@ -126,6 +186,8 @@ static bool slots_fit(size_t count, int64_t limit, const char* who) {
 static int ilu_rows_flat(const Csr* A, int levels, const std::vector<int>& r,
                          const std::vector<int>& ic, SymRows& R) {
   const int n = A->n;
+  if (levels == 0)
+    return rows_level0(A, r, ic, [](int, int) { return true; }, R, true, "ILU");
   R.rs.assign(n + 1, 0);
   R.nL.assign(n, 0);
   R.cols.clear();
@@ -192,6 +254,8 @@ static int ilu_rows_flat(const Csr* A, int levels, const std::vector<int>& r,
 static int icc_rows_flat(const Csr* A, int levels, const std::vector<int>& r,
                          const std::vector<int>& ic, SymRows& R) {
   const int n = A->n;
+  if (levels == 0)
+    return rows_level0(A, r, ic, [](int k, int c) { return c > k; }, R, false, "IC");
   R.rs.assign(n + 1, 0);
   R.nL.assign(n, 0);
   R.cols.clear();
@@ -281,17 +345,21 @@ int ilu_symbolic(const Csr* A, int levels, const std::vector<int>& r, const std:
   out.nnz = (int)total;
   out.bj.assign(std::max<int64_t>(total, 1), 0);
   out.bdiag.assign(n + 1, 0);
-  for (int i = 0; i < n; i++)
-    for (int q = 0; q < R.nL[i]; q++) out.bj[out.bi[i] + q] = R.cols[R.rs[i] + q];
+  // L rows ascending, then the U rows from the last row up, each ending on its
+  // diagonal: bdiag by a suffix sum, then every row copied on host threads
   const int nLtot = out.bi[n];
   out.bdiag[n] = nLtot - 1;
-  int k = nLtot;
-  for (int i = n - 1; i >= 0; i--) {
-    const int nz = R.rs[i + 1] - R.rs[i] - R.nL[i] - 1;
-    for (int q = 0; q < nz; q++) out.bj[k++] = R.cols[R.rs[i] + R.nL[i] + 1 + q];
-    out.bj[k++] = i;
-    out.bdiag[i] = out.bdiag[i + 1] + nz + 1;
-  }
+  for (int i = n - 1; i >= 0; i--)
+    out.bdiag[i] = out.bdiag[i + 1] + (R.rs[i + 1] - R.rs[i] - R.nL[i] - 1) + 1;
+  host_parallel_for(n, [&](int64_t i0, int64_t i1) {
+    for (int i = (int)i0; i < (int)i1; i++) {
+      for (int q = 0; q < R.nL[i]; q++) out.bj[out.bi[i] + q] = R.cols[R.rs[i] + q];
+      const int nz = R.rs[i + 1] - R.rs[i] - R.nL[i] - 1;
+      int k = out.bdiag[i + 1] + 1;  // row i's U block starts right after row i+1's diagonal
+      for (int q = 0; q < nz; q++) out.bj[k++] = R.cols[R.rs[i] + R.nL[i] + 1 + q];
+      out.bj[k] = i;
+    }
+  });
   out.r = r;
   out.ic = ic;
   return GP_OK;
@@ -322,15 +390,18 @@ int icc_symbolic(const Csr* A, int levels, const std::vector<int>& r, const std:
   out.nnz = (int)total;
   out.bj.assign(std::max<int64_t>(total, 1), 0);
   out.bdiag.assign(n + 1, 0);
-  int pos = 0;
-  for (int k = 0; k < n; k++) {
-    out.bi[k] = pos;
-    for (int q = R.rs[k]; q < R.rs[k + 1]; q++) out.bj[pos++] = R.cols[q];
-    out.bdiag[k] = pos;
-    out.bj[pos++] = k;
-  }
-  out.bi[n] = pos;
-  out.bdiag[n] = pos;
+  // row k: its strict upper columns, then its diagonal slot (k rows before it)
+  host_parallel_for(n, [&](int64_t k0, int64_t k1) {
+    for (int k = (int)k0; k < (int)k1; k++) {
+      int pos = R.rs[k] + k;
+      out.bi[k] = pos;
+      for (int q = R.rs[k]; q < R.rs[k + 1]; q++) out.bj[pos++] = R.cols[q];
+      out.bdiag[k] = pos;
+      out.bj[pos] = k;
+    }
+  });
+  out.bi[n] = (int)total;
+  out.bdiag[n] = (int)total;
   out.r = r;
   out.ic = ic;
   return GP_OK;

@@ -166,3 +166,45 @@ def test_oracle_icc_natural_is_the_incomplete_cholesky():
     x = np.random.default_rng(12).normal(size=n)
     got = O.OraclePC("icc", ip, ix, v).apply(x)
     np.testing.assert_allclose(got, dense_ic0_apply(A, x), rtol=1e-12, atol=1e-13)
+
+
+def test_level0_patterns_on_host_threads_match_the_oracle(G):
+    """Level 0 on a grid large enough to be split over several host threads
+    (42^3 = 74,088 rows): ILU(0) in natural and random order and IC(0) give
+    the oracle's staging layouts exactly."""
+    ip, ix, _ = gallery.laplacian_3d(42)
+    ip, ix = O.i64(ip), O.i64(ix)
+    n = len(ip) - 1
+    nnz = int(ip[-1])
+    cap = nnz + n + 100  # level 0 adds no fill
+    rnd = np.random.default_rng(3).permutation(n).astype(np.int64)
+    for r in (np.arange(n, dtype=np.int64), rnd):
+        ic = np.argsort(r).astype(np.int64)
+        res = []
+        for lib in (G, O.lib()):
+            out = [np.zeros(n + 1, np.int64), np.zeros(cap, np.int64), np.zeros(cap, np.int64),
+                   np.zeros(n + 1, np.int64)]
+            scratch = np.zeros(7 * n + 8, np.int64)
+            k = lib.mp_ilu_symbolic(*[a(x) for x in out], a(ip), a(ix), a(r), a(ic), 0, cap,
+                                    a(scratch), n)
+            res.append((k, out))
+        (kg, g), (ko, o) = res
+        assert kg == ko > 0
+        for i in range(4):
+            m = kg if i in (1, 2) else n + 1
+            np.testing.assert_array_equal(g[i][:m], o[i][:m])
+    r = np.arange(n, dtype=np.int64)
+    ic = r.copy()
+    res = []
+    for lib in (G, O.lib()):
+        scratch = np.zeros(6 * (n + 1) + 2 * cap, np.int64)
+        out = [np.zeros(n + 1, np.int64), np.zeros(cap, np.int64), np.zeros(cap, np.int64),
+               np.zeros(n, np.int64)]
+        k = lib.mp_icc_symbolic(*[a(x) for x in out], a(ip), a(ix), a(r), a(ic), 0, cap,
+                                a(scratch), n, len(scratch))
+        res.append((k, out))
+    (kg, g), (ko, o) = res
+    assert kg == ko > 0
+    for i in range(4):
+        m = kg if i in (1, 2) else (n + 1 if i == 0 else n)
+        np.testing.assert_array_equal(g[i][:m], o[i][:m])
