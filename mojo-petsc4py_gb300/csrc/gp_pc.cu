@@ -649,9 +649,11 @@ static int setup_sor(Pc* pc, cudaStream_t s) {
   GP_TRY(plan(pc->fwd, n, lp, lc, true, s, &of));
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
   setup_mark("levels");
-  GP_TRY(ell_build(pc->ef, ELL_SOR_F, n, true, of, lp, lc, ls, none, none, none, &fpos));
+  GP_TRY(ell_build(pc->ef, ELL_SOR_F, n, true, of, lp, lc, ls, none, none, none, &fpos,
+                   pc->fwd.nlevels));
   setup_mark("fwd-layout");
-  GP_TRY(ell_build(pc->eb, ELL_SOR_B, n, false, ob, up, uc, us, fpos, none, none, nullptr));
+  GP_TRY(ell_build(pc->eb, ELL_SOR_B, n, false, ob, up, uc, us, fpos, none, none, nullptr,
+                   pc->bwd.nlevels));
   setup_mark("bwd-layout");
   pc->vlen = std::max({n, pc->ef.n, pc->eb.n});
   GP_TRY(dalloc(&pc->t, pc->vlen));
@@ -713,9 +715,11 @@ static int ilu_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
   GP_TRY(plan(pc->fwd, n, lp, lc, true, s, &of));
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
   setup_mark("levels");
-  GP_TRY(ell_build(pc->ef, ELL_ILU_F, n, true, of, lp, lc, ls, P.r, none, none, &fpos));
+  GP_TRY(ell_build(pc->ef, ELL_ILU_F, n, true, of, lp, lc, ls, P.r, none, none, &fpos,
+                   pc->fwd.nlevels));
   setup_mark("fwd-layout");
-  GP_TRY(ell_build(pc->eb, ELL_ILU_B, n, false, ob, up, uc, us, fpos, perm_c, dsl, nullptr));
+  GP_TRY(ell_build(pc->eb, ELL_ILU_B, n, false, ob, up, uc, us, fpos, perm_c, dsl, nullptr,
+                   pc->bwd.nlevels));
   setup_mark("bwd-layout");
   // the numeric phase's update lists (the searches of the elimination, once);
   // kept to the end of the function: the copies below are asynchronous
@@ -921,9 +925,11 @@ static int icc_prepare(Pc* pc, const std::vector<int>& perm_c, cudaStream_t s) {
   GP_TRY(plan(pc->fwd, n, tptr, trow_deps, true, s, &of));
   GP_TRY(plan(pc->bwd, n, up, uc, false, s, &ob));
   setup_mark("levels");
-  GP_TRY(ell_build(pc->ef, ELL_ICC_F, n, true, of, tptr, trow_deps, tsl, perm_c, none, dsl, &fpos));
+  GP_TRY(ell_build(pc->ef, ELL_ICC_F, n, true, of, tptr, trow_deps, tsl, perm_c, none, dsl, &fpos,
+                   pc->fwd.nlevels));
   setup_mark("fwd-layout");
-  GP_TRY(ell_build(pc->eb, ELL_ICC_B, n, false, ob, up, uc, us, fpos, perm_c, none, nullptr));
+  GP_TRY(ell_build(pc->eb, ELL_ICC_B, n, false, ob, up, uc, us, fpos, perm_c, none, nullptr,
+                   pc->bwd.nlevels));
   setup_mark("bwd-layout");
   GP_TRY(upload(&pc->bi, P.bi, s));
   GP_TRY(upload(&pc->bj, P.bj, s));

@@ -96,13 +96,13 @@ int brick_sweep(int mode, const EllSweep& e, const int* gate, int want, DRef in,
 void set_sweep_bricks(int mode, int lines, int max_ctas);
 // Lay out one sweep.  forward: dependencies precede each row (ascending
 // processing); otherwise they follow it.  `order` is the level order, used
-// when the sweep is not tiled.
+// when the sweep is not tiled; nlevels its depth when known (0: counted here).
 // mode: the EllMode of the kernel that will run the sweep.
 int ell_build(EllSweep& e, int mode, int n, bool forward, const std::vector<int>& order,
               const std::vector<int>& dptr, const std::vector<int>& dcol,
               const std::vector<int>& dsl, const std::vector<int>& in_row,
               const std::vector<int>& out_row, const std::vector<int>& dslot_row,
-              std::vector<int>* pos_of_row);
+              std::vector<int>* pos_of_row, int nlevels = 0);
 int ell_refresh(EllSweep& e, const double* src, cudaStream_t s);
 // ell_build choosing between the level-ordered and the chunked form only (no
 // brick layout: its kernel reads the reference's inputs of each mode only).

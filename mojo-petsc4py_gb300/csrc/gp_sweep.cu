@@ -923,7 +923,7 @@ static int ell_build_impl(EllSweep& e, int mode, int n, bool forward,
                           const std::vector<int>& dsl, const std::vector<int>& in_row,
                           const std::vector<int>& out_row, const std::vector<int>& dslot_row,
                           std::vector<int>* pos_of_row, bool allow_tiles,
-                          bool allow_bricks = true) {
+                          bool allow_bricks = true, int nlevels = 0) {
   ell_free(e);
   int W = 0;
   for (int i = 0; i < n; i++) W = std::max(W, dptr[i + 1] - dptr[i]);
@@ -933,9 +933,9 @@ static int ell_build_impl(EllSweep& e, int mode, int n, bool forward,
   const SweepTuning& tu = sweep_tuning();
   TilePlan tp;
   bool tiled = false;
-  int considered = 0, nlev = 0;
+  int considered = 0, nlev = nlevels;  // the caller's level count, when it has one
   if (tu.tiles && allow_tiles && n > 0) {
-    nlev = sweep_levels(n, dptr, dcol, forward);
+    if (!nlev) nlev = sweep_levels(n, dptr, dcol, forward);
     tiled = tile_choose(mode, n, W, dptr, dcol, forward, nlev, tu, tp, &considered);
     setup_mark("chunk-model");
   }
@@ -1019,9 +1019,9 @@ int ell_build(EllSweep& e, int mode, int n, bool forward, const std::vector<int>
               const std::vector<int>& dptr, const std::vector<int>& dcol,
               const std::vector<int>& dsl, const std::vector<int>& in_row,
               const std::vector<int>& out_row, const std::vector<int>& dslot_row,
-              std::vector<int>* pos_of_row) {
+              std::vector<int>* pos_of_row, int nlevels) {
   return ell_build_impl(e, mode, n, forward, order, dptr, dcol, dsl, in_row, out_row,
-                        dslot_row, pos_of_row, true);
+                        dslot_row, pos_of_row, true, true, nlevels);
 }
 
 int ell_build_chunked(EllSweep& e, int mode, int n, bool forward, const std::vector<int>& order,
