@@ -598,8 +598,10 @@ __global__ void __launch_bounds__(kSpmvRows) k_cgf_spmv(KspState* st, int n,
       const int row = r0 + threadIdx.x;
       if (row < n) {
         const double s = row == row0
-                             ? spmv_row_from<FMA>(pre, colind, val, p, 0.0, pol)
-                             : spmv_row<FMA>(row, rowptr, colind, val, p, 0.0, pol);
+                             ? spmv_row_from<FMA, double, double, CT, false>(pre, colind,
+                                                                            val, p, 0.0, pol)
+                             : spmv_row<FMA, double, double, CT, false>(row, rowptr, colind,
+                                                                        val, p, 0.0, pol);
         w[row] = s;
         v[0] = madd<FMA>(p[row], s, v[0]);
       }

@@ -84,8 +84,12 @@ __device__ __forceinline__ int spmv_col(const short* c, int j, int row, uint64_t
 }
 
 // Row `row`'s sum, starting from `init` (caller checks row < n).  CT: int
-// (column indices) or short (offsets from the row).
-template <bool FMA, typename VT, typename XT, typename CT>
+// (column indices) or short (offsets from the row).  BOUND: each 4-slot
+// batch issues only as many FMAs as the widest row of the warp still needs (a
+// warp maximum a batch), so rows of 7 do not issue an eighth, predicated-off
+// FP64 instruction; measured faster in the standalone multiply and slower in
+// the fused CG pass, which keeps the plain form.
+template <bool FMA, typename VT, typename XT, typename CT, bool BOUND = true>
 __device__ __forceinline__ double spmv_row(int row, const int* __restrict__ rowptr,
                                            const CT* __restrict__ colind,
                                            const VT* __restrict__ val, const XT* __restrict__ x,
@@ -103,9 +107,11 @@ __device__ __forceinline__ double spmv_row(int row, const int* __restrict__ rowp
         cc[u] = spmv_col(colind, j0 + u, row, pol);
         vv[u] = (double)ld_stream(val + j0 + u, pol);
       }
+    // the batch's widest row in the warp bounds the FMAs issued (uniform)
+    const int wb = BOUND ? __reduce_max_sync(__activemask(), e - j0) : 4;
 #pragma unroll
     for (int u = 0; u < 4; u++)
-      if (j0 + u < e) acc = madd<FMA>(vv[u], (double)x[cc[u]], acc);
+      if (u < wb && j0 + u < e) acc = madd<FMA>(vv[u], (double)x[cc[u]], acc);
   }
   return acc;
 }
@@ -135,7 +141,7 @@ __device__ __forceinline__ void spmv_row_preload(int row, const int* __restrict_
     }
 }
 
-template <bool FMA, typename VT, typename XT, typename CT>
+template <bool FMA, typename VT, typename XT, typename CT, bool BOUND = true>
 __device__ __forceinline__ double spmv_row_from(const SpmvPre& pre,
                                                 const CT* __restrict__ colind,
                                                 const VT* __restrict__ val,
@@ -143,9 +149,12 @@ __device__ __forceinline__ double spmv_row_from(const SpmvPre& pre,
                                                 uint64_t pol) {
   double acc = init;
   const int b = pre.j, e = pre.e, row = pre.row;
+  {
+    const int wb = BOUND ? __reduce_max_sync(__activemask(), e - b) : 4;
 #pragma unroll
-  for (int u = 0; u < 4; u++)
-    if (b + u < e) acc = madd<FMA>(pre.vv[u], (double)x[pre.cc[u]], acc);
+    for (int u = 0; u < 4; u++)
+      if (u < wb && b + u < e) acc = madd<FMA>(pre.vv[u], (double)x[pre.cc[u]], acc);
+  }
   for (int j0 = b + 4; j0 < e; j0 += 4) {
     int cc[4];
     double vv[4];
@@ -155,9 +164,11 @@ __device__ __forceinline__ double spmv_row_from(const SpmvPre& pre,
         cc[u] = spmv_col(colind, j0 + u, row, pol);
         vv[u] = (double)ld_stream(val + j0 + u, pol);
       }
+    // the batch's widest row in the warp bounds the FMAs issued (uniform)
+    const int wb = BOUND ? __reduce_max_sync(__activemask(), e - j0) : 4;
 #pragma unroll
     for (int u = 0; u < 4; u++)
-      if (j0 + u < e) acc = madd<FMA>(vv[u], (double)x[cc[u]], acc);
+      if (u < wb && j0 + u < e) acc = madd<FMA>(vv[u], (double)x[cc[u]], acc);
   }
   return acc;
 }
