@@ -189,10 +189,21 @@ class Vec:
         return self._h
 
     def setArray(self, array) -> None:
+        """Copy `array` into the vector.  A large vector takes it straight to
+        its device block (a host-to-device copy runs at the link rate from any
+        host memory, while a copy into the page-locked host array first costs a
+        host memcpy of the same size); the host array is brought up to date by
+        the next getArray, as after any kernel that writes the vector."""
         cur = self._check()
         arr = _f64(array)
         if len(arr) != len(cur):
             raise ValueError(f"incompatible array size: {len(arr)} != {len(cur)}")
+        if len(arr) >= dev.PINNED_MIN and dev.has_device():
+            if self._d is None:
+                self._d = dev.DeviceArray(len(arr))
+            dev.upload(self._d.ptr, arr)
+            self._loc = _DEVICE
+            return
         cur[:] = arr
         self._loc = _HOST
 
