@@ -50,9 +50,11 @@ static int mix_grid(int64_t n) {
                                                      (int64_t)num_sms() * 8));
 }
 
-// y = A x in FP32 (row per thread, matrix streamed with L2 evict-first)
+// y = A x in FP32 (row per thread, matrix streamed with L2 evict-first).  CT:
+// int (column indices) or short (16-bit offsets from the row, Csr::coff16).
+template <typename CT>
 __global__ void __launch_bounds__(kMixBlock) k_spmv32(int n, const int* __restrict__ rp,
-                                                      const int* __restrict__ ci,
+                                                      const CT* __restrict__ ci,
                                                       const float* __restrict__ val,
                                                       const float* __restrict__ x,
                                                       float* __restrict__ y) {
@@ -67,7 +69,7 @@ __global__ void __launch_bounds__(kMixBlock) k_spmv32(int n, const int* __restri
 #pragma unroll
     for (int u = 0; u < 8; u++)
       if (j0 + u < e) {
-        cc[u] = ld_stream(ci + j0 + u, pol);
+        cc[u] = spmv_col(ci, j0 + u, row, pol);
         vv[u] = ld_stream(val + j0 + u, pol);
       }
 #pragma unroll
@@ -897,7 +899,10 @@ int mixed_solve(Mixed* M, Csr* A, Pc* pc, const double* b, double* x, const Mixe
       float* vj = M->V + (size_t)j * n;
       float* zj = M->Z + (size_t)j * n;
       GP_TRY(mixed_pc(M, o.tri_sweeps, vj, zj, s));
-      k_spmv32<<<gr, kMixBlock, 0, s>>>(n, A->rowptr, A->colind, A->val32, zj, M->w);
+      if (A->coff16)
+        k_spmv32<short><<<gr, kMixBlock, 0, s>>>(n, A->rowptr, A->coff16, A->val32, zj, M->w);
+      else
+        k_spmv32<int><<<gr, kMixBlock, 0, s>>>(n, A->rowptr, A->colind, A->val32, zj, M->w);
       // classical Gram-Schmidt against v_0..v_j
       GP_TRY(mdot_host(M, M->V, j + 1, M->w, h.data(), s));
       k_maxpy32<<<g, kMixBlock, 0, s>>>(n, M->V, j + 1, M->h_dev, M->w);
@@ -1123,9 +1128,10 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_tri_ell(
   }
 }
 
+template <typename CT>
 __global__ void __launch_bounds__(kMixBlock) k_mx_spmv32(const int* gate, int n,
                                                          const int* __restrict__ rp,
-                                                         const int* __restrict__ ci,
+                                                         const CT* __restrict__ ci,
                                                          const float* __restrict__ val,
                                                          const float* __restrict__ x,
                                                          float* __restrict__ y) {
@@ -1137,7 +1143,7 @@ __global__ void __launch_bounds__(kMixBlock) k_mx_spmv32(const int* gate, int n,
   const uint64_t pol = l2_evict_first();
   float acc = 0.f;
   for (int j = rp[row]; j < rp[row + 1]; j++)
-    acc = __fmaf_rn(ld_stream(val + j, pol), x[ld_stream(ci + j, pol)], acc);
+    acc = __fmaf_rn(ld_stream(val + j, pol), x[spmv_col(ci, j, row, pol)], acc);
   y[row] = acc;
 }
 
@@ -1492,8 +1498,12 @@ static int record_pass(Mixed* M, const Csr* A, const Pc* pc, const double* b, do
     }
     // the step's kernels start while their predecessor drains (each waits
     // in pdl_wait() before reading it)
-    GP_CUDA(launch_pdl(k_mx_spmv32, gr, kMixBlock, s, act, n, A->rowptr, A->colind, A->val32,
-                       zj, M->w));
+    if (A->coff16)
+      GP_CUDA(launch_pdl(k_mx_spmv32<short>, gr, kMixBlock, s, act, n, A->rowptr,
+                         (const short*)A->coff16, A->val32, zj, M->w));
+    else
+      GP_CUDA(launch_pdl(k_mx_spmv32<int>, gr, kMixBlock, s, act, n, A->rowptr,
+                         (const int*)A->colind, A->val32, zj, M->w));
     GP_CUDA(launch_pdl(k_mx_mdot, mdot_grid(n), kMixBlock, s, act, n, M->V, j + 1, M->w,
                        M->partials, M->ticket, M->h_dev));
     GP_CUDA(launch_pdl(k_mx_maxpy_norm, g, kMixBlock, s, act, n, M->V, j + 1, M->h_dev, M->w,
