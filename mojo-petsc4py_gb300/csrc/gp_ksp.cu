@@ -245,6 +245,18 @@ __global__ void __launch_bounds__(kRedBlock) k_dred(const int* gate, int want, i
   }
 }
 
+// One batch of the multi-dot: v[q] += sum_i x_i basis_q,i for q < JN, over
+// the grid-stride elements of this thread.
+template <bool FMA, int JN>
+__device__ __forceinline__ void mdot_batch(int n, const double* __restrict__ x,
+                                           const double* __restrict__ basis, double (&v)[8]) {
+  GRID_LOOP(i, n) {
+    const double a = x[i];
+#pragma unroll
+    for (int q = 0; q < JN; q++) v[q] = madd<FMA>(a, basis[(size_t)q * n + i], v[q]);
+  }
+}
+
 // VecMDot of x against `*count` contiguous basis vectors (ld = n): one pass
 // over x and the basis, per-block partial sums for every vector, last block
 // folds the partials.  Used by classical Gram-Schmidt.
@@ -265,11 +277,18 @@ __global__ void __launch_bounds__(kRedBlock) k_mdot(const int* gate, int want, i
 #pragma unroll
     for (int q = 0; q < 8; q++) v[q] = 0.0;
     const int jn = min(8, k - j0);
-    GRID_LOOP(i, n) {
-      const double a = x[i];
-#pragma unroll
-      for (int q = 0; q < 8; q++)
-        if (q < jn) v[q] = madd<FMA>(a, basis[(size_t)(j0 + q) * n + i], v[q]);
+    // the batch's width is the same in every thread: a body unrolled for
+    // exactly jn dots, so a partial batch issues no predicated-off FMAs
+    // (each would hold the FP64 unit for a full warp instruction)
+    switch (jn) {
+      case 1: mdot_batch<FMA, 1>(n, x, basis + (size_t)j0 * n, v); break;
+      case 2: mdot_batch<FMA, 2>(n, x, basis + (size_t)j0 * n, v); break;
+      case 3: mdot_batch<FMA, 3>(n, x, basis + (size_t)j0 * n, v); break;
+      case 4: mdot_batch<FMA, 4>(n, x, basis + (size_t)j0 * n, v); break;
+      case 5: mdot_batch<FMA, 5>(n, x, basis + (size_t)j0 * n, v); break;
+      case 6: mdot_batch<FMA, 6>(n, x, basis + (size_t)j0 * n, v); break;
+      case 7: mdot_batch<FMA, 7>(n, x, basis + (size_t)j0 * n, v); break;
+      default: mdot_batch<FMA, 8>(n, x, basis + (size_t)j0 * n, v); break;
     }
     // warp sums of the 8 values by halving exchanges: at offset 16 a lane
     // keeps the half of the values its lane bit selects and adds its
