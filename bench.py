@@ -366,20 +366,28 @@ def spmv_index_bytes(h):
 
 def run_spmv_only(args):
     """SpMV launches alone on the 7-point matrix of a k^3 grid (k =
-    --spmv-grid, the benchmark's 128 by default; the profiling target)."""
+    --spmv-grid, the benchmark's 128 by default; the profiling target), or
+    with --spmv-hubs on the skewed-row operator of the bandwidth form (a path
+    graph of 2^20 rows with 8 hub rows of ~100k entries: the row-stream
+    SpMV and, in the FMA arithmetic, the hubs summed by segments)."""
     import torch
 
     from mojopetsc4py import PETSc
 
     from mojopetsc4py import gallery
 
-    ip, ix, v = gallery.laplacian_3d(args.spmv_grid)
+    if args.spmv_hubs:
+        ip, ix, v = gallery.hub_laplacian(1 << 20, 8, 100_000)
+    else:
+        ip, ix, v = gallery.laplacian_3d(args.spmv_grid)
     n, nnz = len(ip) - 1, int(ip[-1])
-    A = PETSc.Mat().createSeqAIJ((n, n), nnz=7)
+    A = PETSc.Mat().createSeqAIJ((n, n), nnz=None if args.spmv_hubs else 7)
     A.setValuesCSR(ip, ix, v)
     A.assemble()
     algo, t, _ = spmv_roofline(torch, PETSc, A, n, nnz, launches=args.steps)
-    print(json.dumps({"kernel": "k_spmv", "algorithmic_bytes": algo, "launch_us": t * 1e6,
+    print(json.dumps({"kernel": "k_spmv", "matrix": "hubs_2^20" if args.spmv_hubs else
+                      f"poisson3d_{args.spmv_grid}^3", "n": n, "nnz": nnz,
+                      "algorithmic_bytes": algo, "launch_us": t * 1e6,
                       "achieved_gbs": algo / t / 1e9}), flush=True)
 
 
@@ -1033,6 +1041,8 @@ def main():
     ap.add_argument("--spmv-only", action="store_true", help="SpMV launches only")
     ap.add_argument("--spmv-grid", type=int, default=K3,
                     help="grid size k of the k^3 matrix for --spmv-only")
+    ap.add_argument("--spmv-hubs", action="store_true",
+                    help="--spmv-only on the skewed-row operator (2^20 rows, 8 hubs of ~100k)")
     ap.add_argument("--vec-only", type=int, default=None, metavar="P",
                     help="launch each Vec kernel twice on 2^P doubles (profiling)")
     ap.add_argument("--form", choices=["mixed", "batched", "adjoint", "bandwidth"], default=None,

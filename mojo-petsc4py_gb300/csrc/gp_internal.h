@@ -109,6 +109,7 @@ struct DevReduceArgs {
 // part holds the segment sums and ticket counts a row's finished segments).
 struct SpmvLongRows {
   int nlong = 0, nseg = 0;
+  bool short_rows = false;    // the other rows fit the row-per-thread form
   int* rows = nullptr;
   int* seg = nullptr;
   int* seg_long = nullptr;    // [nseg] index into rows

@@ -66,6 +66,7 @@ int long_rows_build(SpmvLongRows& L, int n, const int* h_rowptr, cudaStream_t s)
   long_rows_free(L);
   if (!spmv_split_long_enabled()) return GP_OK;
   std::vector<int> rows, seg(1, 0), seg_long;
+  int64_t short_max = 0, short_nnz = 0;
   for (int i = 0; i < n; i++) {
     const int len = h_rowptr[i + 1] - h_rowptr[i];
     if (len > kSpmvLongRow) {
@@ -73,10 +74,18 @@ int long_rows_build(SpmvLongRows& L, int n, const int* h_rowptr, cudaStream_t s)
       for (int q = 0; q < ns; q++) seg_long.push_back((int)rows.size());
       rows.push_back(i);
       seg.push_back(seg.back() + ns);
+    } else {
+      short_max = std::max<int64_t>(short_max, len);
+      short_nnz += len;
     }
   }
   if (rows.empty()) return GP_OK;
   L.nlong = (int)rows.size();
+  // with the long rows split off, the rest goes one row a thread when it
+  // meets the row form's own bound (as csr_finish chooses the form)
+  const int nshort = n - L.nlong;
+  const double avg = nshort ? (double)short_nnz / nshort : 0.0;
+  L.short_rows = short_max <= kSpmvMaxRowLen && (double)short_max <= 8.0 * avg + 8.0;
   L.nseg = seg.back();
   GP_TRY(dev_upload(&L.rows, rows.data(), rows.size(), s));
   GP_TRY(dev_upload(&L.seg, seg.data(), seg.size(), s));
@@ -393,26 +402,45 @@ __global__ void __launch_bounds__(kSpmvRows) k_spmv(int n, const int* __restrict
 // the CTA that finishes a row's last segment adds the row's segment sums in
 // segment order to its start value (v_i for MatMultAdd, else 0) and stores it.
 // The sum's order is fixed, so results repeat run to run; it differs from one
-// FMA chain by rounding only.
-__global__ void __launch_bounds__(kSpmvRows) k_spmv_long(
-    const int* __restrict__ rowptr, const int* __restrict__ colind, const double* __restrict__ val,
-    DRef xr, const double* __restrict__ v, DRef yr, SpmvLongRows L, const int* gate, int want) {
-  if (gated_off(gate, want)) return;
+// FMA chain by rounding only.  Called by every thread of the CTA.
+__device__ __forceinline__ void spmv_long_segment(int s, const int* __restrict__ rowptr,
+                                                  const int* __restrict__ colind,
+                                                  const double* __restrict__ val,
+                                                  const double* __restrict__ x,
+                                                  const double* __restrict__ v,
+                                                  double* __restrict__ y, const SpmvLongRows& L) {
   const int* __restrict__ long_rows = L.rows;
   const int* __restrict__ long_seg = L.seg;
   const int* __restrict__ seg_long = L.seg_long;
   double* seg_part = L.part;
   unsigned* ticket = L.ticket;
-  const double* __restrict__ x = xr.get();
-  double* __restrict__ y = yr.get();
   __shared__ double red[kSpmvRows / 32];
   __shared__ bool last;
-  const int s = blockIdx.x, li = seg_long[s];
+  const int li = seg_long[s];
   const int row = long_rows[li];
   const int b = rowptr[row] + (s - long_seg[li]) * kSpmvLongSeg;
   const int e = min(b + kSpmvLongSeg, rowptr[row + 1]);
+  // a thread's slots j = b + tid + u * kSpmvRows: all loads first (the
+  // gathers in flight together), then the FMAs in j order
+  static_assert(kSpmvLongSeg % kSpmvRows == 0, "whole slots a thread");
+  constexpr int kPer = kSpmvLongSeg / kSpmvRows;
+  double vv[kPer], xv[kPer];
+  int cc[kPer];
+#pragma unroll
+  for (int u = 0; u < kPer; u++) {
+    const int j = b + threadIdx.x + u * kSpmvRows;
+    if (j < e) {
+      vv[u] = val[j];
+      cc[u] = colind[j];
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kPer; u++)
+    if (b + threadIdx.x + u * kSpmvRows < e) xv[u] = x[cc[u]];
   double acc = 0.0;
-  for (int j = b + threadIdx.x; j < e; j += kSpmvRows) acc = __fma_rn(val[j], x[colind[j]], acc);
+#pragma unroll
+  for (int u = 0; u < kPer; u++)
+    if (b + threadIdx.x + u * kSpmvRows < e) acc = __fma_rn(vv[u], xv[u], acc);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc = __dadd_rn(acc, __shfl_down_sync(0xffffffffu, acc, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
@@ -435,6 +463,34 @@ __global__ void __launch_bounds__(kSpmvRows) k_spmv_long(
   ticket[li] = 0u;
 }
 
+__global__ void __launch_bounds__(kSpmvRows) k_spmv_long(
+    const int* __restrict__ rowptr, const int* __restrict__ colind, const double* __restrict__ val,
+    DRef xr, const double* __restrict__ v, DRef yr, SpmvLongRows L, const int* gate, int want) {
+  if (gated_off(gate, want)) return;
+  spmv_long_segment(blockIdx.x, rowptr, colind, val, xr.get(), v, yr.get(), L);
+}
+
+// FMA arithmetic, long rows split off and the other rows short: one launch,
+// the long rows' segments in CTAs [0, nseg) and the other rows one a thread
+// (the row form's FMA chain, the same per row as the row stream's) in the
+// CTAs after them, so the two run side by side.
+__global__ void __launch_bounds__(kSpmvRows) k_spmv_split(
+    int n, const int* __restrict__ rowptr, const int* __restrict__ colind,
+    const double* __restrict__ val, DRef xr, const double* __restrict__ v, DRef yr,
+    SpmvLongRows L, const int* gate, int want, int evict_first) {
+  if (gated_off(gate, want)) return;
+  const double* __restrict__ x = xr.get();
+  double* __restrict__ y = yr.get();
+  if ((int)blockIdx.x < L.nseg) {
+    spmv_long_segment(blockIdx.x, rowptr, colind, val, x, v, y, L);
+    return;
+  }
+  const int row = ((int)blockIdx.x - L.nseg) * kSpmvRows + (int)threadIdx.x;
+  if (row >= n || rowptr[row + 1] - rowptr[row] > kSpmvLongRow) return;
+  y[row] = spmv_row<true>(row, rowptr, colind, val, x, v ? v[row] : 0.0,
+                          spmv_policy(evict_first));
+}
+
 static void launch_spmv(cudaStream_t s, const Csr* A, DRef x, const double* v, DRef y,
                         const int* gate, int want) {
   const bool f = arith_mode() == kFma;
@@ -447,6 +503,11 @@ static void launch_spmv(cudaStream_t s, const Csr* A, DRef x, const double* v, D
   auto k = A->stream_rows ? (f ? k_spmv<true, true> : k_spmv<false, true>)
                           : (f ? k_spmv<true, false> : k_spmv<false, false>);
   const bool split = f && A->lr.nlong > 0;
+  if (split && A->lr.short_rows) {
+    k_spmv_split<<<A->lr.nseg + spmv_grid(A), kSpmvRows, 0, s>>>(
+        A->n, A->rowptr, A->colind, A->val, x, v, y, A->lr, gate, want, A->l2_evict_first);
+    return;
+  }
   k<<<spmv_grid(A), kSpmvRows, 0, s>>>(A->n, A->rowptr, A->colind, A->val, x, v, y, gate, want,
                                        A->l2_evict_first, split ? kSpmvLongRow : INT_MAX);
   if (split)
@@ -504,6 +565,13 @@ int spmv_t(cudaStream_t s, const Csr* A, DRef x, DRef y, const int* gate, int wa
   auto k = A->t_stream_rows ? (f ? k_spmv<true, true> : k_spmv<false, true>)
                             : (f ? k_spmv<true, false> : k_spmv<false, false>);
   const bool split = f && A->t_lr.nlong > 0;
+  if (split && A->t_lr.short_rows) {
+    k_spmv_split<<<A->t_lr.nseg + (A->ncols + kSpmvRows - 1) / kSpmvRows, kSpmvRows, 0, s>>>(
+        A->ncols, A->t_rowptr, A->t_colind, A->t_val, x, nullptr, y, A->t_lr, gate, want,
+        A->l2_evict_first);
+    GP_CHECK_LAUNCH();
+    return GP_OK;
+  }
   k<<<(A->ncols + kSpmvRows - 1) / kSpmvRows, kSpmvRows, 0, s>>>(
       A->ncols, A->t_rowptr, A->t_colind, A->t_val, x, nullptr, y, gate, want,
       A->l2_evict_first, split ? kSpmvLongRow : INT_MAX);
