@@ -107,6 +107,9 @@ struct DevReduceArgs {
 // summed by segments of kSpmvLongSeg slots, one CTA a segment, instead of by
 // one thread (rows ascending; row i's segments are seg[i] .. seg[i + 1] - 1;
 // part holds the segment sums and ticket counts a row's finished segments).
+// When the other rows meet the row-per-thread bound (short_rows), one launch
+// runs the segments and those rows side by side (k_spmv_split); otherwise the
+// row stream takes them and skips the long ones.
 struct SpmvLongRows {
   int nlong = 0, nseg = 0;
   bool short_rows = false;    // the other rows fit the row-per-thread form
